@@ -1,0 +1,417 @@
+"""Python host layer over libbhk's C ABI (include/bhk.h).
+
+Names and argument meanings mirror the reference's kerr:: primitives (src/kerr.h) and its
+ray-level drivers (trajectory::traceRay, eht::render): `derivatives`, `step_mino`,
+`photon_step_size`, `enforce_constraints`, `normalize_angles`, `observer_frame`,
+`photon_from_frame`, `launch_from_zamo`, plus the batch tracer `Context.trace_frames` /
+`Context.trace_rays`. Arrays are torch tensors on a CUDA device (torch only supplies device
+memory and streams here); every computation runs in libbhk's kernels. There is no CPU
+fallback: without the built library or a GPU these raise.
+
+Struct arrays are float64 tensors with a trailing dimension: constants (n, 4) = (E, L, Q, mu),
+states (n, 6) = (t, r, theta, phi, vr, vtheta), derivatives (n, 6), frames (n, 4, 4).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbhk.so")
+
+OK, EINVAL, ECUDA, EUNFINISHED, ENOMEM = 0, 1, 2, 3, 4
+UNFINISHED, CAPTURED, DISK, ESCAPED = 0, 1, 2, 3
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class BhkError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"bhk status {status}: {msg}")
+        self.status = status
+
+
+class FrameDescC(C.Structure):
+    _fields_ = [("a", C.c_double), ("r_obs", C.c_double), ("theta_obs", C.c_double), ("phi_obs", C.c_double),
+                ("width", C.c_int32), ("height", C.c_int32), ("alpha_lo", C.c_double), ("alpha_hi", C.c_double),
+                ("beta_lo", C.c_double), ("beta_hi", C.c_double), ("r_disk_in", C.c_double),
+                ("r_disk_out", C.c_double)]
+
+
+class TraceOptsC(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_steps", C.c_int32), ("r_escape", C.c_double),
+                ("capture_eps", C.c_double), ("reproject_every", C.c_int32), ("block", C.c_int32),
+                ("chunk", C.c_int32), ("sort_buckets", C.c_int32), ("use_graph", C.c_int32)]
+
+
+class RaysOutC(C.Structure):
+    _fields_ = [("outcome", C.c_void_p), ("r_disk", C.c_void_p), ("phi_disk", C.c_void_p), ("g", C.c_void_p),
+                ("theta_inf", C.c_void_p), ("phi_inf", C.c_void_p), ("steps", C.c_void_p)]
+
+
+class StatsC(C.Structure):
+    _fields_ = [("rays", C.c_int64), ("accepted_steps", C.c_int64), ("rejected_steps", C.c_int64),
+                ("rescued", C.c_int64), ("unfinished", C.c_int64), ("block", C.c_int32), ("chunk", C.c_int32),
+                ("sort_buckets", C.c_int32), ("grid", C.c_int32), ("kernel_ms", C.c_double)]
+
+
+@dataclasses.dataclass
+class Frame:
+    """One ZAMO pinhole camera frame (bhk_frame_desc). Angles in radians."""
+    a: float
+    r_obs: float
+    theta_obs: float
+    width: int
+    height: int
+    alpha_lo: float
+    alpha_hi: float
+    beta_lo: float
+    beta_hi: float
+    r_disk_in: float = 0.0
+    r_disk_out: float = 20.0
+    phi_obs: float = 0.0
+
+    @property
+    def rays(self) -> int:
+        return self.width * self.height
+
+    def c(self) -> FrameDescC:
+        return FrameDescC(self.a, self.r_obs, self.theta_obs, self.phi_obs, self.width, self.height, self.alpha_lo,
+                          self.alpha_hi, self.beta_lo, self.beta_hi, self.r_disk_in, self.r_disk_out)
+
+
+@dataclasses.dataclass
+class TraceOpts:
+    """bhk_trace_opts; zeros mean the library defaults."""
+    precision: str = "fp64"
+    rtol: float = 0.0
+    max_steps: int = 0
+    r_escape: float = 0.0
+    capture_eps: float = 0.0
+    reproject_every: int = 0
+    block: int = 0
+    chunk: int = 0
+    sort_buckets: int = 0
+    use_graph: bool = False
+
+    def c(self) -> TraceOptsC:
+        prec = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[self.precision]
+        return TraceOptsC(prec, self.rtol, self.max_steps, self.r_escape, self.capture_eps, self.reproject_every,
+                          self.block, self.chunk, self.sort_buckets, 1 if self.use_graph else 0)
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    """Loads libbhk.so (built by black_simulation_gb300.build). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with black_simulation_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    vp, i64, d = C.c_void_p, C.c_int64, C.c_double
+    sig = {
+        "bhk_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "bhk_destroy": (C.c_int, [vp]),
+        "bhk_last_error": (C.c_char_p, []),
+        "bhk_version": (C.c_char_p, []),
+        "bhk_flops_per_step": (d, []),
+        "bhk_derivatives": (C.c_int, [d, vp, vp, vp, i64, vp]),
+        "bhk_step_mino": (C.c_int, [d, vp, vp, vp, i64, vp]),
+        "bhk_photon_step_size": (C.c_int, [d, vp, vp, d, vp, i64, vp]),
+        "bhk_enforce_constraints": (C.c_int, [d, vp, vp, i64, vp]),
+        "bhk_normalize_angles": (C.c_int, [vp, i64, vp]),
+        "bhk_potentials": (C.c_int, [d, vp, vp, vp, vp, i64, vp]),
+        "bhk_observer_frame": (C.c_int, [d, vp, vp, vp, vp, i64, vp]),
+        "bhk_photon_from_frame": (C.c_int, [d, d, d, d, vp, vp, vp, vp, i64, vp]),
+        "bhk_launch_from_zamo": (C.c_int, [d, d, d, d, vp, d, vp, vp, i64, vp]),
+        "bhk_cartesian_velocity": (C.c_int, [d, vp, vp, vp, i64, vp]),
+        "bhk_trace_frames": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
+                                       C.POINTER(RaysOutC), vp]),
+        "bhk_trace_frames_host": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
+                                            C.POINTER(RaysOutC)]),
+        "bhk_trace_rays": (C.c_int, [vp, i64, vp, vp, vp, vp, vp, d, d, C.POINTER(TraceOptsC),
+                                     C.POINTER(RaysOutC), vp]),
+        "bhk_get_stats": (C.c_int, [vp, C.POINTER(StatsC)]),
+        "bhk_autotune": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
+                                   C.POINTER(StatsC)]),
+        "bhk_critical_curve": (C.c_int, [d, d, d, C.c_int32, vp, vp, C.c_int32, C.POINTER(C.c_int32)]),
+        "bhk_fp32_fma_peak": (C.c_int, [C.c_int, C.POINTER(d)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int, allow_unfinished: bool = False) -> int:
+    if status == OK or (allow_unfinished and status == EUNFINISHED):
+        return status
+    raise BhkError(status, lib().bhk_last_error().decode())
+
+
+def exported_symbols() -> list[str]:
+    """Symbols include/bhk.h declares (for the load/export test)."""
+    hdr = os.path.join(os.path.dirname(PKG), "include", "bhk.h")
+    import re
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"\b(bhk_[a-z_0-9]+)\s*\(", text)))
+
+
+def _ptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    import torch
+    if isinstance(t, torch.Tensor):
+        if not t.is_cuda:
+            raise ValueError("libbhk arrays must be CUDA tensors")
+        if not t.is_contiguous():
+            raise ValueError("libbhk arrays must be contiguous")
+        return t.data_ptr()
+    return int(t)
+
+
+def _stream(stream) -> Optional[int]:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _n(t, width) -> int:
+    if t.dtype.itemsize != 8:
+        raise ValueError("expected float64")
+    if t.dim() != 2 or t.shape[1] != width:
+        raise ValueError(f"expected shape (n, {width})")
+    return t.shape[0]
+
+
+# --------------------------------------------------------------------------- per-step mirrors ----
+
+def derivatives(a: float, c, s, stream=None):
+    """kerr::derivatives for each row: returns (n, 6) float64 (dt, dr, dtheta, dphi, dvr, dvtheta)."""
+    import torch
+    n = _n(s, 6)
+    d = torch.empty((n, 6), dtype=torch.float64, device=s.device)
+    check(lib().bhk_derivatives(a, _ptr(c), _ptr(s), _ptr(d), n, _stream(stream)))
+    return d
+
+
+def step_mino(a: float, c, s, h, stream=None):
+    """kerr::stepMino in place on each row of s with step h[i]."""
+    check(lib().bhk_step_mino(a, _ptr(c), _ptr(s), _ptr(h), _n(s, 6), _stream(stream)))
+    return s
+
+
+def photon_step_size(a: float, c, s, tolerance: float, stream=None):
+    import torch
+    n = _n(s, 6)
+    h = torch.empty(n, dtype=torch.float64, device=s.device)
+    check(lib().bhk_photon_step_size(a, _ptr(c), _ptr(s), tolerance, _ptr(h), n, _stream(stream)))
+    return h
+
+
+def enforce_constraints(a: float, c, s, stream=None):
+    check(lib().bhk_enforce_constraints(a, _ptr(c), _ptr(s), _n(s, 6), _stream(stream)))
+    return s
+
+
+def normalize_angles(s, stream=None):
+    check(lib().bhk_normalize_angles(_ptr(s), _n(s, 6), _stream(stream)))
+    return s
+
+
+def potentials(a: float, c, s, stream=None):
+    import torch
+    n = _n(s, 6)
+    R = torch.empty(n, dtype=torch.float64, device=s.device)
+    Th = torch.empty(n, dtype=torch.float64, device=s.device)
+    check(lib().bhk_potentials(a, _ptr(c), _ptr(s), _ptr(R), _ptr(Th), n, _stream(stream)))
+    return R, Th
+
+
+def observer_frame(a: float, r, theta, u=None, stream=None):
+    """kerr::observerFrame at each (r[i], theta[i]); u None = the ZAMO. Returns (n, 4, 4)."""
+    import torch
+    n = r.shape[0]
+    f = torch.empty((n, 4, 4), dtype=torch.float64, device=r.device)
+    check(lib().bhk_observer_frame(a, _ptr(r), _ptr(theta), _ptr(u), _ptr(f), n, _stream(stream)))
+    return f
+
+
+def photon_from_frame(a: float, r: float, theta: float, phi: float, frame, look, stream=None):
+    """kerr::photonFromFrame for one camera frame (4, 4) and n look directions (n, 3)."""
+    import torch
+    n = _n(look, 3)
+    c = torch.empty((n, 4), dtype=torch.float64, device=look.device)
+    s = torch.empty((n, 6), dtype=torch.float64, device=look.device)
+    check(lib().bhk_photon_from_frame(a, r, theta, phi, _ptr(frame.contiguous()), _ptr(look), _ptr(c), _ptr(s), n,
+                                      _stream(stream)))
+    return c, s
+
+
+def launch_from_zamo(a: float, r: float, theta: float, phi: float, v, mu: float = 0.0, stream=None):
+    import torch
+    n = _n(v, 3)
+    c = torch.empty((n, 4), dtype=torch.float64, device=v.device)
+    s = torch.empty((n, 6), dtype=torch.float64, device=v.device)
+    check(lib().bhk_launch_from_zamo(a, r, theta, phi, _ptr(v), mu, _ptr(c), _ptr(s), n, _stream(stream)))
+    return c, s
+
+
+def cartesian_velocity(a: float, c, s, stream=None):
+    import torch
+    n = _n(s, 6)
+    out = torch.empty((n, 3), dtype=torch.float64, device=s.device)
+    check(lib().bhk_cartesian_velocity(a, _ptr(c), _ptr(s), _ptr(out), n, _stream(stream)))
+    return out
+
+
+def critical_curve(a: float, r_obs: float, theta_obs: float, samples: int = 400):
+    cap = max(samples, 16) * 16 + 64
+    al = np.zeros(cap)
+    be = np.zeros(cap)
+    n = C.c_int32(0)
+    check(lib().bhk_critical_curve(a, r_obs, theta_obs, samples, al.ctypes.data, be.ctypes.data, cap, C.byref(n)))
+    return al[:n.value].copy(), be[:n.value].copy()
+
+
+def flops_per_step() -> float:
+    return float(lib().bhk_flops_per_step())
+
+
+def fp32_fma_peak_tflops(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+    x = C.c_double(0.0)
+    check(lib().bhk_fp32_fma_peak(device, C.byref(x)))
+    return x.value
+
+
+# ----------------------------------------------------------------------------- batch tracer ----
+
+FIELDS = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf", "steps")
+
+
+def alloc_outputs(n: int, device="cuda"):
+    import torch
+    out = {k: torch.empty(n, dtype=torch.float64, device=device) for k in FIELDS[1:6]}
+    out["outcome"] = torch.empty(n, dtype=torch.uint8, device=device)
+    out["steps"] = torch.empty(n, dtype=torch.int32, device=device)
+    return out
+
+
+def _out_c(out: dict) -> RaysOutC:
+    return RaysOutC(*[_ptr(out.get(k)) for k in FIELDS])
+
+
+class Context:
+    """A bhk_context: stream, scratch, autotuned launch shape, cached CUDA graph."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().bhk_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().bhk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def _frames(frames: Sequence[Frame]):
+        arr = (FrameDescC * len(frames))(*[f.c() for f in frames])
+        return arr, len(frames)
+
+    def trace_frames(self, frames: Sequence[Frame], opts: TraceOpts = TraceOpts(), out: Optional[dict] = None,
+                     stream=None) -> dict:
+        """Traces all pixels of `frames` into device tensors (allocated if out is None)."""
+        arr, nf = self._frames(frames)
+        n = sum(f.rays for f in frames)
+        if out is None:
+            out = alloc_outputs(n, f"cuda:{self.device}")
+        oc = opts.c()
+        outc = _out_c(out)
+        check(lib().bhk_trace_frames(self.h, arr, nf, C.byref(oc), C.byref(outc), _stream(stream)))
+        return out
+
+    def trace_frames_host(self, frames: Sequence[Frame], opts: TraceOpts = TraceOpts(),
+                          out: Optional[dict] = None) -> tuple[dict, int]:
+        """Host-buffer call: numpy outputs (pinned or pageable), synchronous. Returns (out, status)."""
+        n = sum(f.rays for f in frames)
+        if out is None:
+            out = {k: np.empty(n) for k in FIELDS[1:6]}
+            out["outcome"] = np.empty(n, np.uint8)
+            out["steps"] = np.empty(n, np.int32)
+        arr, nf = self._frames(frames)
+        oc = opts.c()
+        ptrs = []
+        for k in FIELDS:
+            v = out.get(k)
+            ptrs.append(None if v is None else (v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data))
+        outc = RaysOutC(*ptrs)
+        st = check(lib().bhk_trace_frames_host(self.h, arr, nf, C.byref(oc), C.byref(outc)), allow_unfinished=True)
+        return out, st
+
+    def trace_rays(self, a, r_obs, theta_obs, alpha, beta, r_disk_in: float = 0.0, r_disk_out: float = 20.0,
+                   opts: TraceOpts = TraceOpts(), out: Optional[dict] = None, stream=None) -> dict:
+        n = a.shape[0]
+        if out is None:
+            out = alloc_outputs(n, a.device)
+        oc = opts.c()
+        outc = _out_c(out)
+        check(lib().bhk_trace_rays(self.h, n, _ptr(a), _ptr(r_obs), _ptr(theta_obs), _ptr(alpha), _ptr(beta),
+                                   r_disk_in, r_disk_out, C.byref(oc), C.byref(outc), _stream(stream)))
+        return out
+
+    def stats(self) -> dict:
+        s = StatsC()
+        check(lib().bhk_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in StatsC._fields_}
+
+    def autotune(self, frames: Sequence[Frame], opts: TraceOpts = TraceOpts()) -> dict:
+        arr, nf = self._frames(frames)
+        oc = opts.c()
+        s = StatsC()
+        check(lib().bhk_autotune(self.h, arr, nf, C.byref(oc), C.byref(s)))
+        return {k: getattr(s, k) for k, _ in StatsC._fields_}
+
+
+# ------------------------------------------------------------------------ standard workloads ----
+
+def isco_prograde(a: float) -> float:
+    """Bardeen-Press-Teukolsky prograde ISCO (host helper for workload set-up and tests)."""
+    z1 = 1 + (1 - a * a) ** (1 / 3) * ((1 + a) ** (1 / 3) + (1 - a) ** (1 / 3))
+    z2 = math.sqrt(3 * a * a + z1 * z1)
+    return 3 + z2 - math.sqrt(max(0.0, (3 - z1) * (3 + z1 + 2 * z2)))
+
+
+def frame_c1(width: int = 128, height: int = 128) -> Frame:
+    """a=0.9, r_obs=50, theta=80 deg, alpha,beta in [-15, 15], disk ISCO..20 (the FP64 parity frame)."""
+    return Frame(0.9, 50.0, math.radians(80.0), width, height, -15.0, 15.0, -15.0, 15.0, 0.0, 20.0)
+
+
+def frame_c2(width: int = 1920, height: int = 1080) -> Frame:
+    """a=0.998, r_obs=1000, theta=60 deg, alpha in +-20 with square pixels, disk ISCO..30 (1080p)."""
+    half_b = 20.0 * height / width
+    return Frame(0.998, 1000.0, math.radians(60.0), width, height, -20.0, 20.0, -half_b, half_b, 0.0, 30.0)

@@ -1,0 +1,464 @@
+// bhk_device.cuh -- device-side Kerr photon physics for sm_103a, templated on the arithmetic type.
+//
+// FP64 (double) functions restate the reference's kerr:: primitives operation for operation
+// (src/kerr.cpp:157-658) so that the batched per-step mirrors and the FP64 tracer agree with the
+// reference to rounding. The FP32 (float) specialisations of the right-hand side are the
+// throughput path: own sine/cosine (Cody-Waite reduction + Taylor polynomials), one approximate
+// reciprocal per evaluation, constants hoisted per ray.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bhk {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kNoRay = -1;
+
+// ----------------------------------------------------------------------------- scalar math ----
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// sin and cos of x for |x| below a few thousand. Reduction x = k pi/2 + r with a two-constant
+// Cody-Waite split of pi/2 (hi = pi/2 rounded to float, lo = the remainder), then the Taylor
+// series of sin and cos on |r| <= pi/4, truncated where the next term is below 3e-9 relative.
+__device__ __forceinline__ void sincos_fast(float x, float* s, float* c) {
+    const float k = rintf(x * 0.636619772367581343f);
+    float r = fmaf(k, -1.57079637050628662109375f, x);
+    r = fmaf(k, 4.37113900018624283e-8f, r);
+    const float r2 = r * r;
+    float ps = fmaf(r2, 2.75573192239858907e-6f, -1.98412698412698413e-4f);  // 1/9!, -1/7!
+    ps = fmaf(r2, ps, 8.33333333333333333e-3f);                               // 1/5!
+    ps = fmaf(r2, ps, -1.66666666666666667e-1f);                              // -1/3!
+    const float sr = fmaf(r * r2, ps, r);
+    float pc = fmaf(r2, -2.75573192239858907e-7f, 2.48015873015873016e-5f);  // -1/10!, 1/8!
+    pc = fmaf(r2, pc, -1.38888888888888889e-3f);                              // -1/6!
+    pc = fmaf(r2, pc, 4.16666666666666667e-2f);                               // 1/4!
+    pc = fmaf(r2, pc, -0.5f);                                                 // -1/2!
+    const float cr = fmaf(r2, pc, 1.0f);
+    const int q = static_cast<int>(k);
+    const float s0 = (q & 1) ? cr : sr;
+    const float c0 = (q & 1) ? sr : cr;
+    *s = (q & 2) ? -s0 : s0;
+    *c = ((q + 1) & 2) ? -c0 : c0;
+}
+
+template <typename T>
+struct Math;
+
+template <>
+struct Math<double> {
+    static __device__ __forceinline__ void sc(double x, double* s, double* c) { sincos(x, s, c); }
+    static __device__ __forceinline__ double div(double n, double d) { return n / d; }
+};
+
+template <>
+struct Math<float> {
+    static __device__ __forceinline__ void sc(float x, float* s, float* c) { sincos_fast(x, s, c); }
+    static __device__ __forceinline__ float div(float n, float d) { return n * rcp_approx(d); }
+};
+
+// ------------------------------------------------------------------- FP64 kerr primitives ----
+
+struct Cons { double E, L, Q, mu; };
+struct St { double t, r, theta, phi, vr, vtheta; };
+struct Der { double dt, dr, dtheta, dphi, dvr, dvtheta; };
+
+__host__ __device__ __forceinline__ double dmaxd(double x, double y) { return x > y ? x : y; }
+__host__ __device__ __forceinline__ double dmind(double x, double y) { return x < y ? x : y; }
+
+__device__ __forceinline__ bool naked(double a) { return fabs(a) > 1.0; }
+
+// r_+ (src/kerr.cpp:157-160).
+__device__ __forceinline__ double horizon_radius(double a) {
+    return naked(a) ? 0.0 : 1.0 + sqrt(dmaxd(0.0, 1.0 - a * a));
+}
+
+// Prograde/retrograde ISCO, Bardeen-Press-Teukolsky (src/kerr.cpp:179-190); NaN past a = 1.
+__device__ __forceinline__ double isco_radius(double a, bool prograde) {
+    if (naked(a)) return __longlong_as_double(0x7ff8000000000000ULL);
+    const double z1 = 1.0 + cbrt(1.0 - a * a) * (cbrt(1.0 + a) + cbrt(1.0 - a));
+    const double z2 = sqrt(3.0 * a * a + z1 * z1);
+    const double w = sqrt(dmaxd(0.0, (3.0 - z1) * (3.0 + z1 + 2.0 * z2)));
+    return prograde ? 3.0 + z2 - w : 3.0 + z2 + w;
+}
+
+// Keplerian angular velocity (src/kerr.cpp:296-299).
+__device__ __forceinline__ double circular_omega(double a, double r, bool prograde) {
+    const double s = prograde ? 1.0 : -1.0;
+    return s / (r * sqrt(r) + s * a);
+}
+
+// Covariant Kerr-Schild metric (src/kerr.cpp:238-254).
+__device__ __forceinline__ void metric_tensor(double a, double r, double theta, double g[4][4]) {
+    double sn, cs;
+    sincos(theta, &sn, &cs);
+    const double sn2 = sn * sn;
+    const double sigma = r * r + a * a * cs * cs;
+    const double rra = r * r + a * a;
+    const double A = rra * rra - a * a * (r * r - 2.0 * r + a * a) * sn2;
+    const double f = 2.0 * r / sigma;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) g[i][j] = 0.0;
+    g[0][0] = -(1.0 - f);
+    g[0][1] = g[1][0] = f;
+    g[0][3] = g[3][0] = -f * a * sn2;
+    g[1][1] = 1.0 + f;
+    g[1][3] = g[3][1] = -a * sn2 * (1.0 + f);
+    g[2][2] = sigma;
+    g[3][3] = A * sn2 / sigma;
+}
+
+__device__ __forceinline__ double metric_dot(const double g[4][4], const double* x, const double* y) {
+    double acc = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc += g[i][j] * x[i] * y[j];
+    return acc;
+}
+
+struct MetricAt { double sigma, delta, A, omega; };
+
+// (src/kerr.cpp:227-236)
+__device__ __forceinline__ MetricAt metric_at(double a, double r, double theta) {
+    double sn, cs;
+    sincos(theta, &sn, &cs);
+    MetricAt m;
+    m.sigma = r * r + a * a * cs * cs;
+    m.delta = r * r - 2.0 * r + a * a;
+    const double rra = r * r + a * a;
+    m.A = rra * rra - a * a * m.delta * sn * sn;
+    m.omega = 2.0 * a * r / m.A;
+    return m;
+}
+
+// (src/kerr.cpp:323-329)
+__device__ __forceinline__ double inflow_factor(double P, double vr, double delta, double K) {
+    if (P * vr < 0.0) return K / (P - vr);
+    const double d = fabs(delta) > 1e-12 ? delta : copysign(1e-12, delta);
+    return (P + vr) / d;
+}
+
+// kerr::derivatives (src/kerr.cpp:331-351), including dt and the rest mass mu.
+__device__ __forceinline__ Der derivatives(double a, const Cons& c, const St& s) {
+    const double r = s.r;
+    double sn, cs;
+    sincos(s.theta, &sn, &cs);
+    const double sn2 = dmaxd(sn * sn, 1e-18);
+    const double a2 = a * a, mu2 = c.mu * c.mu;
+    const double delta = r * r - 2.0 * r + a2;
+    const double rra = r * r + a2;
+    const double P = c.E * rra - a * c.L;
+    const double x = c.L - a * c.E;
+    const double K = mu2 * r * r + x * x + c.Q;
+    const double inflow = inflow_factor(P, s.vr, delta, K);
+    const double m = dmaxd(fabs(sn), 1e-9);
+    const double ssc = (sn < 0.0 ? -m : m) * m * m;
+    Der d;
+    d.dr = s.vr;
+    d.dtheta = s.vtheta;
+    d.dvr = 2.0 * c.E * r * P - (r - 1.0) * K - delta * mu2 * r;
+    d.dvtheta = sn * cs * a2 * (mu2 - c.E * c.E) + c.L * c.L * cs / ssc;
+    d.dphi = a * inflow - a * c.E + c.L / sn2;
+    d.dt = rra * inflow - a * (a * c.E * sn * sn - c.L) - s.vr;
+    return d;
+}
+
+// R(r), Theta(theta) (src/kerr.cpp:353-363).
+__device__ __forceinline__ double radial_potential(double a, const Cons& c, double r) {
+    const double delta = r * r - 2.0 * r + a * a;
+    const double P = c.E * (r * r + a * a) - a * c.L;
+    const double x = c.L - a * c.E;
+    return P * P - delta * (c.mu * c.mu * r * r + x * x + c.Q);
+}
+__device__ __forceinline__ double polar_potential(double a, const Cons& c, double theta) {
+    double sn, cs;
+    sincos(theta, &sn, &cs);
+    return c.Q - cs * cs * (a * a * (c.mu * c.mu - c.E * c.E) + c.L * c.L / dmaxd(sn * sn, 1e-18));
+}
+
+// RK4 step (src/kerr.cpp:502-519).
+__device__ __forceinline__ void step_mino(double a, const Cons& c, St& s, double h) {
+    const Der d1 = derivatives(a, c, s);
+    St y = s;
+    y.r = s.r + 0.5 * h * d1.dr; y.theta = s.theta + 0.5 * h * d1.dtheta; y.phi = s.phi + 0.5 * h * d1.dphi;
+    y.vr = s.vr + 0.5 * h * d1.dvr; y.vtheta = s.vtheta + 0.5 * h * d1.dvtheta;
+    const Der d2 = derivatives(a, c, y);
+    y.r = s.r + 0.5 * h * d2.dr; y.theta = s.theta + 0.5 * h * d2.dtheta; y.phi = s.phi + 0.5 * h * d2.dphi;
+    y.vr = s.vr + 0.5 * h * d2.dvr; y.vtheta = s.vtheta + 0.5 * h * d2.dvtheta;
+    const Der d3 = derivatives(a, c, y);
+    y.r = s.r + h * d3.dr; y.theta = s.theta + h * d3.dtheta; y.phi = s.phi + h * d3.dphi;
+    y.vr = s.vr + h * d3.dvr; y.vtheta = s.vtheta + h * d3.dvtheta;
+    const Der d4 = derivatives(a, c, y);
+    const double w = h / 6.0;
+    s.t += w * (d1.dt + 2.0 * d2.dt + 2.0 * d3.dt + d4.dt);
+    s.r += w * (d1.dr + 2.0 * d2.dr + 2.0 * d3.dr + d4.dr);
+    s.theta += w * (d1.dtheta + 2.0 * d2.dtheta + 2.0 * d3.dtheta + d4.dtheta);
+    s.phi += w * (d1.dphi + 2.0 * d2.dphi + 2.0 * d3.dphi + d4.dphi);
+    s.vr += w * (d1.dvr + 2.0 * d2.dvr + 2.0 * d3.dvr + d4.dvr);
+    s.vtheta += w * (d1.dvtheta + 2.0 * d2.dvtheta + 2.0 * d3.dvtheta + d4.dvtheta);
+}
+
+// Null-constraint re-projection outside a 5% turning zone (src/kerr.cpp:521-542). Returns the
+// state's new (vr, vtheta) through s.
+__device__ __forceinline__ void enforce_constraints(double a, const Cons& c, St& s) {
+    const double zone = 0.05;
+    const double r = s.r;
+    const double delta = r * r - 2.0 * r + a * a;
+    const double P = c.E * (r * r + a * a) - a * c.L;
+    const double x = c.L - a * c.E;
+    const double K = c.mu * c.mu * r * r + x * x + c.Q;
+    const double R = P * P - delta * K;
+    if (R > zone * (P * P + fabs(delta) * K)) s.vr = copysign(sqrt(R), s.vr);
+    double sn, cs;
+    sincos(s.theta, &sn, &cs);
+    const double cot2 = cs * cs / dmaxd(sn * sn, 1e-18);
+    const double pm = a * a * (c.mu * c.mu - c.E * c.E) * cs * cs;
+    const double Th = c.Q - pm - c.L * c.L * cot2;
+    if (Th > zone * (fabs(c.Q) + fabs(pm) + c.L * c.L * cot2)) s.vtheta = copysign(sqrt(Th), s.vtheta);
+}
+
+// (src/kerr.cpp:563-575)
+__device__ __forceinline__ double photon_step_size(double a, const Cons& c, const St& s, double tol) {
+    const Der d = derivatives(a, c, s);
+    double sn, cs;
+    sincos(s.theta, &sn, &cs);
+    sn = fabs(sn);
+    const double rs = naked(a) ? dmaxd(sqrt(s.r * s.r + a * a * cs * cs), 0.02) : s.r;
+    const double t = tol * fmin(fmax(rs / 8.0, 1.0), 4.0);
+    double h = t / (fabs(d.dr) / rs + fabs(d.dtheta) / dmaxd(sn, 1e-4) + fabs(d.dphi) + 1e-6);
+    h = dmind(h, sqrt(t * rs / (fabs(d.dvr) + 1e-6)));
+    h = dmind(h, sqrt(t * dmaxd(sn, 1e-4) / (fabs(d.dvtheta) + 1e-6)));
+    return h;
+}
+
+// Pole reflection (src/kerr.cpp:595-604). Returns true when it reflected.
+__device__ __forceinline__ bool normalize_angles(St& s) {
+    s.theta = fmod(s.theta, 2.0 * kPi);
+    if (s.theta < 0.0) s.theta += 2.0 * kPi;
+    if (s.theta > kPi) {
+        s.theta = 2.0 * kPi - s.theta;
+        s.phi += kPi;
+        s.vtheta = -s.vtheta;
+        return true;
+    }
+    return false;
+}
+
+// ZAMO 4-velocity (src/kerr.cpp:424-430).
+__device__ __forceinline__ void zamo_four_velocity(double a, double r, double theta, double u[4]) {
+    const MetricAt m = metric_at(a, r, theta);
+    const double ut = sqrt(m.A / (m.sigma * m.delta));
+    u[0] = ut; u[1] = 0.0; u[2] = 0.0; u[3] = m.omega * ut;
+}
+
+// Gram-Schmidt observer frame: slots filled in the order theta, phi, r (src/kerr.cpp:432-456).
+__device__ __forceinline__ void observer_frame(double a, double r, double theta, const double u[4], double e[4][4]) {
+    double g[4][4];
+    metric_tensor(a, r, theta, g);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) e[0][i] = u[i];
+    const int coord[3] = {2, 3, 1};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double w[4] = {0.0, 0.0, 0.0, 0.0};
+        w[coord[k]] = 1.0;
+        const double along = metric_dot(g, w, u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) w[i] += along * u[i];
+#pragma unroll
+        for (int j = 0; j < k; ++j) {
+            const double p = metric_dot(g, w, e[coord[j]]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) w[i] -= p * e[coord[j]][i];
+        }
+        const double n = sqrt(dmaxd(metric_dot(g, w, w), 1e-300));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) e[coord[k]][i] = w[i] / n;
+    }
+}
+
+// photonFromFrame with the kAxisSnap rewrite (src/kerr.cpp:458-483, src/kerr.h:115).
+__device__ __forceinline__ void photon_from_frame(double a, double r, double theta, double phi, const double e[4][4],
+                                                  const double look[3], Cons& c, St& s) {
+    double p[4], low[4], g[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] = e[0][i] - look[0] * e[1][i] - look[1] * e[2][i] - look[2] * e[3][i];
+    metric_tensor(a, r, theta, g);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        low[i] = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) low[i] += g[i][j] * p[j];
+    }
+    const double sigma = metric_at(a, r, theta).sigma;
+    double sn, cs;
+    sincos(theta, &sn, &cs);
+    c.mu = 0.0;
+    c.E = -low[0];
+    c.L = low[3];
+    s.t = 0.0; s.r = r; s.theta = theta; s.phi = phi;
+    s.vr = sigma * p[1];
+    s.vtheta = low[2];
+    c.Q = s.vtheta * s.vtheta + cs * cs * (c.L * c.L / dmaxd(sn * sn, 1e-18) - a * a * c.E * c.E);
+    if (fabs(c.L) < 3e-4 * sqrt(dmaxd(c.Q + a * a * c.E * c.E, 0.0))) {
+        c.L = 0.0;
+        c.Q = s.vtheta * s.vtheta - cs * cs * a * a * c.E * c.E;
+    }
+}
+
+// launchFromZamo (src/kerr.cpp:365-407).
+__device__ __forceinline__ void launch_from_zamo(double a, double r, double theta, double phi, const double v[3],
+                                                 double mu, Cons& c, St& s) {
+    const MetricAt m = metric_at(a, r, theta);
+    double sn, cs;
+    sincos(theta, &sn, &cs);
+    double gamma = 1.0;
+    if (mu > 0.0) {
+        const double v2 = dmind(v[0] * v[0] + v[1] * v[1] + v[2] * v[2], 1.0 - 1e-12);
+        gamma = 1.0 / sqrt(1.0 - v2);
+    }
+    c.mu = mu;
+    c.L = gamma * v[2] * sqrt(m.A / m.sigma) * sn;
+    c.E = gamma * sqrt(m.sigma * m.delta / m.A) + m.omega * c.L;
+    s.t = 0.0; s.r = r; s.theta = theta; s.phi = phi;
+    s.vr = gamma * v[0] * sqrt(m.sigma * m.delta);
+    s.vtheta = gamma * v[1] * sqrt(m.sigma);
+    if (mu == 0.0) {
+        const double inv = 1.0 / c.E;
+        c.E = 1.0;
+        c.L *= inv;
+        s.vr *= inv;
+        s.vtheta *= inv;
+    }
+    c.Q = s.vtheta * s.vtheta + cs * cs * (a * a * (mu * mu - c.E * c.E) + c.L * c.L / dmaxd(sn * sn, 1e-18));
+    if (mu == 0.0 && fabs(c.L) < 3e-4 * sqrt(dmaxd(c.Q + a * a, 0.0))) {
+        c.L = 0.0;
+        c.Q = s.vtheta * s.vtheta - cs * cs * a * a;
+    }
+}
+
+// (src/kerr.cpp:651-658)
+template <typename T>
+__device__ __forceinline__ void cartesian_velocity(T a, T r, T theta, T phi, T dr, T dtheta, T dphi, T out[3]) {
+    T sn, cs, sp, cp;
+    Math<T>::sc(theta, &sn, &cs);
+    Math<T>::sc(phi, &sp, &cp);
+    const T re = dr * sn + r * cs * dtheta - a * sn * dphi;
+    const T im = a * cs * dtheta + r * sn * dphi;
+    out[0] = re * cp - im * sp;
+    out[1] = re * sp + im * cp;
+    out[2] = dr * cs - r * sn * dtheta;
+}
+
+// Thin disk of prograde circular orbits: g at crossing radius rc (src/trajectory.cpp:311-318).
+__device__ __forceinline__ bool disk_redshift(double a, double E, double L, double rc, double* g) {
+    const double w = circular_omega(a, rc, true);
+    const double gtt = -(1.0 - 2.0 / rc), gtp = -2.0 * a / rc, gpp = rc * rc + a * a + 2.0 * a * a / rc;
+    const double norm = -(gtt + 2.0 * gtp * w + gpp * w * w);
+    if (!(norm > 0.0)) return false;
+    *g = sqrt(norm) / (E - L * w);
+    return true;
+}
+
+// True when R(r') > 0 on [r_+(1 + eps), r]: a photon falling there (backward in time) cannot turn
+// back and reaches r_+(1 + eps). R = E^2 r^4 + c2 r^2 + c1 r + c0 is expanded about the capture
+// radius and its cubic part bounded from below on the interval.
+__device__ __forceinline__ bool no_radial_root_below(double a, double E, double L, double Q, double r, double eps) {
+    const double x0 = horizon_radius(a) * (1.0 + eps);
+    const double w = r - x0;
+    if (w <= 0.0) return true;
+    const double xx = L - a * E, K = xx * xx + Q;
+    const double c4 = E * E, c2 = -(2.0 * a * E * xx + K), c1 = 2.0 * K, c0 = -a * a * Q;
+    const double R0 = ((c4 * x0 * x0 + c2) * x0 + c1) * x0 + c0;
+    const double R1 = (4.0 * c4 * x0 * x0 + 2.0 * c2) * x0 + c1;
+    const double R2 = 6.0 * c4 * x0 * x0 + c2;
+    const double R3 = 4.0 * c4 * x0;
+    const double lower = R0 - w * dmaxd(0.0, -R1) - w * w * dmaxd(0.0, -R2) - w * w * w * dmaxd(0.0, -R3);
+    return lower > 0.0;
+}
+
+// ------------------------------------------------------------- Dormand-Prince 5(4) tableau ----
+// Dormand & Prince (1980); continuous extension of Shampine (1986) as in Hairer-Norsett-Wanner.
+
+struct DP {
+    static constexpr double a21 = 1.0 / 5.0;
+    static constexpr double a31 = 3.0 / 40.0, a32 = 9.0 / 40.0;
+    static constexpr double a41 = 44.0 / 45.0, a42 = -56.0 / 15.0, a43 = 32.0 / 9.0;
+    static constexpr double a51 = 19372.0 / 6561.0, a52 = -25360.0 / 2187.0, a53 = 64448.0 / 6561.0,
+                            a54 = -212.0 / 729.0;
+    static constexpr double a61 = 9017.0 / 3168.0, a62 = -355.0 / 33.0, a63 = 46732.0 / 5247.0, a64 = 49.0 / 176.0,
+                            a65 = -5103.0 / 18656.0;
+    static constexpr double b1 = 35.0 / 384.0, b3 = 500.0 / 1113.0, b4 = 125.0 / 192.0, b5 = -2187.0 / 6784.0,
+                            b6 = 11.0 / 84.0;
+    static constexpr double e1 = 71.0 / 57600.0, e3 = -71.0 / 16695.0, e4 = 71.0 / 1920.0,
+                            e5 = -17253.0 / 339200.0, e6 = 22.0 / 525.0, e7 = -1.0 / 40.0;
+    static constexpr double d1 = -12715105075.0 / 11282082432.0, d3 = 87487479700.0 / 32700410799.0,
+                            d4 = -10690763975.0 / 1880347072.0, d5 = 701980252875.0 / 199316789632.0,
+                            d6 = -1453857185.0 / 822651844.0, d7 = 69997945.0 / 29380423.0;
+};
+
+// Per-ray constants of the photon right-hand side, hoisted out of the step (mu = 0).
+template <typename T>
+struct RayC {
+    T a, a2, E, aE, aL, L, K, twoE, L2, nA2E2;
+    __device__ __forceinline__ void set(double a_, double E_, double L_, double Q_) {
+        const double x = L_ - a_ * E_;
+        a = T(a_); a2 = T(a_ * a_); E = T(E_); aE = T(a_ * E_); aL = T(a_ * L_); L = T(L_);
+        K = T(x * x + Q_); twoE = T(2.0 * E_); L2 = T(L_ * L_); nA2E2 = T(-(a_ * a_) * E_ * E_);
+    }
+};
+
+// Right-hand side of the 5-component Mino system y = (r, theta, phi, vr, vtheta), photon (mu = 0):
+// kerr::derivatives restated (src/kerr.cpp:331-351) without dt.
+template <typename T>
+__device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5]) {
+    const T r = y[0];
+    T sn, cs;
+    Math<T>::sc(y[1], &sn, &cs);
+    const T delta = r * r - T(2) * r + c.a2;
+    const T rra = r * r + c.a2;
+    const T P = c.E * rra - c.aL;
+    const bool opposite = P * y[3] < T(0);
+    const T dcl = fabs(delta) > T(1e-12) ? delta : copysign(T(1e-12), delta);
+    const T num = opposite ? c.K : P + y[3];
+    const T den = opposite ? P - y[3] : dcl;
+    const T inflow = Math<T>::div(num, den);
+    const T m = fmax(fabs(sn), T(1e-9));
+    k[0] = y[3];
+    k[1] = y[4];
+    k[3] = c.twoE * r * P - (r - T(1)) * c.K;
+    if constexpr (sizeof(T) == 4) {
+        const T inv = rcp_approx(m);
+        const T inv2 = inv * inv;
+        const T ssc_inv = copysignf(inv2 * inv, sn);
+        k[4] = sn * cs * c.nA2E2 + c.L2 * cs * ssc_inv;
+        k[2] = c.a * inflow - c.aE + c.L * inv2;
+    } else {
+        const T ssc = (sn < T(0) ? -m : m) * m * m;
+        const T sn2 = fmax(sn * sn, T(1e-18));
+        k[4] = sn * cs * c.nA2E2 + c.L2 * cs / ssc;
+        k[2] = c.a * inflow - c.aE + c.L / sn2;
+    }
+}
+
+// Dense output of one component at fraction sg of a step (continuous extension above).
+template <typename T>
+__device__ __forceinline__ T dense(T y0, T y1, const T k[7][5], T h, int i, T sg) {
+    const T yd = y1 - y0;
+    const T b = h * k[0][i] - yd;
+    const T c4 = yd - h * k[6][i] - b;
+    const T c5 = h * (T(DP::d1) * k[0][i] + T(DP::d3) * k[2][i] + T(DP::d4) * k[3][i] + T(DP::d5) * k[4][i] +
+                      T(DP::d6) * k[5][i] + T(DP::d7) * k[6][i]);
+    const T s1 = T(1) - sg;
+    return y0 + sg * (yd + s1 * (b + sg * (c4 + s1 * c5)));
+}
+
+}  // namespace bhk

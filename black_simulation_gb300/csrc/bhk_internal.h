@@ -1,0 +1,107 @@
+// bhk_internal.h -- device-memory layouts and kernel launchers shared by the tracer and the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bhk.h"
+
+namespace bhk {
+
+// Per-camera geometry the tracer needs for every ray of that camera (FP64, computed on device).
+struct RayGeom {
+    double a, r0, th0, ph0;       // camera position = launch point
+    double rp, r_cap, r_esc;      // horizon, capture and escape radii
+    double r_in, r_out, zone_top; // disk, and r_+ + width of the analytic capture zone
+};
+
+// Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset.
+struct FrameDev {
+    bhk_frame_desc d;
+    int64_t offset;               // first global ray index of this frame
+    double e[4][4];               // ZAMO frame at the camera
+};
+
+// Launch record of one ray, structure of arrays, written by the FP64 launch kernel.
+struct LaunchSoA {
+    double *E, *L, *Q, *vr, *vth, *h0;
+    int32_t* geom_id;             // index into the RayGeom table
+    uint16_t* key;                // cost bucket for the pre-sort
+};
+
+// Small control block reset at the start of every batch.
+struct Control {
+    unsigned long long queue;     // next position in the ray queue
+    unsigned long long stats[4];  // accepted steps, rejected steps, unfinished rays, rescued rays
+    long long n_rays;             // total rays of the batch (device-resident: graph friendly)
+    unsigned int rescue_count;
+    unsigned int pad;
+};
+
+constexpr int kMaxBuckets = 1024;
+
+struct SortScratch {
+    unsigned int* hist;           // kMaxBuckets counters
+    unsigned int* offs;           // kMaxBuckets running offsets
+    int32_t* order;               // queue position -> ray index
+};
+
+// A ray the FP32 tracer hands to FP64 (capture zone inconclusive, or non-finite state).
+struct Rescue {
+    double y[5];
+    double h;
+    int64_t ray;
+    int32_t accepted, rejected;
+    int32_t from_launch, pad;
+};
+
+struct TraceParams {
+    double rtol, eps, r_escape;
+    int32_t max_steps, reproject_every, chunk, buckets;
+    double tol0;                  // photonStepSize tolerance of the first step
+};
+
+struct Outputs {
+    uint8_t* outcome;
+    double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
+    int32_t* steps;
+};
+
+// ---- launchers (bhk_trace.cu) ----
+void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p,
+                        Control* ctl, cudaStream_t s);
+void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
+                        const Control* ctl, int grid, cudaStream_t s);
+void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
+                          const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
+                          const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
+void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
+void launch_trace(bool fp64, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out, Rescue* rescue,
+                  unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid, cudaStream_t s);
+void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
+                   const TraceParams& p, Control* ctl, cudaStream_t s);
+int trace_blocks_per_sm(bool fp64, int block);
+void launch_critical_curve(double a, double r_obs, double theta_obs, int samples, double* alpha, double* beta,
+                           int* valid, cudaStream_t s);
+
+// ---- per-step mirrors (bhk_steps.cu) ----
+cudaError_t steps_derivatives(double a, const bhk_constants* c, const bhk_state* s, bhk_derivatives_t* d, int64_t n,
+                              cudaStream_t st);
+cudaError_t steps_step_mino(double a, const bhk_constants* c, bhk_state* s, const double* h, int64_t n,
+                            cudaStream_t st);
+cudaError_t steps_photon_step_size(double a, const bhk_constants* c, const bhk_state* s, double tol, double* h,
+                                   int64_t n, cudaStream_t st);
+cudaError_t steps_enforce_constraints(double a, const bhk_constants* c, bhk_state* s, int64_t n, cudaStream_t st);
+cudaError_t steps_normalize_angles(bhk_state* s, int64_t n, cudaStream_t st);
+cudaError_t steps_potentials(double a, const bhk_constants* c, const bhk_state* s, double* R, double* Th, int64_t n,
+                             cudaStream_t st);
+cudaError_t steps_observer_frame(double a, const double* r, const double* th, const double* u, bhk_frame* f, int64_t n,
+                                 cudaStream_t st);
+cudaError_t steps_photon_from_frame(double a, double r, double th, double ph, const bhk_frame* f, const double* look,
+                                    bhk_constants* c, bhk_state* s, int64_t n, cudaStream_t st);
+cudaError_t steps_launch_from_zamo(double a, double r, double th, double ph, const double* v, double mu,
+                                   bhk_constants* c, bhk_state* s, int64_t n, cudaStream_t st);
+cudaError_t steps_cartesian_velocity(double a, const bhk_constants* c, const bhk_state* s, double* out, int64_t n,
+                                     cudaStream_t st);
+
+}  // namespace bhk

@@ -1,0 +1,600 @@
+// bhk_trace.cu -- the batch tracer for sm_103a.
+//
+// Pipeline of one batch (all on one stream, capturable as one CUDA graph):
+//   frame_setup   1 block, FP64: per-frame ZAMO tetrad (kerr::observerFrame), horizon, ISCO, radii
+//   launch        FP64, one thread per ray: pinhole (alpha, beta) -> look -> kerr::photonFromFrame
+//                 -> E, L, Q, vr, vtheta and the first step (kerr::photonStepSize); cost bucket
+//   sort          bucket histogram / scan / scatter: queue order, most expensive bucket first
+//   trace         persistent grid; every lane owns one ray and pulls a new one from the warp's chunk
+//                 of the device queue as soon as its ray ends (step counts vary ~100x near the
+//                 photon ring, so lanes never wait for a warp's slowest ray). Integration is
+//                 Dormand-Prince 5(4) with FSAL and dense-output event location, in FP64 (parity
+//                 mode) or FP32 (mixed mode: FP64 for launch constants, disk g, the analytic capture
+//                 test at the horizon and the periodic null-constraint re-projection)
+//   rescue        FP64 continuation of the rare rays the FP32 kernel hands over
+//
+// The reference's ray semantics (src/trajectory.cpp:259-392): backward march in Mino time; disk
+// where theta crosses pi/2 with r in [r_in, r_out] and g from prograde circular gas; captured when
+// falling below r_+(1 + eps); escaped when rising past max(r_escape, 1.5 r_obs).
+#include "bhk_device.cuh"
+#include "bhk_internal.h"
+
+namespace bhk {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ULL); }
+
+__device__ __forceinline__ double wrap_2pi(double x) {
+    const double t = 2.0 * kPi;
+    double y = x - t * floor(x / t);
+    if (y >= t) y -= t;
+    return y;
+}
+
+__device__ __forceinline__ RayGeom make_geom(double a, double r, double th, double ph, double r_in_opt, double r_out,
+                                             const TraceParams& p) {
+    RayGeom g;
+    g.a = a; g.r0 = r; g.th0 = th; g.ph0 = ph;
+    g.rp = horizon_radius(a);
+    g.r_cap = g.rp * (1.0 + p.eps);
+    g.r_esc = fmax(p.r_escape, 1.5 * r);
+    g.r_in = r_in_opt > 0.0 ? r_in_opt : isco_radius(a, true);
+    g.r_out = r_out;
+    g.zone_top = g.rp + dmind(0.05, 0.5 * (g.r_in - g.rp));
+    return g;
+}
+
+// Cost bucket: photons whose b^2 + q sits near the critical value 27 wind near the photon orbit
+// and take the most steps; bucket 0 holds them, so the queue serves the longest rays first.
+__device__ __forceinline__ uint16_t cost_key(double E, double L, double Q, int buckets) {
+    if (buckets <= 1) return 0;
+    const double u = (L * L + Q) / (E * E);
+    const double d = fabs(log(fmax(u, 1e-30) / 27.0));
+    const int k = static_cast<int>(d * buckets / 3.0);
+    return static_cast<uint16_t>(k < 0 ? 0 : (k >= buckets ? buckets - 1 : k));
+}
+
+__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, const Cons& c, const St& s, double h0,
+                                             int32_t gid, int buckets) {
+    L.E[i] = c.E; L.L[i] = c.L; L.Q[i] = c.Q;
+    L.vr[i] = s.vr; L.vth[i] = s.vtheta; L.h0[i] = h0;
+    L.geom_id[i] = gid;
+    L.key[i] = cost_key(c.E, c.L, c.Q, buckets);
+}
+
+// ------------------------------------------------------------------------- set-up kernels ----
+
+__global__ void frame_setup_kernel(FrameDev* frames, RayGeom* geom, int nframes, TraceParams p, Control* ctl) {
+    if (threadIdx.x == 0) {
+        long long off = 0;
+        for (int f = 0; f < nframes; ++f) {
+            frames[f].offset = off;
+            off += static_cast<long long>(frames[f].d.width) * frames[f].d.height;
+        }
+        ctl->n_rays = off;
+    }
+    for (int f = threadIdx.x; f < nframes; f += blockDim.x) {
+        const bhk_frame_desc d = frames[f].d;
+        double u[4], e[4][4];
+        zamo_four_velocity(d.a, d.r_obs, d.theta_obs, u);
+        observer_frame(d.a, d.r_obs, d.theta_obs, u, e);
+        for (int k = 0; k < 4; ++k)
+            for (int i = 0; i < 4; ++i) frames[f].e[k][i] = e[k][i];
+        geom[f] = make_geom(d.a, d.r_obs, d.theta_obs, d.phi_obs, d.r_disk_in, d.r_disk_out, p);
+    }
+}
+
+__global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nframes, LaunchSoA L, TraceParams p,
+                                     const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = nframes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
+        }
+        const FrameDev& f = frames[lo];
+        const long long local = i - f.offset;
+        const int row = static_cast<int>(local / f.d.width), col = static_cast<int>(local % f.d.width);
+        const double px = (f.d.alpha_hi - f.d.alpha_lo) / f.d.width;
+        const double py = (f.d.beta_hi - f.d.beta_lo) / f.d.height;
+        const double alpha = f.d.alpha_lo + (col + 0.5) * px;
+        const double beta = f.d.beta_hi - (row + 0.5) * py;
+        const double lr = -1.0, lt = -beta / f.d.r_obs, lp = alpha / f.d.r_obs;
+        const double nn = sqrt(lr * lr + lt * lt + lp * lp);
+        const double look[3] = {lr / nn, lt / nn, lp / nn};
+        double e[4][4];
+        for (int k = 0; k < 4; ++k)
+            for (int j = 0; j < 4; ++j) e[k][j] = f.e[k][j];
+        Cons c;
+        St s;
+        photon_from_frame(f.d.a, f.d.r_obs, f.d.theta_obs, f.d.phi_obs, e, look, c, s);
+        const double h0 = photon_step_size(f.d.a, c, s, p.tol0);
+        store_launch(L, i, c, s, h0, lo, p.buckets);
+    }
+}
+
+__global__ void launch_explicit_kernel(const double* __restrict__ a, const double* __restrict__ r_obs,
+                                       const double* __restrict__ th_obs, const double* __restrict__ alpha,
+                                       const double* __restrict__ beta, double r_in, double r_out, RayGeom* geom,
+                                       LaunchSoA L, TraceParams p, const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double ai = a[i], ri = r_obs[i], ti = th_obs[i];
+        double u[4], e[4][4];
+        zamo_four_velocity(ai, ri, ti, u);
+        observer_frame(ai, ri, ti, u, e);
+        const double lr = -1.0, lt = -beta[i] / ri, lp = alpha[i] / ri;
+        const double nn = sqrt(lr * lr + lt * lt + lp * lp);
+        const double look[3] = {lr / nn, lt / nn, lp / nn};
+        Cons c;
+        St s;
+        photon_from_frame(ai, ri, ti, 0.0, e, look, c, s);
+        const double h0 = photon_step_size(ai, c, s, p.tol0);
+        geom[i] = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
+        store_launch(L, i, c, s, h0, static_cast<int32_t>(i), p.buckets);
+    }
+}
+
+// ----------------------------------------------------------------------------- pre-sort ----
+
+__global__ void hist_kernel(LaunchSoA L, SortScratch S, TraceParams p, const Control* __restrict__ ctl) {
+    __shared__ unsigned int h[kMaxBuckets];
+    for (int b = threadIdx.x; b < p.buckets; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        atomicAdd(&h[L.key[i]], 1u);
+    __syncthreads();
+    for (int b = threadIdx.x; b < p.buckets; b += blockDim.x)
+        if (h[b]) atomicAdd(&S.hist[b], h[b]);
+}
+
+__global__ void scan_kernel(SortScratch S, TraceParams p) {
+    if (threadIdx.x == 0) {
+        unsigned int run = 0;
+        for (int b = 0; b < p.buckets; ++b) {
+            S.offs[b] = run;
+            run += S.hist[b];
+        }
+    }
+}
+
+__global__ void scatter_kernel(LaunchSoA L, SortScratch S, const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const unsigned pos = atomicAdd(&S.offs[L.key[i]], 1u);
+        S.order[pos] = static_cast<int32_t>(i);
+    }
+}
+
+// --------------------------------------------------------------------------- the tracer ----
+
+enum : int { kContinue = 0, kFinished = 1, kRescue = 2, kRestart = 3 };
+
+template <typename T>
+struct Lane {
+    RayC<T> c;
+    double a, E, L, Q;
+    T y[5];
+    T k[7][5];
+    T h;
+    T r_cap, r_esc, r_in, r_out, zone_top;
+    int acc, rej;
+    bool last_rej;
+};
+
+template <typename T>
+__device__ __forceinline__ void lane_begin(Lane<T>& s, const RayGeom& g, double E, double L, double Q,
+                                           const double y[5], double h) {
+    s.a = g.a; s.E = E; s.L = L; s.Q = Q;
+    s.c.set(g.a, E, L, Q);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) s.y[i] = T(y[i]);
+    rhs(s.c, s.y, s.k[0]);
+    s.h = T(h);
+    s.r_cap = T(g.r_cap); s.r_esc = T(g.r_esc); s.r_in = T(g.r_in); s.r_out = T(g.r_out);
+    s.zone_top = T(g.zone_top);
+    s.acc = 0; s.rej = 0; s.last_rej = false;
+}
+
+__device__ __forceinline__ void write_out(const Outputs& o, long long ray, int outcome, double rd, double pd, double g,
+                                          double ti, double pi, int steps) {
+    if (o.outcome) o.outcome[ray] = static_cast<uint8_t>(outcome);
+    if (o.r_disk) o.r_disk[ray] = rd;
+    if (o.phi_disk) o.phi_disk[ray] = pd;
+    if (o.g) o.g[ray] = g;
+    if (o.theta_inf) o.theta_inf[ray] = ti;
+    if (o.phi_inf) o.phi_inf[ray] = pi;
+    if (o.steps) o.steps[ray] = steps;
+}
+
+// Fraction of the step where the dense output of component i equals target (bisection).
+template <typename T>
+__device__ __forceinline__ T locate(const T* y0, const T* y1, const T k[7][5], T h, int i, T target) {
+    constexpr int iters = sizeof(T) == 8 ? 60 : 30;
+    T lo = T(0), hi = T(1);
+    const bool neg0 = (y0[i] - target) < T(0);
+    for (int it = 0; it < iters; ++it) {
+        const T mid = T(0.5) * (lo + hi);
+        const T fm = dense(y0[i], y1[i], k, h, i, mid) - target;
+        if ((fm < T(0)) == neg0) lo = mid; else hi = mid;
+    }
+    return T(0.5) * (lo + hi);
+}
+
+// One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
+// kRescue (FP32 only: hand the state to FP64) or kRestart (FP32 only: non-finite state).
+template <typename T>
+__device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long long ray, const Outputs& out,
+                                       bool reproject, Control* ctl) {
+    constexpr bool F64 = sizeof(T) == 8;
+    const T h = s.h;
+    T t[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a21) * s.k[0][i]);
+    rhs(s.c, t, s.k[1]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a31) * s.k[0][i] + T(DP::a32) * s.k[1][i]);
+    rhs(s.c, t, s.k[2]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        t[i] = s.y[i] + h * (T(DP::a41) * s.k[0][i] + T(DP::a42) * s.k[1][i] + T(DP::a43) * s.k[2][i]);
+    rhs(s.c, t, s.k[3]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        t[i] = s.y[i] + h * (T(DP::a51) * s.k[0][i] + T(DP::a52) * s.k[1][i] + T(DP::a53) * s.k[2][i] +
+                             T(DP::a54) * s.k[3][i]);
+    rhs(s.c, t, s.k[4]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        t[i] = s.y[i] + h * (T(DP::a61) * s.k[0][i] + T(DP::a62) * s.k[1][i] + T(DP::a63) * s.k[2][i] +
+                             T(DP::a64) * s.k[3][i] + T(DP::a65) * s.k[4][i]);
+    rhs(s.c, t, s.k[5]);
+    T y5[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
+                              T(DP::b5) * s.k[4][i] + T(DP::b6) * s.k[5][i]);
+    rhs(s.c, y5, s.k[6]);
+    const T rtol = T(p.rtol);
+    T acc = T(0);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const T e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] +
+                         T(DP::e5) * s.k[4][i] + T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
+        const T sc = rtol + rtol * fmax(fabs(s.y[i]), fabs(y5[i]));
+        const T q = Math<T>::div(e, sc);
+        acc += q * q;
+    }
+    // err = sqrt(acc / 5); the FP32 path works with err^2.
+    T err, e2;
+    bool ok;
+    if constexpr (F64) {
+        err = sqrt(acc / T(5));
+        e2 = err;
+        ok = err <= T(1);
+    } else {
+        e2 = acc * T(0.2);
+        err = e2;
+        ok = e2 <= T(1);
+    }
+    if (!ok) {
+        ++s.rej;
+        s.last_rej = true;
+        T fac;
+        if constexpr (F64) fac = isfinite(err) ? fmax(0.2, 0.9 * pow(err, -0.2)) : 0.2;
+        else fac = isfinite(e2) ? fmaxf(0.2f, 0.9f * exp2f(-0.1f * __log2f(e2))) : 0.2f;
+        s.h = h * fac;
+        if (s.rej >= p.max_steps) {
+            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            atomicAdd(&ctl->stats[2], 1ull);
+            return kFinished;
+        }
+        return kContinue;
+    }
+    ++s.acc;
+    T prev[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        prev[i] = s.y[i];
+        s.y[i] = y5[i];
+    }
+    if (!isfinite(s.y[0])) {
+        if constexpr (F64) {
+            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            atomicAdd(&ctl->stats[2], 1ull);
+            return kFinished;
+        } else {
+            return kRestart;
+        }
+    }
+    const T hp = T(0.5 * kPi);
+    // Thin disk: theta crosses pi/2 inside [r_in, r_out].
+    if ((prev[1] - hp) * (s.y[1] - hp) < T(0)) {
+        const T sg = locate(prev, s.y, s.k, h, 1, hp);
+        const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
+        double g;
+        if (rc >= s.r_in && rc <= s.r_out && disk_redshift(s.a, s.E, s.L, double(rc), &g)) {
+            const double ph = wrap_2pi(double(dense(prev[2], s.y[2], s.k, h, 2, sg)));
+            write_out(out, ray, BHK_RAY_DISK, double(rc), ph, g, nan_d(), nan_d(), s.acc);
+            return kFinished;
+        }
+    }
+    const bool falling = s.y[0] < prev[0];
+    if (falling) {
+        if (s.y[0] < s.r_cap) {
+            write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            return kFinished;
+        }
+        if (s.y[0] < s.zone_top) {
+            if (no_radial_root_below(s.a, s.E, s.L, s.Q, double(s.y[0]), p.eps)) {
+                write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+                return kFinished;
+            }
+            if constexpr (!F64) return kRescue;
+        }
+    } else if (s.y[0] > s.r_esc) {
+        const T sg = locate(prev, s.y, s.k, h, 0, s.r_esc);
+        T x[5], kk[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
+        rhs(s.c, x, kk);
+        T v[3];
+        cartesian_velocity<T>(T(s.a), x[0], x[1], x[2], x[3], x[4], kk[2], v);
+        const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
+        const double ti = double(acos(dz));
+        const double pi = double(atan2(-v[1] / nrm, -v[0] / nrm));
+        write_out(out, ray, BHK_RAY_ESCAPED, nan_d(), nan_d(), nan_d(), ti, pi, s.acc);
+        return kFinished;
+    }
+    // Pole reflection (kerr::normalizeAngles) and constraint re-projection, carrying the FSAL
+    // derivative: under theta -> -theta (or 2 pi - theta) Theta'(theta) changes sign.
+    if constexpr (F64) {
+        St st{0.0, s.y[0], s.y[1], s.y[2], s.y[3], s.y[4]};
+        if (normalize_angles(st)) s.k[6][4] = -s.k[6][4];
+        const Cons cc{s.E, s.L, s.Q, 0.0};
+        enforce_constraints(s.a, cc, st);
+        s.y[1] = st.theta; s.y[2] = st.phi; s.y[3] = st.vr; s.y[4] = st.vtheta;
+    } else {
+        const T pi_f = T(kPi);
+        if (s.y[1] < T(0) || s.y[1] > pi_f) {
+            s.y[1] = s.y[1] < T(0) ? -s.y[1] : T(2 * kPi) - s.y[1];
+            s.y[2] += pi_f;
+            s.y[4] = -s.y[4];
+            s.k[6][4] = -s.k[6][4];
+        }
+        if (reproject) {
+            St st{0.0, double(s.y[0]), double(s.y[1]), double(s.y[2]), double(s.y[3]), double(s.y[4])};
+            const Cons cc{s.E, s.L, s.Q, 0.0};
+            enforce_constraints(s.a, cc, st);
+            s.y[3] = T(st.vr);
+            s.y[4] = T(st.vtheta);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) s.k[0][i] = s.k[6][i];
+    s.k[0][0] = s.y[3];
+    s.k[0][1] = s.y[4];
+    T fac;
+    if constexpr (F64) fac = err > 0.0 ? 0.9 * pow(err, -0.2) : 5.0;
+    else fac = e2 > 0.0f ? 0.9f * exp2f(-0.1f * __log2f(e2)) : 5.0f;
+    fac = fmin(fmax(fac, T(0.2)), s.last_rej ? T(1) : T(5));
+    s.h = h * fac;
+    s.last_rej = false;
+    if (s.acc >= p.max_steps) {
+        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+        atomicAdd(&ctl->stats[2], 1ull);
+        return kFinished;
+    }
+    return kContinue;
+}
+
+__device__ __forceinline__ void push_rescue(Rescue* rescue, unsigned cap, Control* ctl, long long ray, const double y[5],
+                                            double h, int acc, int rej, int from_launch, const Outputs& out) {
+    const unsigned idx = atomicAdd(&ctl->rescue_count, 1u);
+    atomicAdd(&ctl->stats[3], 1ull);
+    if (idx < cap) {
+        Rescue r;
+        for (int i = 0; i < 5; ++i) r.y[i] = y[i];
+        r.h = h; r.ray = ray; r.accepted = acc; r.rejected = rej; r.from_launch = from_launch; r.pad = 0;
+        rescue[idx] = r;
+    } else {
+        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), acc);
+        atomicAdd(&ctl->stats[2], 1ull);
+    }
+}
+
+template <typename T>
+__global__ void trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __restrict__ order,
+                             Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl) {
+    const int lane = threadIdx.x & 31;
+    const long long n = ctl->n_rays;
+    const unsigned lt = lanemask_lt();
+    Lane<T> s;
+    long long ray = -1;
+    bool exhausted = false;
+    long long pool_pos = 0, pool_end = 0;
+    unsigned long long n_acc = 0, n_rej = 0;
+    int iter = 0;
+    for (;;) {
+        unsigned need = __ballot_sync(kFull, ray < 0);
+        while (need && !exhausted) {
+            if (pool_pos >= pool_end) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(&ctl->queue, static_cast<unsigned long long>(p.chunk));
+                base = __shfl_sync(kFull, base, 0);
+                if (static_cast<long long>(base) >= n) {
+                    exhausted = true;
+                    break;
+                }
+                pool_pos = static_cast<long long>(base);
+                pool_end = pool_pos + p.chunk < n ? pool_pos + p.chunk : n;
+            }
+            const int avail = static_cast<int>(pool_end - pool_pos);
+            const int rank = __popc(need & lt);
+            if (((need >> lane) & 1u) && rank < avail) {
+                const long long q = pool_pos + rank;
+                ray = order ? order[q] : q;
+                const RayGeom& g = geom[L.geom_id[ray]];
+                const double y0[5] = {g.r0, g.th0, g.ph0, L.vr[ray], L.vth[ray]};
+                lane_begin(s, g, L.E[ray], L.L[ray], L.Q[ray], y0, L.h0[ray]);
+            }
+            const int served = __popc(need) < avail ? __popc(need) : avail;
+            pool_pos += served;
+            need = __ballot_sync(kFull, ray < 0);
+        }
+        if (!__any_sync(kFull, ray >= 0)) break;
+        ++iter;
+        const bool reproject = p.reproject_every > 0 && (iter % p.reproject_every) == 0;
+        if (ray >= 0) {
+            const int r = attempt<T>(s, p, ray, out, reproject, ctl);
+            if (r != kContinue) {
+                n_acc += s.acc;
+                n_rej += s.rej;
+                if (r == kRescue || r == kRestart) {
+                    double y[5];
+                    const bool restart = r == kRestart;
+                    if (restart) {
+                        const RayGeom& g = geom[L.geom_id[ray]];
+                        y[0] = g.r0; y[1] = g.th0; y[2] = g.ph0; y[3] = L.vr[ray]; y[4] = L.vth[ray];
+                    } else {
+                        for (int i = 0; i < 5; ++i) y[i] = double(s.y[i]);
+                    }
+                    push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? L.h0[ray] : double(s.h),
+                                restart ? 0 : s.acc, restart ? 0 : s.rej, restart ? 1 : 0, out);
+                }
+                ray = -1;
+            }
+        }
+    }
+    // Step statistics: one atomic per warp.
+    for (int o = 16; o > 0; o >>= 1) {
+        n_acc += __shfl_down_sync(kFull, n_acc, o);
+        n_rej += __shfl_down_sync(kFull, n_rej, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&ctl->stats[0], n_acc);
+        atomicAdd(&ctl->stats[1], n_rej);
+    }
+}
+
+// FP64 continuation of the rays the FP32 kernel handed over; one thread per record.
+__global__ void rescue_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, Outputs out, const Rescue* rescue,
+                              unsigned cap, TraceParams p, Control* ctl) {
+    const unsigned count = ctl->rescue_count < cap ? ctl->rescue_count : cap;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const Rescue r = rescue[i];
+        const RayGeom& g = geom[L.geom_id[r.ray]];
+        Lane<double> s;
+        double y[5] = {r.y[0], r.y[1], r.y[2], r.y[3], r.y[4]};
+        if (!r.from_launch) {
+            St st{0.0, y[0], y[1], y[2], y[3], y[4]};
+            normalize_angles(st);
+            const Cons cc{L.E[r.ray], L.L[r.ray], L.Q[r.ray], 0.0};
+            enforce_constraints(g.a, cc, st);
+            y[1] = st.theta; y[2] = st.phi; y[3] = st.vr; y[4] = st.vtheta;
+        }
+        lane_begin(s, g, L.E[r.ray], L.L[r.ray], L.Q[r.ray], y, r.h);
+        s.acc = r.accepted;
+        s.rej = r.rejected;
+        int res = kContinue;
+        while (res == kContinue) res = attempt<double>(s, p, r.ray, out, false, ctl);
+        atomicAdd(&ctl->stats[0], static_cast<unsigned long long>(s.acc - r.accepted));
+        atomicAdd(&ctl->stats[1], static_cast<unsigned long long>(s.rej - r.rejected));
+    }
+}
+
+// Analytic critical curve seen by a ZAMO pinhole (one thread per spherical-orbit sample).
+__global__ void critical_curve_kernel(double a, double r_obs, double th, int samples, double* alpha, double* beta,
+                                      int* valid) {
+    const int n = (samples > 16 ? samples : 16) * 8;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > n) return;
+    const double aa = fabs(a) < 1e-6 ? 1e-6 : a;
+    const double r1 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(-aa))), r2 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(aa)));
+    const double x = 0.5 - 0.5 * cos(kPi * k / n);
+    const double r = r1 + (r2 - r1) * x;
+    const double xi = (r * r * (3.0 - r) - aa * aa * (r + 1.0)) / (aa * (r - 1.0));
+    const double eta = r * r * r * (4.0 * aa * aa - r * (r - 3.0) * (r - 3.0)) / (aa * aa * (r - 1.0) * (r - 1.0));
+    const Cons c{1.0, xi, eta, 0.0};
+    const double R = radial_potential(aa, c, r_obs), Th = polar_potential(aa, c, th);
+    const MetricAt m = metric_at(aa, r_obs, th);
+    const double varpi = sqrt(m.A / m.sigma) * sin(th);
+    const double eloc = 1.0 - m.omega * xi;
+    const double nr = sqrt(R) / sqrt(m.sigma * m.delta) / eloc;
+    const double nth = sqrt(fmax(Th, 0.0)) / sqrt(m.sigma) / eloc;
+    const double nph = xi / varpi / eloc;
+    valid[k] = (R > 0.0 && Th >= 0.0) ? 1 : 0;
+    alpha[k] = r_obs * (-nph) / nr;
+    beta[k] = r_obs * nth / nr;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ launchers ----
+
+void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p,
+                        Control* ctl, cudaStream_t s) {
+    (void)in;
+    frame_setup_kernel<<<1, 128, 0, s>>>(frames, geom, nframes, p, ctl);
+}
+
+void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
+                        const Control* ctl, int grid, cudaStream_t s) {
+    (void)geom;
+    launch_frames_kernel<<<grid, 128, 0, s>>>(frames, nframes, L, p, ctl);
+}
+
+void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
+                          const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
+                          const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
+    (void)r_escape;
+    launch_explicit_kernel<<<grid, 128, 0, s>>>(a, r_obs, th_obs, alpha, beta, r_in, r_out, geom, L, p, ctl);
+}
+
+void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
+    hist_kernel<<<grid, 256, 0, s>>>(L, S, p, ctl);
+    scan_kernel<<<1, 32, 0, s>>>(S, p);
+    scatter_kernel<<<grid, 256, 0, s>>>(L, S, ctl);
+}
+
+void launch_trace(bool fp64, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out, Rescue* rescue,
+                  unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid, cudaStream_t s) {
+    if (fp64) trace_kernel<double><<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
+    else trace_kernel<float><<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
+}
+
+void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
+                   const TraceParams& p, Control* ctl, cudaStream_t s) {
+    rescue_kernel<<<152, 64, 0, s>>>(L, geom, out, rescue, rescue_cap, p, ctl);
+}
+
+int trace_blocks_per_sm(bool fp64, int block) {
+    int n = 0;
+    if (fp64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel<double>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel<float>, block, 0);
+    return n;
+}
+
+void launch_critical_curve(double a, double r_obs, double theta_obs, int samples, double* alpha, double* beta,
+                           int* valid, cudaStream_t s) {
+    const int n = (samples > 16 ? samples : 16) * 8 + 1;
+    critical_curve_kernel<<<(n + 127) / 128, 128, 0, s>>>(a, r_obs, theta_obs, samples, alpha, beta, valid);
+}
+
+}  // namespace bhk

@@ -1,0 +1,179 @@
+/*
+ * bhk.h -- C ABI of libbhk, the GB300 (sm_103a) Kerr null-geodesic batch tracer.
+ *
+ * Drop-in for the photon path of Black_simulation: the kerr:: geodesic primitives
+ * (src/kerr.h:101-185) and the ray-level drivers built on them, trajectory::traceRay
+ * (src/trajectory.h:118-119) and eht::render / eht::traceRay (src/eht.h:130-140).
+ *
+ * Conventions
+ *  - Units G = c = M = 1; ingoing Kerr-Schild (t, r, theta, phi); Mino time.
+ *  - Every function returns a bhk_status. Nothing computes on the CPU: the per-step mirrors run
+ *    the same FP64 device code as the tracer, batched over n items of device memory.
+ *  - Pointers documented "device" must be device (or managed) memory; "host" must be host memory.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the context's own stream). Calls are
+ *    asynchronous on that stream unless documented otherwise.
+ *  - A bhk_context is thread-safe: concurrent calls on one context are serialised by its lock.
+ *    Separate contexts are independent.
+ *  - No CPU fallback: without a CUDA device every call returns BHK_ECUDA.
+ */
+#ifndef BHK_H
+#define BHK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BHK_OK = 0,
+    BHK_EINVAL = 1,       /* bad argument (null pointer, size, range) */
+    BHK_ECUDA = 2,        /* CUDA error; bhk_last_error() has the text */
+    BHK_EUNFINISHED = 3,  /* traced, but some rays hit the step cap (outcome BHK_RAY_UNFINISHED) */
+    BHK_ENOMEM = 4        /* device allocation failed */
+} bhk_status;
+
+/* Ray outcomes (trajectory::RayEnd, src/trajectory.h:85, restricted to a bare hole + thin disk). */
+enum { BHK_RAY_UNFINISHED = 0, BHK_RAY_CAPTURED = 1, BHK_RAY_DISK = 2, BHK_RAY_ESCAPED = 3 };
+
+/* Layout-identical to kerr::Constants, kerr::State, kerr::Derivatives, kerr::Frame
+ * (src/kerr.h:81-99, 143-145). */
+typedef struct { double E, L, Q, mu; } bhk_constants;
+typedef struct { double t, r, theta, phi, vr, vtheta; } bhk_state;
+typedef struct { double dt, dr, dtheta, dphi, dvr, dvtheta; } bhk_derivatives_t;
+typedef struct { double e[4][4]; } bhk_frame; /* e[k][mu]: e[0] the 4-velocity, e[1..3] the r, theta, phi axes */
+
+/* ------------------------------------------------------------------ context ---------------- */
+
+typedef struct bhk_context bhk_context;
+
+bhk_status bhk_create(int device, bhk_context** out);
+bhk_status bhk_destroy(bhk_context* ctx);
+const char* bhk_last_error(void);          /* thread-local text of the last failure */
+const char* bhk_version(void);
+
+/* ------------------------------------------------- per-step mirrors (batched) ---------------- */
+/* Each applies the kerr:: function of the same name to n independent items, in FP64, on the GPU.
+ * Spin a is shared by the batch, as in the reference call shape. All arrays are device memory. */
+
+/* kerr::derivatives (src/kerr.h:101; src/kerr.cpp:331-351). */
+bhk_status bhk_derivatives(double a, const bhk_constants* c, const bhk_state* s, bhk_derivatives_t* d, int64_t n,
+                           void* stream);
+/* kerr::stepMino: one classical RK4 step of Mino-time size h[i] (src/kerr.h:165; src/kerr.cpp:502-519). */
+bhk_status bhk_step_mino(double a, const bhk_constants* c, bhk_state* s, const double* h, int64_t n, void* stream);
+/* kerr::photonStepSize (src/kerr.h:176; src/kerr.cpp:563-575). */
+bhk_status bhk_photon_step_size(double a, const bhk_constants* c, const bhk_state* s, double tolerance, double* h,
+                                int64_t n, void* stream);
+/* kerr::enforceConstraints (src/kerr.h:173; src/kerr.cpp:521-542). */
+bhk_status bhk_enforce_constraints(double a, const bhk_constants* c, bhk_state* s, int64_t n, void* stream);
+/* kerr::normalizeAngles (src/kerr.h:185; src/kerr.cpp:595-604). */
+bhk_status bhk_normalize_angles(bhk_state* s, int64_t n, void* stream);
+/* kerr::radialPotential / polarPotential (src/kerr.h:103-104; src/kerr.cpp:353-363). */
+bhk_status bhk_potentials(double a, const bhk_constants* c, const bhk_state* s, double* R, double* Theta, int64_t n,
+                          void* stream);
+/* kerr::observerFrame(a, r[i], theta[i], u[i]) (src/kerr.h:146; src/kerr.cpp:432-456). u: n x 4.
+ * u == NULL uses each point's ZAMO 4-velocity, kerr::zamoFourVelocity (src/kerr.cpp:424-430). */
+bhk_status bhk_observer_frame(double a, const double* r, const double* theta, const double* u, bhk_frame* f,
+                              int64_t n, void* stream);
+/* kerr::photonFromFrame for one camera and n look directions (look: n x 3, unit, on the frame's
+ * r, theta, phi axes), including the kAxisSnap rewrite (src/kerr.h:153-154; src/kerr.cpp:458-483).
+ * frame is a device pointer to one bhk_frame. */
+bhk_status bhk_photon_from_frame(double a, double r, double theta, double phi, const bhk_frame* frame,
+                                 const double* look, bhk_constants* c, bhk_state* s, int64_t n, void* stream);
+/* kerr::launchFromZamo for n directions v (n x 3) from one point (src/kerr.h:124-125; src/kerr.cpp:365-407). */
+bhk_status bhk_launch_from_zamo(double a, double r, double theta, double phi, const double* v, double mu,
+                                bhk_constants* c, bhk_state* s, int64_t n, void* stream);
+/* kerr::cartesianVelocity applied to each state with its own derivatives: out (n x 3) is the
+ * Cartesian direction of motion, unnormalised (src/kerr.cpp:651-658). */
+bhk_status bhk_cartesian_velocity(double a, const bhk_constants* c, const bhk_state* s, double* out, int64_t n,
+                                  void* stream);
+
+/* ------------------------------------------------------------- batch tracer ---------------- */
+
+/* One camera frame: a ZAMO pinhole at (r_obs, theta_obs, phi_obs) around a hole of spin a.
+ * Pixel (col, row), row-major from the top, looks along normalize(-1, -beta/r_obs, alpha/r_obs) on the
+ * ZAMO's (r, theta, phi) axes, with alpha = alpha_lo + (col + 1/2)(alpha_hi - alpha_lo)/width and
+ * beta = beta_hi - (row + 1/2)(beta_hi - beta_lo)/height (the image layout of eht::render,
+ * src/eht.cpp:332-336; the launch is kerr::photonFromFrame, src/kerr.cpp:458-483). As r_obs grows,
+ * (alpha, beta) become Bardeen's impact parameters (src/eht.cpp:263-264). */
+typedef struct {
+    double a, r_obs, theta_obs, phi_obs;
+    int32_t width, height;
+    double alpha_lo, alpha_hi, beta_lo, beta_hi;
+    double r_disk_in;   /* <= 0: the prograde ISCO, kerr::iscoRadius(a, true) */
+    double r_disk_out;
+} bhk_frame_desc;
+
+enum { BHK_PREC_FP64 = 0, BHK_PREC_MIXED = 1 };
+
+typedef struct {
+    int32_t precision;      /* BHK_PREC_FP64 (parity mode) or BHK_PREC_MIXED (FP32 integration) */
+    double rtol;            /* Dormand-Prince relative (= absolute) tolerance; 0 -> 1e-10 FP64, 1e-6 mixed */
+    int32_t max_steps;      /* accepted-step cap per ray; 0 -> 20000 */
+    double r_escape;        /* escaped once r > max(r_escape, 1.5 r_obs) while rising; 0 -> 1000 */
+    double capture_eps;     /* captured once r < r_+(1 + capture_eps) while falling; 0 -> 1e-6 */
+    int32_t reproject_every;/* mixed: FP64 re-projection onto the null constraint every N steps; 0 -> 16, <0 off */
+    int32_t block;          /* threads per block of the tracer; 0 -> autotuned or 128 */
+    int32_t chunk;          /* rays a warp takes from the queue at a time; 0 -> autotuned or 32 */
+    int32_t sort_buckets;   /* rays pre-sorted into this many cost buckets; 0 -> autotuned or 64; 1 = none */
+    int32_t use_graph;      /* 1: replay the whole batch as one captured CUDA graph */
+} bhk_trace_opts;
+
+/* Per-ray outputs, structure of arrays, n entries each (device memory unless stated). Any pointer
+ * may be NULL to skip that field. Undefined fields (r_disk of an escaped ray, ...) are NaN. */
+typedef struct {
+    uint8_t* outcome;    /* BHK_RAY_* */
+    double* r_disk;      /* disk-crossing radius (trajectory RayReport::rEnd for RayEnd::Disk) */
+    double* phi_disk;    /* Kerr-Schild azimuth of the crossing, wrapped to [0, 2 pi) */
+    double* g;           /* observed / emitted frequency, gas on prograde circular orbits (RayReport::g) */
+    double* theta_inf;   /* escape direction, backward tangent at r_escape: acos(d_z) */
+    double* phi_inf;     /*                                                 atan2(d_y, d_x) */
+    int32_t* steps;      /* accepted integration steps */
+} bhk_rays_out;
+
+/* Statistics of the last trace call on a context (filled at the end of that call's stream work). */
+typedef struct {
+    int64_t rays, accepted_steps, rejected_steps, rescued, unfinished;
+    int32_t block, chunk, sort_buckets, grid;
+    double kernel_ms;    /* tracer kernel time measured with CUDA events (when opts requested it) */
+} bhk_trace_stats;
+
+/* Traces every pixel of nframes frames (host descriptors) in one persistent launch. Ray i of frame f
+ * is written at offset (sum of earlier frames' pixels) + i. Outputs are device memory. Returns
+ * BHK_EUNFINISHED if any ray hit the step cap (after synchronising the stream), else BHK_OK. */
+bhk_status bhk_trace_frames(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes,
+                            const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
+/* The same with HOST output buffers: the library traces into its own device buffers and copies the
+ * results back before returning (synchronous). This is the eht::render-style call
+ * (src/eht.cpp:321-347): frames in, images out, in host memory. */
+bhk_status bhk_trace_frames_host(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes,
+                                 const bhk_trace_opts* opts, const bhk_rays_out* host_out);
+/* Per-ray variant: explicit (a, r_obs, theta_obs, alpha, beta) device arrays of n rays, ZAMO pinhole
+ * launch per ray, shared disk radii (r_disk_in <= 0: each ray's prograde ISCO). */
+bhk_status bhk_trace_rays(bhk_context* ctx, int64_t n, const double* a, const double* r_obs, const double* theta_obs,
+                          const double* alpha, const double* beta, double r_disk_in, double r_disk_out,
+                          const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
+bhk_status bhk_get_stats(bhk_context* ctx, bhk_trace_stats* stats);   /* synchronises the context stream */
+/* Times block x chunk x sort-granularity candidates on these frames and keeps the fastest for later
+ * calls on this context (opts fields left 0). The chosen values are returned in stats. */
+bhk_status bhk_autotune(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes, const bhk_trace_opts* opts,
+                        bhk_trace_stats* chosen);
+
+/* Analytic shadow edge seen by a frame's pinhole: spherical photon orbits r in [r_pro, r_retro],
+ * their (xi, eta) mapped through the ZAMO camera at r_obs (src/eht.cpp:52-80 for r_obs -> infinity).
+ * Host outputs alpha, beta (cap entries); returns the count in *n. */
+bhk_status bhk_critical_curve(double a, double r_obs, double theta_obs, int32_t samples, double* alpha, double* beta,
+                              int32_t cap, int32_t* n);
+
+/* FLOPs one accepted FP32 Dormand-Prince step costs in the mixed tracer, counted from its source. */
+double bhk_flops_per_step(void);
+
+/* Diagnostic: the device's FP32 FMA throughput (TFLOP/s, FMA = 2 FLOPs) measured with a
+ * latency-covered FMA chain kernel, the roofline denominator of the tracer. No reference counterpart. */
+bhk_status bhk_fp32_fma_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,151 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Run where the reference tree exists (it builds oracle/_ref/libkerr_ref.so from the reference's
+unmodified kerr.cpp, trajectory.cpp, central.cpp and eht.cpp through oracle/Makefile):
+
+    python tests/golden/make_golden.py
+
+Fixtures (all produced by the reference's own functions, never by this project's code):
+  steps_ref.npz       per-step vectors: derivatives, stepMino, photonStepSize, enforceConstraints,
+                      normalizeAngles, ZAMO frames + photonFromFrame, launchFromZamo, radii, critical
+                      curves, central::bendingAngle (src/kerr.cpp, src/eht.cpp, src/central.cpp)
+  trajectory_ref.npz  trajectory::traceRay end/rEnd/g/skyDirection for ZAMO cameras with a disk
+                      (src/trajectory.cpp:214-396), to pin the loop shape of the oracle
+  c1_rk4_1e-4.npz     128x128 frame, a=0.9, r_obs=50, theta=80 deg, alpha,beta in [-15,15], disk
+                      ISCO..20, escape 1000, capture r_+(1+1e-6): the reference RK4 loop at tolerance 1e-4
+  c2_rk4_1e-4.npz     96x54 frame with the 1080p geometry (a=0.998, r_obs=1000, theta=60 deg,
+                      alpha in +-20, beta in +-11.25, disk ISCO..30) at tolerance 1e-4
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import pyoracle as po  # noqa: E402
+
+
+def steps_fixture(R: po.Oracle) -> dict:
+    rng = np.random.default_rng(20261203)
+    n = 512
+    a = rng.uniform(0.0, 0.999, n)
+    cons = np.stack([rng.uniform(0.5, 1.5, n), rng.uniform(-8, 8, n), rng.uniform(-2, 40, n), np.zeros(n)], 1)
+    st = np.stack([rng.uniform(-5, 5, n), rng.uniform(1.2, 1000, n), rng.uniform(-0.3, np.pi + 0.3, n),
+                   rng.uniform(-10, 10, n), rng.uniform(-1e3, 1e3, n), rng.uniform(-10, 10, n)], 1)
+    h = rng.uniform(-0.02, 0.02, n)
+    tol = 10.0 ** rng.uniform(-4, -1, n)
+    der = np.zeros((n, 6))
+    stepped = np.zeros((n, 6))
+    hstep = np.zeros(n)
+    enforced = np.zeros((n, 6))
+    normalized = np.zeros((n, 6))
+    for i in range(n):
+        c = po.Constants(*cons[i])
+        s = po.State(*st[i])
+        d = R.derivatives(a[i], c, s)
+        der[i] = [d.dt, d.dr, d.dtheta, d.dphi, d.dvr, d.dvtheta]
+        x = R.step_mino(a[i], c, s, h[i])
+        stepped[i] = [x.t, x.r, x.theta, x.phi, x.vr, x.vtheta]
+        hstep[i] = R.photon_step_size(a[i], c, s, tol[i])
+        x = R.enforce_constraints(a[i], c, s)
+        enforced[i] = [x.t, x.r, x.theta, x.phi, x.vr, x.vtheta]
+        big = po.State(st[i][0], st[i][1], st[i][2] * 3.0, st[i][3], st[i][4], st[i][5])
+        x = R.normalize_angles(big)
+        normalized[i] = [x.t, x.r, x.theta, x.phi, x.vr, x.vtheta]
+    # ZAMO frames and the photons they launch
+    m = 128
+    fa = rng.uniform(0.0, 0.999, m)
+    fr = 10.0 ** rng.uniform(0.4, 3.0, m)
+    fth = rng.uniform(0.02, np.pi - 0.02, m)
+    look = rng.normal(size=(m, 3))
+    look /= np.linalg.norm(look, axis=1, keepdims=True)
+    frames = np.zeros((m, 4, 4))
+    pcons = np.zeros((m, 4))
+    pstate = np.zeros((m, 6))
+    for i in range(m):
+        f = R.zamo_frame(fa[i], fr[i], fth[i])
+        frames[i] = np.array([[f.e[k][j] for j in range(4)] for k in range(4)])
+        c, s = R.photon_from_frame(fa[i], fr[i], fth[i], 0.25, f, look[i])
+        pcons[i] = [c.E, c.L, c.Q, c.mu]
+        pstate[i] = [s.t, s.r, s.theta, s.phi, s.vr, s.vtheta]
+    zv = rng.normal(size=(m, 3))
+    zv /= np.linalg.norm(zv, axis=1, keepdims=True)
+    zcons = np.zeros((m, 4))
+    zstate = np.zeros((m, 6))
+    for i in range(m):
+        c, s = R.launch_from_zamo(fa[i], fr[i], fth[i], 0.0, zv[i], 0.0)
+        zcons[i] = [c.E, c.L, c.Q, c.mu]
+        zstate[i] = [s.t, s.r, s.theta, s.phi, s.vr, s.vtheta]
+    spins = np.array([0.0, 0.3, 0.6, 0.9, 0.94, 0.998, 1.0])
+    radii = np.array([[R.horizon_radius_raw(x), R.isco_radius_raw(x, 1), R.isco_radius_raw(x, 0),
+                       R.photon_orbit_radius_raw(x, 1), R.photon_orbit_radius_raw(x, 0)] for x in spins])
+    cc_params = np.array([(0.0, 1.0), (0.9, np.deg2rad(17)), (0.9, np.deg2rad(60)), (0.998, np.deg2rad(60)),
+                          (0.5, np.deg2rad(80))])
+    cc = {"cc_params": cc_params}
+    for i, (sa, incl) in enumerate(cc_params):
+        al, be = R.critical_curve(sa, incl, 400)
+        cc[f"cc{i}_alpha"] = al
+        cc[f"cc{i}_beta"] = be
+    bend_alpha = np.deg2rad([10.0, 40.0, 70.0, 89.0])
+    bend = np.array([R.bending_angle_raw(5.8, x) for x in bend_alpha])
+    return dict(a=a, cons=cons, state=st, h=h, tol=tol, derivatives=der, step_mino=stepped, step_size=hstep,
+                enforced=enforced, normalized=normalized, frame_a=fa, frame_r=fr, frame_theta=fth, look=look,
+                frames=frames, photon_cons=pcons, photon_state=pstate, zamo_v=zv, zamo_cons=zcons,
+                zamo_state=zstate, spins=spins, radii=radii, bend_alpha=bend_alpha, bend=bend, **cc)
+
+
+def trajectory_fixture(R: po.Oracle) -> dict:
+    rng = np.random.default_rng(7)
+    n = 96
+    a = rng.uniform(0.0, 0.998, n)
+    r = 10.0 ** rng.uniform(1.2, 2.0, n)
+    th = rng.uniform(0.2, np.pi - 0.2, n)
+    look = np.stack([-np.ones(n), rng.uniform(-0.35, 0.35, n), rng.uniform(-0.35, 0.35, n)], 1)
+    look /= np.linalg.norm(look, axis=1, keepdims=True)
+    end = np.zeros(n, np.int32)
+    vals = np.zeros((n, 8))
+    r_in = np.array([R.isco_radius_raw(x, 1) for x in a])
+    for i in range(n):
+        out = np.zeros(8)
+        end[i] = R.trajectory_trace_raw(a[i], r[i], th[i], 0.0, po._ptr(np.ascontiguousarray(look[i])), 1, r_in[i],
+                                        20.0, 250.0, po._ptr(out))
+        vals[i] = out
+    return dict(a=a, r=r, theta=th, look=look, r_in=r_in, end=end, values=vals)
+
+
+def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
+    t = time.time()
+    out = R.trace_frame(sc, w, h, *ext)
+    print(f"  traced {w}x{h} in {time.time() - t:.1f} s, outcomes {np.bincount(out['outcome'], minlength=4)}")
+    return dict(outcome=out["outcome"].astype(np.uint8), r_disk=out["r_disk"], phi_disk=out["phi_disk"],
+                g=out["g"], theta_inf=out["theta_inf"], phi_inf=out["phi_inf"], steps=out["steps"],
+                width=w, height=h, extents=np.array(ext),
+                scene=np.array([sc.a, sc.r_obs, sc.theta_obs, sc.phi_obs, sc.r_disk_in, sc.r_disk_out, sc.r_escape,
+                                sc.capture_eps, sc.tol]))
+
+
+def main() -> None:
+    po.build(reference=True)
+    R = po.Oracle(reference=True)
+    print("steps_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "steps_ref.npz"), **steps_fixture(R))
+    print("trajectory_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "trajectory_ref.npz"), **trajectory_fixture(R))
+    print("c1_rk4_1e-4.npz")
+    sc1 = po.scene(a=0.9, r_obs=50.0, theta_obs_deg=80.0, r_disk_out=20.0, tol=1e-4, method=po.RK4,
+                   max_steps=5_000_000)
+    np.savez_compressed(os.path.join(HERE, "c1_rk4_1e-4.npz"),
+                        **frame_fixture(R, sc1, 128, 128, (-15.0, 15.0, -15.0, 15.0)))
+    print("c2_rk4_1e-4.npz")
+    sc2 = po.scene(a=0.998, r_obs=1000.0, theta_obs_deg=60.0, r_disk_out=30.0, tol=1e-4, method=po.RK4,
+                   max_steps=5_000_000)
+    np.savez_compressed(os.path.join(HERE, "c2_rk4_1e-4.npz"),
+                        **frame_fixture(R, sc2, 96, 54, (-20.0, 20.0, -11.25, 11.25)))
+
+
+if __name__ == "__main__":
+    main()

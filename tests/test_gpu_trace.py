@@ -1,0 +1,181 @@
+"""GPU parity of the batch tracer (through the C ABI) against the oracle and the reference fixtures.
+
+FP64 mode: 100% outcome agreement outside a 1e-3 M band of the critical curve, r_disk and g to
+1e-6 relative, phi_disk and the exit angles to 1e-6 rad, against the reference RK4 at tolerance
+1e-4 (tests/golden). Against the oracle's FP64 Dormand-Prince (the same algorithm) the bar is
+1e-8. Mixed precision (FP32 integration): errors against the same references are bounded at
+the 1e-4 level the surrogate comparison uses, and printed.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import pyoracle as po
+from black_simulation_gb300 import bhk
+
+pytestmark = pytest.mark.gpu
+
+
+def host(out):
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def frame_from_fixture(g, a, r_obs, deg, r_out):
+    ext = g["extents"]
+    return bhk.Frame(a, r_obs, math.radians(deg), int(g["width"]), int(g["height"]), ext[0], ext[1], ext[2], ext[3],
+                     0.0, r_out)
+
+
+def band_mask(oracle, g, a, r_obs, deg, width=1e-3):
+    al, be = po.pixel_grid(int(g["width"]), int(g["height"]), *g["extents"])
+    ca, cb = oracle.critical_curve_finite(a, r_obs, math.radians(deg), 800)
+    return po.band_distance(al, be, ca, cb) > width
+
+
+def errors(out, ref):
+    d = (out["outcome"] == bhk.DISK) & (ref["outcome"] == bhk.DISK)
+    e = (out["outcome"] == bhk.ESCAPED) & (ref["outcome"] == bhk.ESCAPED)
+    ang = lambda x, y: np.abs(np.angle(np.exp(1j * (x - y))))  # noqa: E731
+    res = {
+        "r_disk": np.max(np.abs(out["r_disk"][d] / ref["r_disk"][d] - 1), initial=0.0),
+        "g": np.max(np.abs(out["g"][d] / ref["g"][d] - 1), initial=0.0),
+        "phi_disk": np.max(ang(out["phi_disk"][d], ref["phi_disk"][d]), initial=0.0),
+        "theta_inf": np.max(np.abs(out["theta_inf"][e] - ref["theta_inf"][e]), initial=0.0),
+        "phi_inf": np.max(ang(out["phi_inf"][e], ref["phi_inf"][e]), initial=0.0),
+    }
+    return res
+
+
+CASES = [("c1_rk4_1e-4.npz", 0.9, 50.0, 80.0, 20.0), ("c2_rk4_1e-4.npz", 0.998, 1000.0, 60.0, 30.0)]
+
+
+@pytest.mark.parametrize("name,a,r_obs,deg,r_out", CASES)
+def test_fp64_matches_reference_fixture(ctx, oracle, golden, name, a, r_obs, deg, r_out):
+    g = golden(name)
+    out = host(ctx.trace_frames([frame_from_fixture(g, a, r_obs, deg, r_out)], bhk.TraceOpts("fp64", rtol=1e-10)))
+    outside = band_mask(oracle, g, a, r_obs, deg)
+    np.testing.assert_array_equal(out["outcome"][outside], g["outcome"][outside])
+    err = errors(out, g)
+    print(name, "fp64 vs reference RK4(1e-4):", err)
+    for k, v in err.items():
+        assert v <= 1e-6, (k, v)
+    st = ctx.stats()
+    assert st["unfinished"] == 0 and st["accepted_steps"] > 0
+
+
+@pytest.mark.parametrize("name,a,r_obs,deg,r_out", CASES)
+def test_fp64_matches_oracle_dp5(ctx, oracle, golden, name, a, r_obs, deg, r_out):
+    g = golden(name)
+    f = frame_from_fixture(g, a, r_obs, deg, r_out)
+    out = host(ctx.trace_frames([f], bhk.TraceOpts("fp64", rtol=1e-10)))
+    sc = po.scene(a=a, r_obs=r_obs, theta_obs_deg=deg, r_disk_out=r_out, tol=1e-10, method=po.DP5)
+    ref = oracle.trace_frame(sc, f.width, f.height, f.alpha_lo, f.alpha_hi, f.beta_lo, f.beta_hi)
+    outside = band_mask(oracle, g, a, r_obs, deg, 1e-4)
+    np.testing.assert_array_equal(out["outcome"][outside], ref["outcome"][outside])
+    err = errors(out, ref)
+    for k, v in err.items():
+        assert v <= 1e-8, (k, v)
+    # Same algorithm: step counts agree except where rounding flips an accept/reject.
+    assert np.mean(out["steps"] == ref["steps"]) > 0.95
+
+
+@pytest.mark.parametrize("name,a,r_obs,deg,r_out", CASES)
+def test_mixed_precision_errors_vs_fp64(ctx, oracle, golden, name, a, r_obs, deg, r_out):
+    g = golden(name)
+    f = frame_from_fixture(g, a, r_obs, deg, r_out)
+    out = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6)))
+    st = ctx.stats()
+    outside = band_mask(oracle, g, a, r_obs, deg, 1e-2)
+    agree = np.mean(out["outcome"][outside] == g["outcome"][outside])
+    err = errors(out, g)
+    print(name, "mixed vs reference RK4(1e-4): outcome agreement", agree, err, "rescued", st["rescued"])
+    assert agree >= 0.999
+    assert err["r_disk"] < 1e-4 and err["g"] < 1e-4
+    assert err["phi_disk"] < 1e-3
+    assert err["theta_inf"] < 1e-4 and err["phi_inf"] < 1e-4
+    assert st["unfinished"] == 0
+
+
+def test_per_ray_api_equals_frame_api(ctx):
+    f = bhk.frame_c1(20, 12)
+    frame_out = host(ctx.trace_frames([f], bhk.TraceOpts("fp64")))
+    al, be = po.pixel_grid(f.width, f.height, f.alpha_lo, f.alpha_hi, f.beta_lo, f.beta_hi)
+    n = len(al)
+    dev = lambda x: torch.tensor(x, dtype=torch.float64, device="cuda")  # noqa: E731
+    ray_out = host(ctx.trace_rays(dev(np.full(n, f.a)), dev(np.full(n, f.r_obs)), dev(np.full(n, f.theta_obs)),
+                                  dev(al), dev(be), 0.0, f.r_disk_out, bhk.TraceOpts("fp64")))
+    for k in bhk.FIELDS:
+        np.testing.assert_allclose(ray_out[k].astype(float), frame_out[k].astype(float), rtol=1e-12, atol=1e-12,
+                                   equal_nan=True)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_launch_shape_and_order_do_not_change_results(ctx, prec):
+    """Results are a function of the ray alone: block size, chunk size, sort granularity and
+    graph replay leave every output bit-identical."""
+    frames = [bhk.frame_c1(48, 40)]
+    base = host(ctx.trace_frames(frames, bhk.TraceOpts(prec, block=128, chunk=32, sort_buckets=1)))
+    for blk, ch, bu, graph in ((64, 1, 64, False), (256, 256, 512, False), (128, 32, 64, True),
+                               (128, 32, 64, True)):
+        got = host(ctx.trace_frames(frames, bhk.TraceOpts(prec, block=blk, chunk=ch, sort_buckets=bu,
+                                                          use_graph=graph)))
+        for k in bhk.FIELDS:
+            np.testing.assert_array_equal(got[k], base[k], err_msg=f"{k} {blk} {ch} {bu} {graph}")
+
+
+def test_ragged_multi_frame_batch_equals_single_frames(ctx):
+    frames = [bhk.Frame(0.5, 30.0, 1.2, 1, 1, -10, 10, -10, 10, 0.0, 15.0),
+              bhk.Frame(0.998, 600.0, 0.4, 7, 3, -8, 8, -4, 4, 0.0, 25.0),
+              bhk.frame_c1(33, 17),
+              bhk.Frame(0.1, 20.0, 1.5, 16, 16, -12, 12, -12, 12, 7.0, 18.0)]
+    for prec in ("fp64", "mixed"):
+        batch = host(ctx.trace_frames(frames, bhk.TraceOpts(prec, use_graph=True)))
+        off = 0
+        for f in frames:
+            one = host(ctx.trace_frames([f], bhk.TraceOpts(prec)))
+            for k in bhk.FIELDS:
+                np.testing.assert_array_equal(batch[k][off:off + f.rays], one[k], err_msg=k)
+            off += f.rays
+
+
+def test_host_buffer_entry_point_and_step_cap(ctx):
+    f = bhk.frame_c1(16, 16)
+    dev = host(ctx.trace_frames([f], bhk.TraceOpts("fp64")))
+    out, st = ctx.trace_frames_host([f], bhk.TraceOpts("fp64"))
+    assert st == bhk.OK
+    for k in bhk.FIELDS:
+        np.testing.assert_array_equal(out[k], dev[k])
+    capped, st = ctx.trace_frames_host([f], bhk.TraceOpts("fp64", max_steps=5))
+    assert st == bhk.EUNFINISHED
+    assert np.all(capped["outcome"][capped["steps"] >= 5] != bhk.ESCAPED)
+    assert np.any(capped["outcome"] == bhk.UNFINISHED)
+    assert ctx.stats()["unfinished"] == np.sum(capped["outcome"] == bhk.UNFINISHED)
+
+
+def test_invalid_frames_are_rejected(ctx):
+    with pytest.raises(bhk.BhkError) as e:
+        ctx.trace_frames([bhk.Frame(1.2, 50, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())
+    assert e.value.status == bhk.EINVAL
+    with pytest.raises(bhk.BhkError):
+        ctx.trace_frames([bhk.Frame(0.9, 1.5, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())
+    with pytest.raises(bhk.BhkError):
+        ctx.trace_frames([bhk.Frame(0.9, 50, 1.0, 0, 4, -1, 1, -1, 1)], bhk.TraceOpts())
+    with pytest.raises(bhk.BhkError):
+        ctx.trace_frames([], bhk.TraceOpts())
+
+
+def test_autotune_picks_a_valid_shape(ctx):
+    st = ctx.autotune([bhk.frame_c1(64, 64)], bhk.TraceOpts("mixed"))
+    assert st["block"] in (64, 128, 256) and st["chunk"] in (1, 32, 256) and st["sort_buckets"] in (1, 64, 512)
+    assert st["kernel_ms"] > 0
+
+
+def test_critical_curve_matches_oracle(cuda, oracle):
+    for a, r, deg in ((0.9, 50.0, 80.0), (0.998, 1000.0, 60.0)):
+        ga, gb = bhk.critical_curve(a, r, math.radians(deg), 400)
+        oa, ob = oracle.critical_curve_finite(a, r, math.radians(deg), 400)
+        assert len(ga) == len(oa)
+        np.testing.assert_allclose(ga, oa, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(gb, ob, rtol=1e-12, atol=1e-12)
