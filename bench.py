@@ -43,12 +43,13 @@ SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.act
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
 
-def workload(name: str):
+def workload(name: str, scale: int = 1):
     from black_simulation_gb300 import bhk
     if name == "1080p":
-        return [bhk.frame_c2()], bhk.TraceOpts("mixed", rtol=1e-6), dict(
-            workload="1920x1080 frame, a=0.998, r_obs=1000M, theta=60deg, alpha +-20M, disk ISCO-30M",
-            rays=1920 * 1080, precision="mixed FP32/FP64", rtol=1e-6)
+        w, h = 1920 // scale, 1080 // scale
+        return [bhk.frame_c2(w, h)], bhk.TraceOpts("mixed", rtol=1e-6), dict(
+            workload=f"{w}x{h} frame, a=0.998, r_obs=1000M, theta=60deg, alpha +-20M, disk ISCO-30M",
+            rays=w * h, precision="mixed FP32/FP64", rtol=1e-6)
     if name == "c1":
         return [bhk.frame_c1()], bhk.TraceOpts("fp64", rtol=1e-10), dict(
             workload="128x128 frame, a=0.9, r_obs=50M, theta=80deg, alpha,beta +-15M, disk ISCO-20M",
@@ -197,7 +198,8 @@ def run_reference(args):
     world, rank, _ = dist_setup(0)
     if rank != 0:
         return
-    frames, _, cfg = workload(args.workload)
+    frames, _, cfg = workload(args.workload, args.scale)
+    cfg = {k: v for k, v in cfg.items() if k not in ("precision", "rtol")}
     rates = []
     for i in range(args.warmup + args.steps):
         rate, n, dt, threads = cpu_reference_rate(frames, target_s=max(2.0, 30.0 / (args.warmup + args.steps)))
@@ -224,9 +226,11 @@ def run_ours(args):
     world, rank, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    frames, opts, cfg = workload(args.workload)
+    frames, opts, cfg = workload(args.workload, args.scale)
     n_rays = sum(f.rays for f in frames)
     ctx = bhk.Context(local)
+    work_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work_stream)
     tuned = ctx.autotune(frames, opts) if args.autotune else None
     out = bhk.alloc_outputs(n_rays, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
@@ -278,7 +282,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32" if opts.precision == "mixed" else "f64", "data": "synthetic",
         "config": {**cfg, "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between steps",
                    "block": (tuned or {}).get("block"), "chunk": (tuned or {}).get("chunk"),
-                   "sort_buckets": (tuned or {}).get("sort_buckets"), "status": status,
+                   "sort_buckets": (tuned or {}).get("sort_buckets"), "reg_budget": (tuned or {}).get("reg_budget"),
+                   "status": status,
                    "outcomes": {"captured": counts.get(1, 0), "disk": counts.get(2, 0),
                                 "escaped": counts.get(3, 0), "unfinished": counts.get(0, 0)},
                    "mean_accepted_steps_per_ray": float(np.mean(acc_steps)) / n_rays,
@@ -313,6 +318,7 @@ def main():
     ap.add_argument("--autotune", action="store_true", default=True)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=int, default=1, help="divide the frame size (profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

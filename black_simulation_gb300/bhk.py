@@ -45,18 +45,21 @@ class FrameDescC(C.Structure):
 class TraceOptsC(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_steps", C.c_int32), ("r_escape", C.c_double),
                 ("capture_eps", C.c_double), ("reproject_every", C.c_int32), ("block", C.c_int32),
-                ("chunk", C.c_int32), ("sort_buckets", C.c_int32), ("use_graph", C.c_int32)]
+                ("chunk", C.c_int32), ("sort_buckets", C.c_int32), ("use_graph", C.c_int32),
+                ("reg_budget", C.c_int32), ("pole_step_frac", C.c_double)]
 
 
 class RaysOutC(C.Structure):
     _fields_ = [("outcome", C.c_void_p), ("r_disk", C.c_void_p), ("phi_disk", C.c_void_p), ("g", C.c_void_p),
-                ("theta_inf", C.c_void_p), ("phi_inf", C.c_void_p), ("steps", C.c_void_p)]
+                ("theta_inf", C.c_void_p), ("phi_inf", C.c_void_p), ("steps", C.c_void_p),
+                ("rejected", C.c_void_p)]
 
 
 class StatsC(C.Structure):
     _fields_ = [("rays", C.c_int64), ("accepted_steps", C.c_int64), ("rejected_steps", C.c_int64),
                 ("rescued", C.c_int64), ("unfinished", C.c_int64), ("block", C.c_int32), ("chunk", C.c_int32),
-                ("sort_buckets", C.c_int32), ("grid", C.c_int32), ("kernel_ms", C.c_double)]
+                ("sort_buckets", C.c_int32), ("grid", C.c_int32), ("reg_budget", C.c_int32), ("pad", C.c_int32),
+                ("kernel_ms", C.c_double)]
 
 
 @dataclasses.dataclass
@@ -97,11 +100,14 @@ class TraceOpts:
     chunk: int = 0
     sort_buckets: int = 0
     use_graph: bool = False
+    reg_budget: int = 0
+    pole_step_frac: float = 0.0
 
     def c(self) -> TraceOptsC:
         prec = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[self.precision]
         return TraceOptsC(prec, self.rtol, self.max_steps, self.r_escape, self.capture_eps, self.reproject_every,
-                          self.block, self.chunk, self.sort_buckets, 1 if self.use_graph else 0)
+                          self.block, self.chunk, self.sort_buckets, 1 if self.use_graph else 0, self.reg_budget,
+                          self.pole_step_frac)
 
 
 _lib: Optional[C.CDLL] = None
@@ -179,11 +185,17 @@ def _ptr(t) -> Optional[int]:
     return int(t)
 
 
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy: the legacy default stream, which torch's handle 0 denotes
+
+
 def _stream(stream) -> Optional[int]:
+    """The cudaStream_t to pass: torch's current stream unless given. Handle 0 (torch's default
+    stream) goes over as cudaStreamLegacy, since NULL means the context's own stream to libbhk."""
     if stream is None:
         import torch
-        return torch.cuda.current_stream().cuda_stream
-    return int(getattr(stream, "cuda_stream", stream))
+        stream = torch.cuda.current_stream()
+    h = int(getattr(stream, "cuda_stream", stream))
+    return h if h != 0 else CUDA_STREAM_LEGACY
 
 
 def _n(t, width) -> int:
@@ -297,7 +309,7 @@ def fp32_fma_peak_tflops(device: int = 0) -> float:
 
 # ----------------------------------------------------------------------------- batch tracer ----
 
-FIELDS = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf", "steps")
+FIELDS = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf", "steps", "rejected")
 
 
 def alloc_outputs(n: int, device="cuda"):
@@ -305,6 +317,7 @@ def alloc_outputs(n: int, device="cuda"):
     out = {k: torch.empty(n, dtype=torch.float64, device=device) for k in FIELDS[1:6]}
     out["outcome"] = torch.empty(n, dtype=torch.uint8, device=device)
     out["steps"] = torch.empty(n, dtype=torch.int32, device=device)
+    out["rejected"] = torch.empty(n, dtype=torch.int32, device=device)
     return out
 
 
@@ -363,6 +376,7 @@ class Context:
             out = {k: np.empty(n) for k in FIELDS[1:6]}
             out["outcome"] = np.empty(n, np.uint8)
             out["steps"] = np.empty(n, np.int32)
+            out["rejected"] = np.empty(n, np.int32)
         arr, nf = self._frames(frames)
         oc = opts.c()
         ptrs = []

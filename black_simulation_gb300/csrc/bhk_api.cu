@@ -48,7 +48,7 @@ cudaError_t grow(T** p, size_t* cap, size_t need) {
 }
 
 struct GraphKey {
-    int mode = -1, fp64 = 0, nframes = 0, block = 0, chunk = 0, buckets = 0, grid = 0, timed = 0;
+    int mode = -1, fp64 = 0, nframes = 0, block = 0, chunk = 0, buckets = 0, grid = 0, timed = 0, regcap = 0;
     int64_t n_explicit = 0;
     TraceParams p{};
     Outputs out{};
@@ -70,9 +70,9 @@ struct bhk_context {
     std::mutex mu;
 
     // scratch
-    size_t cap_rays = 0, cap_E = 0, cap_L = 0, cap_Q = 0, cap_vr = 0, cap_vth = 0, cap_h0 = 0, cap_gid = 0,
+    size_t cap_rays = 0, cap_E = 0, cap_L = 0, cap_Q = 0, cap_vr = 0, cap_vth = 0, cap_gid = 0,
            cap_key = 0, cap_order = 0, cap_rescue = 0, cap_geom = 0, cap_frames = 0;
-    double *E = nullptr, *L = nullptr, *Q = nullptr, *vr = nullptr, *vth = nullptr, *h0 = nullptr;
+    double *E = nullptr, *L = nullptr, *Q = nullptr, *vr = nullptr, *vth = nullptr;
     int32_t* gid = nullptr;
     uint16_t* key = nullptr;
     int32_t* order = nullptr;
@@ -93,13 +93,14 @@ struct bhk_context {
     bool timed_last = false;
 
     // library-owned outputs for the host-buffer entry point and the autotuner
-    size_t cap_out = 0, cap_o8 = 0, cap_od[5] = {0, 0, 0, 0, 0}, cap_os = 0;
+    size_t cap_out = 0, cap_o8 = 0, cap_od[5] = {0, 0, 0, 0, 0}, cap_os = 0, cap_or = 0;
     uint8_t* o_outcome = nullptr;
     double* o_d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t* o_steps = nullptr;
+    int32_t* o_rej = nullptr;
 
     // launch shape: autotuned per precision, else defaults
-    int tuned_block[2] = {0, 0}, tuned_chunk[2] = {0, 0}, tuned_buckets[2] = {0, 0};
+    int tuned_block[2] = {0, 0}, tuned_chunk[2] = {0, 0}, tuned_buckets[2] = {0, 0}, tuned_regcap[2] = {0, 0};
 
     // cached graph
     GraphKey gkey;
@@ -114,7 +115,7 @@ namespace {
 struct Resolved {
     bool fp64;
     TraceParams p;
-    int block, chunk, buckets, grid;
+    int block, chunk, buckets, grid, regcap;
     bool graph;
 };
 
@@ -128,8 +129,17 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.p.eps = o->capture_eps > 0.0 ? o->capture_eps : 1e-6;
     r.p.r_escape = o->r_escape > 0.0 ? o->r_escape : 1000.0;
     r.p.max_steps = o->max_steps > 0 ? o->max_steps : 20000;
-    r.p.reproject_every = o->reproject_every == 0 ? 16 : (o->reproject_every < 0 ? 0 : o->reproject_every);
+    r.p.reproject_every = o->reproject_every > 0 ? o->reproject_every : 0;
     r.p.tol0 = std::min(std::max(std::pow(r.p.rtol, 0.2), 1e-3), 0.05);
+    r.p.rtol_f = static_cast<float>(r.p.rtol);
+    // Near the Mino-time pole of an outgoing ray the 4th-order error estimate grows as (h / d)^5,
+    // d the Mino time left; measured, it allows h / d ~ 0.12 at rtol 1e-6, scaling as rtol^(1/5).
+    // The cap sits just below, where the controller would otherwise cycle into rejections (on the
+    // a = 0.9, r_obs = 50 frame: 31% rejected steps uncapped, 6% at 0.1, 20% less work in all).
+    r.p.pole_frac = o->pole_step_frac > 0.0 ? static_cast<float>(o->pole_step_frac)
+                    : (o->pole_step_frac < 0.0 ? 0.0f
+                       : static_cast<float>(std::min(0.5, 0.1 * std::pow(r.p.rtol / 1e-6, 0.2))));
+    r.p.tol0_f = static_cast<float>(r.p.tol0);
     r.block = o->block > 0 ? o->block : (ctx->tuned_block[pi] ? ctx->tuned_block[pi] : 128);
     r.chunk = o->chunk > 0 ? o->chunk : (ctx->tuned_chunk[pi] ? ctx->tuned_chunk[pi] : 32);
     r.buckets = o->sort_buckets > 0 ? o->sort_buckets : (ctx->tuned_buckets[pi] ? ctx->tuned_buckets[pi] : 64);
@@ -137,7 +147,11 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.p.chunk = r.chunk;
     r.p.buckets = r.buckets;
     r.graph = o->use_graph != 0;
-    const int bps = trace_blocks_per_sm(r.fp64, r.block);
+    const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 3);
+    r.regcap = (r.fp64 || rb >= 3) ? 0 : rb;
+    if (r.regcap > 0 && r.block > 128) r.block = 128;
+    r.block = std::min(r.block, 256);
+    const int bps = trace_blocks_per_sm(r.fp64, r.regcap, r.block);
     r.grid = std::max(1, bps) * ctx->num_sms;
     return r;
 }
@@ -150,7 +164,6 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     if (e == cudaSuccess) e = grow(&c->Q, &c->cap_Q, rays);
     if (e == cudaSuccess) e = grow(&c->vr, &c->cap_vr, rays);
     if (e == cudaSuccess) e = grow(&c->vth, &c->cap_vth, rays);
-    if (e == cudaSuccess) e = grow(&c->h0, &c->cap_h0, rays);
     if (e == cudaSuccess) e = grow(&c->gid, &c->cap_gid, rays);
     if (e == cudaSuccess) e = grow(&c->key, &c->cap_key, rays);
     if (e == cudaSuccess) e = grow(&c->order, &c->cap_order, rays);
@@ -169,7 +182,7 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     return BHK_OK;
 }
 
-LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->h0, c->gid, c->key}; }
+LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key}; }
 
 struct Batch {
     int mode;  // 0 frames, 1 explicit
@@ -202,8 +215,8 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         order = c->order;
     }
     if (timed) BHK_CUDA(cudaEventRecord(c->ev0, s));
-    launch_trace(r.fp64, L, c->geom, order, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, r.block,
-                 r.grid, s);
+    launch_trace(r.fp64, r.regcap, L, c->geom, order, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl,
+                 r.block, r.grid, s);
     if (!r.fp64) launch_rescue(L, c->geom, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, s);
     if (timed) BHK_CUDA(cudaEventRecord(c->ev1, s));
     BHK_CUDA(cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Control), cudaMemcpyDeviceToHost, s));
@@ -217,7 +230,7 @@ bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Ou
     GraphKey k;
     std::memset(static_cast<void*>(&k), 0, sizeof(GraphKey));  // padding takes part in the comparison
     k.mode = b.mode; k.fp64 = r.fp64; k.nframes = b.nframes; k.block = r.block; k.chunk = r.chunk;
-    k.buckets = r.buckets; k.grid = r.grid; k.timed = timed; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
+    k.buckets = r.buckets; k.grid = r.grid; k.timed = timed; k.regcap = r.regcap; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
     k.n_explicit = b.mode == 1 ? 1 : 0;
     for (int i = 0; i < 5; ++i) k.ex[i] = b.ex[i];
     k.r_in = b.r_in; k.r_out = b.r_out;
@@ -247,7 +260,7 @@ Outputs to_outputs(const bhk_rays_out* o) {
     Outputs r{};
     if (!o) return r;
     r.outcome = o->outcome; r.r_disk = o->r_disk; r.phi_disk = o->phi_disk; r.g = o->g;
-    r.theta_inf = o->theta_inf; r.phi_inf = o->phi_inf; r.steps = o->steps;
+    r.theta_inf = o->theta_inf; r.phi_inf = o->phi_inf; r.steps = o->steps; r.rejected = o->rejected;
     return r;
 }
 
@@ -286,6 +299,7 @@ bhk_status finish_call(bhk_context* c, const Resolved& r, int64_t n, bool timed,
     c->last.chunk = r.chunk;
     c->last.sort_buckets = r.buckets;
     c->last.grid = r.grid;
+    c->last.reg_budget = r.fp64 ? 0 : (r.regcap ? r.regcap : 3);
     c->timed_last = timed;
     return BHK_OK;
 }
@@ -294,12 +308,13 @@ bhk_status ensure_outputs(bhk_context* c, size_t n) {
     cudaError_t e = grow(&c->o_outcome, &c->cap_o8, n);
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = grow(&c->o_d[i], &c->cap_od[i], n);
     if (e == cudaSuccess) e = grow(&c->o_steps, &c->cap_os, n);
+    if (e == cudaSuccess) e = grow(&c->o_rej, &c->cap_or, n);
     if (e != cudaSuccess) return fail(BHK_ENOMEM, "output allocation");
     return BHK_OK;
 }
 
 bhk_rays_out own_outputs(bhk_context* c) {
-    return bhk_rays_out{c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2], c->o_d[3], c->o_d[4], c->o_steps};
+    return bhk_rays_out{c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2], c->o_d[3], c->o_d[4], c->o_steps, c->o_rej};
 }
 
 cudaStream_t pick(bhk_context* c, void* stream) { return stream ? static_cast<cudaStream_t>(stream) : c->stream; }
@@ -365,9 +380,9 @@ bhk_status bhk_destroy(bhk_context* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->exec) cudaGraphExecDestroy(c->exec);
     if (c->graph) cudaGraphDestroy(c->graph);
-    void* dev[] = {c->E, c->L, c->Q, c->vr, c->vth, c->h0, c->gid, c->key, c->order, c->rescue, c->geom,
+    void* dev[] = {c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->order, c->rescue, c->geom,
                    c->frames_dev, c->ctl, c->hist, c->offs, c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2],
-                   c->o_d[3], c->o_d[4], c->o_steps};
+                   c->o_d[3], c->o_d[4], c->o_steps, c->o_rej};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (c->frames_host) cudaFreeHost(c->frames_host);
@@ -477,6 +492,7 @@ bhk_status bhk_trace_frames_host(bhk_context* c, const bhk_frame_desc* frames, i
     use.theta_inf = host_out->theta_inf ? dev.theta_inf : nullptr;
     use.phi_inf = host_out->phi_inf ? dev.phi_inf : nullptr;
     use.steps = host_out->steps ? dev.steps : nullptr;
+    use.rejected = host_out->rejected ? dev.rejected : nullptr;
     cudaStream_t s = c->stream;
     st = trace_frames_locked(c, frames, nframes, opts, &use, s, true);
     if (st != BHK_OK) return st;
@@ -488,6 +504,8 @@ bhk_status bhk_trace_frames_host(bhk_context* c, const bhk_frame_desc* frames, i
         if (hd[i]) BHK_CUDA(cudaMemcpyAsync(hd[i], dd[i], n * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (host_out->steps)
         BHK_CUDA(cudaMemcpyAsync(host_out->steps, use.steps, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (host_out->rejected)
+        BHK_CUDA(cudaMemcpyAsync(host_out->rejected, use.rejected, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     BHK_CUDA(cudaStreamSynchronize(s));
     return c->ctl_host->stats[2] ? fail(BHK_EUNFINISHED, "some rays reached the step cap") : BHK_OK;
 }
@@ -551,19 +569,24 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
     const int blocks[] = {64, 128, 256};
     const int chunks[] = {1, 32, 256};
     const int buckets[] = {1, 64, 512};
+    const int budgets[] = {3, 1, 2};
     const bhk_rays_out out = own_outputs(c);
     float best = 1e30f;
-    int bb = 128, bc = 32, bk = 64;
+    int bb = 128, bc = 32, bk = 64, br = 3;
     cudaEvent_t t0, t1;
     BHK_CUDA(cudaEventCreate(&t0));
     BHK_CUDA(cudaEventCreate(&t1));
+    for (int rb : budgets)
     for (int blk : blocks)
         for (int ch : chunks)
             for (int bu : buckets) {
-                if (trace_blocks_per_sm(pi == 0, blk) < 1) continue;
+                const int rc = (pi == 0 || rb >= 3) ? 0 : rb;
+                if (pi == 0 && rb != 3) continue;
+                if (trace_blocks_per_sm(pi == 0, rc, blk) < 1) continue;
                 o.block = blk;
                 o.chunk = ch;
                 o.sort_buckets = bu;
+                o.reg_budget = rb;
                 float t_best = 1e30f;
                 for (int rep = 0; rep < 2; ++rep) {
                     BHK_CUDA(cudaEventRecord(t0, c->stream));
@@ -581,7 +604,7 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
                 }
                 if (t_best < best) {
                     best = t_best;
-                    bb = blk; bc = ch; bk = bu;
+                    bb = blk; bc = ch; bk = bu; br = rb;
                 }
             }
     cudaEventDestroy(t0);
@@ -589,14 +612,16 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
     c->tuned_block[pi] = bb;
     c->tuned_chunk[pi] = bc;
     c->tuned_buckets[pi] = bk;
+    c->tuned_regcap[pi] = br;
     if (chosen) {
         *chosen = bhk_trace_stats{};
         chosen->block = bb;
         chosen->chunk = bc;
         chosen->sort_buckets = bk;
+        chosen->reg_budget = br;
         chosen->kernel_ms = best;
         chosen->rays = total;
-        o.block = bb; o.chunk = bc; o.sort_buckets = bk;
+        o.block = bb; o.chunk = bc; o.sort_buckets = bk; o.reg_budget = br;
         chosen->grid = resolve(c, &o).grid;
     }
     return BHK_OK;

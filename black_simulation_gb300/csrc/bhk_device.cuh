@@ -408,18 +408,26 @@ struct DP {
 // Per-ray constants of the photon right-hand side, hoisted out of the step (mu = 0).
 template <typename T>
 struct RayC {
-    T a, a2, E, aE, aL, L, K, twoE, L2, nA2E2;
+    T a, a2, E, aE, aL, L, K, twoE, L2, nA2E2, Q;
     __device__ __forceinline__ void set(double a_, double E_, double L_, double Q_) {
         const double x = L_ - a_ * E_;
         a = T(a_); a2 = T(a_ * a_); E = T(E_); aE = T(a_ * E_); aL = T(a_ * L_); L = T(L_);
-        K = T(x * x + Q_); twoE = T(2.0 * E_); L2 = T(L_ * L_); nA2E2 = T(-(a_ * a_) * E_ * E_);
+        K = T(x * x + Q_); twoE = T(2.0 * E_); L2 = T(L_ * L_); nA2E2 = T(-(a_ * a_) * E_ * E_); Q = T(Q_);
     }
 };
 
-// Right-hand side of the 5-component Mino system y = (r, theta, phi, vr, vtheta), photon (mu = 0):
-// kerr::derivatives restated (src/kerr.cpp:331-351) without dt.
+// The potentials R(r), Theta(theta) at an evaluated point and the 5% turning-zone thresholds of
+// kerr::enforceConstraints (src/kerr.cpp:521-542), produced alongside a right-hand side.
 template <typename T>
-__device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5]) {
+struct Proj {
+    T R, Rz, Th, Thz;
+};
+
+// Right-hand side of the 5-component Mino system y = (r, theta, phi, vr, vtheta), photon (mu = 0):
+// kerr::derivatives restated (src/kerr.cpp:331-351) without dt. With kProj it also returns the
+// potentials for the null-constraint re-projection, sharing sin, cos, P and Delta.
+template <typename T, bool kProj = false>
+__device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj<T>* pj = nullptr) {
     const T r = y[0];
     T sn, cs;
     Math<T>::sc(y[1], &sn, &cs);
@@ -435,18 +443,36 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5]) {
     k[0] = y[3];
     k[1] = y[4];
     k[3] = c.twoE * r * P - (r - T(1)) * c.K;
+    T inv2;
     if constexpr (sizeof(T) == 4) {
         const T inv = rcp_approx(m);
-        const T inv2 = inv * inv;
+        inv2 = inv * inv;
         const T ssc_inv = copysignf(inv2 * inv, sn);
         k[4] = sn * cs * c.nA2E2 + c.L2 * cs * ssc_inv;
         k[2] = c.a * inflow - c.aE + c.L * inv2;
     } else {
         const T ssc = (sn < T(0) ? -m : m) * m * m;
         const T sn2 = fmax(sn * sn, T(1e-18));
+        inv2 = T(1) / sn2;
         k[4] = sn * cs * c.nA2E2 + c.L2 * cs / ssc;
         k[2] = c.a * inflow - c.aE + c.L / sn2;
     }
+    if constexpr (kProj) {
+        const T P2 = P * P;
+        pj->R = P2 - delta * c.K;
+        pj->Rz = T(0.05) * (P2 + fabs(delta) * c.K);
+        const T cs2 = cs * cs;
+        const T cot2 = cs2 * inv2;
+        const T pm = c.nA2E2 * cs2;
+        pj->Th = c.Q - pm - c.L2 * cot2;
+        pj->Thz = T(0.05) * (fabs(c.Q) + fabs(pm) + c.L2 * cot2);
+    }
+}
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
 // Dense output of one component at fraction sg of a step (continuous extension above).

@@ -15,16 +15,19 @@ struct RayGeom {
     double r_in, r_out, zone_top; // disk, and r_+ + width of the analytic capture zone
 };
 
-// Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset.
+// Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset, and the per-camera
+// pieces of kerr::photonFromFrame (src/kerr.cpp:458-483) hoisted out of the per-ray launch.
 struct FrameDev {
     bhk_frame_desc d;
     int64_t offset;               // first global ray index of this frame
     double e[4][4];               // ZAMO frame at the camera
+    double el[4][4];              // the same vectors lowered with the camera's metric, g e_k
+    double sigma, cs2, inv_sn2, a2;  // Sigma, cos^2, 1/max(sin^2, 1e-18), a^2 at the camera
 };
 
 // Launch record of one ray, structure of arrays, written by the FP64 launch kernel.
 struct LaunchSoA {
-    double *E, *L, *Q, *vr, *vth, *h0;
+    double *E, *L, *Q, *vr, *vth;
     int32_t* geom_id;             // index into the RayGeom table
     uint16_t* key;                // cost bucket for the pre-sort
 };
@@ -59,12 +62,15 @@ struct TraceParams {
     double rtol, eps, r_escape;
     int32_t max_steps, reproject_every, chunk, buckets;
     double tol0;                  // photonStepSize tolerance of the first step
+    float rtol_f, tol0_f;         // the same for the FP32 path (no conversions in the loop)
+    float pole_frac;              // FP32: outgoing steps capped at pole_frac * r / |vr| (0 = no cap)
 };
 
 struct Outputs {
     uint8_t* outcome;
     double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
     int32_t* steps;
+    int32_t* rejected;
 };
 
 // ---- launchers (bhk_trace.cu) ----
@@ -76,11 +82,12 @@ void launch_rays_explicit(const double* a, const double* r_obs, const double* th
                           const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
-void launch_trace(bool fp64, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out, Rescue* rescue,
-                  unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid, cudaStream_t s);
+void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
+                  Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
+                  cudaStream_t s);
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
                    const TraceParams& p, Control* ctl, cudaStream_t s);
-int trace_blocks_per_sm(bool fp64, int block);
+int trace_blocks_per_sm(bool fp64, int regcap, int block);  // 0 when the pair is not allowed
 void launch_critical_curve(double a, double r_obs, double theta_obs, int samples, double* alpha, double* beta,
                            int* valid, cudaStream_t s);
 

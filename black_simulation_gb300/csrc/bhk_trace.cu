@@ -1,16 +1,17 @@
 // bhk_trace.cu -- the batch tracer for sm_103a.
 //
 // Pipeline of one batch (all on one stream, capturable as one CUDA graph):
-//   frame_setup   1 block, FP64: per-frame ZAMO tetrad (kerr::observerFrame), horizon, ISCO, radii
+//   frame_setup   1 block, FP64: per-frame ZAMO tetrad (kerr::observerFrame), its lowered vectors,
+//                 horizon, ISCO, capture and escape radii
 //   launch        FP64, one thread per ray: pinhole (alpha, beta) -> look -> kerr::photonFromFrame
-//                 -> E, L, Q, vr, vtheta and the first step (kerr::photonStepSize); cost bucket
-//   sort          bucket histogram / scan / scatter: queue order, most expensive bucket first
-//   trace         persistent grid; every lane owns one ray and pulls a new one from the warp's chunk
+//                 -> E, L, Q, vr, vtheta (the axis snap included); cost bucket
+//   sort          bucket histogram / scan / block-aggregated scatter: queue order, costliest first
+//   trace         persistent grid; every lane owns one ray and pulls a new one from its warp's chunk
 //                 of the device queue as soon as its ray ends (step counts vary ~100x near the
-//                 photon ring, so lanes never wait for a warp's slowest ray). Integration is
-//                 Dormand-Prince 5(4) with FSAL and dense-output event location, in FP64 (parity
-//                 mode) or FP32 (mixed mode: FP64 for launch constants, disk g, the analytic capture
-//                 test at the horizon and the periodic null-constraint re-projection)
+//                 photon ring, so lanes never wait for a warp's slowest ray). Dormand-Prince 5(4)
+//                 with FSAL and dense-output event location, in FP64 (parity mode) or FP32 (mixed
+//                 mode: FP64 for the launch constants, the disk g, the analytic capture test near
+//                 the horizon and the optional periodic radial re-projection)
 //   rescue        FP64 continuation of the rare rays the FP32 kernel hands over
 //
 // The reference's ray semantics (src/trajectory.cpp:259-392): backward march in Mino time; disk
@@ -57,18 +58,18 @@ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, doub
 // and take the most steps; bucket 0 holds them, so the queue serves the longest rays first.
 __device__ __forceinline__ uint16_t cost_key(double E, double L, double Q, int buckets) {
     if (buckets <= 1) return 0;
-    const double u = (L * L + Q) / (E * E);
-    const double d = fabs(log(fmax(u, 1e-30) / 27.0));
-    const int k = static_cast<int>(d * buckets / 3.0);
+    const float u = static_cast<float>((L * L + Q) / (E * E));
+    const float d = fabsf(__logf(fmaxf(u, 1e-30f) * (1.0f / 27.0f)));
+    const int k = static_cast<int>(d * buckets * (1.0f / 3.0f));
     return static_cast<uint16_t>(k < 0 ? 0 : (k >= buckets ? buckets - 1 : k));
 }
 
-__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, const Cons& c, const St& s, double h0,
-                                             int32_t gid, int buckets) {
-    L.E[i] = c.E; L.L[i] = c.L; L.Q[i] = c.Q;
-    L.vr[i] = s.vr; L.vth[i] = s.vtheta; L.h0[i] = h0;
+__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, double E, double Lz, double Q, double vr,
+                                             double vth, int32_t gid, int buckets) {
+    L.E[i] = E; L.L[i] = Lz; L.Q[i] = Q;
+    L.vr[i] = vr; L.vth[i] = vth;
     L.geom_id[i] = gid;
-    L.key[i] = cost_key(c.E, c.L, c.Q, buckets);
+    L.key[i] = cost_key(E, Lz, Q, buckets);
 }
 
 // ------------------------------------------------------------------------- set-up kernels ----
@@ -84,15 +85,29 @@ __global__ void frame_setup_kernel(FrameDev* frames, RayGeom* geom, int nframes,
     }
     for (int f = threadIdx.x; f < nframes; f += blockDim.x) {
         const bhk_frame_desc d = frames[f].d;
-        double u[4], e[4][4];
+        double u[4], e[4][4], g[4][4];
         zamo_four_velocity(d.a, d.r_obs, d.theta_obs, u);
         observer_frame(d.a, d.r_obs, d.theta_obs, u, e);
+        metric_tensor(d.a, d.r_obs, d.theta_obs, g);
         for (int k = 0; k < 4; ++k)
-            for (int i = 0; i < 4; ++i) frames[f].e[k][i] = e[k][i];
+            for (int i = 0; i < 4; ++i) {
+                frames[f].e[k][i] = e[k][i];
+                double acc = 0.0;
+                for (int j = 0; j < 4; ++j) acc += g[i][j] * e[k][j];
+                frames[f].el[k][i] = acc;
+            }
+        double sn, cs;
+        sincos(d.theta_obs, &sn, &cs);
+        frames[f].sigma = metric_at(d.a, d.r_obs, d.theta_obs).sigma;
+        frames[f].cs2 = cs * cs;
+        frames[f].inv_sn2 = 1.0 / dmaxd(sn * sn, 1e-18);
+        frames[f].a2 = d.a * d.a;
         geom[f] = make_geom(d.a, d.r_obs, d.theta_obs, d.phi_obs, d.r_disk_in, d.r_disk_out, p);
     }
 }
 
+// kerr::photonFromFrame for pixel (alpha, beta) of a ZAMO pinhole, with the camera's metric
+// contractions precomputed: p_mu = (g e_0)_mu - look^i (g e_i)_mu, p^r = e_0^r - look^i e_i^r.
 __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nframes, LaunchSoA L, TraceParams p,
                                      const Control* __restrict__ ctl) {
     const long long n = ctl->n_rays;
@@ -110,17 +125,25 @@ __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nf
         const double py = (f.d.beta_hi - f.d.beta_lo) / f.d.height;
         const double alpha = f.d.alpha_lo + (col + 0.5) * px;
         const double beta = f.d.beta_hi - (row + 0.5) * py;
-        const double lr = -1.0, lt = -beta / f.d.r_obs, lp = alpha / f.d.r_obs;
-        const double nn = sqrt(lr * lr + lt * lt + lp * lp);
-        const double look[3] = {lr / nn, lt / nn, lp / nn};
-        double e[4][4];
-        for (int k = 0; k < 4; ++k)
-            for (int j = 0; j < 4; ++j) e[k][j] = f.e[k][j];
-        Cons c;
-        St s;
-        photon_from_frame(f.d.a, f.d.r_obs, f.d.theta_obs, f.d.phi_obs, e, look, c, s);
-        const double h0 = photon_step_size(f.d.a, c, s, p.tol0);
-        store_launch(L, i, c, s, h0, lo, p.buckets);
+        const double lt = -beta / f.d.r_obs, lp = alpha / f.d.r_obs;
+        const double inv = 1.0 / sqrt(1.0 + lt * lt + lp * lp);
+        const double l0 = -inv, l1 = lt * inv, l2 = lp * inv;
+        const double pt = f.el[0][0] - l0 * f.el[1][0] - l1 * f.el[2][0] - l2 * f.el[3][0];
+        const double pth = f.el[0][2] - l0 * f.el[1][2] - l1 * f.el[2][2] - l2 * f.el[3][2];
+        const double pph = f.el[0][3] - l0 * f.el[1][3] - l1 * f.el[2][3] - l2 * f.el[3][3];
+        const double pr_up = f.e[0][1] - l0 * f.e[1][1] - l1 * f.e[2][1] - l2 * f.e[3][1];
+        const double E = -pt;
+        double Lz = pph;
+        const double vr = f.sigma * pr_up;
+        const double vth = pth;
+        const double a2E2 = f.a2 * E * E;
+        double Q = vth * vth + f.cs2 * (Lz * Lz * f.inv_sn2 - a2E2);
+        // kAxisSnap (src/kerr.h:115): |L| < 3e-4 sqrt(Q + a^2 E^2), compared squared.
+        if (Lz * Lz < 9e-8 * dmaxd(Q + a2E2, 0.0)) {
+            Lz = 0.0;
+            Q = vth * vth - f.cs2 * a2E2;
+        }
+        store_launch(L, i, E, Lz, Q, vr, vth, lo, p.buckets);
     }
 }
 
@@ -141,9 +164,8 @@ __global__ void launch_explicit_kernel(const double* __restrict__ a, const doubl
         Cons c;
         St s;
         photon_from_frame(ai, ri, ti, 0.0, e, look, c, s);
-        const double h0 = photon_step_size(ai, c, s, p.tol0);
         geom[i] = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
-        store_launch(L, i, c, s, h0, static_cast<int32_t>(i), p.buckets);
+        store_launch(L, i, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
     }
 }
 
@@ -172,12 +194,26 @@ __global__ void scan_kernel(SortScratch S, TraceParams p) {
     }
 }
 
-__global__ void scatter_kernel(LaunchSoA L, SortScratch S, const Control* __restrict__ ctl) {
+// Scatter in tiles of blockDim rays: ranks within a tile from shared-memory counters, one global
+// atomic per (tile, bucket) to reserve the tile's slice of each bucket.
+__global__ void scatter_kernel(LaunchSoA L, SortScratch S, TraceParams p, const Control* __restrict__ ctl) {
+    __shared__ unsigned int cnt[kMaxBuckets];
+    __shared__ unsigned int base[kMaxBuckets];
     const long long n = ctl->n_rays;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const unsigned pos = atomicAdd(&S.offs[L.key[i]], 1u);
-        S.order[pos] = static_cast<int32_t>(i);
+    const long long tiles = (n + blockDim.x - 1) / blockDim.x;
+    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+        for (int b = threadIdx.x; b < p.buckets; b += blockDim.x) cnt[b] = 0;
+        __syncthreads();
+        const long long i = t * blockDim.x + threadIdx.x;
+        const bool live = i < n;
+        const unsigned key = live ? L.key[i] : 0u;
+        const unsigned rank = live ? atomicAdd(&cnt[key], 1u) : 0u;
+        __syncthreads();
+        for (int b = threadIdx.x; b < p.buckets; b += blockDim.x)
+            if (cnt[b]) base[b] = atomicAdd(&S.offs[b], cnt[b]);
+        __syncthreads();
+        if (live) S.order[base[key] + rank] = static_cast<int32_t>(i);
+        __syncthreads();
     }
 }
 
@@ -195,24 +231,62 @@ struct Lane {
     T r_cap, r_esc, r_in, r_out, zone_top;
     int acc, rej;
     bool last_rej;
+    // FP32 only: the ray is in the southern hemisphere and y[1], y[4] hold pi - theta and -vtheta.
+    // The Kerr metric is symmetric under theta -> pi - theta, so the equations are unchanged, and
+    // both poles are approached with the full relative precision of a small angle.
+    bool south;
 };
 
+// Physical (theta, vtheta) of a lane, in FP64.
+template <typename T>
+__device__ __forceinline__ void physical_polar(const Lane<T>& s, double* th, double* vth) {
+    *th = s.south ? kPi - double(s.y[1]) : double(s.y[1]);
+    *vth = s.south ? -double(s.y[4]) : double(s.y[4]);
+}
+
+// kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
+// first step of the backward march.
+template <typename T>
+__device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol) {
+    T sn, cs;
+    Math<T>::sc(y[1], &sn, &cs);
+    sn = fabs(sn);
+    const T rs = y[0];
+    const T t = tol * fmin(fmax(rs / T(8), T(1)), T(4));
+    T h = t / (fabs(k[0]) / rs + fabs(k[1]) / fmax(sn, T(1e-4)) + fabs(k[2]) + T(1e-6));
+    h = fmin(h, sqrt(t * rs / (fabs(k[3]) + T(1e-6))));
+    h = fmin(h, sqrt(t * fmax(sn, T(1e-4)) / (fabs(k[4]) + T(1e-6))));
+    return -h;
+}
+
+// Starts a lane on a ray. h == 0 means a fresh launch: the first step comes from kerr::photonStepSize.
 template <typename T>
 __device__ __forceinline__ void lane_begin(Lane<T>& s, const RayGeom& g, double E, double L, double Q,
-                                           const double y[5], double h) {
+                                           const double y[5], double h, const TraceParams& p) {
     s.a = g.a; s.E = E; s.L = L; s.Q = Q;
     s.c.set(g.a, E, L, Q);
+    s.south = sizeof(T) == 4 && y[1] > 0.5 * kPi;
 #pragma unroll
     for (int i = 0; i < 5; ++i) s.y[i] = T(y[i]);
+    if (s.south) {
+        s.y[1] = T(kPi - y[1]);
+        s.y[4] = T(-y[4]);
+    }
     rhs(s.c, s.y, s.k[0]);
-    s.h = T(h);
+    if (h == 0.0) {
+        if constexpr (sizeof(T) == 8) s.h = first_step<T>(s.y, s.k[0], p.tol0);
+        else s.h = first_step<T>(s.y, s.k[0], p.tol0_f);
+    } else {
+        s.h = T(h);
+    }
     s.r_cap = T(g.r_cap); s.r_esc = T(g.r_esc); s.r_in = T(g.r_in); s.r_out = T(g.r_out);
     s.zone_top = T(g.zone_top);
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
 __device__ __forceinline__ void write_out(const Outputs& o, long long ray, int outcome, double rd, double pd, double g,
-                                          double ti, double pi, int steps) {
+                                          double ti, double pi, int steps, int rejected) {
+    if (o.rejected) o.rejected[ray] = rejected;
     if (o.outcome) o.outcome[ray] = static_cast<uint8_t>(outcome);
     if (o.r_disk) o.r_disk[ray] = rd;
     if (o.phi_disk) o.phi_disk[ray] = pd;
@@ -222,18 +296,39 @@ __device__ __forceinline__ void write_out(const Outputs& o, long long ray, int o
     if (o.steps) o.steps[ray] = steps;
 }
 
-// Fraction of the step where the dense output of component i equals target (bisection).
+// Fraction of the step where the dense output of component i equals target: Newton on the quartic
+// continuous extension from linear interpolation, kept inside the sign-change bracket [lo, hi]
+// (bisection whenever Newton leaves it), until the step in s falls below the type's resolution.
 template <typename T>
 __device__ __forceinline__ T locate(const T* y0, const T* y1, const T k[7][5], T h, int i, T target) {
-    constexpr int iters = sizeof(T) == 8 ? 60 : 30;
+    constexpr int iters = sizeof(T) == 8 ? 64 : 32;
+    constexpr T tiny = sizeof(T) == 8 ? T(1e-15) : T(1e-7);
+    const T yd = y1[i] - y0[i];
+    const T b = h * k[0][i] - yd;
+    const T c4 = yd - h * k[6][i] - b;
+    const T c5 = h * (T(DP::d1) * k[0][i] + T(DP::d3) * k[2][i] + T(DP::d4) * k[3][i] + T(DP::d5) * k[4][i] +
+                      T(DP::d6) * k[5][i] + T(DP::d7) * k[6][i]);
+    const T f0 = y0[i] - target;
+    const bool neg0 = f0 < T(0);
     T lo = T(0), hi = T(1);
-    const bool neg0 = (y0[i] - target) < T(0);
+    T s = fmin(fmax(-f0 / yd, T(0)), T(1));
     for (int it = 0; it < iters; ++it) {
-        const T mid = T(0.5) * (lo + hi);
-        const T fm = dense(y0[i], y1[i], k, h, i, mid) - target;
-        if ((fm < T(0)) == neg0) lo = mid; else hi = mid;
+        const T s1 = T(1) - s;
+        const T u = b + s * (c4 + s1 * c5);
+        const T du = c4 + (T(1) - T(2) * s) * c5;
+        const T w = yd + s1 * u;
+        const T dw = -u + s1 * du;
+        const T f = f0 + s * w;
+        const T df = w + s * dw;
+        if (f == T(0)) break;
+        if ((f < T(0)) == neg0) lo = s; else hi = s;
+        T sn = s - f / df;
+        if (!(sn > lo && sn < hi)) sn = T(0.5) * (lo + hi);
+        const bool done = fabs(sn - s) <= tiny || hi - lo <= tiny;
+        s = sn;
+        if (done) break;
     }
-    return T(0.5) * (lo + hi);
+    return s;
 }
 
 // One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
@@ -269,8 +364,11 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     for (int i = 0; i < 5; ++i)
         y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
                               T(DP::b5) * s.k[4][i] + T(DP::b6) * s.k[5][i]);
-    rhs(s.c, y5, s.k[6]);
-    const T rtol = T(p.rtol);
+    Proj<T> pj;
+    rhs<T, !F64>(s.c, y5, s.k[6], &pj);
+    T rtol;
+    if constexpr (F64) rtol = p.rtol;
+    else rtol = p.rtol_f;
     T acc = T(0);
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
@@ -300,7 +398,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         else fac = isfinite(e2) ? fmaxf(0.2f, 0.9f * exp2f(-0.1f * __log2f(e2))) : 0.2f;
         s.h = h * fac;
         if (s.rej >= p.max_steps) {
-            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
             atomicAdd(&ctl->stats[2], 1ull);
             return kFinished;
         }
@@ -315,7 +413,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     }
     if (!isfinite(s.y[0])) {
         if constexpr (F64) {
-            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
             atomicAdd(&ctl->stats[2], 1ull);
             return kFinished;
         } else {
@@ -330,19 +428,19 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         double g;
         if (rc >= s.r_in && rc <= s.r_out && disk_redshift(s.a, s.E, s.L, double(rc), &g)) {
             const double ph = wrap_2pi(double(dense(prev[2], s.y[2], s.k, h, 2, sg)));
-            write_out(out, ray, BHK_RAY_DISK, double(rc), ph, g, nan_d(), nan_d(), s.acc);
+            write_out(out, ray, BHK_RAY_DISK, double(rc), ph, g, nan_d(), nan_d(), s.acc, s.rej);
             return kFinished;
         }
     }
     const bool falling = s.y[0] < prev[0];
     if (falling) {
         if (s.y[0] < s.r_cap) {
-            write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+            write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
             return kFinished;
         }
         if (s.y[0] < s.zone_top) {
             if (no_radial_root_below(s.a, s.E, s.L, s.Q, double(s.y[0]), p.eps)) {
-                write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+                write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
                 return kFinished;
             }
             if constexpr (!F64) return kRescue;
@@ -354,16 +452,20 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
         rhs(s.c, x, kk);
         T v[3];
+        if (s.south) {  // back to the physical angle: cos(pi - t) = -cos t, d(pi - t) = -dt
+            x[1] = T(kPi) - x[1];
+            x[4] = -x[4];
+        }
         cartesian_velocity<T>(T(s.a), x[0], x[1], x[2], x[3], x[4], kk[2], v);
         const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
         const double ti = double(acos(dz));
         const double pi = double(atan2(-v[1] / nrm, -v[0] / nrm));
-        write_out(out, ray, BHK_RAY_ESCAPED, nan_d(), nan_d(), nan_d(), ti, pi, s.acc);
+        write_out(out, ray, BHK_RAY_ESCAPED, nan_d(), nan_d(), nan_d(), ti, pi, s.acc, s.rej);
         return kFinished;
     }
-    // Pole reflection (kerr::normalizeAngles) and constraint re-projection, carrying the FSAL
-    // derivative: under theta -> -theta (or 2 pi - theta) Theta'(theta) changes sign.
+    // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
+    // carrying the FSAL derivative: under theta -> -theta (or 2 pi - theta) Theta'(theta) changes sign.
     if constexpr (F64) {
         St st{0.0, s.y[0], s.y[1], s.y[2], s.y[3], s.y[4]};
         if (normalize_angles(st)) s.k[6][4] = -s.k[6][4];
@@ -371,19 +473,31 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         enforce_constraints(s.a, cc, st);
         s.y[1] = st.theta; s.y[2] = st.phi; s.y[3] = st.vr; s.y[4] = st.vtheta;
     } else {
-        const T pi_f = T(kPi);
-        if (s.y[1] < T(0) || s.y[1] > pi_f) {
-            s.y[1] = s.y[1] < T(0) ? -s.y[1] : T(2 * kPi) - s.y[1];
-            s.y[2] += pi_f;
+        if (s.y[1] < T(0)) {  // over the pole of this hemisphere
+            s.y[1] = -s.y[1];
+            s.y[2] += T(kPi);
             s.y[4] = -s.y[4];
             s.k[6][4] = -s.k[6][4];
         }
+        if (s.y[1] > T(0.5 * kPi)) {  // across the equator: the other hemisphere's representation
+            s.y[1] = T(kPi) - s.y[1];
+            s.y[4] = -s.y[4];
+            s.k[6][4] = -s.k[6][4];
+            s.south = !s.south;
+        }
+        // Every step, from the FSAL stage's potentials: keeps the FP32 rounding of vr ~ r^2 made
+        // far out from becoming an O(1) error near the hole.
+        if (pj.R > pj.Rz) s.y[3] = copysignf(sqrt_approx(pj.R), s.y[3]);
+        if (pj.Th > pj.Thz) s.y[4] = copysignf(sqrt_approx(pj.Th), s.y[4]);
         if (reproject) {
-            St st{0.0, double(s.y[0]), double(s.y[1]), double(s.y[2]), double(s.y[3]), double(s.y[4])};
-            const Cons cc{s.E, s.L, s.Q, 0.0};
-            enforce_constraints(s.a, cc, st);
-            s.y[3] = T(st.vr);
-            s.y[4] = T(st.vtheta);
+            // Optional FP64 radial re-projection: R(r) = P^2 - Delta K evaluated in FP64.
+            const double r = double(s.y[0]);
+            const double delta = r * r - 2.0 * r + s.a * s.a;
+            const double P = s.E * (r * r + s.a * s.a) - s.a * s.L;
+            const double x = s.L - s.a * s.E;
+            const double K = x * x + s.Q;
+            const double R = P * P - delta * K;
+            if (R > 0.05 * (P * P + fabs(delta) * K)) s.y[3] = T(copysign(sqrt(R), double(s.y[3])));
         }
     }
 #pragma unroll
@@ -395,9 +509,19 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     else fac = e2 > 0.0f ? 0.9f * exp2f(-0.1f * __log2f(e2)) : 5.0f;
     fac = fmin(fmax(fac, T(0.2)), s.last_rej ? T(1) : T(5));
     s.h = h * fac;
+    if constexpr (!F64) {
+        // Outgoing, r(tau) ~ 1 / (E (tau_inf - tau)) runs into a pole at finite Mino time: the step
+        // the tolerance allows shrinks geometrically and the error-per-step controller, which only
+        // looks back, overshoots into a rejection every other step. Cap the step at a fixed fraction
+        // of the Mino time left to the pole, ~ r / |vr|.
+        if (p.pole_frac > 0.0f && s.h * s.y[3] > 0.0f) {
+            const float cap = p.pole_frac * s.y[0] * rcp_approx(fabsf(s.y[3]));
+            s.h = copysignf(fminf(fabsf(s.h), cap), s.h);
+        }
+    }
     s.last_rej = false;
     if (s.acc >= p.max_steps) {
-        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc);
+        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
         atomicAdd(&ctl->stats[2], 1ull);
         return kFinished;
     }
@@ -414,14 +538,18 @@ __device__ __forceinline__ void push_rescue(Rescue* rescue, unsigned cap, Contro
         r.h = h; r.ray = ray; r.accepted = acc; r.rejected = rej; r.from_launch = from_launch; r.pad = 0;
         rescue[idx] = r;
     } else {
-        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), acc);
+        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), acc, rej);
         atomicAdd(&ctl->stats[2], 1ull);
     }
 }
 
-template <typename T>
-__global__ void trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __restrict__ order,
-                             Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl) {
+// kMinBlocks > 0 caps registers through __launch_bounds__(128, kMinBlocks) (blocks of <= 128 threads):
+// 5 -> <= 102 registers (20 warps/SM), 6 -> <= 85 (24 warps/SM); 0 leaves the compiler free (blocks
+// of <= 256 threads).
+template <typename T, int kMinBlocks>
+__global__ void __launch_bounds__(kMinBlocks > 0 ? 128 : 256, kMinBlocks > 0 ? kMinBlocks : 1)
+trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __restrict__ order,
+             Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl) {
     const int lane = threadIdx.x & 31;
     const long long n = ctl->n_rays;
     const unsigned lt = lanemask_lt();
@@ -452,7 +580,7 @@ __global__ void trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, cons
                 ray = order ? order[q] : q;
                 const RayGeom& g = geom[L.geom_id[ray]];
                 const double y0[5] = {g.r0, g.th0, g.ph0, L.vr[ray], L.vth[ray]};
-                lane_begin(s, g, L.E[ray], L.L[ray], L.Q[ray], y0, L.h0[ray]);
+                lane_begin(s, g, L.E[ray], L.L[ray], L.Q[ray], y0, 0.0, p);
             }
             const int served = __popc(need) < avail ? __popc(need) : avail;
             pool_pos += served;
@@ -474,9 +602,10 @@ __global__ void trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, cons
                         y[0] = g.r0; y[1] = g.th0; y[2] = g.ph0; y[3] = L.vr[ray]; y[4] = L.vth[ray];
                     } else {
                         for (int i = 0; i < 5; ++i) y[i] = double(s.y[i]);
+                        physical_polar(s, &y[1], &y[4]);
                     }
-                    push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? L.h0[ray] : double(s.h),
-                                restart ? 0 : s.acc, restart ? 0 : s.rej, restart ? 1 : 0, out);
+                    push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? 0.0 : double(s.h), restart ? 0 : s.acc,
+                                restart ? 0 : s.rej, restart ? 1 : 0, out);
                 }
                 ray = -1;
             }
@@ -509,7 +638,7 @@ __global__ void rescue_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, Out
             enforce_constraints(g.a, cc, st);
             y[1] = st.theta; y[2] = st.phi; y[3] = st.vr; y[4] = st.vtheta;
         }
-        lane_begin(s, g, L.E[r.ray], L.L[r.ray], L.Q[r.ray], y, r.h);
+        lane_begin(s, g, L.E[r.ray], L.L[r.ray], L.Q[r.ray], y, r.h, p);
         s.acc = r.accepted;
         s.rej = r.rejected;
         int res = kContinue;
@@ -570,13 +699,25 @@ void launch_rays_explicit(const double* a, const double* r_obs, const double* th
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
     hist_kernel<<<grid, 256, 0, s>>>(L, S, p, ctl);
     scan_kernel<<<1, 32, 0, s>>>(S, p);
-    scatter_kernel<<<grid, 256, 0, s>>>(L, S, ctl);
+    scatter_kernel<<<grid, 256, 0, s>>>(L, S, p, ctl);
 }
 
-void launch_trace(bool fp64, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out, Rescue* rescue,
-                  unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid, cudaStream_t s) {
-    if (fp64) trace_kernel<double><<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
-    else trace_kernel<float><<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
+namespace {
+using TraceFn = void (*)(LaunchSoA, const RayGeom*, const int32_t*, Outputs, Rescue*, unsigned, TraceParams, Control*);
+
+// Variant by precision and register cap (see trace_kernel).
+TraceFn trace_variant(bool fp64, int regcap) {
+    if (fp64) return trace_kernel<double, 0>;
+    if (regcap == 1) return trace_kernel<float, 5>;
+    if (regcap == 2) return trace_kernel<float, 6>;
+    return trace_kernel<float, 0>;
+}
+}  // namespace
+
+void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
+                  Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
+                  cudaStream_t s) {
+    trace_variant(fp64, regcap)<<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
 }
 
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
@@ -584,10 +725,10 @@ void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue
     rescue_kernel<<<152, 64, 0, s>>>(L, geom, out, rescue, rescue_cap, p, ctl);
 }
 
-int trace_blocks_per_sm(bool fp64, int block) {
+int trace_blocks_per_sm(bool fp64, int regcap, int block) {
+    if (block > 256 || (regcap > 0 && (fp64 || block > 128))) return 0;
     int n = 0;
-    if (fp64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel<double>, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel<float>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_variant(fp64, regcap), block, 0);
     return n;
 }
 

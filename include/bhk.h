@@ -113,11 +113,16 @@ typedef struct {
     int32_t max_steps;      /* accepted-step cap per ray; 0 -> 20000 */
     double r_escape;        /* escaped once r > max(r_escape, 1.5 r_obs) while rising; 0 -> 1000 */
     double capture_eps;     /* captured once r < r_+(1 + capture_eps) while falling; 0 -> 1e-6 */
-    int32_t reproject_every;/* mixed: FP64 re-projection onto the null constraint every N steps; 0 -> 16, <0 off */
+    int32_t reproject_every;/* mixed: besides the FP32 re-projection every step, an FP64 radial one every N
+                               iterations of a warp (results then depend on the launch shape); 0 = off */
     int32_t block;          /* threads per block of the tracer; 0 -> autotuned or 128 */
     int32_t chunk;          /* rays a warp takes from the queue at a time; 0 -> autotuned or 32 */
     int32_t sort_buckets;   /* rays pre-sorted into this many cost buckets; 0 -> autotuned or 64; 1 = none */
     int32_t use_graph;      /* 1: replay the whole batch as one captured CUDA graph */
+    int32_t reg_budget;     /* mixed tracer variant: 0 autotuned (else uncapped), 1: <= 102 registers per
+                               thread (20 warps/SM, blocks <= 128), 2: <= 85 (24 warps/SM), 3: uncapped */
+    double pole_step_frac;  /* mixed: outgoing steps capped at this fraction of the Mino time left before
+                               r runs off to infinity (~ r/|vr|); 0 -> 0.1 (rtol/1e-6)^(1/5), < 0 off */
 } bhk_trace_opts;
 
 /* Per-ray outputs, structure of arrays, n entries each (device memory unless stated). Any pointer
@@ -130,13 +135,14 @@ typedef struct {
     double* theta_inf;   /* escape direction, backward tangent at r_escape: acos(d_z) */
     double* phi_inf;     /*                                                 atan2(d_y, d_x) */
     int32_t* steps;      /* accepted integration steps */
+    int32_t* rejected;   /* rejected integration steps */
 } bhk_rays_out;
 
 /* Statistics of the last trace call on a context (filled at the end of that call's stream work). */
 typedef struct {
     int64_t rays, accepted_steps, rejected_steps, rescued, unfinished;
-    int32_t block, chunk, sort_buckets, grid;
-    double kernel_ms;    /* tracer kernel time measured with CUDA events (when opts requested it) */
+    int32_t block, chunk, sort_buckets, grid, reg_budget, pad;
+    double kernel_ms;    /* tracer + rescue kernel time, CUDA events on the launching stream */
 } bhk_trace_stats;
 
 /* Traces every pixel of nframes frames (host descriptors) in one persistent launch. Ray i of frame f

@@ -34,9 +34,12 @@ def band_mask(oracle, g, a, r_obs, deg, width=1e-3):
     return po.band_distance(al, be, ca, cb) > width
 
 
-def errors(out, ref):
+def errors(out, ref, mask=None):
     d = (out["outcome"] == bhk.DISK) & (ref["outcome"] == bhk.DISK)
     e = (out["outcome"] == bhk.ESCAPED) & (ref["outcome"] == bhk.ESCAPED)
+    if mask is not None:
+        d &= mask
+        e &= mask
     ang = lambda x, y: np.abs(np.angle(np.exp(1j * (x - y))))  # noqa: E731
     res = {
         "r_disk": np.max(np.abs(out["r_disk"][d] / ref["r_disk"][d] - 1), initial=0.0),
@@ -83,17 +86,19 @@ def test_fp64_matches_oracle_dp5(ctx, oracle, golden, name, a, r_obs, deg, r_out
 
 @pytest.mark.parametrize("name,a,r_obs,deg,r_out", CASES)
 def test_mixed_precision_errors_vs_fp64(ctx, oracle, golden, name, a, r_obs, deg, r_out):
+    """FP32 integration (rtol 1e-6) against the reference fixture, outside a 1e-2 M band of the
+    critical curve: near the photon ring rounding grows by e^pi per half orbit."""
     g = golden(name)
     f = frame_from_fixture(g, a, r_obs, deg, r_out)
     out = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6)))
     st = ctx.stats()
     outside = band_mask(oracle, g, a, r_obs, deg, 1e-2)
     agree = np.mean(out["outcome"][outside] == g["outcome"][outside])
-    err = errors(out, g)
+    err = errors(out, g, outside)
     print(name, "mixed vs reference RK4(1e-4): outcome agreement", agree, err, "rescued", st["rescued"])
-    assert agree >= 0.999
+    assert agree == 1.0
     assert err["r_disk"] < 1e-4 and err["g"] < 1e-4
-    assert err["phi_disk"] < 1e-3
+    assert err["phi_disk"] < 1e-4
     assert err["theta_inf"] < 1e-4 and err["phi_inf"] < 1e-4
     assert st["unfinished"] == 0
 
@@ -117,10 +122,10 @@ def test_launch_shape_and_order_do_not_change_results(ctx, prec):
     graph replay leave every output bit-identical."""
     frames = [bhk.frame_c1(48, 40)]
     base = host(ctx.trace_frames(frames, bhk.TraceOpts(prec, block=128, chunk=32, sort_buckets=1)))
-    for blk, ch, bu, graph in ((64, 1, 64, False), (256, 256, 512, False), (128, 32, 64, True),
-                               (128, 32, 64, True)):
+    for blk, ch, bu, graph, rb in ((64, 1, 64, False, 1), (256, 256, 512, False, 3), (128, 32, 64, True, 2),
+                                   (128, 32, 64, True, 2)):
         got = host(ctx.trace_frames(frames, bhk.TraceOpts(prec, block=blk, chunk=ch, sort_buckets=bu,
-                                                          use_graph=graph)))
+                                                          use_graph=graph, reg_budget=rb)))
         for k in bhk.FIELDS:
             np.testing.assert_array_equal(got[k], base[k], err_msg=f"{k} {blk} {ch} {bu} {graph}")
 
@@ -159,7 +164,7 @@ def test_invalid_frames_are_rejected(ctx):
         ctx.trace_frames([bhk.Frame(1.2, 50, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())
     assert e.value.status == bhk.EINVAL
     with pytest.raises(bhk.BhkError):
-        ctx.trace_frames([bhk.Frame(0.9, 1.5, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())
+        ctx.trace_frames([bhk.Frame(0.9, 1.2, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())  # inside r_+
     with pytest.raises(bhk.BhkError):
         ctx.trace_frames([bhk.Frame(0.9, 50, 1.0, 0, 4, -1, 1, -1, 1)], bhk.TraceOpts())
     with pytest.raises(bhk.BhkError):
@@ -169,6 +174,7 @@ def test_invalid_frames_are_rejected(ctx):
 def test_autotune_picks_a_valid_shape(ctx):
     st = ctx.autotune([bhk.frame_c1(64, 64)], bhk.TraceOpts("mixed"))
     assert st["block"] in (64, 128, 256) and st["chunk"] in (1, 32, 256) and st["sort_buckets"] in (1, 64, 512)
+    assert st["reg_budget"] in (1, 2, 3)
     assert st["kernel_ms"] > 0
 
 
