@@ -149,6 +149,8 @@ def lib() -> C.CDLL:
                                    C.POINTER(StatsC)]),
         "bhk_critical_curve": (C.c_int, [d, d, d, C.c_int32, vp, vp, C.c_int32, C.POINTER(C.c_int32)]),
         "bhk_fp32_fma_peak": (C.c_int, [C.c_int, C.POINTER(d)]),
+        "bhk_trace_frames_static": (C.c_int, [C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
+                                              C.POINTER(RaysOutC), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -28,6 +28,7 @@ UNITS = {
     "bhk_api.cu": [],
     "bhk_steps.cu": ["--fmad=false"],
     "bhk_diag.cu": [],
+    "bhk_static.cu": [],
 }
 EXTRA_UNITS: dict[str, list[str]] = {}
 

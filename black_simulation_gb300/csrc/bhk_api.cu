@@ -62,6 +62,8 @@ constexpr double kFlopsPerStep = 772.0;  // FP32 DP5 step, counted from bhk_trac
 
 }  // namespace
 
+void bhk::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct bhk_context {
     int device = 0;
     int num_sms = 0;

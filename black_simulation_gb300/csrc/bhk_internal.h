@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 #include "../../include/bhk.h"
@@ -90,6 +92,9 @@ void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue
 int trace_blocks_per_sm(bool fp64, int regcap, int block);  // 0 when the pair is not allowed
 void launch_critical_curve(double a, double r_obs, double theta_obs, int samples, double* alpha, double* beta,
                            int* valid, cudaStream_t s);
+
+// Sets the text bhk_last_error() returns on this thread (bhk_api.cu).
+void set_last_error(const std::string& msg);
 
 // ---- per-step mirrors (bhk_steps.cu) ----
 cudaError_t steps_derivatives(double a, const bhk_constants* c, const bhk_state* s, bhk_derivatives_t* d, int64_t n,

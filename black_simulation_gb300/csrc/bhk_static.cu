@@ -1,0 +1,192 @@
+// bhk_static.cu -- bhk_trace_frames_static: the batch tracer without any device allocation.
+//
+// Who needs it: callers that may not call cudaMalloc themselves or have the library call it on
+// their behalf -- a host framework that owns the whole device-memory budget through its own pool
+// and forbids side allocations, or a per-frame render loop where cudaMalloc/cudaFree would
+// synchronise the device and stall the frame. This entry point takes the caller's output buffers
+// and keeps every piece of working memory (launch records, queue counter, frame tetrads, rescue
+// list) in one fixed array in the device image of libbhk, reserved when the library is loaded.
+//
+// Costs and limits of that choice:
+//  - the array holds kStaticMaxRays rays and kStaticMaxFrames frames per call (4.6 MB), and
+//    every GPU that loads libbhk keeps it until the process exits;
+//  - all calls share the one array, whose contents persist from the previous call. The control
+//    block (queue counter, statistics) is cleared at the start of each call; everything else is
+//    rewritten before it is read. Calls that overlap on the GPU (two streams, or two host threads
+//    without ordering between them) race on the array: order them on one stream.
+//  - the first call on a device looks up the array's device address (cudaGetSymbolAddress with
+//    that device current) and caches it; make that first call before any stream capture.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "bhk_internal.h"
+
+namespace bhk {
+namespace {
+
+constexpr int kStaticMaxRays = 65536;
+constexpr int kStaticMaxFrames = 64;
+constexpr int kStaticRescue = kStaticMaxRays / 4 + 1024;
+constexpr int kMaxDevices = 64;
+
+// Layout of the working memory inside the static array (offsets, 256-byte aligned).
+struct Layout {
+    size_t ctl, hist, offs, frames, geom, E, L, Q, vr, vth, gid, key, order, rescue, total;
+};
+
+constexpr size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+constexpr Layout make_layout() {
+    Layout l{};
+    size_t o = 0;
+    l.ctl = o; o = up256(o + sizeof(Control));
+    l.hist = o; o = up256(o + sizeof(unsigned) * kMaxBuckets);
+    l.offs = o; o = up256(o + sizeof(unsigned) * kMaxBuckets);
+    l.frames = o; o = up256(o + sizeof(FrameDev) * kStaticMaxFrames);
+    l.geom = o; o = up256(o + sizeof(RayGeom) * kStaticMaxFrames);
+    l.E = o; o = up256(o + sizeof(double) * kStaticMaxRays);
+    l.L = o; o = up256(o + sizeof(double) * kStaticMaxRays);
+    l.Q = o; o = up256(o + sizeof(double) * kStaticMaxRays);
+    l.vr = o; o = up256(o + sizeof(double) * kStaticMaxRays);
+    l.vth = o; o = up256(o + sizeof(double) * kStaticMaxRays);
+    l.gid = o; o = up256(o + sizeof(int32_t) * kStaticMaxRays);
+    l.key = o; o = up256(o + sizeof(uint16_t) * kStaticMaxRays);
+    l.order = o; o = up256(o + sizeof(int32_t) * kStaticMaxRays);
+    l.rescue = o; o = up256(o + sizeof(Rescue) * kStaticRescue);
+    l.total = o;
+    return l;
+}
+
+constexpr Layout kLayout = make_layout();
+
+// The working memory of bhk_trace_frames_static, in the device image: no allocation at run time.
+static __device__ __align__(256) unsigned char g_static_scratch[kLayout.total];
+
+bhk_status fail(bhk_status s, const std::string& m) {
+    set_last_error(m);
+    return s;
+}
+
+// Frame descriptors travel as a kernel parameter (well under the 32 KB parameter limit).
+struct FrameBatch {
+    bhk_frame_desc f[kStaticMaxFrames];
+    int n;
+};
+
+__global__ void stage_frames_kernel(FrameBatch batch, FrameDev* frames) {
+    for (int i = threadIdx.x; i < batch.n; i += blockDim.x) {
+        FrameDev fd;
+        memset(&fd, 0, sizeof(fd));
+        fd.d = batch.f[i];
+        frames[i] = fd;
+    }
+}
+
+std::mutex g_addr_mu;
+void* g_addr[kMaxDevices] = {};
+
+// Device address of the static array on the current device, looked up once per device.
+bhk_status scratch_address(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_addr_mu);
+    if (!g_addr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_addr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_addr[device]);
+    return BHK_OK;
+}
+
+}  // namespace
+}  // namespace bhk
+
+using namespace bhk;
+
+extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int32_t nframes,
+                                              const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream) {
+    if (!frames || nframes <= 0 || !out) return fail(BHK_EINVAL, "frames, nframes and out are required");
+    if (nframes > kStaticMaxFrames)
+        return fail(BHK_EINVAL, "bhk_trace_frames_static takes at most 64 frames per call");
+    int64_t total = 0;
+    for (int i = 0; i < nframes; ++i) {
+        const bhk_frame_desc& f = frames[i];
+        if (f.width <= 0 || f.height <= 0) return fail(BHK_EINVAL, "frame with non-positive size");
+        if (!(std::fabs(f.a) < 1.0)) return fail(BHK_EINVAL, "spin must satisfy |a| < 1");
+        if (!(f.r_obs > 1.0 + std::sqrt(1.0 - f.a * f.a)))
+            return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole)");
+        if (!(f.theta_obs > 0.0 && f.theta_obs < M_PI)) return fail(BHK_EINVAL, "theta_obs outside (0, pi)");
+        if (!(f.r_disk_out > 0.0)) return fail(BHK_EINVAL, "r_disk_out must be positive");
+        total += static_cast<int64_t>(f.width) * f.height;
+    }
+    if (total > kStaticMaxRays)
+        return fail(BHK_EINVAL, "bhk_trace_frames_static takes at most 65536 rays per call (the static scratch)");
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices)
+        return fail(BHK_ECUDA, "no usable CUDA device");
+    unsigned char* base = nullptr;
+    bhk_status st = scratch_address(device, &base);
+    if (st != BHK_OK) return st;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+
+    bhk_trace_opts d{};
+    const bhk_trace_opts& o = opts ? *opts : d;
+    TraceParams p{};
+    const bool fp64 = o.precision == BHK_PREC_FP64;
+    p.rtol = o.rtol > 0.0 ? o.rtol : (fp64 ? 1e-10 : 1e-6);
+    p.eps = o.capture_eps > 0.0 ? o.capture_eps : 1e-6;
+    p.r_escape = o.r_escape > 0.0 ? o.r_escape : 1000.0;
+    p.max_steps = o.max_steps > 0 ? o.max_steps : 20000;
+    p.reproject_every = o.reproject_every > 0 ? o.reproject_every : 0;
+    p.tol0 = std::fmin(std::fmax(std::pow(p.rtol, 0.2), 1e-3), 0.05);
+    p.rtol_f = static_cast<float>(p.rtol);
+    p.tol0_f = static_cast<float>(p.tol0);
+    p.pole_frac = o.pole_step_frac > 0.0 ? static_cast<float>(o.pole_step_frac)
+                  : (o.pole_step_frac < 0.0 ? 0.0f
+                     : static_cast<float>(std::fmin(0.5, 0.1 * std::pow(p.rtol / 1e-6, 0.2))));
+    int block = o.block > 0 ? std::min(o.block, 256) : 128;
+    p.chunk = o.chunk > 0 ? o.chunk : 32;
+    p.buckets = std::min(o.sort_buckets > 0 ? o.sort_buckets : 1, kMaxBuckets);
+    const int rb = o.reg_budget > 0 ? o.reg_budget : 2;
+    const int regcap = (fp64 || rb >= 3) ? 0 : rb;
+    if (regcap > 0) block = std::min(block, 128);
+    const int grid = std::max(1, trace_blocks_per_sm(fp64, regcap, block)) * sms;
+
+    Control* ctl = reinterpret_cast<Control*>(base + kLayout.ctl);
+    FrameDev* fdev = reinterpret_cast<FrameDev*>(base + kLayout.frames);
+    RayGeom* geom = reinterpret_cast<RayGeom*>(base + kLayout.geom);
+    LaunchSoA L{reinterpret_cast<double*>(base + kLayout.E), reinterpret_cast<double*>(base + kLayout.L),
+                reinterpret_cast<double*>(base + kLayout.Q), reinterpret_cast<double*>(base + kLayout.vr),
+                reinterpret_cast<double*>(base + kLayout.vth), reinterpret_cast<int32_t*>(base + kLayout.gid),
+                reinterpret_cast<uint16_t*>(base + kLayout.key)};
+    SortScratch S{reinterpret_cast<unsigned*>(base + kLayout.hist), reinterpret_cast<unsigned*>(base + kLayout.offs),
+                  reinterpret_cast<int32_t*>(base + kLayout.order)};
+    Rescue* rescue = reinterpret_cast<Rescue*>(base + kLayout.rescue);
+    Outputs outs{out->outcome, out->r_disk, out->phi_disk, out->g, out->theta_inf, out->phi_inf, out->steps,
+                 out->rejected};
+
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    FrameBatch batch;
+    std::memset(&batch, 0, sizeof(batch));
+    for (int i = 0; i < nframes; ++i) batch.f[i] = frames[i];
+    batch.n = nframes;
+    cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(Control), s);
+    if (e == cudaSuccess && p.buckets > 1) e = cudaMemsetAsync(S.hist, 0, sizeof(unsigned) * kMaxBuckets, s);
+    if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("clearing the control block: ") + cudaGetErrorString(e));
+    stage_frames_kernel<<<1, 64, 0, s>>>(batch, fdev);
+    launch_frame_setup(fdev, fdev, geom, nframes, p, ctl, s);
+    launch_rays_frames(fdev, geom, nframes, L, p, ctl, sms * 8, s);
+    const int32_t* order = nullptr;
+    if (p.buckets > 1) {
+        launch_sort(L, S, p, ctl, sms * 8, s);
+        order = S.order;
+    }
+    launch_trace(fp64, regcap, L, geom, order, outs, rescue, kStaticRescue, p, ctl, block, grid, s);
+    if (!fp64) launch_rescue(L, geom, outs, rescue, kStaticRescue, p, ctl, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
+    return BHK_OK;
+}

@@ -172,6 +172,20 @@ bhk_status bhk_autotune(bhk_context* ctx, const bhk_frame_desc* frames, int32_t 
 bhk_status bhk_critical_curve(double a, double r_obs, double theta_obs, int32_t samples, double* alpha, double* beta,
                               int32_t cap, int32_t* n);
 
+/* bhk_trace_frames without any device allocation (no counterpart in the reference). For callers that
+ * may not allocate device memory -- a host framework that owns the whole device-memory budget
+ * through its own pool, or a per-frame render loop where cudaMalloc/cudaFree would synchronise the
+ * device. Outputs are the caller's device buffers; all working memory lives in one fixed array in
+ * libbhk's device image (4.6 MB, held by every GPU that loads the library until exit).
+ * Limits: at most 65536 rays and 64 frames per call; larger requests return BHK_EINVAL. No context:
+ * the tracer runs on the current device and on `stream` (NULL = the legacy default stream) with the
+ * opts given (0 fields take the context defaults; no autotuning). All calls share the array, which
+ * keeps the previous call's contents (the control block is cleared at the start of each call):
+ * calls that overlap on the GPU race, so order them on one stream. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make it before any stream capture. */
+bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int32_t nframes, const bhk_trace_opts* opts,
+                                   const bhk_rays_out* out, void* stream);
+
 /* FLOPs one accepted FP32 Dormand-Prince step costs in the mixed tracer, counted from its source. */
 double bhk_flops_per_step(void);
 
