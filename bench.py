@@ -231,7 +231,11 @@ def run_ours(args):
     ctx = bhk.Context(local)
     work_stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(work_stream)
-    tuned = ctx.autotune(frames, opts) if args.autotune else None
+    if args.block or args.chunk or args.buckets or args.reg_budget:
+        opts.block, opts.chunk, opts.sort_buckets, opts.reg_budget = args.block, args.chunk, args.buckets, args.reg_budget
+        tuned = {"block": args.block, "chunk": args.chunk, "sort_buckets": args.buckets, "reg_budget": args.reg_budget}
+    else:
+        tuned = ctx.autotune(frames, opts) if args.autotune else None
     out = bhk.alloc_outputs(n_rays, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
     stream = torch.cuda.current_stream()
@@ -319,6 +323,10 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=int, default=1, help="divide the frame size (profiling captures)")
+    ap.add_argument("--block", type=int, default=0, help="fixed launch shape instead of autotuning")
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--buckets", type=int, default=0)
+    ap.add_argument("--reg-budget", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -77,6 +77,9 @@ struct bhk_context {
     double *E = nullptr, *L = nullptr, *Q = nullptr, *vr = nullptr, *vth = nullptr;
     int32_t* gid = nullptr;
     uint16_t* key = nullptr;
+    float4* cf = nullptr;
+    float2* vf = nullptr;
+    size_t cap_cf = 0, cap_vf = 0;
     int32_t* order = nullptr;
     Rescue* rescue = nullptr;
     RayGeom* geom = nullptr;
@@ -168,12 +171,14 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     if (e == cudaSuccess) e = grow(&c->vth, &c->cap_vth, rays);
     if (e == cudaSuccess) e = grow(&c->gid, &c->cap_gid, rays);
     if (e == cudaSuccess) e = grow(&c->key, &c->cap_key, rays);
+    if (e == cudaSuccess) e = grow(&c->cf, &c->cap_cf, rays);
+    if (e == cudaSuccess) e = grow(&c->vf, &c->cap_vf, rays);
     if (e == cudaSuccess) e = grow(&c->order, &c->cap_order, rays);
     if (e == cudaSuccess) e = grow(&c->rescue, &c->cap_rescue, rc);
     if (e == cudaSuccess) e = grow(&c->geom, &c->cap_geom, geoms);
     if (e == cudaSuccess) e = grow(&c->frames_dev, &c->cap_frames, frames);
     if (e != cudaSuccess) return fail(BHK_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
-    c->cap_rays = std::min({c->cap_E, c->cap_order, c->cap_key});
+    c->cap_rays = std::min({c->cap_E, c->cap_order, c->cap_key, c->cap_cf, c->cap_vf});
     if (frames > c->cap_frames_host) {
         if (c->frames_host) cudaFreeHost(c->frames_host);
         c->frames_host = nullptr;
@@ -184,7 +189,7 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     return BHK_OK;
 }
 
-LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key}; }
+LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf}; }
 
 struct Batch {
     int mode;  // 0 frames, 1 explicit
@@ -229,10 +234,12 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
 bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Outputs& out, bool timed,
                      cudaStream_t s) {
     if (!r.graph) return enqueue(c, b, r, out, timed, s);
+    // In a graph the timing events bracket the whole replay, recorded on the launching stream:
+    // events recorded inside a captured graph cannot be read back with cudaEventElapsedTime.
     GraphKey k;
     std::memset(static_cast<void*>(&k), 0, sizeof(GraphKey));  // padding takes part in the comparison
     k.mode = b.mode; k.fp64 = r.fp64; k.nframes = b.nframes; k.block = r.block; k.chunk = r.chunk;
-    k.buckets = r.buckets; k.grid = r.grid; k.timed = timed; k.regcap = r.regcap; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
+    k.buckets = r.buckets; k.grid = r.grid; k.timed = 0; k.regcap = r.regcap; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
     k.n_explicit = b.mode == 1 ? 1 : 0;
     for (int i = 0; i < 5; ++i) k.ex[i] = b.ex[i];
     k.r_in = b.r_in; k.r_out = b.r_out;
@@ -242,7 +249,7 @@ bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Ou
         c->exec = nullptr;
         c->graph = nullptr;
         BHK_CUDA(cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal));
-        const bhk_status st = enqueue(c, b, r, out, timed, c->capture_stream);
+        const bhk_status st = enqueue(c, b, r, out, false, c->capture_stream);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(c->capture_stream, &g);
         if (st != BHK_OK) {
@@ -254,7 +261,9 @@ bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Ou
         BHK_CUDA(cudaGraphInstantiate(&c->exec, g, 0));
         c->gkey = k;
     }
+    if (timed) BHK_CUDA(cudaEventRecord(c->ev0, s));
     BHK_CUDA(cudaGraphLaunch(c->exec, s));
+    if (timed) BHK_CUDA(cudaEventRecord(c->ev1, s));
     return BHK_OK;
 }
 
@@ -382,7 +391,7 @@ bhk_status bhk_destroy(bhk_context* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->exec) cudaGraphExecDestroy(c->exec);
     if (c->graph) cudaGraphDestroy(c->graph);
-    void* dev[] = {c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->order, c->rescue, c->geom,
+    void* dev[] = {c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf, c->order, c->rescue, c->geom,
                    c->frames_dev, c->ctl, c->hist, c->offs, c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2],
                    c->o_d[3], c->o_d[4], c->o_steps, c->o_rej};
     for (void* p : dev)
@@ -549,6 +558,7 @@ bhk_status bhk_get_stats(bhk_context* c, bhk_trace_stats* stats) {
     if (c->timed_last) {
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) s.kernel_ms = ms;
+        else cudaGetLastError();  // leave no stale error behind for the caller's next CUDA call
     }
     *stats = s;
     return BHK_OK;

@@ -10,11 +10,14 @@
 
 namespace bhk {
 
-// Per-camera geometry the tracer needs for every ray of that camera (FP64, computed on device).
+// Per-camera geometry the tracer needs for every ray of that camera (FP64, computed on device),
+// with FP32 copies for the FP32 tracer (which then issues no FP64 conversions per ray).
 struct RayGeom {
     double a, r0, th0, ph0;       // camera position = launch point
     double rp, r_cap, r_esc;      // horizon, capture and escape radii
     double r_in, r_out, zone_top; // disk, and r_+ + width of the analytic capture zone
+    float af, r0f, th0f, ph0f, r_capf, r_escf, r_inf, r_outf, zone_topf, rpf;
+    int32_t south0;               // camera below the equator: th0f holds pi - theta_obs
 };
 
 // Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset, and the per-camera
@@ -27,11 +30,15 @@ struct FrameDev {
     double sigma, cs2, inv_sn2, a2;  // Sigma, cos^2, 1/max(sin^2, 1e-18), a^2 at the camera
 };
 
-// Launch record of one ray, structure of arrays, written by the FP64 launch kernel.
+// Launch record of one ray, structure of arrays, written by the FP64 launch kernel: the FP64
+// constants, and their FP32 roundings for the FP32 tracer -- (E, L, Q, K = (L - aE)^2 + Q) and
+// (vr, vtheta) -- so that it loads ready operands.
 struct LaunchSoA {
     double *E, *L, *Q, *vr, *vth;
     int32_t* geom_id;             // index into the RayGeom table
     uint16_t* key;                // cost bucket for the pre-sort
+    float4* cf;
+    float2* vf;
 };
 
 // Small control block reset at the start of every batch.

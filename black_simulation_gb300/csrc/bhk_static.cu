@@ -8,7 +8,7 @@
 // list) in one fixed array in the device image of libbhk, reserved when the library is loaded.
 //
 // Costs and limits of that choice:
-//  - the array holds kStaticMaxRays rays and kStaticMaxFrames frames per call (4.6 MB), and
+//  - the array holds kStaticMaxRays rays and kStaticMaxFrames frames per call (6.1 MB), and
 //    every GPU that loads libbhk keeps it until the process exits;
 //  - all calls share the one array, whose contents persist from the previous call. The control
 //    block (queue counter, statistics) is cleared at the start of each call; everything else is
@@ -33,7 +33,7 @@ constexpr int kMaxDevices = 64;
 
 // Layout of the working memory inside the static array (offsets, 256-byte aligned).
 struct Layout {
-    size_t ctl, hist, offs, frames, geom, E, L, Q, vr, vth, gid, key, order, rescue, total;
+    size_t ctl, hist, offs, frames, geom, E, L, Q, vr, vth, gid, key, order, cf, vf, rescue, total;
 };
 
 constexpr size_t up256(size_t x) { return (x + 255) / 256 * 256; }
@@ -54,6 +54,8 @@ constexpr Layout make_layout() {
     l.gid = o; o = up256(o + sizeof(int32_t) * kStaticMaxRays);
     l.key = o; o = up256(o + sizeof(uint16_t) * kStaticMaxRays);
     l.order = o; o = up256(o + sizeof(int32_t) * kStaticMaxRays);
+    l.cf = o; o = up256(o + sizeof(float4) * kStaticMaxRays);
+    l.vf = o; o = up256(o + sizeof(float2) * kStaticMaxRays);
     l.rescue = o; o = up256(o + sizeof(Rescue) * kStaticRescue);
     l.total = o;
     return l;
@@ -161,7 +163,8 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     LaunchSoA L{reinterpret_cast<double*>(base + kLayout.E), reinterpret_cast<double*>(base + kLayout.L),
                 reinterpret_cast<double*>(base + kLayout.Q), reinterpret_cast<double*>(base + kLayout.vr),
                 reinterpret_cast<double*>(base + kLayout.vth), reinterpret_cast<int32_t*>(base + kLayout.gid),
-                reinterpret_cast<uint16_t*>(base + kLayout.key)};
+                reinterpret_cast<uint16_t*>(base + kLayout.key), reinterpret_cast<float4*>(base + kLayout.cf),
+                reinterpret_cast<float2*>(base + kLayout.vf)};
     SortScratch S{reinterpret_cast<unsigned*>(base + kLayout.hist), reinterpret_cast<unsigned*>(base + kLayout.offs),
                   reinterpret_cast<int32_t*>(base + kLayout.order)};
     Rescue* rescue = reinterpret_cast<Rescue*>(base + kLayout.rescue);

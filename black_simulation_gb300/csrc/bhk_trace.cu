@@ -51,6 +51,12 @@ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, doub
     g.r_in = r_in_opt > 0.0 ? r_in_opt : isco_radius(a, true);
     g.r_out = r_out;
     g.zone_top = g.rp + dmind(0.05, 0.5 * (g.r_in - g.rp));
+    // FP32 copies; the launch polar angle is stored relative to the camera's hemisphere (the FP32
+    // tracer integrates pi - theta in the south).
+    g.south0 = th > 0.5 * kPi ? 1 : 0;
+    g.af = float(a); g.r0f = float(r); g.th0f = float(g.south0 ? kPi - th : th); g.ph0f = float(ph);
+    g.r_capf = float(g.r_cap); g.r_escf = float(g.r_esc); g.r_inf = float(g.r_in); g.r_outf = float(g.r_out);
+    g.zone_topf = float(g.zone_top); g.rpf = float(g.rp);
     return g;
 }
 
@@ -64,12 +70,15 @@ __device__ __forceinline__ uint16_t cost_key(double E, double L, double Q, int b
     return static_cast<uint16_t>(k < 0 ? 0 : (k >= buckets ? buckets - 1 : k));
 }
 
-__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, double E, double Lz, double Q, double vr,
-                                             double vth, int32_t gid, int buckets) {
+__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, double a, double E, double Lz, double Q,
+                                             double vr, double vth, int32_t gid, int buckets) {
     L.E[i] = E; L.L[i] = Lz; L.Q[i] = Q;
     L.vr[i] = vr; L.vth[i] = vth;
     L.geom_id[i] = gid;
     L.key[i] = cost_key(E, Lz, Q, buckets);
+    const double x = Lz - a * E;
+    L.cf[i] = make_float4(float(E), float(Lz), float(Q), float(x * x + Q));
+    L.vf[i] = make_float2(float(vr), float(vth));
 }
 
 // ------------------------------------------------------------------------- set-up kernels ----
@@ -143,7 +152,7 @@ __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nf
             Lz = 0.0;
             Q = vth * vth - f.cs2 * a2E2;
         }
-        store_launch(L, i, E, Lz, Q, vr, vth, lo, p.buckets);
+        store_launch(L, i, f.d.a, E, Lz, Q, vr, vth, lo, p.buckets);
     }
 }
 
@@ -165,7 +174,7 @@ __global__ void launch_explicit_kernel(const double* __restrict__ a, const doubl
         St s;
         photon_from_frame(ai, ri, ti, 0.0, e, look, c, s);
         geom[i] = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
-        store_launch(L, i, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
+        store_launch(L, i, ai, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
     }
 }
 
@@ -221,10 +230,63 @@ __global__ void scatter_kernel(LaunchSoA L, SortScratch S, TraceParams p, const 
 
 enum : int { kContinue = 0, kFinished = 1, kRescue = 2, kRestart = 3 };
 
+// float -> double by assembling the bits with integer operations: the FP32 tracer writes its double
+// outputs without issuing conversions to the narrow FP64 pipe. Subnormal floats become zero.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u;
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned m = u & 0x7fffffu;
+    unsigned hi;
+    if (e == 0u) hi = sign;
+    else if (e == 0xffu) hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+    else hi = sign | ((e + 896u) << 20) | (m >> 3);
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(m << 29));
+}
+
+__device__ __forceinline__ float nan_f() { return __int_as_float(0x7fc00000); }
+
+// x wrapped to [0, 2 pi) in FP32: nearest multiple of 2 pi by the 1.5 * 2^23 rounding, removed with
+// a two-constant split of 2 pi.
+__device__ __forceinline__ float wrap_2pi_f(float x) {
+    const float n = fmaf(x, 0.159154943091895336f, 12582912.0f) - 12582912.0f;
+    float y = fmaf(n, -6.28318548202514648f, x);
+    y = fmaf(n, 1.74845553e-7f, y);
+    return y < 0.0f ? y + 6.28318548202514648f : y;
+}
+
+// disk_redshift in FP32 (src/trajectory.cpp:311-318): no cancellation at the disk radii.
+__device__ __forceinline__ bool disk_redshift_f(float a, float E, float L, float rc, float* g) {
+    const float irc = rcp_approx(rc);
+    const float w = rcp_approx(rc * sqrt_approx(rc) + a);
+    const float gtt = -(1.0f - 2.0f * irc), gtp = -2.0f * a * irc, gpp = rc * rc + a * a + 2.0f * a * a * irc;
+    const float norm = -(gtt + 2.0f * gtp * w + gpp * w * w);
+    if (!(norm > 0.0f)) return false;
+    *g = sqrt_approx(norm) * rcp_approx(E - L * w);
+    return true;
+}
+
+// FP32 tier of the capture test: no_radial_root_below with the bound required to clear FP32
+// rounding by a wide margin (1e-4 of the polynomial's magnitude). False means "not proven": the
+// FP64 test decides.
+__device__ __forceinline__ bool no_radial_root_below_f(const RayC<float>& c, float x0, float r) {
+    const float w = r - x0;
+    if (w <= 0.0f) return true;
+    const float xx = c.L - c.aE;
+    const float c4 = c.E * c.E, c2 = -(2.0f * c.aE * xx + c.K), c1 = 2.0f * c.K, c0 = -c.a2 * c.Q;
+    const float x2 = x0 * x0;
+    const float R0 = ((c4 * x2 + c2) * x0 + c1) * x0 + c0;
+    const float R1 = (4.0f * c4 * x2 + 2.0f * c2) * x0 + c1;
+    const float R2 = 6.0f * c4 * x2 + c2;
+    const float R3 = 4.0f * c4 * x0;
+    const float lower = R0 - w * fmaxf(0.0f, -R1) - w * w * fmaxf(0.0f, -R2) - w * w * w * fmaxf(0.0f, -R3);
+    const float scale = c4 * x2 * x2 + fabsf(c2) * x2 + fabsf(c1) * x0 + fabsf(c0);
+    return lower > 1e-4f * scale;
+}
+
 template <typename T>
 struct Lane {
     RayC<T> c;
-    double a, E, L, Q;
     T y[5];
     T k[7][5];
     T h;
@@ -236,13 +298,6 @@ struct Lane {
     // both poles are approached with the full relative precision of a small angle.
     bool south;
 };
-
-// Physical (theta, vtheta) of a lane, in FP64.
-template <typename T>
-__device__ __forceinline__ void physical_polar(const Lane<T>& s, double* th, double* vth) {
-    *th = s.south ? kPi - double(s.y[1]) : double(s.y[1]);
-    *vth = s.south ? -double(s.y[4]) : double(s.y[4]);
-}
 
 // kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
 // first step of the backward march.
@@ -259,34 +314,39 @@ __device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol) {
     return -h;
 }
 
-// Starts a lane on a ray. h == 0 means a fresh launch: the first step comes from kerr::photonStepSize.
 template <typename T>
-__device__ __forceinline__ void lane_begin(Lane<T>& s, const RayGeom& g, double E, double L, double Q,
-                                           const double y[5], double h, const TraceParams& p) {
-    s.a = g.a; s.E = E; s.L = L; s.Q = Q;
-    s.c.set(g.a, E, L, Q);
-    s.south = sizeof(T) == 4 && y[1] > 0.5 * kPi;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) s.y[i] = T(y[i]);
-    if (s.south) {
-        s.y[1] = T(kPi - y[1]);
-        s.y[4] = T(-y[4]);
-    }
-    rhs(s.c, s.y, s.k[0]);
-    if (h == 0.0) {
-        if constexpr (sizeof(T) == 8) s.h = first_step<T>(s.y, s.k[0], p.tol0);
-        else s.h = first_step<T>(s.y, s.k[0], p.tol0_f);
+__device__ __forceinline__ void lane_radii(Lane<T>& s, const RayGeom& g) {
+    if constexpr (sizeof(T) == 4) {
+        s.r_cap = g.r_capf; s.r_esc = g.r_escf; s.r_in = g.r_inf; s.r_out = g.r_outf; s.zone_top = g.zone_topf;
     } else {
-        s.h = T(h);
+        s.r_cap = g.r_cap; s.r_esc = g.r_esc; s.r_in = g.r_in; s.r_out = g.r_out; s.zone_top = g.zone_top;
     }
-    s.r_cap = T(g.r_cap); s.r_esc = T(g.r_esc); s.r_in = T(g.r_in); s.r_out = T(g.r_out);
-    s.zone_top = T(g.zone_top);
+}
+
+// Starts a lane on ray `ray` at its launch point, first step from kerr::photonStepSize.
+template <typename T>
+__device__ __forceinline__ void lane_begin_launch(Lane<T>& s, const RayGeom& g, const LaunchSoA& L, long long ray,
+                                                  const TraceParams& p) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 cf = L.cf[ray];
+        const float2 vf = L.vf[ray];
+        s.c.set_t(g.af, cf.x, cf.y, cf.z, cf.w);
+        s.south = g.south0 != 0;
+        s.y[0] = g.r0f; s.y[1] = g.th0f; s.y[2] = g.ph0f; s.y[3] = vf.x; s.y[4] = s.south ? -vf.y : vf.y;
+    } else {
+        s.c.set(g.a, L.E[ray], L.L[ray], L.Q[ray]);
+        s.south = false;
+        s.y[0] = g.r0; s.y[1] = g.th0; s.y[2] = g.ph0; s.y[3] = L.vr[ray]; s.y[4] = L.vth[ray];
+    }
+    lane_radii(s, g);
+    rhs(s.c, s.y, s.k[0]);
+    if constexpr (sizeof(T) == 4) s.h = first_step<T>(s.y, s.k[0], p.tol0_f);
+    else s.h = first_step<T>(s.y, s.k[0], p.tol0);
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
 __device__ __forceinline__ void write_out(const Outputs& o, long long ray, int outcome, double rd, double pd, double g,
                                           double ti, double pi, int steps, int rejected) {
-    if (o.rejected) o.rejected[ray] = rejected;
     if (o.outcome) o.outcome[ray] = static_cast<uint8_t>(outcome);
     if (o.r_disk) o.r_disk[ray] = rd;
     if (o.phi_disk) o.phi_disk[ray] = pd;
@@ -294,6 +354,28 @@ __device__ __forceinline__ void write_out(const Outputs& o, long long ray, int o
     if (o.theta_inf) o.theta_inf[ray] = ti;
     if (o.phi_inf) o.phi_inf[ray] = pi;
     if (o.steps) o.steps[ray] = steps;
+    if (o.rejected) o.rejected[ray] = rejected;
+}
+
+template <typename T>
+__device__ __forceinline__ void write_out_t(const Outputs& o, long long ray, int outcome, T rd, T pd, T g, T ti, T pi,
+                                            int steps, int rejected) {
+    if constexpr (sizeof(T) == 4) write_out(o, ray, outcome, f2d(rd), f2d(pd), f2d(g), f2d(ti), f2d(pi), steps, rejected);
+    else write_out(o, ray, outcome, rd, pd, g, ti, pi, steps, rejected);
+}
+
+template <typename T>
+__device__ __forceinline__ T nan_t() {
+    if constexpr (sizeof(T) == 4) return nan_f();
+    else return nan_d();
+}
+
+template <typename T>
+__device__ __forceinline__ int finish(const Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl) {
+    const T n = nan_t<T>();
+    write_out_t<T>(o, ray, outcome, n, n, n, n, n, s.acc, s.rej);
+    if (outcome == BHK_RAY_UNFINISHED) atomicAdd(&ctl->stats[2], 1ull);
+    return kFinished;
 }
 
 // Fraction of the step where the dense output of component i equals target: Newton on the quartic
@@ -335,7 +417,8 @@ __device__ __forceinline__ T locate(const T* y0, const T* y1, const T k[7][5], T
 // kRescue (FP32 only: hand the state to FP64) or kRestart (FP32 only: non-finite state).
 template <typename T>
 __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long long ray, const Outputs& out,
-                                       bool reproject, Control* ctl) {
+                                       bool reproject, Control* ctl, const LaunchSoA& L,
+                                       const RayGeom* __restrict__ geom) {
     constexpr bool F64 = sizeof(T) == 8;
     const T h = s.h;
     T t[5];
@@ -397,11 +480,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if constexpr (F64) fac = isfinite(err) ? fmax(0.2, 0.9 * pow(err, -0.2)) : 0.2;
         else fac = isfinite(e2) ? fmaxf(0.2f, 0.9f * exp2f(-0.1f * __log2f(e2))) : 0.2f;
         s.h = h * fac;
-        if (s.rej >= p.max_steps) {
-            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
-            atomicAdd(&ctl->stats[2], 1ull);
-            return kFinished;
-        }
+        if (s.rej >= p.max_steps) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
         return kContinue;
     }
     ++s.acc;
@@ -412,38 +491,47 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         s.y[i] = y5[i];
     }
     if (!isfinite(s.y[0])) {
-        if constexpr (F64) {
-            write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
-            atomicAdd(&ctl->stats[2], 1ull);
-            return kFinished;
-        } else {
-            return kRestart;
-        }
+        if constexpr (F64) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
+        else return kRestart;
     }
     const T hp = T(0.5 * kPi);
     // Thin disk: theta crosses pi/2 inside [r_in, r_out].
     if ((prev[1] - hp) * (s.y[1] - hp) < T(0)) {
         const T sg = locate(prev, s.y, s.k, h, 1, hp);
         const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
-        double g;
-        if (rc >= s.r_in && rc <= s.r_out && disk_redshift(s.a, s.E, s.L, double(rc), &g)) {
-            const double ph = wrap_2pi(double(dense(prev[2], s.y[2], s.k, h, 2, sg)));
-            write_out(out, ray, BHK_RAY_DISK, double(rc), ph, g, nan_d(), nan_d(), s.acc, s.rej);
-            return kFinished;
+        if (rc >= s.r_in && rc <= s.r_out) {
+            if constexpr (F64) {
+                double g;
+                if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
+                    const double ph = wrap_2pi(dense(prev[2], s.y[2], s.k, h, 2, sg));
+                    write_out(out, ray, BHK_RAY_DISK, rc, ph, g, nan_d(), nan_d(), s.acc, s.rej);
+                    return kFinished;
+                }
+            } else {
+                float g;
+                if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
+                    const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
+                    write_out_t<float>(out, ray, BHK_RAY_DISK, rc, ph, g, nan_f(), nan_f(), s.acc, s.rej);
+                    return kFinished;
+                }
+            }
         }
     }
     const bool falling = s.y[0] < prev[0];
     if (falling) {
-        if (s.y[0] < s.r_cap) {
-            write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
-            return kFinished;
-        }
+        if (s.y[0] < s.r_cap) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
         if (s.y[0] < s.zone_top) {
-            if (no_radial_root_below(s.a, s.E, s.L, s.Q, double(s.y[0]), p.eps)) {
-                write_out(out, ray, BHK_RAY_CAPTURED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
-                return kFinished;
+            if constexpr (F64) {
+                if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
+                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+            } else {
+                if (no_radial_root_below_f(s.c, s.r_cap, s.y[0])) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
+                const RayGeom& G = geom[L.geom_id[ray]];
+                if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
+                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                return kRescue;
             }
-            if constexpr (!F64) return kRescue;
         }
     } else if (s.y[0] > s.r_esc) {
         const T sg = locate(prev, s.y, s.k, h, 0, s.r_esc);
@@ -456,12 +544,11 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
             x[1] = T(kPi) - x[1];
             x[4] = -x[4];
         }
-        cartesian_velocity<T>(T(s.a), x[0], x[1], x[2], x[3], x[4], kk[2], v);
+        cartesian_velocity<T>(s.c.a, x[0], x[1], x[2], x[3], x[4], kk[2], v);
         const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
-        const double ti = double(acos(dz));
-        const double pi = double(atan2(-v[1] / nrm, -v[0] / nrm));
-        write_out(out, ray, BHK_RAY_ESCAPED, nan_d(), nan_d(), nan_d(), ti, pi, s.acc, s.rej);
+        const T n = nan_t<T>();
+        write_out_t<T>(out, ray, BHK_RAY_ESCAPED, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
         return kFinished;
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
@@ -469,8 +556,8 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     if constexpr (F64) {
         St st{0.0, s.y[0], s.y[1], s.y[2], s.y[3], s.y[4]};
         if (normalize_angles(st)) s.k[6][4] = -s.k[6][4];
-        const Cons cc{s.E, s.L, s.Q, 0.0};
-        enforce_constraints(s.a, cc, st);
+        const Cons cc{s.c.E, s.c.L, s.c.Q, 0.0};
+        enforce_constraints(s.c.a, cc, st);
         s.y[1] = st.theta; s.y[2] = st.phi; s.y[3] = st.vr; s.y[4] = st.vtheta;
     } else {
         if (s.y[1] < T(0)) {  // over the pole of this hemisphere
@@ -491,11 +578,12 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if (pj.Th > pj.Thz) s.y[4] = copysignf(sqrt_approx(pj.Th), s.y[4]);
         if (reproject) {
             // Optional FP64 radial re-projection: R(r) = P^2 - Delta K evaluated in FP64.
+            const double a = geom[L.geom_id[ray]].a, E = L.E[ray], Lz = L.L[ray], Q = L.Q[ray];
             const double r = double(s.y[0]);
-            const double delta = r * r - 2.0 * r + s.a * s.a;
-            const double P = s.E * (r * r + s.a * s.a) - s.a * s.L;
-            const double x = s.L - s.a * s.E;
-            const double K = x * x + s.Q;
+            const double delta = r * r - 2.0 * r + a * a;
+            const double P = E * (r * r + a * a) - a * Lz;
+            const double x = Lz - a * E;
+            const double K = x * x + Q;
             const double R = P * P - delta * K;
             if (R > 0.05 * (P * P + fabs(delta) * K)) s.y[3] = T(copysign(sqrt(R), double(s.y[3])));
         }
@@ -520,11 +608,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         }
     }
     s.last_rej = false;
-    if (s.acc >= p.max_steps) {
-        write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), s.acc, s.rej);
-        atomicAdd(&ctl->stats[2], 1ull);
-        return kFinished;
-    }
+    if (s.acc >= p.max_steps) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
     return kContinue;
 }
 
@@ -578,9 +662,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             if (((need >> lane) & 1u) && rank < avail) {
                 const long long q = pool_pos + rank;
                 ray = order ? order[q] : q;
-                const RayGeom& g = geom[L.geom_id[ray]];
-                const double y0[5] = {g.r0, g.th0, g.ph0, L.vr[ray], L.vth[ray]};
-                lane_begin(s, g, L.E[ray], L.L[ray], L.Q[ray], y0, 0.0, p);
+                lane_begin_launch(s, geom[L.geom_id[ray]], L, ray, p);
             }
             const int served = __popc(need) < avail ? __popc(need) : avail;
             pool_pos += served;
@@ -590,7 +672,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
         ++iter;
         const bool reproject = p.reproject_every > 0 && (iter % p.reproject_every) == 0;
         if (ray >= 0) {
-            const int r = attempt<T>(s, p, ray, out, reproject, ctl);
+            const int r = attempt<T>(s, p, ray, out, reproject, ctl, L, geom);
             if (r != kContinue) {
                 n_acc += s.acc;
                 n_rej += s.rej;
@@ -602,7 +684,10 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                         y[0] = g.r0; y[1] = g.th0; y[2] = g.ph0; y[3] = L.vr[ray]; y[4] = L.vth[ray];
                     } else {
                         for (int i = 0; i < 5; ++i) y[i] = double(s.y[i]);
-                        physical_polar(s, &y[1], &y[4]);
+                        if (s.south) {
+                            y[1] = kPi - y[1];
+                            y[4] = -y[4];
+                        }
                     }
                     push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? 0.0 : double(s.h), restart ? 0 : s.acc,
                                 restart ? 0 : s.rej, restart ? 1 : 0, out);
@@ -630,19 +715,25 @@ __global__ void rescue_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, Out
         const Rescue r = rescue[i];
         const RayGeom& g = geom[L.geom_id[r.ray]];
         Lane<double> s;
-        double y[5] = {r.y[0], r.y[1], r.y[2], r.y[3], r.y[4]};
-        if (!r.from_launch) {
-            St st{0.0, y[0], y[1], y[2], y[3], y[4]};
+        if (r.from_launch) {
+            lane_begin_launch(s, g, L, r.ray, p);
+        } else {
+            St st{0.0, r.y[0], r.y[1], r.y[2], r.y[3], r.y[4]};
             normalize_angles(st);
             const Cons cc{L.E[r.ray], L.L[r.ray], L.Q[r.ray], 0.0};
             enforce_constraints(g.a, cc, st);
-            y[1] = st.theta; y[2] = st.phi; y[3] = st.vr; y[4] = st.vtheta;
+            s.c.set(g.a, cc.E, cc.L, cc.Q);
+            s.south = false;
+            s.y[0] = st.r; s.y[1] = st.theta; s.y[2] = st.phi; s.y[3] = st.vr; s.y[4] = st.vtheta;
+            lane_radii(s, g);
+            rhs(s.c, s.y, s.k[0]);
+            s.h = r.h;
+            s.last_rej = false;
         }
-        lane_begin(s, g, L.E[r.ray], L.L[r.ray], L.Q[r.ray], y, r.h, p);
         s.acc = r.accepted;
         s.rej = r.rejected;
         int res = kContinue;
-        while (res == kContinue) res = attempt<double>(s, p, r.ray, out, false, ctl);
+        while (res == kContinue) res = attempt<double>(s, p, r.ray, out, false, ctl, L, geom);
         atomicAdd(&ctl->stats[0], static_cast<unsigned long long>(s.acc - r.accepted));
         atomicAdd(&ctl->stats[1], static_cast<unsigned long long>(s.rej - r.rejected));
     }
@@ -728,7 +819,10 @@ void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue
 int trace_blocks_per_sm(bool fp64, int regcap, int block) {
     if (block > 256 || (regcap > 0 && (fp64 || block > 128))) return 0;
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_variant(fp64, regcap), block, 0);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_variant(fp64, regcap), block, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     return n;
 }
 

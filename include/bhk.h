@@ -142,7 +142,8 @@ typedef struct {
 typedef struct {
     int64_t rays, accepted_steps, rejected_steps, rescued, unfinished;
     int32_t block, chunk, sort_buckets, grid, reg_budget, pad;
-    double kernel_ms;    /* tracer + rescue kernel time, CUDA events on the launching stream */
+    double kernel_ms;    /* CUDA events on the launching stream: tracer + rescue kernels, or the
+                            whole batch when it ran as a CUDA graph */
 } bhk_trace_stats;
 
 /* Traces every pixel of nframes frames (host descriptors) in one persistent launch. Ray i of frame f
@@ -176,7 +177,7 @@ bhk_status bhk_critical_curve(double a, double r_obs, double theta_obs, int32_t 
  * may not allocate device memory -- a host framework that owns the whole device-memory budget
  * through its own pool, or a per-frame render loop where cudaMalloc/cudaFree would synchronise the
  * device. Outputs are the caller's device buffers; all working memory lives in one fixed array in
- * libbhk's device image (4.6 MB, held by every GPU that loads the library until exit).
+ * libbhk's device image (6.1 MB, held by every GPU that loads the library until exit).
  * Limits: at most 65536 rays and 64 frames per call; larger requests return BHK_EINVAL. No context:
  * the tracer runs on the current device and on `stream` (NULL = the legacy default stream) with the
  * opts given (0 fields take the context defaults; no autotuning). All calls share the array, which
