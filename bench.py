@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "geodesics/s"
 REF_TOL = 1e-2          # reference product tolerance (src/trajectory.cpp:261); meets the 1e-4 bar
+# DRAM bytes (read + write) of one tracer launch from ncu, by workload: the 960x540 capture of
+# profiles/trace_kernel_1080p_mixed.md (14.61 MB) scaled by rays to the full frame.
+NCU_TRAFFIC = {"1080p": 58.4e6}
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -296,7 +299,8 @@ def run_ours(args):
         "e2e": {"value": world * n_rays / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": NCU_TRAFFIC.get(args.workload) if args.scale == 1 else None,
                      "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run",
                      "kernel_ms": k_ms, "flops_per_step": fps},
         "gpu_launches": 7 * args.steps,

@@ -58,7 +58,13 @@ struct GraphKey {
     bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 
-constexpr double kFlopsPerStep = 772.0;  // FP32 DP5 step, counted from bhk_trace.cu / bhk_device.cuh
+// FP32 FLOPs of one Dormand-Prince attempt of the mixed tracer, counted from the source (an FMA is 2):
+//   right-hand side (bhk_device.cuh rhs<float>): sine/cosine 27 (12 FMA, 2 MUL, 1 ADD), Delta and
+//     r^2 + a^2 4, P 2, inflow 5, R'/2 5, 1/sin powers 2, Theta'/2 5, dphi 4 -> 55, x 6 stages = 330;
+//     the FSAL stage's constraint potentials 18;
+//   stage sums y + h sum a_ij k_j over 5 components: 15 + 25 + 35 + 45 + 55 + 55 = 230;
+//   error estimate and weighted norm: 5 x 17 = 85;  step control and pole cap: 8.
+constexpr double kFlopsPerStep = 671.0;
 
 }  // namespace
 
@@ -284,7 +290,7 @@ bhk_status check_frames(const bhk_frame_desc* f, int32_t nframes, int64_t* total
         if (!(f[i].r_obs > 1.0 + std::sqrt(1.0 - f[i].a * f[i].a)))
             return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole)");
         if (!(f[i].theta_obs > 0.0 && f[i].theta_obs < M_PI)) return fail(BHK_EINVAL, "theta_obs outside (0, pi)");
-        if (!(f[i].r_disk_out > 0.0)) return fail(BHK_EINVAL, "r_disk_out must be positive");
+        if (!(f[i].r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
         t += static_cast<int64_t>(f[i].width) * f[i].height;
     }
     if (t > (int64_t(1) << 31) - 1) return fail(BHK_EINVAL, "more than 2^31 - 1 rays in one batch");
@@ -529,7 +535,7 @@ bhk_status bhk_trace_rays(bhk_context* c, int64_t n, const double* a, const doub
     if (!out) return fail(BHK_EINVAL, "out is null");
     if (n == 0) return BHK_OK;
     if (!a || !r_obs || !theta_obs || !alpha || !beta) return fail(BHK_EINVAL, "null ray array");
-    if (!(r_disk_out > 0.0)) return fail(BHK_EINVAL, "r_disk_out must be positive");
+    if (!(r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
     std::lock_guard<std::mutex> lock(c->mu);
     BHK_CUDA(cudaSetDevice(c->device));
     bhk_status st = ensure_scratch(c, static_cast<size_t>(n), static_cast<size_t>(n), 1);

@@ -28,6 +28,7 @@ struct FrameDev {
     double e[4][4];               // ZAMO frame at the camera
     double el[4][4];              // the same vectors lowered with the camera's metric, g e_k
     double sigma, cs2, inv_sn2, a2;  // Sigma, cos^2, 1/max(sin^2, 1e-18), a^2 at the camera
+    double inv_r, px, py;         // 1/r_obs and the pixel pitch in alpha and beta
 };
 
 // Launch record of one ray, structure of arrays, written by the FP64 launch kernel: the FP64

@@ -120,7 +120,7 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
         if (!(f.r_obs > 1.0 + std::sqrt(1.0 - f.a * f.a)))
             return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole)");
         if (!(f.theta_obs > 0.0 && f.theta_obs < M_PI)) return fail(BHK_EINVAL, "theta_obs outside (0, pi)");
-        if (!(f.r_disk_out > 0.0)) return fail(BHK_EINVAL, "r_disk_out must be positive");
+        if (!(f.r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
         total += static_cast<int64_t>(f.width) * f.height;
     }
     if (total > kStaticMaxRays)

@@ -111,8 +111,22 @@ __global__ void frame_setup_kernel(FrameDev* frames, RayGeom* geom, int nframes,
         frames[f].cs2 = cs * cs;
         frames[f].inv_sn2 = 1.0 / dmaxd(sn * sn, 1e-18);
         frames[f].a2 = d.a * d.a;
+        frames[f].inv_r = 1.0 / d.r_obs;
+        frames[f].px = (d.alpha_hi - d.alpha_lo) / d.width;
+        frames[f].py = (d.beta_hi - d.beta_lo) / d.height;
         geom[f] = make_geom(d.a, d.r_obs, d.theta_obs, d.phi_obs, d.r_disk_in, d.r_disk_out, p);
     }
+}
+
+// 1/sqrt(x) in FP64 for x in [1, ~10]: FP32 seed (rsqrt.approx, ~2^-22 relative) refined by two Newton
+// steps y <- y (3 - x y^2) / 2 (each squares the relative error): ~1 ulp without a DP divide or sqrt.
+__device__ __forceinline__ double rsqrt_newton(double x) {
+    float yf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(static_cast<float>(x)));
+    double y = yf;
+    y = y * (1.5 - 0.5 * x * y * y);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y;
 }
 
 // kerr::photonFromFrame for pixel (alpha, beta) of a ZAMO pinhole, with the camera's metric
@@ -128,14 +142,12 @@ __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nf
             if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
         }
         const FrameDev& f = frames[lo];
-        const long long local = i - f.offset;
-        const int row = static_cast<int>(local / f.d.width), col = static_cast<int>(local % f.d.width);
-        const double px = (f.d.alpha_hi - f.d.alpha_lo) / f.d.width;
-        const double py = (f.d.beta_hi - f.d.beta_lo) / f.d.height;
-        const double alpha = f.d.alpha_lo + (col + 0.5) * px;
-        const double beta = f.d.beta_hi - (row + 0.5) * py;
-        const double lt = -beta / f.d.r_obs, lp = alpha / f.d.r_obs;
-        const double inv = 1.0 / sqrt(1.0 + lt * lt + lp * lp);
+        const int local = static_cast<int>(i - f.offset);  // < 2^31 rays per batch
+        const int row = local / f.d.width, col = local - row * f.d.width;
+        const double alpha = f.d.alpha_lo + (col + 0.5) * f.px;
+        const double beta = f.d.beta_hi - (row + 0.5) * f.py;
+        const double lt = -beta * f.inv_r, lp = alpha * f.inv_r;
+        const double inv = rsqrt_newton(1.0 + lt * lt + lp * lp);
         const double l0 = -inv, l1 = lt * inv, l2 = lp * inv;
         const double pt = f.el[0][0] - l0 * f.el[1][0] - l1 * f.el[2][0] - l2 * f.el[3][0];
         const double pth = f.el[0][2] - l0 * f.el[1][2] - l1 * f.el[2][2] - l2 * f.el[3][2];

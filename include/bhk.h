@@ -102,7 +102,7 @@ typedef struct {
     int32_t width, height;
     double alpha_lo, alpha_hi, beta_lo, beta_hi;
     double r_disk_in;   /* <= 0: the prograde ISCO, kerr::iscoRadius(a, true) */
-    double r_disk_out;
+    double r_disk_out;  /* 0: no disk (a shadow-only image, as eht::render's) */
 } bhk_frame_desc;
 
 enum { BHK_PREC_FP64 = 0, BHK_PREC_MIXED = 1 };

@@ -213,3 +213,51 @@ def test_graph_replay_timing_leaves_no_stale_cuda_error(ctx):
     x = torch.ones(1024, device="cuda") * 2
     torch.cuda.synchronize()
     assert float(x.sum()) == 2048.0
+
+
+def test_traced_shadow_edge_follows_critical_curve(ctx, oracle):
+    """testEht shadow edge (tests/test_kerr.cpp:2283-2304): bisect, along 8 directions of the image
+    plane, the radius where rays stop falling in, for (a, i) = (0.9, 17), (0.9, 60), (0, 40) degrees,
+    with a camera at r = 1000 and no disk; compare with the analytic critical curve seen by that
+    camera. The reference's bar is 2e-3 relative."""
+    cases = [(0.9, 17.0), (0.9, 60.0), (0.0, 40.0)]
+    psis = 2 * np.pi * (np.arange(8) + 0.25) / 8
+    lo = np.ones(len(cases) * 8)
+    hi = np.full(len(cases) * 8, 12.0)
+    a = np.repeat([c[0] for c in cases], 8)
+    th = np.repeat([math.radians(c[1]) for c in cases], 8)
+    ps = np.tile(psis, len(cases))
+    dev = lambda x: torch.tensor(x, dtype=torch.float64, device="cuda")  # noqa: E731
+    for _ in range(30):
+        mid = 0.5 * (lo + hi)
+        out = ctx.trace_rays(dev(a), dev(np.full_like(a, 1000.0)), dev(th), dev(mid * np.cos(ps)),
+                             dev(mid * np.sin(ps)), 0.0, 0.0, bhk.TraceOpts("fp64", rtol=1e-9))
+        captured = out["outcome"].cpu().numpy() == bhk.CAPTURED
+        lo = np.where(captured, mid, lo)
+        hi = np.where(captured, hi, mid)
+    edge = 0.5 * (lo + hi)
+    worst = 0.0
+    for c, (sa, deg) in enumerate(cases):
+        ca, cb = bhk.critical_curve(sa, 1000.0, math.radians(deg), 400)
+        for k, psi in enumerate(psis):
+            want = oracle.critical_radius(ca, cb, psi)
+            worst = max(worst, abs(edge[8 * c + k] / want - 1.0))
+    print("shadow edge vs critical curve, worst relative:", worst)
+    assert worst < 2e-3
+
+
+def test_ray_outcomes_of_the_reference_ray_trace_test(ctx):
+    """testRayTrace (tests/test_kerr.cpp:496-543) with a ZAMO pinhole: looking at the hole ends in the
+    horizon, looking well aside reaches the sky, looking down at the disk from above lands on it
+    with a plausible g."""
+    dev = lambda x: torch.tensor(x, dtype=torch.float64, device="cuda")  # noqa: E731
+    r, th = 30.0, [math.pi / 2, math.pi / 2, 1.35]
+    look_down = np.array([-0.95, 0.3122, 0.0])
+    alpha = [0.0, 25.0, r * look_down[2] / -look_down[0]]
+    beta = [0.0, 0.0, r * look_down[1] / look_down[0]]
+    for prec in ("fp64", "mixed"):
+        out = host(ctx.trace_rays(dev([0.9] * 3), dev([r] * 3), dev(th), dev(alpha), dev(beta), 0.0, 20.0,
+                                  bhk.TraceOpts(prec)))
+        assert out["outcome"][0] == bhk.CAPTURED
+        assert out["outcome"][1] == bhk.ESCAPED
+        assert out["outcome"][2] == bhk.DISK and 0.2 < out["g"][2] < 3.0
