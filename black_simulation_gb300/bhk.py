@@ -149,8 +149,19 @@ def lib() -> C.CDLL:
                                    C.POINTER(StatsC)]),
         "bhk_critical_curve": (C.c_int, [d, d, d, C.c_int32, vp, vp, C.c_int32, C.POINTER(C.c_int32)]),
         "bhk_fp32_fma_peak": (C.c_int, [C.c_int, C.POINTER(d)]),
+        "bhk_tc_gemm": (C.c_int, [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp]),
         "bhk_trace_frames_static": (C.c_int, [C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
                                               C.POINTER(RaysOutC), vp]),
+        "bhk_surrogate_num_params": (i64, []),
+        "bhk_surrogate_create": (C.c_int, [C.c_int, C.c_uint64, C.c_int32, C.POINTER(vp)]),
+        "bhk_surrogate_destroy": (C.c_int, [vp]),
+        "bhk_surrogate_params": (C.c_int, [vp, vp, C.c_int32]),
+        "bhk_surrogate_fourier": (C.c_int, [vp, vp, C.c_int32]),
+        "bhk_surrogate_loss_weights": (C.c_int, [vp, vp]),
+        "bhk_surrogate_adam_state": (C.c_int, [vp, vp, vp, C.POINTER(i64), C.c_int32]),
+        "bhk_surrogate_gradients": (C.c_int, [vp, vp, vp, vp, C.c_int32, vp, vp]),
+        "bhk_surrogate_train": (C.c_int, [vp, vp, vp, vp, i64, C.c_int32, i64, C.c_float, vp, vp]),
+        "bhk_surrogate_predict": (C.c_int, [vp, vp, i64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -300,6 +311,16 @@ def critical_curve(a: float, r_obs: float, theta_obs: float, samples: int = 400)
 
 def flops_per_step() -> float:
     return float(lib().bhk_flops_per_step())
+
+
+def tc_gemm(A, B, splits: int = 1, stream=None):
+    """C = A @ B.T on the tcgen05 GEMM kernel (A: M x K, B: N x K, BF16 CUDA tensors) -> FP32 M x N."""
+    import torch
+    M, K = A.shape
+    N = B.shape[0]
+    Cm = torch.zeros((M, N), dtype=torch.float32, device=A.device)
+    check(lib().bhk_tc_gemm(_ptr(A.contiguous()), _ptr(B.contiguous()), _ptr(Cm), M, N, K, splits, _stream(stream)))
+    return Cm
 
 
 def fp32_fma_peak_tflops(device: int = 0) -> float:

@@ -29,6 +29,7 @@ UNITS = {
     "bhk_steps.cu": ["--fmad=false"],
     "bhk_diag.cu": [],
     "bhk_static.cu": [],
+    "bhk_surrogate.cu": [],
 }
 EXTRA_UNITS: dict[str, list[str]] = {}
 

@@ -1,0 +1,961 @@
+// bhk_surrogate.cu -- the learned part: a BF16 MLP surrogate of the tracer, trained and run by
+// hand-written tcgen05 kernels (FP32 accumulation in TMEM, FP32 master weights and Adam state).
+//
+// Network (per ray): inputs (a, theta_obs, log10 r_obs, alpha, beta) -> normalised to [-1, 1]^5 ->
+// 64 Fourier features [sin, cos](2 pi B u) with a fixed seeded B (32 x 5) -> 4 x (256, SiLU) ->
+// head of 8 (3 outcome logits, r_disk / 30, log g, unit escape vector), padded to 16 for the MMA.
+//
+// Every GEMM is C = A * B^T with A (M x K) and B (N x K) both K-major BF16 in global memory:
+//   forward   Y   = X * W^T         A = activations [rows x K],  B = W [N x K]
+//   backward  dX  = dY * W          A = dY [rows x N],           B = W^T stored [K x N]
+//             dW  = dY^T * X        A = dY^T [N x rows],         B = X^T [K x rows] (split over rows)
+// so activations and gradients are kept in both layouts (the epilogues write both).
+//
+// GEMM kernel: one CTA computes a 128 x BN tile; TMA brings 64-wide K chunks of A and B into a ring
+// of 4 shared-memory stages (128-byte swizzle); one thread issues tcgen05.mma (M = 128, N = BN,
+// K = 16 per instruction) into a TMEM accumulator and commits each stage back to the producer; after
+// the last chunk four warps read the accumulator with tcgen05.ld (warp w owns rows 32w..32w+31) and
+// run the epilogue. Every wait is bounded; a timeout sets an error flag the host checks.
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bhk_internal.h"
+#include "bhk_tc.cuh"
+
+namespace bhk {
+namespace sur {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kStages = 4;
+constexpr int kTileM = 128;
+constexpr int kChunkK = 64;
+constexpr int kABytes = kTileM * kChunkK * 2;  // 16 KB
+
+enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3 };
+
+struct EpiArgs {
+    int M, N;              // logical output extent (rows, columns)
+    const float* bias;     // [N] or null
+    float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32
+    int ld_f32;
+    bf16* rm;              // row-major BF16 output [M x ld_rm]
+    int ld_rm;
+    bf16* t;               // transposed BF16 output [N x ld_t]
+    int ld_t;
+    bf16* z;               // kBiasSilu: pre-activation written here; kDsilu: pre-activation read here
+    float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
+};
+
+template <int BN>
+constexpr int gemm_smem_bytes() {
+    return kStages * (kABytes + BN * kChunkK * 2) + 1024 + 256;
+}
+
+// Logistic sigmoid as 1/2 + tanh(z/2)/2 on the hardware tanh (one MUFU operation; relative error of
+// tanh.approx.f32 about 2^-11). Training and inference use this same SiLU.
+__device__ __forceinline__ float sigmoidf(float z) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return fmaf(0.5f, t, 0.5f);
+}
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(128, 1)
+gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
+            int k_per_split, int* err) {
+    constexpr int kBBytes = BN * kChunkK * 2;
+    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+    constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, BN);
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kStages * kABytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * kBBytes);
+    uint64_t* empty = full + kStages;
+    uint64_t* accbar = empty + kStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accbar + 1);
+    int* fail = reinterpret_cast<int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * BN;
+    const int k_begin = blockIdx.z * k_per_split;
+    const int k_end = min(K, k_begin + k_per_split);
+    const int nchunks = k_end > k_begin ? (k_end - k_begin + kChunkK - 1) / kChunkK : 0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(accbar, 1);
+        *fail = 0;
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 0) tc::tmem_alloc(tmem_slot, kCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0) {
+        auto load = [&](int stage, int chunk) {
+            tc::mbar_expect_tx(&full[stage], kABytes + kBBytes);
+            const int kx = k_begin + chunk * kChunkK;
+            tc::tma_load_2d(sA + stage * kABytes, &tmA, kx, m0, &full[stage]);
+            tc::tma_load_2d(sB + stage * kBBytes, &tmB, kx, n0, &full[stage]);
+        };
+        bool ok = true;
+        int loaded = 0;
+        for (; loaded < nchunks && loaded < kStages; ++loaded) load(loaded, loaded);
+        int c = 0;
+        for (; c < nchunks; ++c) {
+            const int s = c % kStages;
+            if (!tc::mbar_wait(&full[s], (c / kStages) & 1)) {
+                ok = false;
+                break;
+            }
+            tc::fence_after_sync();
+            const uint64_t ad = tc::smem_desc_sw128(sA + s * kABytes);
+            const uint64_t bd = tc::smem_desc_sw128(sB + s * kBBytes);
+#pragma unroll
+            for (int kk = 0; kk < kChunkK / 16; ++kk)  // +32 bytes per K = 16 slice inside the atom
+                tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_commit(&empty[s]);
+            // Refill the stage of the previous chunk once its MMAs are done (they run in order).
+            if (c >= 1 && loaded < nchunks) {
+                const int pc = c - 1, ps = pc % kStages;
+                if (!tc::mbar_wait(&empty[ps], (pc / kStages) & 1)) {
+                    ok = false;
+                    ++c;
+                    break;
+                }
+                load(ps, loaded);
+                ++loaded;
+            }
+        }
+        tc::mma_commit(accbar);
+        if (!ok) {
+            *fail = 1;
+            atomicExch(err, 1);
+            // Let the loads already in flight land before the CTA exits (bounded).
+            for (int q = c; q < loaded; ++q) tc::mbar_wait(&full[q % kStages], (q / kStages) & 1);
+        }
+    }
+    const bool acc_ready = tc::mbar_wait(accbar, 0);
+    tc::fence_after_sync();
+    __syncthreads();
+    if (!acc_ready && threadIdx.x == 0) atomicExch(err, 1);
+    if (acc_ready && !*fail && nchunks > 0) {
+        const int row = 32 * warp + lane;
+        const int m = m0 + row;
+        const bool live = m < ea.M;
+#pragma unroll 1
+        for (int j = 0; j < BN / 16; ++j) {
+            float v[16];
+            tc::tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + 16 * j, v);
+            const int nb = n0 + 16 * j;
+            if (nb >= ea.N) continue;
+            if constexpr (EPI == kStoreF32) {
+                if (live)
+                    for (int i = 0; i < 16; ++i)
+                        if (nb + i < ea.N) ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i] = v[i] + (ea.bias ? ea.bias[nb + i] : 0.0f);
+            } else if constexpr (EPI == kAtomicF32) {
+                if (live)
+                    for (int i = 0; i < 16; ++i)
+                        if (nb + i < ea.N) atomicAdd(&ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i], v[i]);
+            } else if constexpr (EPI == kBiasSilu) {
+                if (live) {
+                    __align__(16) bf16 zb[16], ab[16];
+                    for (int i = 0; i < 16; ++i) {
+                        const float z = v[i] + ea.bias[nb + i];
+                        zb[i] = __float2bfloat16_rn(z);
+                        ab[i] = __float2bfloat16_rn(z * sigmoidf(z));
+                    }
+                    uint4* zd = reinterpret_cast<uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
+                    uint4* ad = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
+                    zd[0] = reinterpret_cast<const uint4*>(zb)[0];
+                    zd[1] = reinterpret_cast<const uint4*>(zb)[1];
+                    ad[0] = reinterpret_cast<const uint4*>(ab)[0];
+                    ad[1] = reinterpret_cast<const uint4*>(ab)[1];
+                    if (ea.t)
+                        for (int i = 0; i < 16; ++i) ea.t[static_cast<size_t>(nb + i) * ea.ld_t + m] = ab[i];
+                }
+            } else {  // kDsilu: d(pre-activation) = dA * silu'(z); bias gradient = column sums
+                float dz[16];
+                if (live) {
+                    __align__(16) bf16 zin[16], ob[16];
+                    const uint4* zs = reinterpret_cast<const uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
+                    reinterpret_cast<uint4*>(zin)[0] = zs[0];
+                    reinterpret_cast<uint4*>(zin)[1] = zs[1];
+                    for (int i = 0; i < 16; ++i) {
+                        const float z = __bfloat162float(zin[i]);
+                        const float sg = sigmoidf(z);
+                        dz[i] = v[i] * sg * (1.0f + z * (1.0f - sg));
+                        ob[i] = __float2bfloat16_rn(dz[i]);
+                    }
+                    uint4* od = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
+                    od[0] = reinterpret_cast<const uint4*>(ob)[0];
+                    od[1] = reinterpret_cast<const uint4*>(ob)[1];
+                    if (ea.t)
+                        for (int i = 0; i < 16; ++i) ea.t[static_cast<size_t>(nb + i) * ea.ld_t + m] = ob[i];
+                } else {
+                    for (int i = 0; i < 16; ++i) dz[i] = 0.0f;
+                }
+                if (ea.colsum) {
+                    for (int i = 0; i < 16; ++i) {
+                        float x = dz[i];
+                        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                        if (lane == 0) atomicAdd(&ea.colsum[nb + i], x);
+                    }
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+// ------------------------------------------------------------------------------ host side ----
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// Tensor map of a row-major BF16 matrix [rows x cols] read in boxes of box_rows x 64 (128-byte
+// swizzle; reads past the matrix are zero).
+bool make_tmap(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((cols * 2) & 15)) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kChunkK), box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, int EPI>
+cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K,
+                           int splits, int* err, cudaStream_t s) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem_bytes<BN>());
+    });
+    splits = splits < 1 ? 1 : splits;
+    const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
+    const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
+    gemm_kernel<BN, EPI><<<grid, 128, gemm_smem_bytes<BN>(), s>>>(a, b, ea, K, per, err);
+    return cudaGetLastError();
+}
+
+// C = A * B^T tile-width choice by N.
+template <int EPI>
+cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K, int splits,
+                        int* err, cudaStream_t s) {
+    if (N <= 16) return launch_gemm_bn<16, EPI>(a, b, ea, M, N, K, splits, err, s);
+    if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s);
+    return launch_gemm_bn<256, EPI>(a, b, ea, M, N, K, splits, err, s);
+}
+
+int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
+
+}  // namespace sur
+}  // namespace bhk
+
+using namespace bhk;
+using namespace bhk::sur;
+
+// Diagnostic: C (M x N, FP32, row-major) = A (M x K) * B (N x K)^T with A, B BF16 row-major in device
+// memory, on the tensor-core GEMM kernel the surrogate uses. With splits > 1 the K range is split
+// across CTAs and C is accumulated atomically (the caller zeroes it).
+extern "C" bhk_status bhk_tc_gemm(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K,
+                                  int32_t splits, void* stream) {
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || N > 256 || (K % 8) != 0) {
+        set_last_error("bhk_tc_gemm: needs M, N, K > 0, N <= 256, K a multiple of 8");
+        return BHK_EINVAL;
+    }
+    CUtensorMap ta, tb;
+    if (!make_tmap(&ta, A, M, K, kTileM) || !make_tmap(&tb, B, N, K, box_rows_for(N))) {
+        set_last_error("bhk_tc_gemm: tensor map creation failed (16-byte alignment of A, B and rows)");
+        return BHK_EINVAL;
+    }
+    int* err = nullptr;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return BHK_ENOMEM;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaMemsetAsync(err, 0, sizeof(int), s);
+    EpiArgs ea{};
+    ea.M = M;
+    ea.N = N;
+    ea.f32 = C;
+    ea.ld_f32 = N;
+    cudaError_t e = splits > 1 ? launch_gemm<kAtomicF32>(ta, tb, ea, M, N, K, splits, err, s)
+                               : launch_gemm<kStoreF32>(ta, tb, ea, M, N, K, 1, err, s);
+    int h_err = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(err);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_tc_gemm: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    if (h_err) {
+        set_last_error("bhk_tc_gemm: a pipeline wait timed out");
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}
+
+// ============================================================================ the network ====
+
+namespace bhk {
+namespace sur {
+
+constexpr int kIn = 5, kFreq = 32, kFeat = 64, kHid = 256, kOut = 8, kOutPad = 16, kLayers = 5;
+__host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kFeat : kHid; }
+__host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOutPad : kHid; }
+
+// Flat FP32 parameter vector: W_l (fan_out x fan_in, row-major) then b_l, for l = 1..5.
+struct ParamLayout {
+    size_t w[kLayers], b[kLayers], total;
+    ParamLayout() {
+        size_t o = 0;
+        for (int l = 0; l < kLayers; ++l) {
+            w[l] = o;
+            o += static_cast<size_t>(fan_out(l)) * fan_in(l);
+            b[l] = o;
+            o += fan_out(l);
+        }
+        total = o;
+    }
+};
+
+// Input normalisation to [-1, 1]: spin over [0, 0.998], inclination over [5, 89] degrees, log10 r
+// over [log10 20, 3], alpha and beta over +-kImageScale M.
+constexpr float kImageScale = 12.0f;
+
+__device__ __forceinline__ void normalise(const float* x, float u[kIn]) {
+    u[0] = x[0] * (2.0f / 0.998f) - 1.0f;
+    u[1] = (x[1] - 0.0872664626f) * (2.0f / 1.4660765717f) - 1.0f;
+    u[2] = (x[2] - 1.3010299957f) * (2.0f / 1.6989700043f) - 1.0f;
+    u[3] = x[3] * (1.0f / kImageScale);
+    u[4] = x[4] * (1.0f / kImageScale);
+}
+
+// Fourier features f = [sin(2 pi B u), cos(2 pi B u)] of n rays: row-major [n x 64] and, when t is
+// given, transposed [64 x ld_t].
+__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm,
+                               bf16* __restrict__ t, int ld_t, int n) {
+    __shared__ float sb[kFreq * kIn];
+    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float u[kIn];
+    normalise(x + static_cast<size_t>(r) * kIn, u);
+    __align__(16) bf16 f[kFeat];
+#pragma unroll 4
+    for (int j = 0; j < kFreq; ++j) {
+        float p = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) p += sb[j * kIn + i] * u[i];
+        float s, c;
+        sincospif(2.0f * p, &s, &c);
+        f[j] = __float2bfloat16_rn(s);
+        f[kFreq + j] = __float2bfloat16_rn(c);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(rm + static_cast<size_t>(r) * kFeat);
+#pragma unroll
+    for (int q = 0; q < kFeat / 8; ++q) dst[q] = reinterpret_cast<const uint4*>(f)[q];
+    if (t)
+        for (int j = 0; j < kFeat; ++j) t[static_cast<size_t>(j) * ld_t + r] = f[j];
+}
+
+// Loss of a batch and its gradient with respect to the head outputs Y (n x 16, FP32):
+//   cross-entropy over the 3 outcome logits (targets cls in {1 captured, 2 disk, 3 escaped});
+//   disk rays: squared error of r_disk / 30 and of log g;  escaped rays: squared error of the
+//   3-vector escape direction. Mean over the batch. The gradient is that of the weighted sum
+//   w.x CE + w.y MSE(r) + w.z MSE(ln g) + w.w MSE(dir); the loss terms are reported unweighted. dY goes
+//   out as BF16 in both layouts, the head's bias gradient and the loss terms are summed atomically.
+__global__ void loss_kernel(const float* __restrict__ Y, const uint8_t* __restrict__ cls,
+                            const float* __restrict__ tgt, bf16* __restrict__ dy_rm, bf16* __restrict__ dy_t, int ld_t,
+                            float* __restrict__ db, float* __restrict__ loss, int n, float inv_n, float4 w) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    float d[kOutPad];
+#pragma unroll
+    for (int i = 0; i < kOutPad; ++i) d[i] = 0.0f;
+    float ce = 0.0f, lr_ = 0.0f, lg = 0.0f, le = 0.0f;
+    if (r < n) {
+        const float* y = Y + static_cast<size_t>(r) * kOutPad;
+        const float* tg = tgt + static_cast<size_t>(r) * kOut;
+        const int c = static_cast<int>(cls[r]) - 1;
+        const float mx = fmaxf(y[0], fmaxf(y[1], y[2]));
+        const float e0 = __expf(y[0] - mx), e1 = __expf(y[1] - mx), e2 = __expf(y[2] - mx);
+        const float z = e0 + e1 + e2;
+        const float p[3] = {e0 / z, e1 / z, e2 / z};
+        if (c >= 0 && c < 3) {
+            ce = -__logf(fmaxf(p[c], 1e-30f));
+            for (int k = 0; k < 3; ++k) d[k] = w.x * (p[k] - (k == c ? 1.0f : 0.0f)) * inv_n;
+        }
+        if (c == 1) {  // disk
+            const float er = y[3] - tg[3], eg = y[4] - tg[4];
+            lr_ = er * er;
+            lg = eg * eg;
+            d[3] = w.y * 2.0f * er * inv_n;
+            d[4] = w.z * 2.0f * eg * inv_n;
+        } else if (c == 2) {  // escaped
+            for (int k = 5; k < 8; ++k) {
+                const float ev = y[k] - tg[k];
+                le += ev * ev;
+                d[k] = w.w * 2.0f * ev * inv_n;
+            }
+        }
+        __align__(16) bf16 ob[kOutPad];
+#pragma unroll
+        for (int i = 0; i < kOutPad; ++i) ob[i] = __float2bfloat16_rn(d[i]);
+        uint4* dst = reinterpret_cast<uint4*>(dy_rm + static_cast<size_t>(r) * kOutPad);
+        dst[0] = reinterpret_cast<const uint4*>(ob)[0];
+        dst[1] = reinterpret_cast<const uint4*>(ob)[1];
+#pragma unroll
+        for (int i = 0; i < kOutPad; ++i) dy_t[static_cast<size_t>(i) * ld_t + r] = ob[i];
+    }
+#pragma unroll
+    for (int i = 0; i < kOutPad; ++i) {
+        float v = d[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0f) atomicAdd(&db[i], v);
+    }
+    float terms[4] = {ce, lr_, lg, le};
+    for (int k = 0; k < 4; ++k) {
+        float v = terms[k] * inv_n;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) atomicAdd(&loss[k], v);
+    }
+}
+
+// Adam on the flat FP32 parameters; refreshes the BF16 copies W (fan_out x fan_in) and W^T.
+struct AdamArgs {
+    float* p;
+    const float* g;
+    float* m;
+    float* v;
+    bf16* w_rm[kLayers];
+    bf16* w_t[kLayers];
+    size_t wofs[kLayers];
+    size_t total;
+    float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
+};
+
+__global__ void adam_kernel(AdamArgs a) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const float g = a.g[i];
+        const float m = a.b1 * a.m[i] + (1.0f - a.b1) * g;
+        const float v = a.b2 * a.v[i] + (1.0f - a.b2) * g * g;
+        a.m[i] = m;
+        a.v[i] = v;
+        const float w = a.p[i] - a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
+        a.p[i] = w;
+        for (int l = 0; l < kLayers; ++l) {
+            const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+            if (i >= a.wofs[l] && i < a.wofs[l] + n) {
+                const size_t j = i - a.wofs[l];
+                const int o = static_cast<int>(j / fan_in(l)), k = static_cast<int>(j % fan_in(l));
+                const bf16 wb = __float2bfloat16_rn(w);
+                a.w_rm[l][j] = wb;
+                a.w_t[l][static_cast<size_t>(k) * fan_out(l) + o] = wb;
+            }
+        }
+    }
+}
+
+// Writes the BF16 copies of the weights from the FP32 parameters (after initialisation or a set).
+__global__ void refresh_bf16_kernel(AdamArgs a) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        for (int l = 0; l < kLayers; ++l) {
+            const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+            if (i >= a.wofs[l] && i < a.wofs[l] + n) {
+                const size_t j = i - a.wofs[l];
+                const int o = static_cast<int>(j / fan_in(l)), k = static_cast<int>(j % fan_in(l));
+                const bf16 wb = __float2bfloat16_rn(a.p[i]);
+                a.w_rm[l][j] = wb;
+                a.w_t[l][static_cast<size_t>(k) * fan_out(l) + o] = wb;
+            }
+        }
+    }
+}
+
+}  // namespace sur
+}  // namespace bhk
+
+// ======================================================================= the C ABI object ====
+
+struct bhk_surrogate {
+    int device = 0;
+    int cap = 0;  // batch capacity (rows of every activation buffer)
+    bhk::sur::ParamLayout L;
+    float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    bhk::sur::bf16* w_rm[bhk::sur::kLayers] = {};
+    bhk::sur::bf16* w_t[bhk::sur::kLayers] = {};
+    float* Bm = nullptr;
+    bhk::sur::bf16 *F_rm = nullptr, *F_t = nullptr, *dy_rm = nullptr, *dy_t = nullptr;
+    bhk::sur::bf16 *z[4] = {}, *a_rm[4] = {}, *a_t[4] = {}, *dz_rm[2] = {}, *dz_t[2] = {};
+    float* Y = nullptr;
+    float* loss = nullptr;
+    int* err = nullptr;
+    int64_t step = 0;
+    float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
+    std::vector<void*> allocs;
+    std::mutex mu;
+};
+
+namespace bhk {
+namespace sur {
+
+template <typename T>
+bool dalloc(bhk_surrogate* s, T** p, size_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
+    s->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return true;
+}
+
+AdamArgs adam_args(bhk_surrogate* s) {
+    AdamArgs a{};
+    a.p = s->p;
+    a.g = s->g;
+    a.m = s->m;
+    a.v = s->v;
+    for (int l = 0; l < kLayers; ++l) {
+        a.w_rm[l] = s->w_rm[l];
+        a.w_t[l] = s->w_t[l];
+        a.wofs[l] = s->L.w[l];
+    }
+    a.total = s->L.total;
+    return a;
+}
+
+struct Maps {
+    CUtensorMap F_rm, F_t, dy_rm, dy_t, W[kLayers], Wt[kLayers], a_rm[4], a_t[4], dz_rm[2], dz_t[2];
+};
+
+// Tensor maps of the row-major operands for batches of n rows (weights, features, activations,
+// gradients), and with `transposed` also of the transposed copies, whose rows are `cap` long (the
+// K extent of each gradient GEMM, n, bounds what is read of them).
+bool build_maps(bhk_surrogate* s, int n, bool transposed, Maps* M) {
+    bool ok = make_tmap(&M->F_rm, s->F_rm, n, kFeat, kTileM) && make_tmap(&M->dy_rm, s->dy_rm, n, kOutPad, kTileM);
+    for (int l = 0; l < kLayers && ok; ++l) {
+        ok = make_tmap(&M->W[l], s->w_rm[l], fan_out(l), fan_in(l), box_rows_for(fan_out(l))) &&
+             make_tmap(&M->Wt[l], s->w_t[l], fan_in(l), fan_out(l), box_rows_for(fan_in(l)));
+    }
+    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_rm[i], s->a_rm[i], n, kHid, kTileM);
+    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, kHid, kTileM);
+    if (!transposed) return ok;
+    ok = ok && make_tmap(&M->F_t, s->F_t, kFeat, s->cap, 64) && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM);
+    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_t[i], s->a_t[i], kHid, s->cap, 256);
+    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_t[i], s->dz_t[i], kHid, s->cap, kTileM);
+    return ok;
+}
+
+EpiArgs epi(int M, int N) {
+    EpiArgs e{};
+    e.M = M;
+    e.N = N;
+    return e;
+}
+
+// Forward pass of n rows (features already in F): z, activations in both layouts, head into Y.
+cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, bool keep_t, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
+        EpiArgs ea = epi(n, kHid);
+        ea.bias = s->p + s->L.b[l];
+        ea.rm = s->a_rm[l];
+        ea.ld_rm = kHid;
+        ea.t = keep_t ? s->a_t[l] : nullptr;
+        ea.ld_t = s->cap;
+        ea.z = s->z[l];
+        const CUtensorMap& A = l == 0 ? M.F_rm : M.a_rm[l - 1];
+        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, kHid, fan_in(l), 1, s->err, st);
+    }
+    if (e == cudaSuccess) {
+        EpiArgs ea = epi(n, kOutPad);
+        ea.bias = s->p + s->L.b[4];
+        ea.f32 = s->Y;
+        ea.ld_f32 = kOutPad;
+        e = launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, kHid, 1, s->err, st);
+    }
+    return e;
+}
+
+int split_for(int n) {
+    const int s = n / 1024;
+    return s < 1 ? 1 : (s > 96 ? 96 : s);
+}
+
+// Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss.
+cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const float* tgt, int n, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s->g, 0, sizeof(float) * s->L.total, st);
+    if (e != cudaSuccess) return e;
+    loss_kernel<<<(n + 255) / 256, 256, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
+                                                 s->loss, n, 1.0f / n, s->w);
+    const int splits = split_for(n);
+    // Head: dW5 = dY^T A4, then dA4 = dY W5 -> dZ4.
+    {
+        EpiArgs ea = epi(kOutPad, kHid);
+        ea.f32 = s->g + s->L.w[4];
+        ea.ld_f32 = kHid;
+        e = launch_gemm<kAtomicF32>(M.dy_t, M.a_t[3], ea, kOutPad, kHid, n, splits, s->err, st);
+    }
+    if (e == cudaSuccess) {
+        EpiArgs ea = epi(n, kHid);
+        ea.rm = s->dz_rm[0];
+        ea.ld_rm = kHid;
+        ea.t = s->dz_t[0];
+        ea.ld_t = s->cap;
+        ea.z = s->z[3];
+        ea.colsum = s->g + s->L.b[3];
+        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, kHid, kOutPad, 1, s->err, st);
+    }
+    // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
+    int cur = 0;
+    for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
+        EpiArgs ew = epi(kHid, fan_in(l));
+        ew.f32 = s->g + s->L.w[l];
+        ew.ld_f32 = fan_in(l);
+        const CUtensorMap& Bop = l == 0 ? M.F_t : M.a_t[l - 1];
+        e = launch_gemm<kAtomicF32>(M.dz_t[cur], Bop, ew, kHid, fan_in(l), n, splits, s->err, st);
+        if (e != cudaSuccess || l == 0) break;
+        EpiArgs ex = epi(n, kHid);
+        ex.rm = s->dz_rm[1 - cur];
+        ex.ld_rm = kHid;
+        ex.t = s->dz_t[1 - cur];
+        ex.ld_t = s->cap;
+        ex.z = s->z[l - 1];
+        ex.colsum = s->g + s->L.b[l - 1];
+        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, kHid, kHid, 1, s->err, st);
+        cur = 1 - cur;
+    }
+    return e;
+}
+
+bhk_status check_err(bhk_surrogate* s, cudaStream_t st) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("surrogate: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    if (h) {
+        set_last_error("surrogate: a tensor-core pipeline wait timed out");
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}
+
+}  // namespace sur
+}  // namespace bhk
+
+extern "C" {
+
+int64_t bhk_surrogate_num_params(void) { return static_cast<int64_t>(bhk::sur::ParamLayout().total); }
+
+bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bhk_surrogate** out) {
+    using namespace bhk::sur;
+    if (!out || max_batch <= 0 || max_batch % kTileM) {
+        set_last_error("bhk_surrogate_create: max_batch must be a positive multiple of 128");
+        return BHK_EINVAL;
+    }
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        set_last_error("bhk_surrogate_create: no CUDA device (no CPU fallback)");
+        return BHK_ECUDA;
+    }
+    if (!encode_fn()) {
+        set_last_error("bhk_surrogate_create: cuTensorMapEncodeTiled unavailable");
+        return BHK_ECUDA;
+    }
+    auto* s = new bhk_surrogate();
+    s->device = device;
+    s->cap = max_batch;
+    const size_t P = s->L.total, B = static_cast<size_t>(max_batch);
+    bool ok = dalloc(s, &s->p, P) && dalloc(s, &s->g, P) && dalloc(s, &s->m, P) && dalloc(s, &s->v, P) &&
+              dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) && dalloc(s, &s->F_t, B * kFeat) &&
+              dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
+              dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1);
+    for (int l = 0; l < kLayers && ok; ++l) {
+        const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+        ok = dalloc(s, &s->w_rm[l], n) && dalloc(s, &s->w_t[l], n);
+    }
+    for (int i = 0; i < 4 && ok; ++i)
+        ok = dalloc(s, &s->z[i], B * kHid) && dalloc(s, &s->a_rm[i], B * kHid) && dalloc(s, &s->a_t[i], B * kHid);
+    for (int i = 0; i < 2 && ok; ++i) ok = dalloc(s, &s->dz_rm[i], B * kHid) && dalloc(s, &s->dz_t[i], B * kHid);
+    if (!ok) {
+        bhk_surrogate_destroy(s);
+        set_last_error("bhk_surrogate_create: device allocation failed");
+        return BHK_ENOMEM;
+    }
+    // Initialisation (seeded): uniform +-sqrt(6 / fan_in) weights (He-uniform for SiLU), zero biases,
+    // head scaled by 0.1.
+    std::vector<float> hp(P, 0.0f);
+    uint64_t st = seed ? seed : 0x9E3779B97F4A7C15ull;
+    auto next = [&st]() {  // splitmix64
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    auto uni = [&]() { return (next() >> 11) * (1.0 / 9007199254740992.0); };
+    for (int l = 0; l < kLayers; ++l) {
+        const double lim = std::sqrt(6.0 / fan_in(l)) * (l == kLayers - 1 ? 0.1 : 1.0);
+        for (int o = 0; o < fan_out(l); ++o)
+            for (int k = 0; k < fan_in(l); ++k)
+                hp[s->L.w[l] + static_cast<size_t>(o) * fan_in(l) + k] =
+                    (l == kLayers - 1 && o >= kOut) ? 0.0f : static_cast<float>((2.0 * uni() - 1.0) * lim);
+    }
+    // Fourier matrix: row j = f_j d_j with d_j a random unit direction and f_j growing geometrically
+    // from 0.1 to 4 cycles per unit of the normalised input, so that smooth trends and sharp edges
+    // (the shadow, the disk's rim) both have features at their scale.
+    std::vector<float> hb(kFreq * kIn);
+    for (int j = 0; j < kFreq; ++j) {
+        double d[kIn], nrm = 0.0;
+        for (int i = 0; i < kIn; ++i) {
+            const double u1 = std::max(uni(), 1e-300), u2 = uni();
+            d[i] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+            nrm += d[i] * d[i];
+        }
+        const double f = 0.1 * std::pow(40.0, static_cast<double>(j) / (kFreq - 1)) / std::sqrt(nrm);
+        for (int i = 0; i < kIn; ++i) hb[j * kIn + i] = static_cast<float>(f * d[i]);
+    }
+    cudaError_t e = cudaMemcpy(s->p, hp.data(), P * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->Bm, hb.data(), hb.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(s->m, 0, P * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(s->v, 0, P * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(s->err, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        refresh_bf16_kernel<<<256, 256>>>(adam_args(s));
+        e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
+        bhk_surrogate_destroy(s);
+        set_last_error(std::string("bhk_surrogate_create: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    *out = s;
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_destroy(bhk_surrogate* s) {
+    if (!s) return BHK_OK;
+    cudaSetDevice(s->device);
+    cudaDeviceSynchronize();
+    for (void* q : s->allocs) cudaFree(q);
+    delete s;
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_params(bhk_surrogate* s, float* host, int32_t set) {
+    if (!s || !host) return BHK_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    const size_t bytes = s->L.total * sizeof(float);
+    cudaError_t e = set ? cudaMemcpy(s->p, host, bytes, cudaMemcpyHostToDevice)
+                        : cudaMemcpy(host, s->p, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && set) {
+        bhk::sur::refresh_bf16_kernel<<<256, 256>>>(bhk::sur::adam_args(s));
+        e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_surrogate_params: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_fourier(bhk_surrogate* s, float* host, int32_t set) {
+    if (!s || !host) return BHK_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    const size_t bytes = sizeof(float) * bhk::sur::kFreq * bhk::sur::kIn;
+    const cudaError_t e = set ? cudaMemcpy(s->Bm, host, bytes, cudaMemcpyHostToDevice)
+                              : cudaMemcpy(host, s->Bm, bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_surrogate_fourier: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_loss_weights(bhk_surrogate* s, const float* w4) {
+    if (!s || !w4 || !(w4[0] >= 0.0f && w4[1] >= 0.0f && w4[2] >= 0.0f && w4[3] >= 0.0f)) {
+        set_last_error("bhk_surrogate_loss_weights: four non-negative weights expected");
+        return BHK_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->w = make_float4(w4[0], w4[1], w4[2], w4[3]);
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_adam_state(bhk_surrogate* s, float* m, float* v, int64_t* step, int32_t set) {
+    if (!s || !m || !v || !step) return BHK_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    const size_t bytes = s->L.total * sizeof(float);
+    cudaError_t e;
+    if (set) {
+        e = cudaMemcpy(s->m, m, bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->v, v, bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) s->step = *step;
+    } else {
+        e = cudaMemcpy(m, s->m, bytes, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(v, s->v, bytes, cudaMemcpyDeviceToHost);
+        *step = s->step;
+    }
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_surrogate_adam_state: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8_t* cls, const float* tgt, int32_t n,
+                                   float* grads, float* loss) {
+    using namespace bhk::sur;
+    if (!s || !x || !cls || !tgt || n <= 0 || n > s->cap || n % kTileM) {
+        set_last_error("bhk_surrogate_gradients: n must be a multiple of 128 within the batch capacity");
+        return BHK_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    Maps M;
+    if (!build_maps(s, n, true, &M)) {
+        set_last_error("bhk_surrogate_gradients: tensor map creation failed");
+        return BHK_ECUDA;
+    }
+    cudaStream_t st = nullptr;
+    cudaMemsetAsync(s->err, 0, sizeof(int), st);
+    cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
+    feature_kernel<<<(n + 127) / 128, 128, 0, st>>>(x, s->Bm, s->F_rm, s->F_t, s->cap, n);
+    cudaError_t e = forward(s, M, n, true, st);
+    if (e == cudaSuccess) e = backward(s, M, cls, tgt, n, st);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_surrogate_gradients: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    bhk_status rs = check_err(s, st);
+    if (rs != BHK_OK) return rs;
+    if (grads && cudaMemcpy(grads, s->g, sizeof(float) * s->L.total, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return BHK_ECUDA;
+    if (loss && cudaMemcpy(loss, s->loss, 4 * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) return BHK_ECUDA;
+    return BHK_OK;
+}
+
+bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* cls, const float* tgt, int64_t n,
+                               int32_t batch, int64_t steps, float lr0, float* loss_history, void* stream) {
+    using namespace bhk::sur;
+    if (!s || !x || !cls || !tgt || batch <= 0 || batch > s->cap || batch % kTileM || n < batch || steps <= 0 ||
+        !(lr0 > 0.0f)) {
+        set_last_error("bhk_surrogate_train: bad arguments (batch a multiple of 128 within capacity, n >= batch)");
+        return BHK_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    Maps M;
+    if (!build_maps(s, batch, true, &M)) {
+        set_last_error("bhk_surrogate_train: tensor map creation failed");
+        return BHK_ECUDA;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float* hist = nullptr;
+    if (loss_history && cudaMalloc(&hist, sizeof(float) * 4 * steps) != cudaSuccess) return BHK_ENOMEM;
+    cudaMemsetAsync(s->err, 0, sizeof(int), st);
+    const int64_t nb = n / batch;
+    cudaError_t e = cudaSuccess;
+    AdamArgs aa = adam_args(s);
+    aa.b1 = 0.9f;
+    aa.b2 = 0.999f;
+    aa.eps = 1e-8f;
+    for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
+        const int64_t off = (t % nb) * batch;
+        cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
+        feature_kernel<<<(batch + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, s->F_t, s->cap, batch);
+        e = forward(s, M, batch, true, st);
+        if (e == cudaSuccess) e = backward(s, M, cls + off, tgt + off * kOut, batch, st);
+        ++s->step;
+        aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
+        aa.c1 = static_cast<float>(1.0 / (1.0 - std::pow(0.9, static_cast<double>(s->step))));
+        aa.c2 = static_cast<float>(1.0 / (1.0 - std::pow(0.999, static_cast<double>(s->step))));
+        if (e == cudaSuccess) {
+            adam_kernel<<<256, 256, 0, st>>>(aa);
+            e = cudaGetLastError();
+        }
+        if (hist && e == cudaSuccess)
+            e = cudaMemcpyAsync(hist + 4 * t, s->loss, 4 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    }
+    bhk_status rs = e == cudaSuccess ? check_err(s, st) : BHK_ECUDA;
+    if (e != cudaSuccess) set_last_error(std::string("bhk_surrogate_train: ") + cudaGetErrorString(e));
+    if (hist) {
+        if (rs == BHK_OK && cudaMemcpy(loss_history, hist, sizeof(float) * 4 * steps, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rs = BHK_ECUDA;
+        cudaFree(hist);
+    }
+    return rs;
+}
+
+// Surrogate outputs for n rays (n x 8 FP32 per ray: 3 outcome logits, r_disk / 30, log g, escape
+// unit vector) through the layer-by-layer tcgen05 GEMMs.
+bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, float* out, void* stream) {
+    using namespace bhk::sur;
+    if (!s || !x || !out || n < 0) return BHK_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    cudaSetDevice(s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaMemsetAsync(s->err, 0, sizeof(int), st);
+    for (int64_t off = 0; off < n; off += s->cap) {
+        const int rows = static_cast<int>(std::min<int64_t>(s->cap, n - off));
+        Maps M;
+        if (!build_maps(s, rows, false, &M)) {
+            set_last_error("bhk_surrogate_predict: tensor map creation failed");
+            return BHK_ECUDA;
+        }
+        feature_kernel<<<(rows + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, nullptr, 0, rows);
+        cudaError_t e = forward(s, M, rows, false, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(out + off * kOut, kOut * sizeof(float), s->Y, kOutPad * sizeof(float),
+                                  kOut * sizeof(float), rows, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            set_last_error(std::string("bhk_surrogate_predict: ") + cudaGetErrorString(e));
+            return BHK_ECUDA;
+        }
+    }
+    return check_err(s, st);
+}
+
+}  // extern "C"

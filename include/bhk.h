@@ -190,6 +190,50 @@ bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int32_t nframes
 /* FLOPs one accepted FP32 Dormand-Prince step costs in the mixed tracer, counted from its source. */
 double bhk_flops_per_step(void);
 
+/* Diagnostic: C (M x N, FP32, row-major) = A (M x K) * B (N x K)^T, A and B BF16 row-major in device
+ * memory, on the surrogate's tcgen05 GEMM kernel (TMA, TMEM accumulator). N <= 256, K % 8 == 0.
+ * splits > 1 splits K across CTAs and accumulates into C atomically (zero C first). Synchronous. */
+bhk_status bhk_tc_gemm(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t splits,
+                       void* stream);
+
+/* ---- Surrogate (no counterpart in the reference: the reference has no learned model) ----
+ * A BF16 MLP of the tracer: per ray (a, theta_obs, log10 r_obs, alpha, beta) -> 64 Fourier features
+ * -> 4 x (256, SiLU) -> 8 outputs: 3 outcome logits (captured, disk, escaped), r_disk / 30, ln g and
+ * the unit escape direction (sin th cos ph, sin th sin ph, cos th) of (theta_inf, phi_inf). Trained and
+ * run by hand-written tcgen05 kernels (BF16 operands, FP32 accumulation, FP32 master weights and
+ * Adam state). Inputs are FP32 [n x 5] rows in device memory; class labels are 1/2/3 (the
+ * bhk_ray_outcome values), targets FP32 [n x 8] rows in the output convention above. */
+typedef struct bhk_surrogate bhk_surrogate;
+int64_t bhk_surrogate_num_params(void);
+/* max_batch: rows of every activation buffer (a multiple of 128). Seeded initialisation. */
+bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bhk_surrogate** out);
+bhk_status bhk_surrogate_destroy(bhk_surrogate* s);
+/* Copies the FP32 parameter vector out (set = 0) or in (set != 0); host memory. Layout: for each
+ * layer W (fan_out x fan_in, row-major) then b; fan (64->256, 256->256 x 3, 256->16 with the head's
+ * rows 8..15 padding that stays zero). */
+bhk_status bhk_surrogate_params(bhk_surrogate* s, float* host, int32_t set);
+/* The Fourier matrix B (32 x 5, host) of the features [sin, cos](2 pi B u): read (set = 0) or
+ * replaced (set != 0). It is not trained; the default is seeded (random directions, frequencies
+ * 0.1 .. 4 cycles per unit of the normalised input). */
+bhk_status bhk_surrogate_fourier(bhk_surrogate* s, float* host, int32_t set);
+/* Weights of the loss terms in the gradient (CE, r_disk MSE, ln g MSE, direction MSE; default
+ * 1, 10, 10, 10: the regression terms are ~100x smaller than the cross-entropy at the start). */
+bhk_status bhk_surrogate_loss_weights(bhk_surrogate* s, const float* w4);
+/* Adam moments (host, num_params floats each) and step count, read or restored (set != 0), for
+ * checkpoint and resume together with bhk_surrogate_params and bhk_surrogate_fourier. */
+bhk_status bhk_surrogate_adam_state(bhk_surrogate* s, float* m, float* v, int64_t* step, int32_t set);
+/* Loss terms (host float[4]: cross-entropy, r_disk MSE, ln g MSE, direction MSE, batch means) and the
+ * FP32 gradient of their sum (host, num_params) for n rows (n % 128 == 0), without an update. */
+bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8_t* cls, const float* target,
+                                   int32_t n, float* grads, float* loss);
+/* steps Adam updates (beta 0.9 / 0.999) on consecutive batches of `batch` rows cycling through the n
+ * rows given, with learning rate lr0 * (1 + cos(pi t / steps)) / 2. loss_history (host, 4 x steps
+ * floats) may be NULL. Synchronous. */
+bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* cls, const float* target, int64_t n,
+                               int32_t batch, int64_t steps, float lr0, float* loss_history, void* stream);
+/* Network outputs (FP32 [n x 8], device) for n rays, layer by layer. Synchronous. */
+bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, float* out, void* stream);
+
 /* Diagnostic: the device's FP32 FMA throughput (TFLOP/s, FMA = 2 FLOPs) measured with a
  * latency-covered FMA chain kernel, the roofline denominator of the tracer. No reference counterpart. */
 bhk_status bhk_fp32_fma_peak(int device, double* tflops);
