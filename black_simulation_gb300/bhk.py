@@ -62,6 +62,14 @@ class StatsC(C.Structure):
                 ("kernel_ms", C.c_double)]
 
 
+class RenderOptsC(C.Structure):
+    _fields_ = [("p_min", C.c_double), ("band", C.c_double), ("fallback", C.c_int32), ("pad", C.c_int32)]
+
+
+class RenderStatsC(C.Structure):
+    _fields_ = [("rays", C.c_int64), ("fallback", C.c_int64), ("infer_ms", C.c_double), ("trace_ms", C.c_double)]
+
+
 @dataclasses.dataclass
 class Frame:
     """One ZAMO pinhole camera frame (bhk_frame_desc). Angles in radians."""
@@ -162,6 +170,11 @@ def lib() -> C.CDLL:
         "bhk_surrogate_gradients": (C.c_int, [vp, vp, vp, vp, C.c_int32, vp, vp]),
         "bhk_surrogate_train": (C.c_int, [vp, vp, vp, vp, i64, C.c_int32, i64, C.c_float, vp, vp]),
         "bhk_surrogate_predict": (C.c_int, [vp, vp, i64, vp, vp]),
+        "bhk_surrogate_render": (C.c_int, [vp, vp, C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
+                                           C.POINTER(RenderOptsC), C.POINTER(RaysOutC), C.POINTER(RenderStatsC), vp]),
+        "bhk_surrogate_fallback_list": (C.c_int, [vp, vp, i64, C.POINTER(i64)]),
+        "bhk_trace_pixels": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, vp, i64, C.POINTER(TraceOptsC),
+                                       C.POINTER(RaysOutC), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -419,6 +432,20 @@ class Context:
         outc = _out_c(out)
         check(lib().bhk_trace_rays(self.h, n, _ptr(a), _ptr(r_obs), _ptr(theta_obs), _ptr(alpha), _ptr(beta),
                                    r_disk_in, r_disk_out, C.byref(oc), C.byref(outc), _stream(stream)))
+        return out
+
+    def trace_pixels(self, frames: Sequence[Frame], pixels, opts: TraceOpts = TraceOpts(), out: Optional[dict] = None,
+                     stream=None) -> dict:
+        """Traces the listed global pixel indices (int32 CUDA tensor) of `frames`; compact outputs."""
+        if pixels.dtype.itemsize != 4:
+            raise ValueError("pixels must be int32")
+        arr, nf = self._frames(frames)
+        n = pixels.shape[0]
+        if out is None:
+            out = alloc_outputs(n, f"cuda:{self.device}")
+        oc = opts.c()
+        outc = _out_c(out)
+        check(lib().bhk_trace_pixels(self.h, arr, nf, _ptr(pixels), n, C.byref(oc), C.byref(outc), _stream(stream)))
         return out
 
     def stats(self) -> dict:

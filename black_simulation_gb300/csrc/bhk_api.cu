@@ -198,7 +198,7 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
 LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf}; }
 
 struct Batch {
-    int mode;  // 0 frames, 1 explicit
+    int mode;  // 0 frames, 1 explicit, 2 a list of pixels of the frames (ex[0] = the device list)
     int nframes;
     int64_t n;
     const double* ex[5];
@@ -216,6 +216,14 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
                                  s));
         launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
         launch_rays_frames(c->frames_dev, c->geom, b.nframes, L, r.p, c->ctl, lgrid, s);
+    } else if (b.mode == 2) {
+        BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
+                                 s));
+        launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
+        // The set-up writes the frames' pixel total; the batch is the list.
+        BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
+        launch_rays_list(c->frames_dev, b.nframes, static_cast<const int32_t*>(static_cast<const void*>(b.ex[0])), L,
+                         r.p, c->ctl, lgrid, s);
     } else {
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
         launch_rays_explicit(b.ex[0], b.ex[1], b.ex[2], b.ex[3], b.ex[4], b.r_in, b.r_out, r.p.r_escape, c->geom, L,
@@ -246,7 +254,7 @@ bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Ou
     std::memset(static_cast<void*>(&k), 0, sizeof(GraphKey));  // padding takes part in the comparison
     k.mode = b.mode; k.fp64 = r.fp64; k.nframes = b.nframes; k.block = r.block; k.chunk = r.chunk;
     k.buckets = r.buckets; k.grid = r.grid; k.timed = 0; k.regcap = r.regcap; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
-    k.n_explicit = b.mode == 1 ? 1 : 0;
+    k.n_explicit = b.mode != 0 ? 1 : 0;
     for (int i = 0; i < 5; ++i) k.ex[i] = b.ex[i];
     k.r_in = b.r_in; k.r_out = b.r_out;
     if (!c->exec || !(k == c->gkey)) {
@@ -355,7 +363,50 @@ bhk_status trace_frames_locked(bhk_context* c, const bhk_frame_desc* frames, int
 
 }  // namespace
 
+bhk_status bhk::trace_pixel_list(bhk_context* c, const bhk_frame_desc* frames, int32_t nframes, const int32_t* list,
+                                 int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, bhk_rays_out* used,
+                                 cudaStream_t s) {
+    int64_t total = 0;
+    bhk_status st = check_frames(frames, nframes, &total);
+    if (st != BHK_OK) return st;
+    if (n < 0 || n > total) return fail(BHK_EINVAL, "pixel count out of range");
+    if (n > 0 && !list) return fail(BHK_EINVAL, "pixel list is null");
+    bhk_rays_out o{};
+    if (out) {
+        o = *out;
+    } else {
+        st = ensure_outputs(c, static_cast<size_t>(std::max<int64_t>(n, 1)));
+        if (st != BHK_OK) return st;
+        o = own_outputs(c);
+    }
+    if (used) *used = o;
+    if (n == 0) return BHK_OK;
+    st = ensure_scratch(c, static_cast<size_t>(n), static_cast<size_t>(nframes), static_cast<size_t>(nframes));
+    if (st != BHK_OK) return st;
+    const Resolved r = resolve(c, opts);
+    st = stage_frames(c, frames, nframes);  // also waits until the pinned ray count is free
+    if (st != BHK_OK) return st;
+    *c->n_host = n;
+    Batch b{2, nframes, n, {reinterpret_cast<const double*>(list), nullptr, nullptr, nullptr, nullptr}, 0.0, 0.0};
+    st = run_batch(c, b, r, to_outputs(&o), true, s);
+    if (st != BHK_OK) return st;
+    return finish_call(c, r, n, true, s);
+}
+
+std::mutex& bhk::context_mutex(bhk_context* c) { return c->mu; }
+cudaStream_t bhk::context_stream(bhk_context* c, void* stream) { return pick(c, stream); }
+int bhk::context_device(bhk_context* c) { return c->device; }
+
 extern "C" {
+
+bhk_status bhk_trace_pixels(bhk_context* c, const bhk_frame_desc* frames, int32_t nframes, const int32_t* pixels,
+                            int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream) {
+    if (!c) return fail(BHK_EINVAL, "context is null");
+    if (!out) return fail(BHK_EINVAL, "out is null");
+    std::lock_guard<std::mutex> lock(c->mu);
+    BHK_CUDA(cudaSetDevice(c->device));
+    return trace_pixel_list(c, frames, nframes, pixels, n, opts, out, nullptr, pick(c, stream));
+}
 
 const char* bhk_last_error(void) { return g_last_error.c_str(); }
 const char* bhk_version(void) { return "bhk 0.1 (sm_103a)"; }

@@ -496,4 +496,28 @@ __device__ __forceinline__ T dense(T y0, T y1, const T k[7][5], T h, int i, T sg
     return y0 + sg * (yd + s1 * (b + sg * (c4 + s1 * c5)));
 }
 
+// One point of the analytic critical curve seen by a ZAMO pinhole at (r_obs, theta): the spherical
+// photon orbit at x in [0, 1] along [r_pro, r_retro] (cosine spacing), its (xi, eta) of
+// src/eht.cpp:52-80 launched back through the camera's frame. Returns false where that orbit's
+// photons cannot reach the camera (R(r_obs) <= 0 or Theta(theta) < 0); beta >= 0 (upper half).
+__device__ __forceinline__ bool critical_point(double a, double r_obs, double th, double x, double* alpha,
+                                               double* beta) {
+    const double aa = fabs(a) < 1e-6 ? 1e-6 : a;
+    const double r1 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(-aa))), r2 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(aa)));
+    const double r = r1 + (r2 - r1) * (0.5 - 0.5 * cos(kPi * x));
+    const double xi = (r * r * (3.0 - r) - aa * aa * (r + 1.0)) / (aa * (r - 1.0));
+    const double eta = r * r * r * (4.0 * aa * aa - r * (r - 3.0) * (r - 3.0)) / (aa * aa * (r - 1.0) * (r - 1.0));
+    const Cons c{1.0, xi, eta, 0.0};
+    const double R = radial_potential(aa, c, r_obs), Th = polar_potential(aa, c, th);
+    const MetricAt m = metric_at(aa, r_obs, th);
+    const double varpi = sqrt(m.A / m.sigma) * sin(th);
+    const double eloc = 1.0 - m.omega * xi;
+    const double nr = sqrt(fmax(R, 0.0)) / sqrt(m.sigma * m.delta) / eloc;
+    const double nth = sqrt(fmax(Th, 0.0)) / sqrt(m.sigma) / eloc;
+    const double nph = xi / varpi / eloc;
+    *alpha = r_obs * (-nph) / nr;
+    *beta = r_obs * nth / nr;
+    return R > 0.0 && Th >= 0.0;
+}
+
 }  // namespace bhk

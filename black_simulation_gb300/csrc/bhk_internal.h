@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -88,6 +89,8 @@ void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int
                         Control* ctl, cudaStream_t s);
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s);
+void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, LaunchSoA L, const TraceParams& p,
+                      const Control* ctl, int grid, cudaStream_t s);
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
                           const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
@@ -103,6 +106,17 @@ void launch_critical_curve(double a, double r_obs, double theta_obs, int samples
 
 // Sets the text bhk_last_error() returns on this thread (bhk_api.cu).
 void set_last_error(const std::string& msg);
+
+// ---- context internals for the other translation units (bhk_api.cu) ----
+// Traces pixels list[0..n) (device memory, global pixel indices of the frames) into `out` (compact:
+// entry i is pixel list[i]), or into context-owned device buffers when out is null; *used (if given)
+// receives the buffers written. The caller holds context_mutex(c) and has selected the device.
+bhk_status trace_pixel_list(bhk_context* c, const bhk_frame_desc* frames, int32_t nframes, const int32_t* list,
+                            int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, bhk_rays_out* used,
+                            cudaStream_t s);
+std::mutex& context_mutex(bhk_context* c);
+cudaStream_t context_stream(bhk_context* c, void* stream);  // stream, or the context's own when null
+int context_device(bhk_context* c);
 
 // ---- per-step mirrors (bhk_steps.cu) ----
 cudaError_t steps_derivatives(double a, const bhk_constants* c, const bhk_state* s, bhk_derivatives_t* d, int64_t n,

@@ -25,6 +25,7 @@
 #include <string>
 #include <vector>
 
+#include "bhk_device.cuh"
 #include "bhk_internal.h"
 #include "bhk_tc.cuh"
 
@@ -365,19 +366,11 @@ __device__ __forceinline__ void normalise(const float* x, float u[kIn]) {
     u[4] = x[4] * (1.0f / kImageScale);
 }
 
-// Fourier features f = [sin(2 pi B u), cos(2 pi B u)] of n rays: row-major [n x 64] and, when t is
-// given, transposed [64 x ld_t].
-__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm,
-                               bf16* __restrict__ t, int ld_t, int n) {
-    __shared__ float sb[kFreq * kIn];
-    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
-    __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
+// Fourier features f = [sin(2 pi B u), cos(2 pi B u)] of one ray (x: a, theta, log10 r, alpha, beta).
+__device__ __forceinline__ void fourier_features(const float* x, const float* sb, bf16 f[kFeat]) {
     float u[kIn];
-    normalise(x + static_cast<size_t>(r) * kIn, u);
-    __align__(16) bf16 f[kFeat];
-#pragma unroll 4
+    normalise(x, u);
+#pragma unroll
     for (int j = 0; j < kFreq; ++j) {
         float p = 0.0f;
 #pragma unroll
@@ -387,6 +380,18 @@ __global__ void feature_kernel(const float* __restrict__ x, const float* __restr
         f[j] = __float2bfloat16_rn(s);
         f[kFreq + j] = __float2bfloat16_rn(c);
     }
+}
+
+// Fourier features of n rays: row-major [n x 64] and, when t is given, transposed [64 x ld_t].
+__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm,
+                               bf16* __restrict__ t, int ld_t, int n) {
+    __shared__ float sb[kFreq * kIn];
+    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    __align__(16) bf16 f[kFeat];
+    fourier_features(x + static_cast<size_t>(r) * kIn, sb, f);
     uint4* dst = reinterpret_cast<uint4*>(rm + static_cast<size_t>(r) * kFeat);
 #pragma unroll
     for (int q = 0; q < kFeat / 8; ++q) dst[q] = reinterpret_cast<const uint4*>(f)[q];
@@ -529,6 +534,14 @@ struct bhk_surrogate {
     float* loss = nullptr;
     int* err = nullptr;
     int64_t step = 0;
+    // render scratch (grow-only)
+    void* frames_dev = nullptr;
+    size_t cap_frames = 0;
+    int32_t* list = nullptr;
+    size_t cap_list = 0;
+    unsigned long long* n_list = nullptr;
+    unsigned long long* n_list_host = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
     std::vector<void*> allocs;
     std::mutex mu;
@@ -709,7 +722,9 @@ bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bh
     bool ok = dalloc(s, &s->p, P) && dalloc(s, &s->g, P) && dalloc(s, &s->m, P) && dalloc(s, &s->v, P) &&
               dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) && dalloc(s, &s->F_t, B * kFeat) &&
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
-              dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1);
+              dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
+              dalloc(s, &s->n_list, 1) && cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
+    for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreate(&s->ev[i]) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
         const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
         ok = dalloc(s, &s->w_rm[l], n) && dalloc(s, &s->w_t[l], n);
@@ -777,6 +792,11 @@ bhk_status bhk_surrogate_destroy(bhk_surrogate* s) {
     cudaSetDevice(s->device);
     cudaDeviceSynchronize();
     for (void* q : s->allocs) cudaFree(q);
+    if (s->frames_dev) cudaFree(s->frames_dev);
+    if (s->list) cudaFree(s->list);
+    if (s->n_list_host) cudaFreeHost(s->n_list_host);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
     delete s;
     return BHK_OK;
 }
@@ -959,3 +979,581 @@ bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, fl
 }
 
 }  // extern "C"
+
+// ====================================================== fused inference with integrator fallback ====
+//
+// One persistent kernel runs the whole network for 128-ray tiles: the rays' inputs come from the
+// frame table (no input array), features and activations live in shared memory as the next layer's
+// tcgen05 A operand (K-major, 128-byte swizzled, as TMA would have written them), accumulators in
+// TMEM (256 columns per CTA, two CTAs per SM so that one CTA's epilogue overlaps the other's MMAs),
+// and the weights stream from L2 through a 2-stage TMA ring in 128-row x 64-K chunks (30 per tile).
+// Warp 0 loads, warp 1 issues the MMAs, warps 2-5 (one TMEM lane quadrant each, thread = ray) compute
+// the features, the SiLU epilogues, the head's decode and the fallback decision, appending fallback
+// rays to a list with one atomic per warp.
+
+namespace bhk {
+namespace sur {
+
+constexpr int kCurveBins = 512;
+constexpr int kCurveSamples = 2048;
+
+// Per frame: pixel mapping, the network's per-frame inputs, and the critical curve in polar form
+// about its centre (alpha_c, 0) for the band test.
+struct SurFrame {
+    double alpha_lo, beta_hi, px, py;
+    long long offset;
+    int width, height;
+    float a, th, log_r, alpha_c;
+    float snap;              // |alpha| below this: the axis-snap strip of kerr.h's kAxisSnap
+    int curve_ok;
+    float pad[2];
+    float rho[kCurveBins];   // curve radius at psi_j = pi (j + 0.5) / kCurveBins, psi = atan2(|beta|, alpha - alpha_c)
+    float kn[kCurveBins];    // rho / sqrt(rho^2 + (d rho / d psi)^2): radial offset -> normal distance
+};
+
+// Polar table of each frame's critical curve (one block per frame).
+__global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc) {
+    __shared__ float sa[kCurveSamples], sbt[kCurveSamples];
+    __shared__ float s_min, s_max;
+    __shared__ int s_any;
+    SurFrame& f = frames[blockIdx.x];
+    const bhk_frame_desc d = desc[blockIdx.x];
+    for (int k = threadIdx.x; k < kCurveSamples; k += blockDim.x) {
+        double al, be;
+        const bool ok = critical_point(d.a, d.r_obs, d.theta_obs, static_cast<double>(k) / (kCurveSamples - 1), &al, &be);
+        sa[k] = ok ? static_cast<float>(al) : nanf("");
+        sbt[k] = ok ? static_cast<float>(be) : nanf("");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float mn = 1e30f, mx = -1e30f;
+        int any = 0;
+        for (int k = 0; k < kCurveSamples; ++k)
+            if (sa[k] == sa[k]) {
+                mn = fminf(mn, sa[k]);
+                mx = fmaxf(mx, sa[k]);
+                any = 1;
+            }
+        s_min = mn;
+        s_max = mx;
+        s_any = any;
+    }
+    __syncthreads();
+    const float ac = 0.5f * (s_min + s_max);
+    // psi and rho of the samples (in place)
+    for (int k = threadIdx.x; k < kCurveSamples; k += blockDim.x) {
+        const float da = sa[k] - ac, b = sbt[k];
+        sa[k] = atan2f(b, da);  // NaN stays NaN
+        sbt[k] = sqrtf(da * da + b * b);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kCurveBins; j += blockDim.x) {
+        const float psi = 3.14159265f * (j + 0.5f) / kCurveBins;
+        float rho = -1.0f, best = 1e30f, near_rho = -1.0f;
+        for (int k = 0; k + 1 < kCurveSamples; ++k) {
+            const float p0 = sa[k], p1 = sa[k + 1];
+            if (!(p0 == p0) || !(p1 == p1)) continue;
+            if ((psi - p0) * (psi - p1) <= 0.0f && p0 != p1) {
+                const float t = (psi - p0) / (p1 - p0);
+                rho = sbt[k] + t * (sbt[k + 1] - sbt[k]);
+                break;
+            }
+            const float dd = fabsf(psi - p0);
+            if (dd < best) {
+                best = dd;
+                near_rho = sbt[k];
+            }
+        }
+        f.rho[j] = rho > 0.0f ? rho : near_rho;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kCurveBins; j += blockDim.x) {
+        const int jm = j > 0 ? j - 1 : 0, jp = j + 1 < kCurveBins ? j + 1 : kCurveBins - 1;
+        const float dpsi = 3.14159265f * (jp - jm) / kCurveBins;
+        const float drho = (f.rho[jp] - f.rho[jm]) / dpsi, r = f.rho[j];
+        f.kn[j] = r > 0.0f ? r / sqrtf(r * r + drho * drho) : 1.0f;
+    }
+    if (threadIdx.x == 0) {
+        f.alpha_c = ac;
+        f.curve_ok = s_any;
+    }
+}
+
+constexpr int kInfStages = 2;
+constexpr int kTileRays = 128;
+constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 (activations or weights)
+constexpr int kHeadChunkBytes = 16 * 64 * 2;
+constexpr int kChunksPerTile = 2 + 3 * 8 + 4;
+constexpr int kInfThreads = 192;
+constexpr int kInfSmem = 4 * kChunkBytes + kInfStages * kChunkBytes + 1024 + 1024;
+
+struct InferArgs {
+    const SurFrame* frames;
+    int nframes;
+    long long n;
+    const float* Bm;
+    const float* bias[kLayers];
+    uint8_t* outcome;
+    double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
+    int32_t *steps, *rejected;
+    int32_t* list;
+    unsigned long long* n_list;
+    float p_min, band;
+    int* err;
+};
+
+// Byte offset of (row, col) in a 128-row x 64-column BF16 tile with the 128-byte swizzle.
+__device__ __forceinline__ uint32_t sw128(int row, int col) {
+    return static_cast<uint32_t>(row * 128 + ((((col >> 3) ^ (row & 7))) << 4) + ((col & 7) << 1));
+}
+
+// Stores 16 BF16 of `row`, columns c0 .. c0+15 of the 256-wide activation (4 chunks of 64 columns).
+__device__ __forceinline__ void store_act16(uint8_t* act, int row, int c0, const bf16* v) {
+    uint8_t* chunk = act + (c0 >> 6) * kChunkBytes;
+    const int c = c0 & 63;
+    *reinterpret_cast<uint4*>(chunk + sw128(row, c)) = reinterpret_cast<const uint4*>(v)[0];
+    *reinterpret_cast<uint4*>(chunk + sw128(row, c + 8)) = reinterpret_cast<const uint4*>(v)[1];
+}
+
+__global__ void __launch_bounds__(kInfThreads, 2)
+infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
+             const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
+             const __grid_constant__ CUtensorMap tW4, InferArgs ia) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* act = base;
+    uint8_t* ring = base + 4 * kChunkBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kChunkBytes);
+    uint64_t* empty = full + kInfStages;
+    uint64_t* act_ready = empty + kInfStages;
+    uint64_t* acc_full = act_ready + 1;
+    uint64_t* drain = acc_full + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    float* sB = reinterpret_cast<float*>(tmem_slot + 4);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
+    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < kInfStages; ++st) {
+            tc::mbar_init(&full[st], 1);
+            tc::mbar_init(&empty[st], 1);
+        }
+        tc::mbar_init(act_ready, 128);
+        tc::mbar_init(acc_full, 1);
+        tc::mbar_init(drain, 1);
+        *abort_flag = 0;
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tW0);
+        tc::prefetch_tmap(&tW1);
+        tc::prefetch_tmap(&tW2);
+        tc::prefetch_tmap(&tW3);
+        tc::prefetch_tmap(&tW4);
+    }
+    if (warp == 1) tc::tmem_alloc(tmem_slot, 256);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    auto give_up = [&]() {
+        *abort_flag = 1;
+        atomicExch(ia.err, 1);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---- TMA producer: 30 weight chunks per tile, in the MMA's order
+            long long k = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int c = 0; c < kChunksPerTile; ++c, ++k) {
+                    if (*abort_flag) { ok = false; break; }
+                    const int st = static_cast<int>(k % kInfStages);
+                    const long long j = k / kInfStages;
+                    if (j > 0 && !tc::mbar_wait(&empty[st], static_cast<uint32_t>((j - 1) & 1))) {
+                        give_up();
+                        ok = false;
+                        break;
+                    }
+                    int l, nh, kc;
+                    if (c < 2) { l = 0; nh = c; kc = 0; }
+                    else if (c < 26) { const int q = c - 2; l = 1 + q / 8; nh = (q & 7) >> 2; kc = q & 3; }
+                    else { l = 4; nh = 0; kc = c - 26; }
+                    const CUtensorMap* m = l == 0 ? &tW0 : l == 1 ? &tW1 : l == 2 ? &tW2 : l == 3 ? &tW3 : &tW4;
+                    tc::mbar_expect_tx(&full[st], l < 4 ? kChunkBytes : kHeadChunkBytes);
+                    tc::tma_load_2d(ring + st * kChunkBytes, m, kc * 64, nh * 128, &full[st]);
+                }
+            }
+            // Let every load issued land before the CTA may exit (bounded).
+            for (long long q = k - kInfStages; q < k; ++q)
+                if (q >= 0) tc::mbar_wait(&full[q % kInfStages], static_cast<uint32_t>((q / kInfStages) & 1));
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // ---- MMA issuer
+            constexpr uint32_t kId128 = tc::idesc_bf16(128, 128), kId16 = tc::idesc_bf16(128, 16);
+            long long k = 0;
+            uint32_t act_n = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int l = 0; l < kLayers && ok; ++l) {
+                    if (*abort_flag || !tc::mbar_wait(act_ready, act_n & 1)) {
+                        if (!*abort_flag) give_up();
+                        ok = false;
+                        break;
+                    }
+                    ++act_n;
+                    tc::fence_after_sync();
+                    const int nch = l == 0 ? 2 : (l < 4 ? 8 : 4);
+                    for (int q = 0; q < nch; ++q, ++k) {
+                        const int st = static_cast<int>(k % kInfStages);
+                        if (!tc::mbar_wait(&full[st], static_cast<uint32_t>((k / kInfStages) & 1))) {
+                            give_up();
+                            ok = false;
+                            break;
+                        }
+                        tc::fence_after_sync();
+                        const int nh = l == 0 ? q : (l < 4 ? q >> 2 : 0);
+                        const int kc = l == 0 ? 0 : (l < 4 ? q & 3 : q);
+                        const uint64_t ad = tc::smem_desc_sw128(act + kc * kChunkBytes);
+                        const uint64_t bd = tc::smem_desc_sw128(ring + st * kChunkBytes);
+                        const uint32_t d = tmem + static_cast<uint32_t>(l < 4 ? nh * 128 : 0);
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                            tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId128 : kId16, (kc | kk) ? 1u : 0u);
+                        tc::mma_commit(&empty[st]);
+                    }
+                    if (ok) tc::mma_commit(acc_full);
+                }
+            }
+            // All MMAs issued have finished before TMEM is released (bounded).
+            tc::mma_commit(drain);
+            tc::mbar_wait(drain, 0);
+        }
+    } else {  // ---- warps 2..5: features, epilogues, decode (thread = ray of the tile)
+        const int q4 = warp & 3;
+        const int row = 32 * q4 + lane;
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16);
+        uint32_t acc_n = 0;
+        // Every exit decision is taken by the whole warp (the TMEM loads and the list append are
+        // warp-collective).
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            if (__any_sync(0xffffffffu, *abort_flag)) break;
+            const long long ray = tile * kTileRays + row;
+            const bool live = ray < ia.n;
+            int fi = 0;
+            float alpha = 0.0f, beta = 0.0f;
+            __align__(16) bf16 feat[kFeat];
+            if (live) {
+                int lo = 0, hi = ia.nframes - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
+                }
+                fi = lo;
+                const SurFrame& f = ia.frames[fi];
+                const int local = static_cast<int>(ray - f.offset);
+                const int pr = local / f.width, pc = local - pr * f.width;
+                alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
+                beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
+                const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
+                fourier_features(x, sB, feat);
+            } else {
+#pragma unroll
+                for (int i = 0; i < kFeat; ++i) feat[i] = __float2bfloat16_rn(0.0f);
+            }
+#pragma unroll
+            for (int c = 0; c < kFeat; c += 16) store_act16(act, row, c, feat + c);
+            tc::fence_proxy_async();
+            tc::fence_before_sync();
+            tc::mbar_arrive(act_ready);
+            bool ok = true;
+            for (int l = 0; l < 4; ++l) {
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(acc_full, acc_n & 1))) {
+                    if (lane == 0) give_up();
+                    ok = false;
+                    break;
+                }
+                ++acc_n;
+                tc::fence_after_sync();
+                const float* bl = ia.bias[l];
+#pragma unroll 1
+                for (int j = 0; j < 16; ++j) {
+                    float v[16];
+                    tc::tmem_ld16(trow + 16 * j, v);
+                    __align__(16) bf16 ab[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const float z = v[i] + __ldg(bl + 16 * j + i);
+                        ab[i] = __float2bfloat16_rn(z * sigmoidf(z));
+                    }
+                    store_act16(act, row, 16 * j, ab);
+                }
+                tc::fence_proxy_async();
+                tc::fence_before_sync();
+                tc::mbar_arrive(act_ready);
+            }
+            if (!ok) break;
+            if (!__all_sync(0xffffffffu, tc::mbar_wait(acc_full, acc_n & 1))) {
+                if (lane == 0) give_up();
+                break;
+            }
+            ++acc_n;
+            tc::fence_after_sync();
+            float y[16];
+            tc::tmem_ld16(trow, y);
+            tc::fence_before_sync();
+            bool fb = false;
+            if (live) {
+                const float* b4 = ia.bias[4];
+#pragma unroll
+                for (int i = 0; i < kOut; ++i) y[i] += __ldg(b4 + i);
+                int cls = 0;
+                float mx = y[0];
+                if (y[1] > mx) { mx = y[1]; cls = 1; }
+                if (y[2] > mx) { mx = y[2]; cls = 2; }
+                const float zsum = __expf(y[0] - mx) + __expf(y[1] - mx) + __expf(y[2] - mx);
+                const float pmax = 1.0f / zsum;
+                const double nan = __longlong_as_double(0x7ff8000000000000ll);
+                double rd = nan, gg = nan, ti = nan, pi = nan;
+                if (cls == 1) {
+                    rd = 30.0 * y[3];
+                    gg = __expf(y[4]);
+                } else if (cls == 2) {
+                    const float nrm = sqrtf(y[5] * y[5] + y[6] * y[6] + y[7] * y[7]);
+                    const float dz = fminf(1.0f, fmaxf(-1.0f, y[7] / nrm));
+                    ti = acosf(dz);
+                    pi = atan2f(y[6], y[5]);
+                }
+                const SurFrame& f = ia.frames[fi];
+                bool band = false;
+                if (f.curve_ok) {
+                    const float da = alpha - f.alpha_c, ab_ = fabsf(beta);
+                    const float psi = atan2f(ab_, da);
+                    const int jb = min(kCurveBins - 1, max(0, static_cast<int>(psi * (kCurveBins / 3.14159265f))));
+                    band = fabsf(sqrtf(da * da + ab_ * ab_) - f.rho[jb]) * f.kn[jb] < ia.band;
+                }
+                fb = pmax < ia.p_min || band || fabsf(alpha) < f.snap || !(zsum == zsum);
+                ia.outcome[ray] = static_cast<uint8_t>(cls + 1);
+                if (ia.r_disk) ia.r_disk[ray] = rd;
+                if (ia.phi_disk) ia.phi_disk[ray] = nan;
+                if (ia.g) ia.g[ray] = gg;
+                if (ia.theta_inf) ia.theta_inf[ray] = ti;
+                if (ia.phi_inf) ia.phi_inf[ray] = pi;
+                if (ia.steps) ia.steps[ray] = 0;
+                if (ia.rejected) ia.rejected[ray] = 0;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, fb);
+            if (m) {
+                unsigned long long b0 = 0;
+                if (lane == 0) b0 = atomicAdd(ia.n_list, static_cast<unsigned long long>(__popc(m)));
+                b0 = __shfl_sync(0xffffffffu, b0, 0);
+                if (fb) ia.list[b0 + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(ray);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 1) tc::tmem_dealloc(tmem, 256);
+}
+
+// Copies compact fallback results (entry i = pixel list[i]) into the full-image outputs.
+__global__ void scatter_kernel(const int32_t* __restrict__ list, long long n, bhk_rays_out src, bhk_rays_out dst) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long p = list[i];
+        if (dst.outcome) dst.outcome[p] = src.outcome[i];
+        if (dst.r_disk) dst.r_disk[p] = src.r_disk[i];
+        if (dst.phi_disk) dst.phi_disk[p] = src.phi_disk[i];
+        if (dst.g) dst.g[p] = src.g[i];
+        if (dst.theta_inf) dst.theta_inf[p] = src.theta_inf[i];
+        if (dst.phi_inf) dst.phi_inf[p] = src.phi_inf[i];
+        if (dst.steps) dst.steps[p] = src.steps[i];
+        if (dst.rejected) dst.rejected[p] = src.rejected[i];
+    }
+}
+
+}  // namespace sur
+}  // namespace bhk
+
+extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, const bhk_frame_desc* frames,
+                                           int32_t nframes, const bhk_trace_opts* opts,
+                                           const bhk_render_opts* ropts, const bhk_rays_out* out,
+                                           bhk_render_stats* stats, void* stream) {
+    using namespace bhk::sur;
+    if (!s || !ctx || !frames || nframes <= 0 || !out || !out->outcome) {
+        set_last_error("bhk_surrogate_render: null argument (outcome output required)");
+        return BHK_EINVAL;
+    }
+    long long total = 0;
+    for (int i = 0; i < nframes; ++i) {
+        const bhk_frame_desc& d = frames[i];
+        if (d.width <= 0 || d.height <= 0 || !(std::fabs(d.a) < 1.0) || !(d.theta_obs > 0.0 && d.theta_obs < M_PI) ||
+            !(d.r_obs > 1.0 + std::sqrt(1.0 - d.a * d.a)) || !(d.r_disk_out >= 0.0)) {
+            set_last_error("bhk_surrogate_render: invalid frame");
+            return BHK_EINVAL;
+        }
+        total += static_cast<long long>(d.width) * d.height;
+    }
+    if (total > (1ll << 31) - 1) {
+        set_last_error("bhk_surrogate_render: more than 2^31 - 1 rays in one call");
+        return BHK_EINVAL;
+    }
+    bhk_render_opts ro{};
+    ro.p_min = 0.99;
+    ro.band = 0.05;
+    ro.fallback = 1;
+    if (ropts) ro = *ropts;
+    std::lock_guard<std::mutex> lock_ctx(bhk::context_mutex(ctx));
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (cudaSetDevice(s->device) != cudaSuccess || bhk::context_device(ctx) != s->device) {
+        set_last_error("bhk_surrogate_render: surrogate and context must share the device");
+        return BHK_EINVAL;
+    }
+    cudaStream_t st = bhk::context_stream(ctx, stream);
+    // scratch
+    auto fail_cuda = [](cudaError_t e, const char* what) {
+        set_last_error(std::string("bhk_surrogate_render: ") + what + ": " + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    };
+    cudaError_t e = cudaSuccess;
+    const size_t fbytes = sizeof(SurFrame) * nframes + sizeof(bhk_frame_desc) * nframes;
+    if (fbytes > s->cap_frames) {
+        if (s->frames_dev) cudaFree(s->frames_dev);
+        s->frames_dev = nullptr;
+        e = cudaMalloc(&s->frames_dev, fbytes);
+        s->cap_frames = e == cudaSuccess ? fbytes : 0;
+        if (e != cudaSuccess) return fail_cuda(e, "frame table");
+    }
+    if (static_cast<size_t>(total) > s->cap_list) {
+        if (s->list) cudaFree(s->list);
+        s->list = nullptr;
+        e = cudaMalloc(reinterpret_cast<void**>(&s->list), sizeof(int32_t) * total);
+        s->cap_list = e == cudaSuccess ? static_cast<size_t>(total) : 0;
+        if (e != cudaSuccess) return fail_cuda(e, "fallback list");
+    }
+    std::vector<SurFrame> hf(nframes);
+    long long off = 0;
+    for (int i = 0; i < nframes; ++i) {
+        const bhk_frame_desc& d = frames[i];
+        SurFrame& f = hf[i];
+        std::memset(static_cast<void*>(&f), 0, sizeof(SurFrame));
+        f.alpha_lo = d.alpha_lo;
+        f.beta_hi = d.beta_hi;
+        f.px = (d.alpha_hi - d.alpha_lo) / d.width;
+        f.py = (d.beta_hi - d.beta_lo) / d.height;
+        f.offset = off;
+        f.width = d.width;
+        f.height = d.height;
+        f.a = static_cast<float>(d.a);
+        f.th = static_cast<float>(d.theta_obs);
+        f.log_r = static_cast<float>(std::log10(d.r_obs));
+        // L = 0 snapping acts where |L| < 3e-4 sqrt(Q + a^2 E^2); with L ~ -alpha sin(theta) and
+        // Q + a^2 E^2 below 40 M^2 inside the images this is |alpha| sin(theta) < 2e-3: widened 2x.
+        f.snap = static_cast<float>(4e-3 / std::max(std::sin(d.theta_obs), 0.05));
+        off += static_cast<long long>(d.width) * d.height;
+    }
+    SurFrame* dframes = static_cast<SurFrame*>(s->frames_dev);
+    bhk_frame_desc* ddesc = reinterpret_cast<bhk_frame_desc*>(dframes + nframes);
+    e = cudaMemcpyAsync(dframes, hf.data(), sizeof(SurFrame) * nframes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ddesc, frames, sizeof(bhk_frame_desc) * nframes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail_cuda(e, "frame upload");
+    curve_table_kernel<<<nframes, 256, 0, st>>>(dframes, ddesc);
+    Maps M;
+    CUtensorMap w4;
+    if (!make_tmap(&M.W[0], s->w_rm[0], kHid, kFeat, 128) || !make_tmap(&M.W[1], s->w_rm[1], kHid, kHid, 128) ||
+        !make_tmap(&M.W[2], s->w_rm[2], kHid, kHid, 128) || !make_tmap(&M.W[3], s->w_rm[3], kHid, kHid, 128) ||
+        !make_tmap(&w4, s->w_rm[4], kOutPad, kHid, 16)) {
+        set_last_error("bhk_surrogate_render: tensor map creation failed");
+        return BHK_ECUDA;
+    }
+    static std::once_flag attr;
+    std::call_once(attr, [] { cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem); });
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel, kInfThreads, kInfSmem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    per_sm = std::max(1, std::min(per_sm, 2));  // TMEM: 256 columns per CTA, 512 per SM
+    const long long ntiles = (total + kTileRays - 1) / kTileRays;
+    const int grid = static_cast<int>(std::min<long long>(ntiles, static_cast<long long>(per_sm) * sms));
+    InferArgs ia{};
+    ia.frames = dframes;
+    ia.nframes = nframes;
+    ia.n = total;
+    ia.Bm = s->Bm;
+    for (int l = 0; l < kLayers; ++l) ia.bias[l] = s->p + s->L.b[l];
+    ia.outcome = out->outcome;
+    ia.r_disk = out->r_disk;
+    ia.phi_disk = out->phi_disk;
+    ia.g = out->g;
+    ia.theta_inf = out->theta_inf;
+    ia.phi_inf = out->phi_inf;
+    ia.steps = out->steps;
+    ia.rejected = out->rejected;
+    ia.list = s->list;
+    ia.n_list = s->n_list;
+    ia.p_min = static_cast<float>(ro.p_min);
+    ia.band = static_cast<float>(ro.band);
+    ia.err = s->err;
+    e = cudaMemsetAsync(s->n_list, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
+    if (e != cudaSuccess) return fail_cuda(e, "launch set-up");
+    infer_kernel<<<grid, kInfThreads, kInfSmem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->n_list_host, s->n_list, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail_cuda(e, "inference");
+    {
+        int herr = 0;
+        cudaMemcpy(&herr, s->err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (herr) {
+            set_last_error("bhk_surrogate_render: a tensor-core pipeline wait timed out");
+            return BHK_ECUDA;
+        }
+    }
+    const long long nfb = static_cast<long long>(*s->n_list_host);
+    double trace_ms = 0.0;
+    bhk_status rs = BHK_OK;
+    if (ro.fallback && nfb > 0) {
+        bhk_rays_out used{};
+        rs = bhk::trace_pixel_list(ctx, frames, nframes, s->list, nfb, opts, nullptr, &used, st);
+        if (rs != BHK_OK) return rs;
+        scatter_kernel<<<1024, 256, 0, st>>>(s->list, nfb, used, *out);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev[2], st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_cuda(e, "fallback trace");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, s->ev[1], s->ev[2]) == cudaSuccess) trace_ms = ms;
+        else cudaGetLastError();
+    }
+    if (stats) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]) != cudaSuccess) {
+            cudaGetLastError();
+            ms = 0.0f;
+        }
+        stats->rays = total;
+        stats->fallback = nfb;
+        stats->infer_ms = ms;
+        stats->trace_ms = trace_ms;
+    }
+    return rs;
+}
+
+extern "C" bhk_status bhk_surrogate_fallback_list(bhk_surrogate* s, int32_t* dst, int64_t cap, int64_t* n) {
+    if (!s || !n || cap < 0 || (cap > 0 && !dst)) return BHK_EINVAL;
+    std::lock_guard<std::mutex> lock(s->mu);
+    const int64_t have = s->n_list_host ? static_cast<int64_t>(*s->n_list_host) : 0;
+    *n = have;
+    const int64_t m = std::min(have, cap);
+    if (m > 0) {
+        cudaSetDevice(s->device);
+        if (cudaMemcpy(dst, s->list, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice) != cudaSuccess) {
+            set_last_error("bhk_surrogate_fallback_list: copy failed");
+            return BHK_ECUDA;
+        }
+    }
+    return BHK_OK;
+}

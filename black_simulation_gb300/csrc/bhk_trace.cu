@@ -131,41 +131,55 @@ __device__ __forceinline__ double rsqrt_newton(double x) {
 
 // kerr::photonFromFrame for pixel (alpha, beta) of a ZAMO pinhole, with the camera's metric
 // contractions precomputed: p_mu = (g e_0)_mu - look^i (g e_i)_mu, p^r = e_0^r - look^i e_i^r.
+// Launch record i for global pixel `pix` of the frame table (binary search over frame offsets).
+__device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, int nframes, long long pix,
+                                             long long i, LaunchSoA& L, const TraceParams& p) {
+    int lo = 0, hi = nframes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (frames[mid].offset <= pix) lo = mid; else hi = mid - 1;
+    }
+    const FrameDev& f = frames[lo];
+    const int local = static_cast<int>(pix - f.offset);  // < 2^31 rays per batch
+    const int row = local / f.d.width, col = local - row * f.d.width;
+    const double alpha = f.d.alpha_lo + (col + 0.5) * f.px;
+    const double beta = f.d.beta_hi - (row + 0.5) * f.py;
+    const double lt = -beta * f.inv_r, lp = alpha * f.inv_r;
+    const double inv = rsqrt_newton(1.0 + lt * lt + lp * lp);
+    const double l0 = -inv, l1 = lt * inv, l2 = lp * inv;
+    const double pt = f.el[0][0] - l0 * f.el[1][0] - l1 * f.el[2][0] - l2 * f.el[3][0];
+    const double pth = f.el[0][2] - l0 * f.el[1][2] - l1 * f.el[2][2] - l2 * f.el[3][2];
+    const double pph = f.el[0][3] - l0 * f.el[1][3] - l1 * f.el[2][3] - l2 * f.el[3][3];
+    const double pr_up = f.e[0][1] - l0 * f.e[1][1] - l1 * f.e[2][1] - l2 * f.e[3][1];
+    const double E = -pt;
+    double Lz = pph;
+    const double vr = f.sigma * pr_up;
+    const double vth = pth;
+    const double a2E2 = f.a2 * E * E;
+    double Q = vth * vth + f.cs2 * (Lz * Lz * f.inv_sn2 - a2E2);
+    // kAxisSnap (src/kerr.h:115): |L| < 3e-4 sqrt(Q + a^2 E^2), compared squared.
+    if (Lz * Lz < 9e-8 * dmaxd(Q + a2E2, 0.0)) {
+        Lz = 0.0;
+        Q = vth * vth - f.cs2 * a2E2;
+    }
+    store_launch(L, i, f.d.a, E, Lz, Q, vr, vth, lo, p.buckets);
+}
+
 __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nframes, LaunchSoA L, TraceParams p,
                                      const Control* __restrict__ ctl) {
     const long long n = ctl->n_rays;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        int lo = 0, hi = nframes - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
-        }
-        const FrameDev& f = frames[lo];
-        const int local = static_cast<int>(i - f.offset);  // < 2^31 rays per batch
-        const int row = local / f.d.width, col = local - row * f.d.width;
-        const double alpha = f.d.alpha_lo + (col + 0.5) * f.px;
-        const double beta = f.d.beta_hi - (row + 0.5) * f.py;
-        const double lt = -beta * f.inv_r, lp = alpha * f.inv_r;
-        const double inv = rsqrt_newton(1.0 + lt * lt + lp * lp);
-        const double l0 = -inv, l1 = lt * inv, l2 = lp * inv;
-        const double pt = f.el[0][0] - l0 * f.el[1][0] - l1 * f.el[2][0] - l2 * f.el[3][0];
-        const double pth = f.el[0][2] - l0 * f.el[1][2] - l1 * f.el[2][2] - l2 * f.el[3][2];
-        const double pph = f.el[0][3] - l0 * f.el[1][3] - l1 * f.el[2][3] - l2 * f.el[3][3];
-        const double pr_up = f.e[0][1] - l0 * f.e[1][1] - l1 * f.e[2][1] - l2 * f.e[3][1];
-        const double E = -pt;
-        double Lz = pph;
-        const double vr = f.sigma * pr_up;
-        const double vth = pth;
-        const double a2E2 = f.a2 * E * E;
-        double Q = vth * vth + f.cs2 * (Lz * Lz * f.inv_sn2 - a2E2);
-        // kAxisSnap (src/kerr.h:115): |L| < 3e-4 sqrt(Q + a^2 E^2), compared squared.
-        if (Lz * Lz < 9e-8 * dmaxd(Q + a2E2, 0.0)) {
-            Lz = 0.0;
-            Q = vth * vth - f.cs2 * a2E2;
-        }
-        store_launch(L, i, f.d.a, E, Lz, Q, vr, vth, lo, p.buckets);
-    }
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        launch_pixel(frames, nframes, i, i, L, p);
+}
+
+// Launch records for a list of global pixel indices (record i traces pixel list[i]).
+__global__ void launch_list_kernel(const FrameDev* __restrict__ frames, int nframes, const int32_t* __restrict__ list,
+                                   LaunchSoA L, TraceParams p, const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        launch_pixel(frames, nframes, list[i], i, L, p);
 }
 
 __global__ void launch_explicit_kernel(const double* __restrict__ a, const double* __restrict__ r_obs,
@@ -757,23 +771,10 @@ __global__ void critical_curve_kernel(double a, double r_obs, double th, int sam
     const int n = (samples > 16 ? samples : 16) * 8;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > n) return;
-    const double aa = fabs(a) < 1e-6 ? 1e-6 : a;
-    const double r1 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(-aa))), r2 = 2.0 * (1.0 + cos(2.0 / 3.0 * acos(aa)));
-    const double x = 0.5 - 0.5 * cos(kPi * k / n);
-    const double r = r1 + (r2 - r1) * x;
-    const double xi = (r * r * (3.0 - r) - aa * aa * (r + 1.0)) / (aa * (r - 1.0));
-    const double eta = r * r * r * (4.0 * aa * aa - r * (r - 3.0) * (r - 3.0)) / (aa * aa * (r - 1.0) * (r - 1.0));
-    const Cons c{1.0, xi, eta, 0.0};
-    const double R = radial_potential(aa, c, r_obs), Th = polar_potential(aa, c, th);
-    const MetricAt m = metric_at(aa, r_obs, th);
-    const double varpi = sqrt(m.A / m.sigma) * sin(th);
-    const double eloc = 1.0 - m.omega * xi;
-    const double nr = sqrt(R) / sqrt(m.sigma * m.delta) / eloc;
-    const double nth = sqrt(fmax(Th, 0.0)) / sqrt(m.sigma) / eloc;
-    const double nph = xi / varpi / eloc;
-    valid[k] = (R > 0.0 && Th >= 0.0) ? 1 : 0;
-    alpha[k] = r_obs * (-nph) / nr;
-    beta[k] = r_obs * nth / nr;
+    double al, be;
+    valid[k] = critical_point(a, r_obs, th, static_cast<double>(k) / n, &al, &be) ? 1 : 0;
+    alpha[k] = al;
+    beta[k] = be;
 }
 
 }  // namespace
@@ -790,6 +791,11 @@ void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes
                         const Control* ctl, int grid, cudaStream_t s) {
     (void)geom;
     launch_frames_kernel<<<grid, 128, 0, s>>>(frames, nframes, L, p, ctl);
+}
+
+void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, LaunchSoA L, const TraceParams& p,
+                      const Control* ctl, int grid, cudaStream_t s) {
+    launch_list_kernel<<<grid, 128, 0, s>>>(frames, nframes, list, L, p, ctl);
 }
 
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,

@@ -178,6 +178,33 @@ class Surrogate:
         return y
 
 
+    def render(self, ctx, frames, opts=None, p_min: float = 0.99, band: float = 0.05, fallback: bool = True,
+               out: Optional[dict] = None, stream=None):
+        """Surrogate + integrator-fallback render of `frames` (bhk.Frame list) through the fused
+        inference kernel; returns (outputs as bhk.alloc_outputs gives, stats dict)."""
+        n = sum(f.rays for f in frames)
+        if out is None:
+            out = bhk.alloc_outputs(n, f"cuda:{self.device}")
+        arr = (bhk.FrameDescC * len(frames))(*[f.c() for f in frames])
+        oc = (opts or bhk.TraceOpts("mixed")).c()
+        ro = bhk.RenderOptsC(p_min, band, 1 if fallback else 0, 0)
+        st = bhk.RenderStatsC()
+        outc = bhk._out_c(out)
+        bhk.check(bhk.lib().bhk_surrogate_render(self._h, ctx.h, arr, len(frames), C.byref(oc), C.byref(ro),
+                                                 C.byref(outc), C.byref(st), bhk._stream(stream)))
+        return out, {k: getattr(st, k) for k, _ in bhk.RenderStatsC._fields_}
+
+    def fallback_list(self):
+        """The last render's fallback pixels (int32 CUDA tensor, unordered)."""
+        import torch
+        n = C.c_int64()
+        bhk.check(bhk.lib().bhk_surrogate_fallback_list(self._h, None, 0, C.byref(n)))
+        t = torch.empty(n.value, dtype=torch.int32, device=f"cuda:{self.device}")
+        if n.value:
+            bhk.check(bhk.lib().bhk_surrogate_fallback_list(self._h, t.data_ptr(), n.value, C.byref(n)))
+        return t
+
+
 def _torch():
     import torch
     return torch
@@ -204,3 +231,43 @@ def sample_rays(n: int, seed: int, device="cuda", shadow_radius=None):
     ang = rng.uniform(0.0, 2.0 * np.pi, n)
     al, be = rad * np.cos(ang), rad * np.sin(ang)
     return tuple(torch.from_numpy(np.ascontiguousarray(v)).to(device) for v in (a, r, th, al, be))
+
+
+def shadow_radius(a: float, r_obs: float, theta_obs: float) -> float:
+    """Largest distance of the analytic critical curve from the image centre (M, pinhole units)."""
+    al, be = bhk.critical_curve(a, r_obs, theta_obs)
+    return float(np.max(np.hypot(al, be)))
+
+
+def orbit_frames(poses: int = 60, width: int = 3840, height: int = 2160, a: float = 0.998, r_obs: float = 30.0,
+                 theta_from: float = 85.0, theta_to: float = 45.0, half_width_factor: float = 1.2,
+                 r_disk_out: float = 30.0):
+    """Camera poses along a circular orbit at r_obs with the inclination moving linearly from
+    theta_from to theta_to (degrees), phi advancing 2 pi / poses per frame; image half-width
+    half_width_factor x the frame's shadow radius, square pixels, disk from the ISCO to r_disk_out."""
+    frames = []
+    for k in range(poses):
+        th = np.deg2rad(theta_from + (theta_to - theta_from) * (k / max(poses - 1, 1)))
+        hw = half_width_factor * shadow_radius(a, r_obs, th)
+        hh = hw * height / width
+        f = bhk.Frame(a, r_obs, float(th), width, height, -hw, hw, -hh, hh, 0.0, r_disk_out)
+        f.phi_obs = 2 * np.pi * k / poses
+        frames.append(f)
+    return frames
+
+
+def pixel_inputs(frame, pixels=None):
+    """Network inputs (float32 numpy, n x 5) of a frame's pixels (all, or the given local indices),
+    computed as the fused inference kernel does."""
+    n = frame.width * frame.height
+    idx = np.arange(n) if pixels is None else np.asarray(pixels)
+    row, col = idx // frame.width, idx % frame.width
+    px = (frame.alpha_hi - frame.alpha_lo) / frame.width
+    py = (frame.beta_hi - frame.beta_lo) / frame.height
+    x = np.empty((idx.size, N_IN), np.float32)
+    x[:, 0] = np.float32(frame.a)
+    x[:, 1] = np.float32(frame.theta_obs)
+    x[:, 2] = np.float32(np.log10(frame.r_obs))
+    x[:, 3] = (frame.alpha_lo + (col + 0.5) * px).astype(np.float32)
+    x[:, 4] = (frame.beta_hi - (row + 0.5) * py).astype(np.float32)
+    return x

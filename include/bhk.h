@@ -161,6 +161,12 @@ bhk_status bhk_trace_frames_host(bhk_context* ctx, const bhk_frame_desc* frames,
 bhk_status bhk_trace_rays(bhk_context* ctx, int64_t n, const double* a, const double* r_obs, const double* theta_obs,
                           const double* alpha, const double* beta, double r_disk_in, double r_disk_out,
                           const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
+/* Traces selected pixels of frames: pixels[0..n) are global pixel indices (device memory, int32) over
+ * the frames' concatenated row-major pixels, as bhk_trace_frames numbers them; outputs are compact
+ * (entry i belongs to pixels[i]). Re-traces and spot checks of rendered images (no counterpart in
+ * the reference, whose renderers always trace every pixel). */
+bhk_status bhk_trace_pixels(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes, const int32_t* pixels,
+                            int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
 bhk_status bhk_get_stats(bhk_context* ctx, bhk_trace_stats* stats);   /* synchronises the context stream */
 /* Times block x chunk x sort-granularity candidates on these frames and keeps the fastest for later
  * calls on this context (opts fields left 0). The chosen values are returned in stats. */
@@ -233,6 +239,33 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
                                int32_t batch, int64_t steps, float lr0, float* loss_history, void* stream);
 /* Network outputs (FP32 [n x 8], device) for n rays, layer by layer. Synchronous. */
 bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, float* out, void* stream);
+
+typedef struct bhk_render_opts {
+    double p_min;        /* rays whose largest class probability is below this fall back (0.99) */
+    double band;         /* rays within this image-plane distance (M) of the critical curve fall back (0.05) */
+    int32_t fallback;    /* 1: trace the fallback rays (the product); 0: only list them (measurement) */
+    int32_t pad;
+} bhk_render_opts;
+
+typedef struct bhk_render_stats {
+    int64_t rays, fallback;  /* rays rendered, rays handed to the integrator */
+    double infer_ms;         /* fused inference kernel (CUDA events) */
+    double trace_ms;         /* fallback trace incl. its launch and the scatter (CUDA events) */
+} bhk_render_stats;
+
+/* Renders frames with the surrogate and integrator fallback: one fused tcgen05 inference kernel over
+ * every pixel (inputs from the frame table; outputs in the bhk_rays_out convention with phi_disk NaN
+ * and steps 0 where the network answered), then the mixed/FP64 tracer (opts) on the fallback list:
+ * rays with max class probability < p_min, within `band` of the analytic critical curve, in the
+ * axis-snap strip (|alpha| sin(theta_obs) < 4e-3) or with a non-finite output. Outputs are device
+ * memory for all pixels (outcome required). ctx supplies the tracer; both on one device. Synchronous.
+ * opts and ropts may be NULL (defaults). */
+bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes,
+                                const bhk_trace_opts* opts, const bhk_render_opts* ropts, const bhk_rays_out* out,
+                                bhk_render_stats* stats, void* stream);
+/* The fallback list of the last render: its length in *n, and up to cap global pixel indices (in no
+ * particular order) copied into the device buffer dst. */
+bhk_status bhk_surrogate_fallback_list(bhk_surrogate* s, int32_t* dst, int64_t cap, int64_t* n);
 
 /* Diagnostic: the device's FP32 FMA throughput (TFLOP/s, FMA = 2 FLOPs) measured with a
  * latency-covered FMA chain kernel, the roofline denominator of the tracer. No reference counterpart. */
