@@ -173,6 +173,7 @@ def lib() -> C.CDLL:
         "bhk_surrogate_render": (C.c_int, [vp, vp, C.POINTER(FrameDescC), C.c_int32, C.POINTER(TraceOptsC),
                                            C.POINTER(RenderOptsC), C.POINTER(RaysOutC), C.POINTER(RenderStatsC), vp]),
         "bhk_surrogate_fallback_list": (C.c_int, [vp, vp, i64, C.POINTER(i64)]),
+        "bhk_surrogate_dataset": (C.c_int, [vp, i64, C.c_uint64, d, C.POINTER(TraceOptsC), vp, vp, vp, vp, vp]),
         "bhk_trace_pixels": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, vp, i64, C.POINTER(TraceOptsC),
                                        C.POINTER(RaysOutC), vp]),
     }

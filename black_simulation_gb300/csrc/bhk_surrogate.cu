@@ -1557,3 +1557,173 @@ extern "C" bhk_status bhk_surrogate_fallback_list(bhk_surrogate* s, int32_t* dst
     }
     return BHK_OK;
 }
+
+// ============================================================================ training set ====
+//
+// Rays drawn as the surrogate's training set specifies -- a uniform on [0, 0.998], theta_obs uniform
+// on [5, 89] degrees, log10 r_obs uniform on [log10 20, 3], (alpha, beta) uniform in a disk of radius
+// 1.5 x the shadow radius -- traced by the mixed tracer and turned into (inputs, classes, targets).
+// The shadow radius (largest distance of the analytic critical curve from the image centre) comes
+// from a table over (a, theta, log10 r) built on the device and interpolated trilinearly.
+
+namespace bhk {
+namespace sur {
+
+constexpr int kTabA = 24, kTabT = 24, kTabR = 12, kTabSamples = 512;
+constexpr double kAMax = 0.998, kThLo = 5.0 * kPi / 180.0, kThHi = 89.0 * kPi / 180.0;
+constexpr double kLogRLo = 1.3010299956639813, kLogRHi = 3.0;
+
+__global__ void shadow_table_kernel(float* tab) {
+    __shared__ float red[128];
+    const int id = blockIdx.x;
+    const int ia = id / (kTabT * kTabR), it = (id / kTabR) % kTabT, ir = id % kTabR;
+    const double a = kAMax * ia / (kTabA - 1);
+    const double th = kThLo + (kThHi - kThLo) * it / (kTabT - 1);
+    const double r = pow(10.0, kLogRLo + (kLogRHi - kLogRLo) * ir / (kTabR - 1));
+    float best = 0.0f;
+    for (int k = threadIdx.x; k < kTabSamples; k += blockDim.x) {
+        double al, be;
+        if (critical_point(a, r, th, static_cast<double>(k) / (kTabSamples - 1), &al, &be))
+            best = fmaxf(best, static_cast<float>(sqrt(al * al + be * be)));
+    }
+    red[threadIdx.x] = best;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tab[id] = red[0];
+}
+
+__device__ __forceinline__ double uniform01(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ float table_lookup(const float* tab, double a, double th, double lr) {
+    const double fa = fmin(fmax(a / kAMax, 0.0), 1.0) * (kTabA - 1);
+    const double ft = fmin(fmax((th - kThLo) / (kThHi - kThLo), 0.0), 1.0) * (kTabT - 1);
+    const double fr = fmin(fmax((lr - kLogRLo) / (kLogRHi - kLogRLo), 0.0), 1.0) * (kTabR - 1);
+    const int i0 = min(static_cast<int>(fa), kTabA - 2), j0 = min(static_cast<int>(ft), kTabT - 2),
+              k0 = min(static_cast<int>(fr), kTabR - 2);
+    const double wa = fa - i0, wt = ft - j0, wr = fr - k0;
+    double v = 0.0;
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj)
+            for (int dk = 0; dk < 2; ++dk) {
+                const double w = (di ? wa : 1.0 - wa) * (dj ? wt : 1.0 - wt) * (dk ? wr : 1.0 - wr);
+                v += w * tab[((i0 + di) * kTabT + (j0 + dj)) * kTabR + (k0 + dk)];
+            }
+    return static_cast<float>(v);
+}
+
+__global__ void sample_kernel(const float* __restrict__ tab, uint64_t seed, long long n, double* a, double* r,
+                              double* th, double* al, double* be, float* x) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const uint64_t k = 6ull * static_cast<uint64_t>(i);
+        const double ai = kAMax * uniform01(seed, k);
+        const double ti = kThLo + (kThHi - kThLo) * uniform01(seed, k + 1);
+        const double lr = kLogRLo + (kLogRHi - kLogRLo) * uniform01(seed, k + 2);
+        const double ri = pow(10.0, lr);
+        const double R = 1.5 * table_lookup(tab, ai, ti, lr);
+        const double rad = R * sqrt(uniform01(seed, k + 3)), ang = 2.0 * kPi * uniform01(seed, k + 4);
+        double sn, cs;
+        sincos(ang, &sn, &cs);
+        a[i] = ai;
+        r[i] = ri;
+        th[i] = ti;
+        al[i] = rad * cs;
+        be[i] = rad * sn;
+        float* xi = x + 5 * i;
+        xi[0] = static_cast<float>(ai);
+        xi[1] = static_cast<float>(ti);
+        xi[2] = static_cast<float>(log10(ri));
+        xi[3] = static_cast<float>(rad * cs);
+        xi[4] = static_cast<float>(rad * sn);
+    }
+}
+
+// Classes and targets from tracer outputs (the convention of bhk_surrogate_train).
+__global__ void label_kernel(long long n, const uint8_t* __restrict__ oc, const double* __restrict__ rd,
+                             const double* __restrict__ g, const double* __restrict__ ti,
+                             const double* __restrict__ pi, uint8_t* cls, float* tgt) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const uint8_t c = oc[i];
+        float t[kOut] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (c == BHK_RAY_DISK) {
+            t[3] = static_cast<float>(rd[i] / 30.0);
+            t[4] = static_cast<float>(log(fmax(g[i], 1e-30)));
+        } else if (c == BHK_RAY_ESCAPED) {
+            double s, co, sp, cp;
+            sincos(ti[i], &s, &co);
+            sincos(pi[i], &sp, &cp);
+            t[5] = static_cast<float>(s * cp);
+            t[6] = static_cast<float>(s * sp);
+            t[7] = static_cast<float>(co);
+        }
+        cls[i] = c;
+        for (int k = 0; k < kOut; ++k) tgt[kOut * i + k] = t[k];
+    }
+}
+
+}  // namespace sur
+}  // namespace bhk
+
+extern "C" bhk_status bhk_surrogate_dataset(bhk_context* ctx, int64_t n, uint64_t seed, double r_disk_out,
+                                            const bhk_trace_opts* opts, float* x, uint8_t* cls, float* target,
+                                            double* rays5, void* stream) {
+    using namespace bhk::sur;
+    if (!ctx || n <= 0 || n > (int64_t(1) << 31) - 1 || !x || !cls || !target || !(r_disk_out >= 0.0)) {
+        set_last_error("bhk_surrogate_dataset: bad arguments");
+        return BHK_EINVAL;
+    }
+    cudaSetDevice(bhk::context_device(ctx));
+    cudaStream_t st = bhk::context_stream(ctx, stream);  // the tracer below runs on the same stream
+    float* tab = nullptr;
+    double* d = rays5;
+    uint8_t* oc = nullptr;
+    double* o5 = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&tab), sizeof(float) * kTabA * kTabT * kTabR);
+    if (e == cudaSuccess && !rays5) e = cudaMalloc(reinterpret_cast<void**>(&d), sizeof(double) * 5 * n);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&oc), n);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&o5), sizeof(double) * 5 * n);
+    bhk_status rs = BHK_OK;
+    if (e == cudaSuccess) {
+        shadow_table_kernel<<<kTabA * kTabT * kTabR, 128, 0, st>>>(tab);
+        sample_kernel<<<1024, 256, 0, st>>>(tab, seed, n, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, x);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        bhk_trace_opts o{};
+        if (opts) o = *opts;
+        else o.precision = BHK_PREC_MIXED;
+        bhk_rays_out out{};
+        out.outcome = oc;
+        out.r_disk = o5;
+        out.phi_disk = o5 + n;
+        out.g = o5 + 2 * n;
+        out.theta_inf = o5 + 3 * n;
+        out.phi_inf = o5 + 4 * n;
+        rs = bhk_trace_rays(ctx, n, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, 0.0, r_disk_out, &o, &out, st);
+        if (rs == BHK_OK) {
+            label_kernel<<<1024, 256, 0, st>>>(n, oc, o5, o5 + 2 * n, o5 + 3 * n, o5 + 4 * n, cls, target);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        }
+    }
+    if (tab) cudaFree(tab);
+    if (d && d != rays5) cudaFree(d);
+    if (oc) cudaFree(oc);
+    if (o5) cudaFree(o5);
+    if (rs != BHK_OK) return rs;
+    if (e != cudaSuccess) {
+        set_last_error(std::string("bhk_surrogate_dataset: ") + cudaGetErrorString(e));
+        return BHK_ECUDA;
+    }
+    return BHK_OK;
+}

@@ -205,6 +205,22 @@ class Surrogate:
         return t
 
 
+def make_dataset(ctx, n: int, seed: int = 1, r_disk_out: float = 30.0, opts=None, keep_rays: bool = False,
+                 stream=None):
+    """The surrogate's training set, generated on the device by bhk_surrogate_dataset: (x, classes,
+    targets) CUDA tensors, plus the rays (5 x n float64: a, r_obs, theta_obs, alpha, beta) if asked."""
+    import torch
+    dev = f"cuda:{ctx.device}"
+    x = torch.empty((n, N_IN), dtype=torch.float32, device=dev)
+    cls = torch.empty(n, dtype=torch.uint8, device=dev)
+    tgt = torch.empty((n, N_OUT), dtype=torch.float32, device=dev)
+    rays = torch.empty((5, n), dtype=torch.float64, device=dev) if keep_rays else None
+    oc = (opts or bhk.TraceOpts("mixed")).c()
+    bhk.check(bhk.lib().bhk_surrogate_dataset(ctx.h, n, seed, r_disk_out, C.byref(oc), bhk._ptr(x), bhk._ptr(cls),
+                                              bhk._ptr(tgt), bhk._ptr(rays), bhk._stream(stream)))
+    return (x, cls, tgt, rays) if keep_rays else (x, cls, tgt)
+
+
 def _torch():
     import torch
     return torch

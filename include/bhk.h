@@ -240,6 +240,16 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
 /* Network outputs (FP32 [n x 8], device) for n rays, layer by layer. Synchronous. */
 bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, float* out, void* stream);
 
+/* The training set of the surrogate: n rays with a uniform on [0, 0.998], theta_obs uniform on
+ * [5, 89] deg, log10 r_obs uniform on [log10 20, 3] and (alpha, beta) uniform in a disk of radius 1.5 x
+ * the frame's shadow radius (seeded counter-based draws), traced by ctx (opts NULL: mixed precision)
+ * with a disk from each ray's prograde ISCO to r_disk_out, and written as inputs x [n x 5], classes and
+ * targets [n x 8] (device memory, the bhk_surrogate_train convention). rays5 (device, 5 x n doubles:
+ * a, r_obs, theta_obs, alpha, beta) receives the rays when not NULL. Synchronous. */
+bhk_status bhk_surrogate_dataset(bhk_context* ctx, int64_t n, uint64_t seed, double r_disk_out,
+                                 const bhk_trace_opts* opts, float* x, uint8_t* cls, float* target, double* rays5,
+                                 void* stream);
+
 typedef struct bhk_render_opts {
     double p_min;        /* rays whose largest class probability is below this fall back (0.99) */
     double band;         /* rays within this image-plane distance (M) of the critical curve fall back (0.05) */

@@ -139,3 +139,30 @@ def test_checkpoint_round_trip(cuda, tmp_path):
         # atomically summed bias gradients make the last bits order-dependent
         assert np.allclose(ha, hb, rtol=1e-4, atol=1e-7)
         assert np.allclose(a.params(), b.params(), rtol=1e-4, atol=1e-6)
+
+
+def test_dataset_follows_the_training_distribution(cuda, ctx):
+    """bhk_surrogate_dataset: inputs inside the stated ranges, (alpha, beta) within 1.5 x the shadow
+    radius, and labels identical to tracing the same rays directly."""
+    from black_simulation_gb300 import bhk
+    from black_simulation_gb300.surrogate import make_dataset, shadow_radius, targets_from_rays
+    n = 200_000
+    x, cls, tgt, rays = make_dataset(ctx, n, seed=17, keep_rays=True)
+    xs = x.cpu().numpy()
+    assert xs[:, 0].min() >= 0 and xs[:, 0].max() <= 0.998
+    assert np.deg2rad(5) - 1e-6 <= xs[:, 1].min() and xs[:, 1].max() <= np.deg2rad(89) + 1e-6
+    assert np.log10(20) - 1e-6 <= xs[:, 2].min() and xs[:, 2].max() <= 3 + 1e-6
+    # roughly uniform in log r and in a
+    assert abs(np.median(xs[:, 2]) - 0.5 * (np.log10(20) + 3)) < 0.02
+    rng = np.random.default_rng(0)
+    for i in rng.choice(n, 25, replace=False):
+        R = shadow_radius(float(rays[0, i]), float(rays[1, i]), float(rays[2, i]))
+        rho = float(np.hypot(rays[3, i].item(), rays[4, i].item()))
+        assert rho <= 1.5 * R * 1.01
+    cnt = np.bincount(cls.cpu().numpy(), minlength=4)
+    assert cnt[1] > 0.1 * n and cnt[2] > 0.1 * n and cnt[3] > 0.01 * n
+    out = ctx.trace_rays(*[rays[k].contiguous() for k in range(5)], r_disk_in=0.0, r_disk_out=30.0,
+                         opts=bhk.TraceOpts("mixed"))
+    c2, t2 = targets_from_rays(out)
+    assert torch.equal(c2, cls)
+    assert torch.allclose(t2, tgt, rtol=1e-6, atol=1e-7)
