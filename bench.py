@@ -316,13 +316,217 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+# --------------------------------------------------------------------------- the surrogate ----
+
+SURROGATE_METRIC = "geodesics/s at <=1e-4 rad exit-angle err vs FP64: surrogate vs plain GPU tracer"
+# MACs per ray of the network (64 -> 256 -> 256 -> 256 -> 256 -> 16 padded head): forward, and the
+# backward's weight and input gradients (no input gradient of the first layer).
+MAC_FWD = 64 * 256 + 3 * 256 * 256 + 256 * 16
+MAC_TRAIN = 2 * MAC_FWD + 256 * 16 + 3 * 256 * 256
+
+
+def measured_peak(key: str, fallback: float):
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)[key]), "measured (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        return fallback, "fallback (no measured peaks file)"
+
+
+def train_surrogate(ctx, args, log=None):
+    """Training set and training run of the surrogate (50M tracer-labelled rays, batch 65,536, Adam,
+    cosine learning rate from 1e-3). Returns (surrogate, info)."""
+    import torch
+    from black_simulation_gb300.surrogate import Surrogate, make_dataset
+    s = Surrogate(ctx.device, seed=args.seed, max_batch=65536)
+    if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
+        s.load(args.surrogate_ckpt)
+        return s, {"checkpoint": args.surrogate_ckpt}
+    t0 = time.perf_counter()
+    x, cls, tgt = make_dataset(ctx, args.train_rays, seed=args.seed)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hist = s.train(x, cls, tgt, batch=65536, steps=args.train_steps, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    if args.surrogate_ckpt:
+        s.save(args.surrogate_ckpt)
+    del x, cls, tgt
+    return s, {"train_rays": args.train_rays, "train_steps": args.train_steps, "dataset_s": t_data,
+               "train_s": t_train, "train_rays_per_s": args.train_steps * 65536 / t_train,
+               "final_loss": [float(v) for v in hist[-50:].mean(axis=0)]}
+
+
+def angle_between(t1, p1, t2, p2):
+    c = np.sin(t1) * np.sin(t2) * np.cos(p1 - p2) + np.cos(t1) * np.cos(t2)
+    return np.arccos(np.clip(c, -1.0, 1.0))
+
+
+def error_stats(test, ref):
+    """Errors of `test` against the FP64 `ref` on the same pixels (dicts of numpy arrays)."""
+    oc_t, oc_r = test["outcome"], ref["outcome"]
+    res = {"pixels": int(oc_r.size), "outcome_agreement": float(np.mean(oc_t == oc_r))}
+    esc = (oc_t == 3) & (oc_r == 3)
+    if esc.any():
+        ang = angle_between(test["theta_inf"][esc], test["phi_inf"][esc], ref["theta_inf"][esc], ref["phi_inf"][esc])
+        res["exit_angle_rad"] = {"median": float(np.median(ang)), "p99": float(np.quantile(ang, 0.99)),
+                                 "max": float(ang.max()), "n": int(esc.sum())}
+    disk = (oc_t == 2) & (oc_r == 2)
+    if disk.any():
+        er = np.abs(test["r_disk"][disk] / ref["r_disk"][disk] - 1.0)
+        eg = np.abs(test["g"][disk] / ref["g"][disk] - 1.0)
+        res["r_disk_rel"] = {"median": float(np.median(er)), "p99": float(np.quantile(er, 0.99)), "max": float(er.max()),
+                             "n": int(disk.sum())}
+        res["g_rel"] = {"median": float(np.median(eg)), "p99": float(np.quantile(eg, 0.99)), "max": float(eg.max())}
+    return res
+
+
+def run_orbit(args):
+    """Surrogate + integrator fallback against the plain mixed tracer on the orbit sequence:
+    60 poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 (divided by --scale)."""
+    import torch
+    from black_simulation_gb300 import bhk, build
+    from black_simulation_gb300.surrogate import orbit_frames
+    build.build()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    ctx = bhk.Context(0)
+    work_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work_stream)
+    stream = torch.cuda.current_stream()
+    sur, train_info = train_surrogate(ctx, args)
+    frames = orbit_frames(args.poses, 3840 // args.scale, 2160 // args.scale)
+    n = sum(f.rays for f in frames)
+    opts = bhk.TraceOpts("mixed", rtol=1e-6)
+    out_s = bhk.alloc_outputs(n, dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms, extra = [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            extra.append(r)
+        return float(np.mean(ms)), extra
+
+    with Clocks(0) as clk:
+        ms_s, stats = timed(lambda: sur.render(ctx, frames, opts, out=out_s)[1])
+    ms_infer = float(np.mean([st["infer_ms"] for st in stats]))
+    fb = float(np.mean([st["fallback"] for st in stats]))
+    out_t = bhk.alloc_outputs(n, dev)
+    ms_t, _ = timed(lambda: ctx.trace_frames(frames, opts, out=out_t))
+    # 1% held-out pixels per frame (seeded), traced in FP64 as the judge
+    rng = np.random.default_rng(args.seed + 1)
+    held, off = [], 0
+    for f in frames:
+        held.append(off + rng.choice(f.rays, max(1, f.rays // 100), replace=False))
+        off += f.rays
+    held = np.sort(np.concatenate(held)).astype(np.int32)
+    hd = torch.from_numpy(held).to(dev)
+    t0 = time.perf_counter()
+    ref = ctx.trace_pixels(frames, hd, bhk.TraceOpts("fp64", rtol=1e-10))
+    torch.cuda.synchronize()
+    t_fp64 = time.perf_counter() - t0
+    fbl = np.zeros(n, bool)
+    sur.render(ctx, frames, opts, out=out_s, fallback=True)
+    fbl[sur.fallback_list().cpu().numpy()] = True
+    keys = ("outcome", "r_disk", "g", "theta_inf", "phi_inf")
+    pick = lambda o: {k: o[k][hd].cpu().numpy() for k in keys}
+    ref_h = {k: ref[k].cpu().numpy() for k in keys}   # compact: entry i is pixel held[i]
+    sur_h, tr_h = pick(out_s), pick(out_t)
+    answered = ~fbl[held]
+    err_s = error_stats(sur_h, ref_h)
+    err_t = error_stats(tr_h, ref_h)
+    err_net = error_stats({k: v[answered] for k, v in sur_h.items()}, {k: v[answered] for k, v in ref_h.items()})
+    infer_rays_s = n / (ms_infer * 1e-3)
+    peak, src = measured_peak("bf16_tflops", 1900.0)
+    achieved = n * 2 * MAC_FWD / (ms_infer * 1e-3) / 1e12
+    line = {
+        "metric": SURROGATE_METRIC, "value": n / (ms_s * 1e-3), "unit": "rays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32", "data": "synthetic",
+        "config": {"workload": f"{args.poses} orbit poses r=30M a=0.998 theta 85->45deg, "
+                               f"{3840 // args.scale}x{2160 // args.scale}, half-width 1.2x shadow radius, "
+                               "disk ISCO-30M; surrogate + mixed-precision fallback (p_min 0.99, band 0.05M)",
+                   "rays": n, "l2": "flushed (256 MB write) between steps", "training": train_info},
+        "plain_tracer": {"value": n / (ms_t * 1e-3), "ms_per_step": ms_t},
+        "speedup_vs_plain_tracer": ms_t / ms_s,
+        "fallback_fraction": fb / n,
+        "inference": {"value": infer_rays_s, "ms": ms_infer},
+        "errors_vs_fp64": {"surrogate_path": err_s, "network_answered_only": err_net, "plain_tracer": err_t,
+                           "fp64_judge_s": t_fp64},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": src,
+                     "kernel": "infer_kernel (fused tcgen05 network)", "flops_per_ray": 2 * MAC_FWD},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    sur.close()
+    ctx.close()
+    print(json.dumps(line))
+
+
+def run_train(args):
+    """Surrogate training throughput (config: 50M tracer-labelled rays, batch 65,536)."""
+    import torch
+    from black_simulation_gb300 import bhk, build
+    from black_simulation_gb300.surrogate import Surrogate, make_dataset
+    build.build()
+    torch.cuda.set_device(0)
+    ctx = bhk.Context(0)
+    t0 = time.perf_counter()
+    x, cls, tgt = make_dataset(ctx, args.train_rays, seed=args.seed)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    s = Surrogate(0, seed=args.seed, max_batch=65536)
+    s.train(x, cls, tgt, batch=65536, steps=max(3, args.warmup), lr=1e-3)
+    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        hist = s.train(x, cls, tgt, batch=65536, steps=args.train_steps, lr=1e-3)
+        b.record()
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    rays_s = args.train_steps * 65536 / (ms * 1e-3)
+    peak, src = measured_peak("bf16_tflops_sustained", 1700.0)
+    achieved = rays_s * 2 * MAC_TRAIN / 1e12
+    line = {
+        "metric": "surrogate training rays/s", "value": rays_s, "unit": "rays/s", "n_gpus": 1,
+        "steps": args.train_steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.train_steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32", "data": "synthetic",
+        "config": {"workload": f"{args.train_rays} tracer-labelled rays, batch 65536, Adam, cosine lr from 1e-3",
+                   "dataset_s": t_data, "final_loss": [float(v) for v in hist[-50:].mean(axis=0)]},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": src, "flops_per_ray": 2 * MAC_TRAIN},
+        "clocks": clk.summary(),
+    }
+    s.close()
+    ctx.close()
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="1080p", choices=["1080p", "c1", "batch64"])
+    ap.add_argument("--workload", default="1080p", choices=["1080p", "c1", "batch64", "orbit", "train"])
+    ap.add_argument("--poses", type=int, default=60, help="orbit: camera poses")
+    ap.add_argument("--train-rays", type=int, default=50_000_000, help="orbit/train: training-set size")
+    ap.add_argument("--train-steps", type=int, default=10_000, help="orbit/train: Adam steps")
+    ap.add_argument("--surrogate-ckpt", default="", help="orbit: load (if present) or save the trained network")
+    ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--autotune", action="store_true", default=True)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -334,6 +538,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "orbit":
+        run_orbit(args)
+    elif args.workload == "train":
+        run_train(args)
     else:
         run_ours(args)
 
