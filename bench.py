@@ -342,6 +342,8 @@ def train_surrogate(ctx, args, log=None):
     if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
         s.load(args.surrogate_ckpt)
         return s, {"checkpoint": args.surrogate_ckpt}
+    if args.train_steps == 0:  # untrained network (kernel profiling: the work per ray is the same)
+        return s, {"untrained": True}
     t0 = time.perf_counter()
     x, cls, tgt = make_dataset(ctx, args.train_rays, seed=args.seed)
     torch.cuda.synchronize()

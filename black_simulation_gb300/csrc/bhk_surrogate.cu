@@ -67,6 +67,18 @@ __device__ __forceinline__ float sigmoidf(float z) {
     return fmaf(0.5f, t, 0.5f);
 }
 
+// The network's activation: SiLU of two pre-activations passed as halves h = z / 2 (FP32),
+// silu(z) = h + h tanh(h), evaluated in BF16x2 -- h rounded to BF16, the hardware BF16x2 tanh, one
+// fused multiply-add rounded to BF16 -- and returned packed (element 0 in the low half). One MUFU
+// operation per two activations; training and inference both use exactly this.
+__device__ __forceinline__ uint32_t silu2_half(float h0, float h1) {
+    uint32_t hb, t, a;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hb) : "f"(h1), "f"(h0));
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(hb));
+    asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(a) : "r"(hb), "r"(t));
+    return a;
+}
+
 template <int BN, int EPI>
 __global__ void __launch_bounds__(128, 1)
 gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
@@ -176,10 +188,12 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             } else if constexpr (EPI == kBiasSilu) {
                 if (live) {
                     __align__(16) bf16 zb[16], ab[16];
-                    for (int i = 0; i < 16; ++i) {
-                        const float z = v[i] + ea.bias[nb + i];
-                        zb[i] = __float2bfloat16_rn(z);
-                        ab[i] = __float2bfloat16_rn(z * sigmoidf(z));
+                    for (int i = 0; i < 16; i += 2) {
+                        const float z0 = v[i] + ea.bias[nb + i], z1 = v[i + 1] + ea.bias[nb + i + 1];
+                        zb[i] = __float2bfloat16_rn(z0);
+                        zb[i + 1] = __float2bfloat16_rn(z1);
+                        const uint32_t a2 = silu2_half(0.5f * z0, 0.5f * z1);
+                        *reinterpret_cast<uint32_t*>(&ab[i]) = a2;
                     }
                     uint4* zd = reinterpret_cast<uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
                     uint4* ad = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
@@ -375,8 +389,10 @@ __device__ __forceinline__ void fourier_features(const float* x, const float* sb
         float p = 0.0f;
 #pragma unroll
         for (int i = 0; i < kIn; ++i) p += sb[j * kIn + i] * u[i];
+        // sin and cos of 2 pi p: exact reduction to r = p - rint(p) in [-1/2, 1/2], then the hardware
+        // sine and cosine (absolute error ~2^-21 on [-pi, pi], far below the BF16 rounding that follows).
         float s, c;
-        sincospif(2.0f * p, &s, &c);
+        __sincosf(6.28318530717958648f * (p - rintf(p)), &s, &c);
         f[j] = __float2bfloat16_rn(s);
         f[kFreq + j] = __float2bfloat16_rn(c);
     }
@@ -1079,13 +1095,17 @@ __global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc)
     }
 }
 
-constexpr int kInfStages = 2;
+constexpr int kInfStages = 5;               // weight ring: 5 x 16 KB in flight
 constexpr int kTileRays = 128;
 constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 (activations or weights)
+constexpr int kActBytes = 4 * kChunkBytes; // one tile's 256-wide activations
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
-constexpr int kChunksPerTile = 2 + 3 * 8 + 4;
-constexpr int kInfThreads = 192;
-constexpr int kInfSmem = 4 * kChunkBytes + kInfStages * kChunkBytes + 1024 + 1024;
+constexpr int kEpiWarps = 16;              // per tile slot: 4 TMEM lane quadrants x 2 column halves
+constexpr int kInfThreads = 64 + 32 * kEpiWarps;
+constexpr int kInfMisc = 128 + 16 + kFreq * kIn * 4 + 4 * kHid * 4;  // barriers, TMEM slot/flag, B, biases
+constexpr int kInfSmem = 2 * kActBytes + kInfStages * kChunkBytes + 1024 + kInfMisc;
+
+__host__ __device__ constexpr int layer_chunks(int l) { return l == 0 ? 2 : (l < 4 ? 8 : 4); }
 
 struct InferArgs {
     const SurFrame* frames;
@@ -1107,41 +1127,67 @@ __device__ __forceinline__ uint32_t sw128(int row, int col) {
     return static_cast<uint32_t>(row * 128 + ((((col >> 3) ^ (row & 7))) << 4) + ((col & 7) << 1));
 }
 
-// Stores 16 BF16 of `row`, columns c0 .. c0+15 of the 256-wide activation (4 chunks of 64 columns).
-__device__ __forceinline__ void store_act16(uint8_t* act, int row, int c0, const bf16* v) {
+// Stores 16 BF16 (8 packed words) of `row` at columns c0 .. c0+15 of the 256-wide activation.
+__device__ __forceinline__ void store_act16(uint8_t* act, int row, int c0, const uint32_t* w) {
     uint8_t* chunk = act + (c0 >> 6) * kChunkBytes;
     const int c = c0 & 63;
-    *reinterpret_cast<uint4*>(chunk + sw128(row, c)) = reinterpret_cast<const uint4*>(v)[0];
-    *reinterpret_cast<uint4*>(chunk + sw128(row, c + 8)) = reinterpret_cast<const uint4*>(v)[1];
+    *reinterpret_cast<uint4*>(chunk + sw128(row, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(chunk + sw128(row, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
-__global__ void __launch_bounds__(kInfThreads, 2)
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+// SiLU of 32 accumulator columns (raw FP32 bits) with halved biases hb -> 16 packed BF16x2 words.
+__device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb, uint32_t (&w)[16]) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const float4 b = reinterpret_cast<const float4*>(hb)[q];
+        w[2 * q] = silu2_half(fmaf(__uint_as_float(v[4 * q]), 0.5f, b.x), fmaf(__uint_as_float(v[4 * q + 1]), 0.5f, b.y));
+        w[2 * q + 1] =
+            silu2_half(fmaf(__uint_as_float(v[4 * q + 2]), 0.5f, b.z), fmaf(__uint_as_float(v[4 * q + 3]), 0.5f, b.w));
+    }
+}
+
+// Two tiles in flight per CTA (one CTA per SM): while the tensor core runs one tile's layer, the
+// other tile's epilogue warps turn their accumulators into the next layer's operand. Each tile
+// slot owns 256 TMEM columns and a 64 KB activation buffer; the weight ring is shared and filled
+// in the MMA's order (pair of tiles, layer, slot, chunk).
+__global__ void __launch_bounds__(kInfThreads, 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
              const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
              const __grid_constant__ CUtensorMap tW4, InferArgs ia) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t* act = base;
-    uint8_t* ring = base + 4 * kChunkBytes;
+    uint8_t* ring = base + 2 * kActBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kChunkBytes);
     uint64_t* empty = full + kInfStages;
-    uint64_t* act_ready = empty + kInfStages;
-    uint64_t* acc_full = act_ready + 1;
-    uint64_t* drain = acc_full + 1;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    uint64_t* act_ready = empty + kInfStages;  // [2]
+    uint64_t* acc_full = act_ready + 2;        // [2]
+    uint64_t* drain = acc_full + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + 16);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* sB = reinterpret_cast<float*>(tmem_slot + 4);
+    float* sHb = sB + kFreq * kIn;  // hidden layers' biases halved: [4][256]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
+    const long long n_my = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const long long pairs = (n_my + 1) / 2;
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
+    for (int i = threadIdx.x; i < 4 * kHid; i += blockDim.x) sHb[i] = 0.5f * ia.bias[i / kHid][i % kHid];
     if (threadIdx.x == 0) {
         for (int st = 0; st < kInfStages; ++st) {
             tc::mbar_init(&full[st], 1);
             tc::mbar_init(&empty[st], 1);
         }
-        tc::mbar_init(act_ready, 128);
-        tc::mbar_init(acc_full, 1);
+        for (int sl = 0; sl < 2; ++sl) {
+            tc::mbar_init(&act_ready[sl], 32 * kEpiWarps / 2);
+            tc::mbar_init(&acc_full[sl], 1);
+        }
         tc::mbar_init(drain, 1);
         *abort_flag = 0;
         tc::fence_mbar_init();
@@ -1151,7 +1197,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         tc::prefetch_tmap(&tW3);
         tc::prefetch_tmap(&tW4);
     }
-    if (warp == 1) tc::tmem_alloc(tmem_slot, 256);
+    if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -1162,143 +1208,174 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     };
 
     if (warp == 0) {
-        if (lane == 0) {  // ---- TMA producer: 30 weight chunks per tile, in the MMA's order
-            long long k = 0;
+        if (lane == 0) {  // ---- TMA producer, in the MMA's order
+            long long q = 0;
             bool ok = true;
-            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-                for (int c = 0; c < kChunksPerTile; ++c, ++k) {
-                    if (*abort_flag) { ok = false; break; }
-                    const int st = static_cast<int>(k % kInfStages);
-                    const long long j = k / kInfStages;
-                    if (j > 0 && !tc::mbar_wait(&empty[st], static_cast<uint32_t>((j - 1) & 1))) {
-                        give_up();
-                        ok = false;
-                        break;
+            for (long long p = 0; p < pairs && ok; ++p)
+                for (int l = 0; l < kLayers && ok; ++l)
+                    for (int sl = 0; sl < 2 && ok; ++sl) {
+                        if (2 * p + sl >= n_my) continue;
+                        for (int c = 0; c < layer_chunks(l); ++c, ++q) {
+                            if (*abort_flag) { ok = false; break; }
+                            const int st = static_cast<int>(q % kInfStages);
+                            const long long j = q / kInfStages;
+                            if (j > 0 && !tc::mbar_wait(&empty[st], static_cast<uint32_t>((j - 1) & 1))) {
+                                give_up();
+                                ok = false;
+                                break;
+                            }
+                            const int nh = l == 0 ? c : (l < 4 ? c >> 2 : 0);
+                            const int kc = l == 0 ? 0 : (l < 4 ? c & 3 : c);
+                            const CUtensorMap* m = l == 0 ? &tW0 : l == 1 ? &tW1 : l == 2 ? &tW2 : l == 3 ? &tW3 : &tW4;
+                            tc::mbar_expect_tx(&full[st], l < 4 ? kChunkBytes : kHeadChunkBytes);
+                            tc::tma_load_2d(ring + st * kChunkBytes, m, kc * 64, nh * 128, &full[st]);
+                        }
                     }
-                    int l, nh, kc;
-                    if (c < 2) { l = 0; nh = c; kc = 0; }
-                    else if (c < 26) { const int q = c - 2; l = 1 + q / 8; nh = (q & 7) >> 2; kc = q & 3; }
-                    else { l = 4; nh = 0; kc = c - 26; }
-                    const CUtensorMap* m = l == 0 ? &tW0 : l == 1 ? &tW1 : l == 2 ? &tW2 : l == 3 ? &tW3 : &tW4;
-                    tc::mbar_expect_tx(&full[st], l < 4 ? kChunkBytes : kHeadChunkBytes);
-                    tc::tma_load_2d(ring + st * kChunkBytes, m, kc * 64, nh * 128, &full[st]);
-                }
-            }
             // Let every load issued land before the CTA may exit (bounded).
-            for (long long q = k - kInfStages; q < k; ++q)
-                if (q >= 0) tc::mbar_wait(&full[q % kInfStages], static_cast<uint32_t>((q / kInfStages) & 1));
+            for (long long r = q - kInfStages; r < q; ++r)
+                if (r >= 0) tc::mbar_wait(&full[r % kInfStages], static_cast<uint32_t>((r / kInfStages) & 1));
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---- MMA issuer
             constexpr uint32_t kId128 = tc::idesc_bf16(128, 128), kId16 = tc::idesc_bf16(128, 16);
-            long long k = 0;
-            uint32_t act_n = 0;
+            long long q = 0;
+            uint32_t act_n[2] = {0u, 0u};
             bool ok = true;
-            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-                for (int l = 0; l < kLayers && ok; ++l) {
-                    if (*abort_flag || !tc::mbar_wait(act_ready, act_n & 1)) {
-                        if (!*abort_flag) give_up();
-                        ok = false;
-                        break;
-                    }
-                    ++act_n;
-                    tc::fence_after_sync();
-                    const int nch = l == 0 ? 2 : (l < 4 ? 8 : 4);
-                    for (int q = 0; q < nch; ++q, ++k) {
-                        const int st = static_cast<int>(k % kInfStages);
-                        if (!tc::mbar_wait(&full[st], static_cast<uint32_t>((k / kInfStages) & 1))) {
-                            give_up();
+            for (long long p = 0; p < pairs && ok; ++p)
+                for (int l = 0; l < kLayers && ok; ++l)
+                    for (int sl = 0; sl < 2 && ok; ++sl) {
+                        if (2 * p + sl >= n_my) continue;
+                        if (*abort_flag || !tc::mbar_wait(&act_ready[sl], act_n[sl] & 1)) {
+                            if (!*abort_flag) give_up();
                             ok = false;
                             break;
                         }
+                        ++act_n[sl];
                         tc::fence_after_sync();
-                        const int nh = l == 0 ? q : (l < 4 ? q >> 2 : 0);
-                        const int kc = l == 0 ? 0 : (l < 4 ? q & 3 : q);
-                        const uint64_t ad = tc::smem_desc_sw128(act + kc * kChunkBytes);
-                        const uint64_t bd = tc::smem_desc_sw128(ring + st * kChunkBytes);
-                        const uint32_t d = tmem + static_cast<uint32_t>(l < 4 ? nh * 128 : 0);
+                        uint8_t* act = base + sl * kActBytes;
+                        for (int c = 0; c < layer_chunks(l); ++c, ++q) {
+                            const int st = static_cast<int>(q % kInfStages);
+                            if (!tc::mbar_wait(&full[st], static_cast<uint32_t>((q / kInfStages) & 1))) {
+                                give_up();
+                                ok = false;
+                                break;
+                            }
+                            tc::fence_after_sync();
+                            const int nh = l == 0 ? c : (l < 4 ? c >> 2 : 0);
+                            const int kc = l == 0 ? 0 : (l < 4 ? c & 3 : c);
+                            const uint64_t ad = tc::smem_desc_sw128(act + kc * kChunkBytes);
+                            const uint64_t bd = tc::smem_desc_sw128(ring + st * kChunkBytes);
+                            const uint32_t d = tmem + static_cast<uint32_t>(256 * sl + (l < 4 ? nh * 128 : 0));
 #pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)
-                            tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId128 : kId16, (kc | kk) ? 1u : 0u);
-                        tc::mma_commit(&empty[st]);
+                            for (int kk = 0; kk < 4; ++kk)
+                                tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId128 : kId16, (kc | kk) ? 1u : 0u);
+                            tc::mma_commit(&empty[st]);
+                        }
+                        if (ok) tc::mma_commit(&acc_full[sl]);
                     }
-                    if (ok) tc::mma_commit(acc_full);
-                }
-            }
             // All MMAs issued have finished before TMEM is released (bounded).
             tc::mma_commit(drain);
             tc::mbar_wait(drain, 0);
         }
-    } else {  // ---- warps 2..5: features, epilogues, decode (thread = ray of the tile)
-        const int q4 = warp & 3;
+    } else {  // ---- warps 2..17: features, epilogues, decode (thread = ray of its slot's tile)
+        const int ew = warp - 2;
+        const int slot = ew >> 3;          // tile slot
+        const int half = (ew >> 2) & 1;    // columns 128 half .. 128 half + 127 (and 16 of the 32 frequencies)
+        const int q4 = warp & 3;           // TMEM lane quadrant this warp may access
         const int row = 32 * q4 + lane;
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16);
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16) + 256u * slot;
+        uint8_t* act = base + slot * kActBytes;
         uint32_t acc_n = 0;
         // Every exit decision is taken by the whole warp (the TMEM loads and the list append are
         // warp-collective).
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (long long k = slot; k < n_my; k += 2) {
             if (__any_sync(0xffffffffu, *abort_flag)) break;
+            const long long tile = blockIdx.x + k * gridDim.x;
             const long long ray = tile * kTileRays + row;
             const bool live = ray < ia.n;
             int fi = 0;
             float alpha = 0.0f, beta = 0.0f;
-            __align__(16) bf16 feat[kFeat];
-            if (live) {
-                int lo = 0, hi = ia.nframes - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
+            {
+                uint32_t fs[8], fc[8];  // this half's 16 sines and 16 cosines, packed
+                if (live) {
+                    int lo = 0, hi = ia.nframes - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
+                    }
+                    fi = lo;
+                    const SurFrame& f = ia.frames[fi];
+                    const int local = static_cast<int>(ray - f.offset);
+                    const int pr = local / f.width, pc = local - pr * f.width;
+                    alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
+                    beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
+                    const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
+                    float u[kIn];
+                    normalise(x, u);
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) {
+                        float sv[2], cv[2];
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) {
+                            const int jj = 16 * half + j + e;
+                            float p = 0.0f;
+#pragma unroll
+                            for (int i = 0; i < kIn; ++i) p += sB[jj * kIn + i] * u[i];
+                            __sincosf(6.28318530717958648f * (p - rintf(p)), &sv[e], &cv[e]);
+                        }
+                        fs[j >> 1] = pack_bf16(sv[0], sv[1]);
+                        fc[j >> 1] = pack_bf16(cv[0], cv[1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) fs[j] = fc[j] = 0u;
                 }
-                fi = lo;
-                const SurFrame& f = ia.frames[fi];
-                const int local = static_cast<int>(ray - f.offset);
-                const int pr = local / f.width, pc = local - pr * f.width;
-                alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
-                beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
-                const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
-                fourier_features(x, sB, feat);
-            } else {
-#pragma unroll
-                for (int i = 0; i < kFeat; ++i) feat[i] = __float2bfloat16_rn(0.0f);
+                store_act16(act, row, 16 * half, fs);
+                store_act16(act, row, kFreq + 16 * half, fc);
             }
-#pragma unroll
-            for (int c = 0; c < kFeat; c += 16) store_act16(act, row, c, feat + c);
             tc::fence_proxy_async();
             tc::fence_before_sync();
-            tc::mbar_arrive(act_ready);
+            tc::mbar_arrive(&act_ready[slot]);
             bool ok = true;
             for (int l = 0; l < 4; ++l) {
-                if (!__all_sync(0xffffffffu, tc::mbar_wait(acc_full, acc_n & 1))) {
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n & 1))) {
                     if (lane == 0) give_up();
                     ok = false;
                     break;
                 }
                 ++acc_n;
                 tc::fence_after_sync();
-                const float* bl = ia.bias[l];
-#pragma unroll 1
-                for (int j = 0; j < 16; ++j) {
-                    float v[16];
-                    tc::tmem_ld16(trow + 16 * j, v);
-                    __align__(16) bf16 ab[16];
+                const float* hb = sHb + l * kHid + 128 * half;
+                const uint32_t cb = trow + 128u * half;
+                uint32_t ra[32], rb[32];
+                tc::tmem_ld32_issue(cb, ra);
+                tc::tmem_wait32(ra);
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const float z = v[i] + __ldg(bl + 16 * j + i);
-                        ab[i] = __float2bfloat16_rn(z * sigmoidf(z));
-                    }
-                    store_act16(act, row, 16 * j, ab);
+                for (int jj = 0; jj < 4; ++jj) {
+                    uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
+                    uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
+                    if (jj + 1 < 4) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
+                    uint32_t w[16];
+                    silu32(cur, hb + 32 * jj, w);
+                    store_act16(act, row, 128 * half + 32 * jj, w);
+                    store_act16(act, row, 128 * half + 32 * jj + 16, w + 8);
+                    if (jj + 1 < 4) tc::tmem_wait32(nxt);
                 }
                 tc::fence_proxy_async();
                 tc::fence_before_sync();
-                tc::mbar_arrive(act_ready);
+                tc::mbar_arrive(&act_ready[slot]);
             }
             if (!ok) break;
-            if (!__all_sync(0xffffffffu, tc::mbar_wait(acc_full, acc_n & 1))) {
+            if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n & 1))) {
                 if (lane == 0) give_up();
                 break;
             }
             ++acc_n;
             tc::fence_after_sync();
+            if (half == 1) {
+                tc::fence_before_sync();
+                continue;  // the head's 8 outputs are decoded by the first half
+            }
             float y[16];
             tc::tmem_ld16(trow, y);
             tc::fence_before_sync();
@@ -1353,7 +1430,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 1) tc::tmem_dealloc(tmem, 256);
+    if (warp == 1) tc::tmem_dealloc(tmem, 512);
 }
 
 // Copies compact fallback results (entry i = pixel list[i]) into the full-image outputs.
@@ -1472,7 +1549,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     int per_sm = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel, kInfThreads, kInfSmem);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    per_sm = std::max(1, std::min(per_sm, 2));  // TMEM: 256 columns per CTA, 512 per SM
+    per_sm = 1;  // one CTA per SM: it holds all 512 TMEM columns
     const long long ntiles = (total + kTileRays - 1) / kTileRays;
     const int grid = static_cast<int>(std::min<long long>(ntiles, static_cast<long long>(per_sm) * sms));
     InferArgs ia{};

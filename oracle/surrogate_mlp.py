@@ -8,8 +8,9 @@ cross-entropy over 3 logits + squared errors of r_disk / 30 and ln g (disk rays)
 unit vector (escaped rays), batch means.
 
 With `emulate_bf16=True` the values the GPU stores in BF16 are rounded the same way (features,
-weights, pre-activations z, activations, dY, dZ); everything else stays float64, so the difference
-from the GPU is its FP32 accumulation order and the hardware tanh (relative error ~2^-11).
+weights, pre-activations z, activations, dY, dZ) and the activation is evaluated as the GPU does it
+(BF16 half-argument, BF16 tanh, one BF16 multiply-add); everything else stays float64, so the
+difference from the GPU is its FP32 accumulation order and the hardware tanh approximations.
 """
 from __future__ import annotations
 
@@ -64,6 +65,13 @@ def sigmoid(z):
     return 0.5 + 0.5 * np.tanh(0.5 * z)
 
 
+def silu_bf16(z):
+    """The GPU's activation: with h = bf16(z / 2), t = tanh(h) in BF16, silu = bf16(h t + h)."""
+    h = bf16(0.5 * np.asarray(z, dtype=np.float64))
+    t = bf16(np.tanh(h))
+    return bf16(h * t + h)
+
+
 def forward(p, B, x, emulate_bf16=False):
     """Returns (Y [n x 16], cache) with cache = (F, [z_l], [a_l], weights used)."""
     rnd = bf16 if emulate_bf16 else (lambda v: np.asarray(v, dtype=np.float64))
@@ -72,7 +80,7 @@ def forward(p, B, x, emulate_bf16=False):
     h, zs, acts = F, [], []
     for W, b in layers[:4]:
         z = h @ W.T + b
-        a = rnd(z * sigmoid(z))
+        a = silu_bf16(z) if emulate_bf16 else z * sigmoid(z)
         zs.append(rnd(z))
         acts.append(a)
         h = a
