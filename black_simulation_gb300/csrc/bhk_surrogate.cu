@@ -556,6 +556,7 @@ struct bhk_surrogate {
     int32_t* list = nullptr;
     size_t cap_list = 0;
     unsigned long long* n_list = nullptr;
+    float* half_bias = nullptr;
     unsigned long long* n_list_host = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
@@ -739,7 +740,8 @@ bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bh
               dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) && dalloc(s, &s->F_t, B * kFeat) &&
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
               dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
-              dalloc(s, &s->n_list, 1) && cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
+              dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * kHid) &&
+              cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreate(&s->ev[i]) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
         const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
@@ -1095,17 +1097,19 @@ __global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc)
     }
 }
 
-constexpr int kInfStages = 5;               // weight ring: 5 x 16 KB in flight
+constexpr int kInfStages = 3;               // weight ring: 3 x 32 KB in flight
 constexpr int kTileRays = 128;
-constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 (activations or weights)
+constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 of activations
 constexpr int kActBytes = 4 * kChunkBytes; // one tile's 256-wide activations
+constexpr int kWChunkBytes = 256 * 64 * 2; // 32 KB: all 256 output rows x 64 K of a hidden layer's weights
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
 constexpr int kEpiWarps = 16;              // per tile slot: 4 TMEM lane quadrants x 2 column halves
 constexpr int kInfThreads = 64 + 32 * kEpiWarps;
-constexpr int kInfMisc = 128 + 16 + kFreq * kIn * 4 + 4 * kHid * 4;  // barriers, TMEM slot/flag, B, biases
-constexpr int kInfSmem = 2 * kActBytes + kInfStages * kChunkBytes + 1024 + kInfMisc;
+constexpr int kInfMisc = 128 + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
+constexpr int kInfSmem = 2 * kActBytes + kInfStages * kWChunkBytes + 1024 + kInfMisc;
 
-__host__ __device__ constexpr int layer_chunks(int l) { return l == 0 ? 2 : (l < 4 ? 8 : 4); }
+// Weight chunks per layer: 64-wide K slices of all output rows (N = 256 per MMA; the head N = 16).
+__host__ __device__ constexpr int layer_chunks(int l) { return l == 0 ? 1 : 4; }
 
 struct InferArgs {
     const SurFrame* frames;
@@ -1113,6 +1117,7 @@ struct InferArgs {
     long long n;
     const float* Bm;
     const float* bias[kLayers];
+    const float* half_bias;  // [4][256]: the hidden layers' biases halved
     uint8_t* outcome;
     double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
     int32_t *steps, *rejected;
@@ -1120,6 +1125,7 @@ struct InferArgs {
     unsigned long long* n_list;
     float p_min, band;
     int* err;
+    int cl;  // CTAs per cluster sharing each weight chunk by TMA multicast (1, 2 or 4)
 };
 
 // Byte offset of (row, col) in a 128-row x 64-column BF16 tile with the 128-byte swizzle.
@@ -1145,7 +1151,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb, uint32_t (&w)[16]) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const float4 b = reinterpret_cast<const float4*>(hb)[q];
+        const float4 b = __ldg(reinterpret_cast<const float4*>(hb) + q);
         w[2 * q] = silu2_half(fmaf(__uint_as_float(v[4 * q]), 0.5f, b.x), fmaf(__uint_as_float(v[4 * q + 1]), 0.5f, b.y));
         w[2 * q + 1] =
             silu2_half(fmaf(__uint_as_float(v[4 * q + 2]), 0.5f, b.z), fmaf(__uint_as_float(v[4 * q + 3]), 0.5f, b.w));
@@ -1155,7 +1161,10 @@ __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb,
 // Two tiles in flight per CTA (one CTA per SM): while the tensor core runs one tile's layer, the
 // other tile's epilogue warps turn their accumulators into the next layer's operand. Each tile
 // slot owns 256 TMEM columns and a 64 KB activation buffer; the weight ring is shared and filled
-// in the MMA's order (pair of tiles, layer, slot, chunk).
+// in the MMA's order (pair of tiles, layer, slot, chunk). Every MMA is 128 x 256 x 16, so each
+// activation slice is read from shared memory once per layer. The CTAs of a cluster (cl of them) walk
+// the same chunk sequence: each loads 1/cl of every weight chunk and multicasts it to all, and each
+// MMA commit releases the ring stage in every CTA, so L2 serves each chunk once per cluster.
 __global__ void __launch_bounds__(kInfThreads, 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
              const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
@@ -1163,7 +1172,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* ring = base + 2 * kActBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kChunkBytes);
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kWChunkBytes);
     uint64_t* empty = full + kInfStages;
     uint64_t* act_ready = empty + kInfStages;  // [2]
     uint64_t* acc_full = act_ready + 2;        // [2]
@@ -1171,18 +1180,23 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + 16);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* sB = reinterpret_cast<float*>(tmem_slot + 4);
-    float* sHb = sB + kFreq * kIn;  // hidden layers' biases halved: [4][256]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cl = ia.cl;
+    const int rank = cl > 1 ? static_cast<int>(tc::cluster_rank()) : 0;
+    const uint16_t mask = static_cast<uint16_t>((1u << cl) - 1u);
     const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
-    const long long n_my = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    // Cluster-uniform schedule: at step k cluster c takes tile group c + k * ncl, CTA `rank` its tile
+    // group * cl + rank (past the end: an empty tile), so every CTA of a cluster has the same steps.
+    const long long ngroups = (ntiles + cl - 1) / cl;
+    const long long cid = blockIdx.x / cl, ncl = gridDim.x / cl;
+    const long long n_my = cid < ngroups ? (ngroups - cid + ncl - 1) / ncl : 0;
     const long long pairs = (n_my + 1) / 2;
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
-    for (int i = threadIdx.x; i < 4 * kHid; i += blockDim.x) sHb[i] = 0.5f * ia.bias[i / kHid][i % kHid];
     if (threadIdx.x == 0) {
         for (int st = 0; st < kInfStages; ++st) {
             tc::mbar_init(&full[st], 1);
-            tc::mbar_init(&empty[st], 1);
+            tc::mbar_init(&empty[st], cl);  // one commit from every CTA of the cluster
         }
         for (int sl = 0; sl < 2; ++sl) {
             tc::mbar_init(&act_ready[sl], 32 * kEpiWarps / 2);
@@ -1200,6 +1214,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
     tc::fence_before_sync();
     __syncthreads();
+    if (cl > 1) tc::cluster_sync();  // every CTA's barriers exist before any multicast reaches them
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     auto give_up = [&]() {
@@ -1224,20 +1239,32 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                                 ok = false;
                                 break;
                             }
-                            const int nh = l == 0 ? c : (l < 4 ? c >> 2 : 0);
-                            const int kc = l == 0 ? 0 : (l < 4 ? c & 3 : c);
+                            const int kc = c;
                             const CUtensorMap* m = l == 0 ? &tW0 : l == 1 ? &tW1 : l == 2 ? &tW2 : l == 3 ? &tW3 : &tW4;
-                            tc::mbar_expect_tx(&full[st], l < 4 ? kChunkBytes : kHeadChunkBytes);
-                            tc::tma_load_2d(ring + st * kChunkBytes, m, kc * 64, nh * 128, &full[st]);
+                            tc::mbar_expect_tx(&full[st], l < 4 ? kWChunkBytes : kHeadChunkBytes);
+                            uint8_t* dst = ring + st * kWChunkBytes;
+                            if (cl == 1) {
+                                tc::tma_load_2d(dst, m, kc * 64, 0, &full[st]);
+                            } else if (l < 4) {  // this CTA's 256 / cl rows of the chunk, to all
+                                const int rows = 256 / cl;
+                                tc::tma_load_2d_multicast(dst + rank * rows * 128, m, kc * 64, rank * rows,
+                                                          &full[st], mask);
+                            } else if (rank == 0) {  // the head's 16 rows come from the first CTA
+                                tc::tma_load_2d_multicast(dst, m, kc * 64, 0, &full[st], mask);
+                            }
                         }
                     }
-            // Let every load issued land before the CTA may exit (bounded).
+            // Before the CTA may exit (bounded): every load of the last ring round has landed here, and
+            // with clusters every CTA's release of those stages has reached this CTA's barriers.
             for (long long r = q - kInfStages; r < q; ++r)
                 if (r >= 0) tc::mbar_wait(&full[r % kInfStages], static_cast<uint32_t>((r / kInfStages) & 1));
+            if (cl > 1 && ok)
+                for (long long r = q - kInfStages; r < q; ++r)
+                    if (r >= 0) tc::mbar_wait(&empty[r % kInfStages], static_cast<uint32_t>((r / kInfStages) & 1));
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---- MMA issuer
-            constexpr uint32_t kId128 = tc::idesc_bf16(128, 128), kId16 = tc::idesc_bf16(128, 16);
+            constexpr uint32_t kId256 = tc::idesc_bf16(128, 256), kId16 = tc::idesc_bf16(128, 16);
             long long q = 0;
             uint32_t act_n[2] = {0u, 0u};
             bool ok = true;
@@ -1261,15 +1288,15 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                                 break;
                             }
                             tc::fence_after_sync();
-                            const int nh = l == 0 ? c : (l < 4 ? c >> 2 : 0);
-                            const int kc = l == 0 ? 0 : (l < 4 ? c & 3 : c);
+                            const int kc = c;
                             const uint64_t ad = tc::smem_desc_sw128(act + kc * kChunkBytes);
-                            const uint64_t bd = tc::smem_desc_sw128(ring + st * kChunkBytes);
-                            const uint32_t d = tmem + static_cast<uint32_t>(256 * sl + (l < 4 ? nh * 128 : 0));
+                            const uint64_t bd = tc::smem_desc_sw128(ring + st * kWChunkBytes);
+                            const uint32_t d = tmem + static_cast<uint32_t>(256 * sl);
 #pragma unroll
                             for (int kk = 0; kk < 4; ++kk)
-                                tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId128 : kId16, (kc | kk) ? 1u : 0u);
-                            tc::mma_commit(&empty[st]);
+                                tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId256 : kId16, (kc | kk) ? 1u : 0u);
+                            if (cl == 1) tc::mma_commit(&empty[st]);
+                            else tc::mma_commit_multicast(&empty[st], mask);  // the stage is free in no CTA until all used it
                         }
                         if (ok) tc::mma_commit(&acc_full[sl]);
                     }
@@ -1290,7 +1317,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         // warp-collective).
         for (long long k = slot; k < n_my; k += 2) {
             if (__any_sync(0xffffffffu, *abort_flag)) break;
-            const long long tile = blockIdx.x + k * gridDim.x;
+            const long long tile = (cid + k * ncl) * cl + rank;
             const long long ray = tile * kTileRays + row;
             const bool live = ray < ia.n;
             int fi = 0;
@@ -1345,7 +1372,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                 }
                 ++acc_n;
                 tc::fence_after_sync();
-                const float* hb = sHb + l * kHid + 128 * half;
+                const float* hb = ia.half_bias + l * kHid + 128 * half;
                 const uint32_t cb = trow + 128u * half;
                 uint32_t ra[32], rb[32];
                 tc::tmem_ld32_issue(cb, ra);
@@ -1431,6 +1458,12 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 1) tc::tmem_dealloc(tmem, 512);
+    if (cl > 1) tc::cluster_sync();  // no CTA leaves while another may still deliver to or signal it
+}
+
+__global__ void halve_bias_kernel(const float* b0, const float* b1, const float* b2, const float* b3, float* out) {
+    const float* b = blockIdx.x == 0 ? b0 : blockIdx.x == 1 ? b1 : blockIdx.x == 2 ? b2 : b3;
+    out[blockIdx.x * kHid + threadIdx.x] = 0.5f * b[threadIdx.x];
 }
 
 // Copies compact fallback results (entry i = pixel list[i]) into the full-image outputs.
@@ -1480,6 +1513,10 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     ro.band = 0.05;
     ro.fallback = 1;
     if (ropts) ro = *ropts;
+    if (ro.cluster != 0 && ro.cluster != 1 && ro.cluster != 2 && ro.cluster != 4) {
+        set_last_error("bhk_surrogate_render: cluster must be 0 (automatic), 1, 2 or 4");
+        return BHK_EINVAL;
+    }
     std::lock_guard<std::mutex> lock_ctx(bhk::context_mutex(ctx));
     std::lock_guard<std::mutex> lock(s->mu);
     if (cudaSetDevice(s->device) != cudaSuccess || bhk::context_device(ctx) != s->device) {
@@ -1536,23 +1573,55 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
         e = cudaMemcpyAsync(ddesc, frames, sizeof(bhk_frame_desc) * nframes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail_cuda(e, "frame upload");
     curve_table_kernel<<<nframes, 256, 0, st>>>(dframes, ddesc);
+    static std::once_flag attr;
+    std::call_once(attr, [] { cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem); });
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    // One CTA per SM (it holds all 512 TMEM columns), optionally in clusters sharing the weight
+    // stream by multicast. Measured on GB300 (60 x 960x540 orbit frames): 1.98 G rays/s without
+    // clusters, 1.91 with pairs, 1.81 with fours -- L2 is not the limit (shared-memory bandwidth is),
+    // so the default is no cluster. The grid is the number of clusters resident at once (a static
+    // schedule must not need a second wave).
+    int cl = 1, resident = sms;
+    const int want = ro.cluster > 0 ? ro.cluster : 1;
+    for (int c : {4, 2, 1}) {
+        if (c != want) continue;
+        cudaLaunchConfig_t q{};
+        cudaLaunchAttribute at{};
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = c;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        q.gridDim = dim3((sms / c) * c);
+        q.blockDim = dim3(kInfThreads);
+        q.dynamicSmemBytes = kInfSmem;
+        q.attrs = &at;
+        q.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, infer_kernel, &q) == cudaSuccess && nclusters > 0) {
+            cl = c;
+            resident = nclusters;
+            break;
+        }
+        cudaGetLastError();
+    }
     Maps M;
     CUtensorMap w4;
-    if (!make_tmap(&M.W[0], s->w_rm[0], kHid, kFeat, 128) || !make_tmap(&M.W[1], s->w_rm[1], kHid, kHid, 128) ||
-        !make_tmap(&M.W[2], s->w_rm[2], kHid, kHid, 128) || !make_tmap(&M.W[3], s->w_rm[3], kHid, kHid, 128) ||
+    const uint32_t slice = 256u / cl;
+    if (!make_tmap(&M.W[0], s->w_rm[0], kHid, kFeat, slice) || !make_tmap(&M.W[1], s->w_rm[1], kHid, kHid, slice) ||
+        !make_tmap(&M.W[2], s->w_rm[2], kHid, kHid, slice) || !make_tmap(&M.W[3], s->w_rm[3], kHid, kHid, slice) ||
         !make_tmap(&w4, s->w_rm[4], kOutPad, kHid, 16)) {
         set_last_error("bhk_surrogate_render: tensor map creation failed");
         return BHK_ECUDA;
     }
-    static std::once_flag attr;
-    std::call_once(attr, [] { cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem); });
-    int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel, kInfThreads, kInfSmem);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    per_sm = 1;  // one CTA per SM: it holds all 512 TMEM columns
     const long long ntiles = (total + kTileRays - 1) / kTileRays;
-    const int grid = static_cast<int>(std::min<long long>(ntiles, static_cast<long long>(per_sm) * sms));
+    const long long groups = (ntiles + cl - 1) / cl;
+    const int grid = static_cast<int>(std::min<long long>(groups, resident) * cl);
+    halve_bias_kernel<<<4, 256, 0, st>>>(s->p + s->L.b[0], s->p + s->L.b[1], s->p + s->L.b[2], s->p + s->L.b[3],
+                                         s->half_bias);
     InferArgs ia{};
+    ia.cl = cl;
+    ia.half_bias = s->half_bias;
     ia.frames = dframes;
     ia.nframes = nframes;
     ia.n = total;
@@ -1575,8 +1644,22 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
     if (e != cudaSuccess) return fail_cuda(e, "launch set-up");
-    infer_kernel<<<grid, kInfThreads, kInfSmem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
-    e = cudaGetLastError();
+    {
+        cudaLaunchConfig_t q{};
+        cudaLaunchAttribute at{};
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = cl;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        q.gridDim = dim3(grid);
+        q.blockDim = dim3(kInfThreads);
+        q.dynamicSmemBytes = kInfSmem;
+        q.stream = st;
+        q.attrs = &at;
+        q.numAttrs = 1;
+        e = cudaLaunchKernelEx(&q, infer_kernel, M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->n_list_host, s->n_list, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1615,6 +1698,8 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
         stats->fallback = nfb;
         stats->infer_ms = ms;
         stats->trace_ms = trace_ms;
+        stats->cluster = cl;
+        stats->grid = grid;
     }
     return rs;
 }

@@ -179,7 +179,7 @@ class Surrogate:
 
 
     def render(self, ctx, frames, opts=None, p_min: float = 0.99, band: float = 0.05, fallback: bool = True,
-               out: Optional[dict] = None, stream=None):
+               out: Optional[dict] = None, stream=None, cluster: int = 0):
         """Surrogate + integrator-fallback render of `frames` (bhk.Frame list) through the fused
         inference kernel; returns (outputs as bhk.alloc_outputs gives, stats dict)."""
         n = sum(f.rays for f in frames)
@@ -187,7 +187,7 @@ class Surrogate:
             out = bhk.alloc_outputs(n, f"cuda:{self.device}")
         arr = (bhk.FrameDescC * len(frames))(*[f.c() for f in frames])
         oc = (opts or bhk.TraceOpts("mixed")).c()
-        ro = bhk.RenderOptsC(p_min, band, 1 if fallback else 0, 0)
+        ro = bhk.RenderOptsC(p_min, band, 1 if fallback else 0, cluster)
         st = bhk.RenderStatsC()
         outc = bhk._out_c(out)
         bhk.check(bhk.lib().bhk_surrogate_render(self._h, ctx.h, arr, len(frames), C.byref(oc), C.byref(ro),

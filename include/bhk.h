@@ -254,13 +254,14 @@ typedef struct bhk_render_opts {
     double p_min;        /* rays whose largest class probability is below this fall back (0.99) */
     double band;         /* rays within this image-plane distance (M) of the critical curve fall back (0.05) */
     int32_t fallback;    /* 1: trace the fallback rays (the product); 0: only list them (measurement) */
-    int32_t pad;
+    int32_t cluster;     /* CTAs sharing each weight chunk by TMA multicast: 1, 2 or 4 (0: 1) */
 } bhk_render_opts;
 
 typedef struct bhk_render_stats {
     int64_t rays, fallback;  /* rays rendered, rays handed to the integrator */
     double infer_ms;         /* fused inference kernel (CUDA events) */
     double trace_ms;         /* fallback trace incl. its launch and the scatter (CUDA events) */
+    int32_t cluster, grid;   /* launch shape of the inference kernel */
 } bhk_render_stats;
 
 /* Renders frames with the surrogate and integrator fallback: one fused tcgen05 inference kernel over

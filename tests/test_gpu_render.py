@@ -130,3 +130,15 @@ def test_band_rule_covers_the_critical_curve(ctx, trained, oracle):
 def band_distance(alpha, beta, ca, cb):
     import pyoracle
     return pyoracle.band_distance(alpha, beta, ca, cb)
+
+
+@pytest.mark.parametrize("cluster", [2, 4])
+def test_multicast_clusters_give_identical_results(ctx, trained, cluster):
+    """Clusters that share the weight stream by TMA multicast compute exactly what single CTAs do."""
+    frames = [_frame(160, 90, 70.0), _frame(96, 96, 50.0)]
+    a, sa = trained.render(ctx, frames, p_min=0.0, band=0.0, fallback=False, cluster=1)
+    b, sb = trained.render(ctx, frames, p_min=0.0, band=0.0, fallback=False, cluster=cluster)
+    assert sb["cluster"] == cluster and sa["cluster"] == 1
+    assert torch.equal(a["outcome"], b["outcome"])
+    for k in FIELDS_D:
+        assert _same(a[k].cpu().numpy(), b[k].cpu().numpy()), k
