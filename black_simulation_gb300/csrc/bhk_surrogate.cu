@@ -34,17 +34,17 @@ namespace sur {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kStages = 4;
 constexpr int kTileM = 128;
 constexpr int kChunkK = 64;
 constexpr int kABytes = kTileM * kChunkK * 2;  // 16 KB
 
-enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3 };
+enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3, kPartialF32 = 4 };
 
 struct EpiArgs {
     int M, N;              // logical output extent (rows, columns)
     const float* bias;     // [N] or null
-    float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32
+    float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32; kPartialF32: split z
+                           // writes its partial product at f32 + z * M * ld_f32
     int ld_f32;
     bf16* rm;              // row-major BF16 output [M x ld_rm]
     int ld_rm;
@@ -54,9 +54,17 @@ struct EpiArgs {
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
 };
 
+// Pipeline depth by tile width: two CTAs (each 256 TMEM columns at most) fit on an SM, so one
+// CTA's epilogue overlaps the other's main loop; the network's K is at most 256 (4 chunks), except
+// for split-K weight gradients.
 template <int BN>
-constexpr int gemm_smem_bytes() {
-    return kStages * (kABytes + BN * kChunkK * 2) + 1024 + 256;
+__host__ __device__ constexpr int gemm_stages() {
+    return BN >= 256 ? 2 : 4;
+}
+
+template <int BN>
+__host__ __device__ constexpr int gemm_smem_bytes() {
+    return gemm_stages<BN>() * (kABytes + BN * kChunkK * 2) + 1024 + 256;
 }
 
 // Logistic sigmoid as 1/2 + tanh(z/2)/2 on the hardware tanh (one MUFU operation; relative error of
@@ -79,10 +87,51 @@ __device__ __forceinline__ uint32_t silu2_half(float h0, float h1) {
     return a;
 }
 
+// Writes this warp's 32 rows x 16 columns (lane = row, vals = its 16 values) transposed into
+// t[(nb + i) * ld + m0w + lane], through a 1 KB per-warp staging area in shared memory, as 16-byte
+// vectors (rows at or past M are not written).
+__device__ __forceinline__ void store_transposed16(bf16* t, int ld, int nb, int m0w, int M, const bf16* vals,
+                                                   bf16* stage, int lane) {
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) stage[i * 32 + lane] = vals[i];
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int v = lane + 32 * k, i = v >> 2, part = v & 3;
+        const int r0 = m0w + part * 8;
+        bf16* dst = t + static_cast<size_t>(nb + i) * ld + r0;
+        const bf16* src = stage + i * 32 + part * 8;
+        if (r0 + 8 <= M) {
+            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
+        } else {
+            for (int q = 0; q < 8 && r0 + q < M; ++q) dst[q] = src[q];
+        }
+    }
+}
+
+// Sums each of 16 per-lane values over the warp's 32 lanes by recursive halving (16 shuffles). The
+// total of column `col` (= bits 4..1 of the lane) is returned in lanes 2 col and 2 col + 1.
+__device__ __forceinline__ float warp_colsum16(const float (&x)[16], int lane, int& col) {
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
+    float y[8], z[4], w[2];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = (b4 ? x[8 + i] : x[i]) + __shfl_xor_sync(0xffffffffu, b4 ? x[i] : x[8 + i], 16);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) z[i] = (b3 ? y[4 + i] : y[i]) + __shfl_xor_sync(0xffffffffu, b3 ? y[i] : y[4 + i], 8);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) w[i] = (b2 ? z[2 + i] : z[i]) + __shfl_xor_sync(0xffffffffu, b2 ? z[i] : z[2 + i], 4);
+    float v = (b1 ? w[1] : w[0]) + __shfl_xor_sync(0xffffffffu, b1 ? w[0] : w[1], 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    col = (b4 ? 8 : 0) + (b3 ? 4 : 0) + (b2 ? 2 : 0) + (b1 ? 1 : 0);
+    return v;
+}
+
 template <int BN, int EPI>
 __global__ void __launch_bounds__(128, 1)
 gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
             int k_per_split, int* err) {
+    constexpr int kStages = gemm_stages<BN>();
     constexpr int kBBytes = BN * kChunkK * 2;
     constexpr uint32_t kCols = BN < 32 ? 32 : BN;
     constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, BN);
@@ -163,14 +212,22 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int q = c; q < loaded; ++q) tc::mbar_wait(&full[q % kStages], (q / kStages) & 1);
         }
     }
-    const bool acc_ready = tc::mbar_wait(accbar, 0);
+    // The decision to run the epilogue is taken by the whole CTA (it contains block barriers).
+    const int acc_ready = __syncthreads_and(tc::mbar_wait(accbar, 0) ? 1 : 0);
     tc::fence_after_sync();
-    __syncthreads();
     if (!acc_ready && threadIdx.x == 0) atomicExch(err, 1);
     if (acc_ready && !*fail && nchunks > 0) {
         const int row = 32 * warp + lane;
         const int m = m0 + row;
         const bool live = m < ea.M;
+        // The pipeline's shared memory is idle now: 1 KB of transpose staging per warp, then the
+        // CTA's column sums.
+        bf16* stage = reinterpret_cast<bf16*>(sA + warp * 1024);
+        float* scol = reinterpret_cast<float*>(sA + 4096);
+        if constexpr (EPI == kDsilu) {
+            for (int i = threadIdx.x; i < BN; i += blockDim.x) scol[i] = 0.0f;
+            __syncthreads();
+        }
 #pragma unroll 1
         for (int j = 0; j < BN / 16; ++j) {
             float v[16];
@@ -185,9 +242,21 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 if (live)
                     for (int i = 0; i < 16; ++i)
                         if (nb + i < ea.N) atomicAdd(&ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i], v[i]);
-            } else if constexpr (EPI == kBiasSilu) {
+            } else if constexpr (EPI == kPartialF32) {
                 if (live) {
-                    __align__(16) bf16 zb[16], ab[16];
+                    float* dst = ea.f32 + static_cast<size_t>(blockIdx.z) * ea.M * ea.ld_f32 +
+                                 static_cast<size_t>(m) * ea.ld_f32 + nb;
+                    if (nb + 16 <= ea.N) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    } else {
+                        for (int i = 0; i < 16 && nb + i < ea.N; ++i) dst[i] = v[i];
+                    }
+                }
+            } else if constexpr (EPI == kBiasSilu) {
+                __align__(16) bf16 zb[16], ab[16];
+                if (live) {
                     for (int i = 0; i < 16; i += 2) {
                         const float z0 = v[i] + ea.bias[nb + i], z1 = v[i + 1] + ea.bias[nb + i + 1];
                         zb[i] = __float2bfloat16_rn(z0);
@@ -201,13 +270,15 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                     zd[1] = reinterpret_cast<const uint4*>(zb)[1];
                     ad[0] = reinterpret_cast<const uint4*>(ab)[0];
                     ad[1] = reinterpret_cast<const uint4*>(ab)[1];
-                    if (ea.t)
-                        for (int i = 0; i < 16; ++i) ea.t[static_cast<size_t>(nb + i) * ea.ld_t + m] = ab[i];
+                } else {
+                    for (int i = 0; i < 16; ++i) ab[i] = __float2bfloat16_rn(0.0f);
                 }
+                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * warp, ea.M, ab, stage, lane);
             } else {  // kDsilu: d(pre-activation) = dA * silu'(z); bias gradient = column sums
                 float dz[16];
+                __align__(16) bf16 ob[16];
                 if (live) {
-                    __align__(16) bf16 zin[16], ob[16];
+                    __align__(16) bf16 zin[16];
                     const uint4* zs = reinterpret_cast<const uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
                     reinterpret_cast<uint4*>(zin)[0] = zs[0];
                     reinterpret_cast<uint4*>(zin)[1] = zs[1];
@@ -220,24 +291,46 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                     uint4* od = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
                     od[0] = reinterpret_cast<const uint4*>(ob)[0];
                     od[1] = reinterpret_cast<const uint4*>(ob)[1];
-                    if (ea.t)
-                        for (int i = 0; i < 16; ++i) ea.t[static_cast<size_t>(nb + i) * ea.ld_t + m] = ob[i];
                 } else {
-                    for (int i = 0; i < 16; ++i) dz[i] = 0.0f;
-                }
-                if (ea.colsum) {
                     for (int i = 0; i < 16; ++i) {
-                        float x = dz[i];
-                        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                        if (lane == 0) atomicAdd(&ea.colsum[nb + i], x);
+                        dz[i] = 0.0f;
+                        ob[i] = __float2bfloat16_rn(0.0f);
                     }
                 }
+                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * warp, ea.M, ob, stage, lane);
+                if (ea.colsum) {
+                    int col;
+                    const float tot = warp_colsum16(dz, lane, col);
+                    if (!(lane & 1)) atomicAdd(&scol[16 * j + col], tot);
+                }
             }
+        }
+        if constexpr (EPI == kDsilu) {
+            __syncthreads();
+            if (ea.colsum)
+                for (int i = threadIdx.x; i < BN && n0 + i < ea.N; i += blockDim.x) atomicAdd(&ea.colsum[n0 + i], scol[i]);
         }
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+// dst[i] += sum over the splits of ws[split * count + i] (count a multiple of 4, 16-byte aligned).
+__global__ void reduce_splits_kernel(const float* __restrict__ ws, int splits, long long count, float* dst) {
+    const long long n4 = count / 4;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n4;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        float4 acc = reinterpret_cast<float4*>(dst)[i];
+        for (int sp = 0; sp < splits; ++sp) {
+            const float4 w = reinterpret_cast<const float4*>(ws + sp * count)[i];
+            acc.x += w.x;
+            acc.y += w.y;
+            acc.z += w.z;
+            acc.w += w.w;
+        }
+        reinterpret_cast<float4*>(dst)[i] = acc;
+    }
 }
 
 // ------------------------------------------------------------------------------ host side ----
@@ -297,6 +390,13 @@ cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArg
 }
 
 int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
+
+// K splits launch_gemm makes for `splits` requested (grid z).
+int grid_splits(int K, int splits) {
+    splits = splits < 1 ? 1 : splits;
+    const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
+    return (K + per - 1) / per;
+}
 
 }  // namespace sur
 }  // namespace bhk
@@ -557,6 +657,7 @@ struct bhk_surrogate {
     size_t cap_list = 0;
     unsigned long long* n_list = nullptr;
     float* half_bias = nullptr;
+    float* ws = nullptr;  // split-K partial products of the weight gradients (96 x 256 x 256)
     unsigned long long* n_list_host = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
@@ -649,6 +750,19 @@ int split_for(int n) {
     return s < 1 ? 1 : (s > 96 ? 96 : s);
 }
 
+// dst (M x N FP32, dense) += A^T-style weight gradient: the split-K partial products go to the
+// workspace with plain stores, then one pass sums them into dst.
+cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, int splits,
+                        float* dst, cudaStream_t st) {
+    EpiArgs ea = epi(M, N);
+    ea.f32 = s->ws;
+    ea.ld_f32 = N;
+    cudaError_t e = launch_gemm<kPartialF32>(A, B, ea, M, N, K, splits, s->err, st);
+    if (e != cudaSuccess) return e;
+    reduce_splits_kernel<<<256, 256, 0, st>>>(s->ws, grid_splits(K, splits), static_cast<long long>(M) * N, dst);
+    return cudaGetLastError();
+}
+
 // Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss.
 cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const float* tgt, int n, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(s->g, 0, sizeof(float) * s->L.total, st);
@@ -657,12 +771,7 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
                                                  s->loss, n, 1.0f / n, s->w);
     const int splits = split_for(n);
     // Head: dW5 = dY^T A4, then dA4 = dY W5 -> dZ4.
-    {
-        EpiArgs ea = epi(kOutPad, kHid);
-        ea.f32 = s->g + s->L.w[4];
-        ea.ld_f32 = kHid;
-        e = launch_gemm<kAtomicF32>(M.dy_t, M.a_t[3], ea, kOutPad, kHid, n, splits, s->err, st);
-    }
+    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, kHid, n, splits, s->g + s->L.w[4], st);
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, kHid);
         ea.rm = s->dz_rm[0];
@@ -676,11 +785,8 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
-        EpiArgs ew = epi(kHid, fan_in(l));
-        ew.f32 = s->g + s->L.w[l];
-        ew.ld_f32 = fan_in(l);
         const CUtensorMap& Bop = l == 0 ? M.F_t : M.a_t[l - 1];
-        e = launch_gemm<kAtomicF32>(M.dz_t[cur], Bop, ew, kHid, fan_in(l), n, splits, s->err, st);
+        e = weight_grad(s, M.dz_t[cur], Bop, kHid, fan_in(l), n, splits, s->g + s->L.w[l], st);
         if (e != cudaSuccess || l == 0) break;
         EpiArgs ex = epi(n, kHid);
         ex.rm = s->dz_rm[1 - cur];
@@ -741,6 +847,7 @@ bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bh
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
               dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
               dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * kHid) &&
+              dalloc(s, &s->ws, static_cast<size_t>(96) * kHid * kHid) &&
               cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreate(&s->ev[i]) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
