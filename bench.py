@@ -95,7 +95,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={SMI_FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -520,7 +520,9 @@ def run_train(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 for the GPU arm, so that the clock sampler sees the timed "
+                         "region; 5 bounded CPU samples for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="1080p", choices=["1080p", "c1", "batch64", "orbit", "train"])
@@ -538,6 +540,8 @@ def main():
     ap.add_argument("--buckets", type=int, default=0)
     ap.add_argument("--reg-budget", type=int, default=0)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.impl == "reference" or args.workload in ("orbit", "c1") else 200
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "orbit":

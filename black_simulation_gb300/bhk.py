@@ -177,6 +177,8 @@ def lib() -> C.CDLL:
         "bhk_surrogate_dataset": (C.c_int, [vp, i64, C.c_uint64, d, C.POINTER(TraceOptsC), vp, vp, vp, vp, vp]),
         "bhk_trace_pixels": (C.c_int, [vp, C.POINTER(FrameDescC), C.c_int32, vp, i64, C.POINTER(TraceOptsC),
                                        C.POINTER(RaysOutC), vp]),
+        "bhk_trace_rays_framed": (C.c_int, [vp, i64, vp, vp, vp, vp, vp, vp, d, d, C.POINTER(TraceOptsC),
+                                            C.POINTER(RaysOutC), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -448,6 +450,22 @@ class Context:
         oc = opts.c()
         outc = _out_c(out)
         check(lib().bhk_trace_pixels(self.h, arr, nf, _ptr(pixels), n, C.byref(oc), C.byref(outc), _stream(stream)))
+        return out
+
+    def trace_rays_framed(self, a, r, theta, phi, frames, look, r_disk_in: float = 0.0, r_disk_out: float = 20.0,
+                          opts: TraceOpts = TraceOpts(), out: Optional[dict] = None, stream=None) -> dict:
+        """trajectory::traceRay's call shape, batched: per-ray camera position (float64 (n,) each), frame
+        (float64 (n, 4, 4), e[k][mu]) and unit look direction on the frame's (r, theta, phi) axes ((n, 3))."""
+        n = a.shape[0]
+        if tuple(frames.shape) != (n, 4, 4) or tuple(look.shape) != (n, 3):
+            raise ValueError("frames must be (n, 4, 4) and look (n, 3)")
+        if out is None:
+            out = alloc_outputs(n, a.device)
+        oc = opts.c()
+        outc = _out_c(out)
+        check(lib().bhk_trace_rays_framed(self.h, n, _ptr(a), _ptr(r), _ptr(theta), _ptr(phi), _ptr(frames),
+                                          _ptr(look), r_disk_in, r_disk_out, C.byref(oc), C.byref(outc),
+                                          _stream(stream)))
         return out
 
     def stats(self) -> dict:

@@ -52,7 +52,7 @@ struct GraphKey {
     int64_t n_explicit = 0;
     TraceParams p{};
     Outputs out{};
-    const void* ex[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    const void* ex[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double r_in = 0.0, r_out = 0.0;
     size_t cap_rays = 0;
     bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
@@ -198,10 +198,11 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
 LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf}; }
 
 struct Batch {
-    int mode;  // 0 frames, 1 explicit, 2 a list of pixels of the frames (ex[0] = the device list)
+    int mode;  // 0 frames, 1 explicit, 2 a list of pixels of the frames (ex[0] = the device list),
+               // 3 framed cameras (ex = a, r, theta, phi, frames, look)
     int nframes;
     int64_t n;
-    const double* ex[5];
+    const double* ex[6];
     double r_in, r_out;
 };
 
@@ -224,6 +225,10 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
         launch_rays_list(c->frames_dev, b.nframes, static_cast<const int32_t*>(static_cast<const void*>(b.ex[0])), L,
                          r.p, c->ctl, lgrid, s);
+    } else if (b.mode == 3) {
+        BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
+        launch_rays_framed(b.ex[0], b.ex[1], b.ex[2], b.ex[3], reinterpret_cast<const bhk_frame*>(b.ex[4]), b.ex[5],
+                           b.r_in, b.r_out, c->geom, L, r.p, c->ctl, lgrid, s);
     } else {
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
         launch_rays_explicit(b.ex[0], b.ex[1], b.ex[2], b.ex[3], b.ex[4], b.r_in, b.r_out, r.p.r_escape, c->geom, L,
@@ -255,7 +260,7 @@ bhk_status run_batch(bhk_context* c, const Batch& b, const Resolved& r, const Ou
     k.mode = b.mode; k.fp64 = r.fp64; k.nframes = b.nframes; k.block = r.block; k.chunk = r.chunk;
     k.buckets = r.buckets; k.grid = r.grid; k.timed = 0; k.regcap = r.regcap; k.p = r.p; k.out = out; k.cap_rays = c->cap_rays;
     k.n_explicit = b.mode != 0 ? 1 : 0;
-    for (int i = 0; i < 5; ++i) k.ex[i] = b.ex[i];
+    for (int i = 0; i < 6; ++i) k.ex[i] = b.ex[i];
     k.r_in = b.r_in; k.r_out = b.r_out;
     if (!c->exec || !(k == c->gkey)) {
         if (c->exec) cudaGraphExecDestroy(c->exec);
@@ -355,7 +360,7 @@ bhk_status trace_frames_locked(bhk_context* c, const bhk_frame_desc* frames, int
     const Resolved r = resolve(c, opts);
     st = stage_frames(c, frames, nframes);
     if (st != BHK_OK) return st;
-    Batch b{0, nframes, total, {nullptr, nullptr, nullptr, nullptr, nullptr}, 0.0, 0.0};
+    Batch b{0, nframes, total, {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}, 0.0, 0.0};
     st = run_batch(c, b, r, to_outputs(out), timed, s);
     if (st != BHK_OK) return st;
     return finish_call(c, r, total, timed, s);
@@ -387,7 +392,8 @@ bhk_status bhk::trace_pixel_list(bhk_context* c, const bhk_frame_desc* frames, i
     st = stage_frames(c, frames, nframes);  // also waits until the pinned ray count is free
     if (st != BHK_OK) return st;
     *c->n_host = n;
-    Batch b{2, nframes, n, {reinterpret_cast<const double*>(list), nullptr, nullptr, nullptr, nullptr}, 0.0, 0.0};
+    Batch b{2, nframes, n, {reinterpret_cast<const double*>(list), nullptr, nullptr, nullptr, nullptr, nullptr},
+            0.0, 0.0};
     st = run_batch(c, b, r, to_outputs(&o), true, s);
     if (st != BHK_OK) return st;
     return finish_call(c, r, n, true, s);
@@ -595,10 +601,34 @@ bhk_status bhk_trace_rays(bhk_context* c, int64_t n, const double* a, const doub
     cudaStream_t s = pick(c, stream);
     if (c->staging_free) BHK_CUDA(cudaEventSynchronize(c->staging_free));
     *c->n_host = n;
-    Batch b{1, 0, n, {a, r_obs, theta_obs, alpha, beta}, r_disk_in, r_disk_out};
+    Batch b{1, 0, n, {a, r_obs, theta_obs, alpha, beta, nullptr}, r_disk_in, r_disk_out};
     st = run_batch(c, b, r, to_outputs(out), true, s);
     if (st != BHK_OK) return st;
     return finish_call(c, r, n, true, s);
+}
+
+bhk_status bhk_trace_rays_framed(bhk_context* c, int64_t n, const double* a, const double* r, const double* theta,
+                                 const double* phi, const bhk_frame* frames, const double* look, double r_disk_in,
+                                 double r_disk_out, const bhk_trace_opts* opts, const bhk_rays_out* out,
+                                 void* stream) {
+    if (!c) return fail(BHK_EINVAL, "context is null");
+    if (n < 0 || n > (int64_t(1) << 31) - 1) return fail(BHK_EINVAL, "ray count out of range");
+    if (!out) return fail(BHK_EINVAL, "out is null");
+    if (n == 0) return BHK_OK;
+    if (!a || !r || !theta || !phi || !frames || !look) return fail(BHK_EINVAL, "null ray array");
+    if (!(r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
+    std::lock_guard<std::mutex> lock(c->mu);
+    BHK_CUDA(cudaSetDevice(c->device));
+    bhk_status st = ensure_scratch(c, static_cast<size_t>(n), static_cast<size_t>(n), 1);
+    if (st != BHK_OK) return st;
+    const Resolved rs = resolve(c, opts);
+    cudaStream_t s = pick(c, stream);
+    if (c->staging_free) BHK_CUDA(cudaEventSynchronize(c->staging_free));
+    *c->n_host = n;
+    Batch b{3, 0, n, {a, r, theta, phi, reinterpret_cast<const double*>(frames), look}, r_disk_in, r_disk_out};
+    st = run_batch(c, b, rs, to_outputs(out), true, s);
+    if (st != BHK_OK) return st;
+    return finish_call(c, rs, n, true, s);
 }
 
 bhk_status bhk_get_stats(bhk_context* c, bhk_trace_stats* stats) {

@@ -19,6 +19,8 @@ struct RayGeom {
     double r_in, r_out, zone_top; // disk, and r_+ + width of the analytic capture zone
     float af, r0f, th0f, ph0f, r_capf, r_escf, r_inf, r_outf, zone_topf, rpf;
     int32_t south0;               // camera below the equator: th0f holds pi - theta_obs
+    int32_t dead;                 // per-ray geometry only: a camera inside the horizon sees the hole
+                                  // (trajectory::traceRay's rule, src/trajectory.cpp:236-244)
 };
 
 // Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset, and the per-camera
@@ -94,6 +96,10 @@ void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, 
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
                           const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
+// Per-ray cameras with arbitrary frames (moving, or inside the horizon): kerr::photonFromFrame.
+void launch_rays_framed(const double* a, const double* r, const double* th, const double* ph, const bhk_frame* frames,
+                        const double* look, double r_in, double r_out, RayGeom* geom, LaunchSoA L, const TraceParams& p,
+                        const Control* ctl, int grid, cudaStream_t s);
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,

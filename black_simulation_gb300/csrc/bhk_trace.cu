@@ -57,6 +57,7 @@ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, doub
     g.af = float(a); g.r0f = float(r); g.th0f = float(g.south0 ? kPi - th : th); g.ph0f = float(ph);
     g.r_capf = float(g.r_cap); g.r_escf = float(g.r_esc); g.r_inf = float(g.r_in); g.r_outf = float(g.r_out);
     g.zone_topf = float(g.zone_top); g.rpf = float(g.rp);
+    g.dead = 0;
     return g;
 }
 
@@ -200,6 +201,32 @@ __global__ void launch_explicit_kernel(const double* __restrict__ a, const doubl
         St s;
         photon_from_frame(ai, ri, ti, 0.0, e, look, c, s);
         geom[i] = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
+        store_launch(L, i, ai, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
+    }
+}
+
+// Launch records for cameras given by frame: trajectory::traceRay's launch (src/trajectory.cpp:
+// 214-219) per ray, with its inside-horizon rule: a photon seen from inside the horizon with
+// 2 r_+ E - a L < 0 came through the far side of the eternal spacetime (the hole) -- flagged dead.
+__global__ void launch_framed_kernel(const double* __restrict__ a, const double* __restrict__ r,
+                                     const double* __restrict__ th, const double* __restrict__ ph,
+                                     const bhk_frame* __restrict__ frames, const double* __restrict__ look,
+                                     double r_in, double r_out, RayGeom* geom, LaunchSoA L, TraceParams p,
+                                     const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double ai = a[i], ri = r[i], ti = th[i], pi = ph[i];
+        double e[4][4];
+        for (int k = 0; k < 4; ++k)
+            for (int m = 0; m < 4; ++m) e[k][m] = frames[i].e[k][m];
+        const double lk[3] = {look[3 * i], look[3 * i + 1], look[3 * i + 2]};
+        Cons c;
+        St s;
+        photon_from_frame(ai, ri, ti, pi, e, lk, c, s);
+        RayGeom g = make_geom(ai, ri, ti, pi, r_in, r_out, p);
+        g.dead = (ri < g.rp && 2.0 * g.rp * c.E - ai * c.L < 0.0) ? 1 : 0;
+        geom[i] = g;
         store_launch(L, i, ai, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
     }
 }
@@ -688,7 +715,12 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             if (((need >> lane) & 1u) && rank < avail) {
                 const long long q = pool_pos + rank;
                 ray = order ? order[q] : q;
-                lane_begin_launch(s, geom[L.geom_id[ray]], L, ray, p);
+                const RayGeom& G = geom[L.geom_id[ray]];
+                lane_begin_launch(s, G, L, ray, p);
+                if (G.dead) {  // seen from inside the horizon: the hole, with no step taken
+                    finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                    ray = -1;
+                }
             }
             const int served = __popc(need) < avail ? __popc(need) : avail;
             pool_pos += served;
@@ -791,6 +823,12 @@ void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes
                         const Control* ctl, int grid, cudaStream_t s) {
     (void)geom;
     launch_frames_kernel<<<grid, 128, 0, s>>>(frames, nframes, L, p, ctl);
+}
+
+void launch_rays_framed(const double* a, const double* r, const double* th, const double* ph, const bhk_frame* frames,
+                        const double* look, double r_in, double r_out, RayGeom* geom, LaunchSoA L, const TraceParams& p,
+                        const Control* ctl, int grid, cudaStream_t s) {
+    launch_framed_kernel<<<grid, 128, 0, s>>>(a, r, th, ph, frames, look, r_in, r_out, geom, L, p, ctl);
 }
 
 void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, LaunchSoA L, const TraceParams& p,

@@ -167,6 +167,17 @@ bhk_status bhk_trace_rays(bhk_context* ctx, int64_t n, const double* a, const do
  * the reference, whose renderers always trace every pixel). */
 bhk_status bhk_trace_pixels(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes, const int32_t* pixels,
                             int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
+/* Per-ray cameras with arbitrary frames -- the call shape of trajectory::traceRay(a, r, theta, phi,
+ * frame, look, scene) (src/trajectory.h:118-119), batched: camera position (a, r, theta, phi), its
+ * frame (kerr::observerFrame of any 4-velocity: ZAMO, boosted, geodesic; bhk_observer_frame builds
+ * them) and a unit look direction on the frame's (r, theta, phi) axes (3 doubles per ray), all device
+ * memory. Cameras may be inside the horizon: there a photon with 2 r_+ E - a L < 0 ends captured at
+ * once (src/trajectory.cpp:236-244), the others are traced back out through r_+. Disk radii as in
+ * bhk_trace_rays. */
+bhk_status bhk_trace_rays_framed(bhk_context* ctx, int64_t n, const double* a, const double* r, const double* theta,
+                                 const double* phi, const bhk_frame* frames, const double* look, double r_disk_in,
+                                 double r_disk_out, const bhk_trace_opts* opts, const bhk_rays_out* out,
+                                 void* stream);
 bhk_status bhk_get_stats(bhk_context* ctx, bhk_trace_stats* stats);   /* synchronises the context stream */
 /* Times block x chunk x sort-granularity candidates on these frames and keeps the fastest for later
  * calls on this context (opts fields left 0). The chosen values are returned in stats. */

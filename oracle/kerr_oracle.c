@@ -518,11 +518,7 @@ static double disk_inner(const orc_scene* sc) {
 
 /* The reference loop shape (src/trajectory.cpp:259-392) at tolerance sc->tol, with the scene's
  * capture and escape radii. The escape point is interpolated linearly to r_escape. */
-static void trace_rk4(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
-    ray_init(out);
-    orc_constants c;
-    orc_state s;
-    orc_pinhole_launch(sc, alpha, beta, &c, &s);
+static void trace_rk4(const orc_scene* sc, orc_constants c, orc_state s, orc_ray* out) {
     out->E = c.E, out->L = c.L, out->Q = c.Q;
     const double a = sc->a;
     const double r_cap = orc_horizon_radius(a) * (1.0 + sc->capture_eps);
@@ -621,11 +617,7 @@ static double locate(const double* y0, const double* y1, const vec5 k[7], double
     return 0.5 * (lo + hi);
 }
 
-static void trace_dp5(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
-    ray_init(out);
-    orc_constants c;
-    orc_state s;
-    orc_pinhole_launch(sc, alpha, beta, &c, &s);
+static void trace_dp5(const orc_scene* sc, orc_constants c, orc_state s, orc_ray* out) {
     out->E = c.E, out->L = c.L, out->Q = c.Q;
     const double a = sc->a;
     const double rp = orc_horizon_radius(a);
@@ -729,9 +721,36 @@ static void trace_dp5(const orc_scene* sc, double alpha, double beta, orc_ray* o
     }
 }
 
+static void trace_launched(const orc_scene* sc, const orc_constants* c, const orc_state* s, orc_ray* out) {
+    if (sc->method == ORC_METHOD_DP5) trace_dp5(sc, *c, *s, out);
+    else trace_rk4(sc, *c, *s, out);
+}
+
 void orc_trace_ray(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
-    if (sc->method == ORC_METHOD_DP5) trace_dp5(sc, alpha, beta, out);
-    else trace_rk4(sc, alpha, beta, out);
+    ray_init(out);
+    orc_constants c;
+    orc_state s;
+    orc_pinhole_launch(sc, alpha, beta, &c, &s);
+    trace_launched(sc, &c, &s, out);
+}
+
+/* A camera with an arbitrary frame (moving, or inside the horizon), as trajectory::traceRay takes it
+ * (src/trajectory.cpp:214-247): photonFromFrame at the scene's camera position; inside the horizon a
+ * photon with 2 r_+ E - a L < 0 crossed into the hole from the far side of the eternal spacetime and
+ * ends on the horizon at once (src/trajectory.cpp:236-244); otherwise it is traced backward (it rises
+ * through the horizon first). */
+void orc_trace_framed(const orc_scene* sc, const orc_frame* f, const double look[3], orc_ray* out) {
+    ray_init(out);
+    orc_constants c;
+    orc_state s;
+    orc_photon_from_frame(sc->a, sc->r_obs, sc->theta_obs, sc->phi_obs, f, look, &c, &s);
+    const double rh = orc_horizon_radius(sc->a);
+    if (sc->r_obs < rh && 2.0 * rh * c.E - sc->a * c.L < 0.0) {
+        out->E = c.E, out->L = c.L, out->Q = c.Q;
+        out->outcome = ORC_CAPTURED;
+        return;
+    }
+    trace_launched(sc, &c, &s, out);
 }
 
 /* -------------------------------------------------- thread-pool drivers ---- */

@@ -93,6 +93,11 @@ void orc_trace_rays(const orc_scene* sc, int64_t n, const double* a, const doubl
                     int32_t* outcome, double* r_disk, double* phi_disk, double* g, double* theta_inf,
                     double* phi_inf, int32_t* steps);
 
+/* A camera at (sc->r_obs, sc->theta_obs, sc->phi_obs) with any frame (moving; inside the horizon
+ * too) and a look direction on its (r, theta, phi) axes: trajectory::traceRay's launch and its
+ * inside-horizon rule (src/trajectory.cpp:214-247), then the scene's tracer. */
+void orc_trace_framed(const orc_scene* sc, const orc_frame* f, const double look[3], orc_ray* out);
+
 /* Capture test used by the DP5 tracer near the horizon: 1 if R(r') > 0 on [r_+(1+eps), r]. */
 int orc_no_radial_root_below(double a, double E, double L, double Q, double r, double eps);
 

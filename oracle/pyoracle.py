@@ -114,10 +114,13 @@ class Oracle:
             f("no_radial_root_below", C.c_int, [C.c_double] * 6)
             f("pinhole_launch", None, [C.POINTER(Scene), C.c_double, C.c_double, C.POINTER(Constants),
                                        C.POINTER(State)])
+            f("trace_framed", None, [C.POINTER(Scene), C.POINTER(Frame), _dp, C.POINTER(Ray)])
         else:
             f("eht_captured", C.c_int, [C.c_double] * 4)
             f("bending_angle", C.c_double, [C.c_double, C.c_double])
             f("trajectory_trace", C.c_int, [C.c_double] * 4 + [_dp, C.c_int] + [C.c_double] * 3 + [_dp])
+            f("trajectory_trace_framed", C.c_int, [C.c_double] * 4 + [_dp, _dp, C.c_int] + [C.c_double] * 3 + [_dp])
+            f("trace_framed", None, [C.POINTER(Scene), _dp, _dp, C.POINTER(Ray)])
         del L
 
     def _f(self, name, res, args):
@@ -185,6 +188,23 @@ class Oracle:
         al = np.ascontiguousarray(al, dtype=np.float64)
         be = np.ascontiguousarray(be, dtype=np.float64)
         return self.critical_radius_raw(_ptr(al), _ptr(be), len(al), psi)
+
+    def trace_framed(self, sc: Scene, frame, look) -> "Ray":
+        """A camera at the scene's (r_obs, theta_obs, phi_obs) with an arbitrary frame (4 x 4 array
+        e[k][i] or a Frame)."""
+        r = Ray()
+        lk = np.ascontiguousarray(look, dtype=np.float64)
+        if self.reference:
+            fr = np.ascontiguousarray(np.asarray(frame if not isinstance(frame, Frame) else
+                                                 np.ctypeslib.as_array(frame.e), dtype=np.float64).reshape(16))
+            self.trace_framed_raw(C.byref(sc), _ptr(fr), _ptr(lk), C.byref(r))
+        else:
+            if not isinstance(frame, Frame):
+                f = Frame()
+                np.ctypeslib.as_array(f.e)[:] = np.asarray(frame, dtype=np.float64).reshape(4, 4)
+                frame = f
+            self.trace_framed_raw(C.byref(sc), C.byref(frame), _ptr(lk), C.byref(r))
+        return r
 
     def trace_ray(self, sc: Scene, alpha, beta) -> Ray:
         r = Ray()

@@ -55,12 +55,13 @@ void sky(double a, const kerr::Constants& c, const kerr::State& x, double* th, d
     *ph = std::atan2(-v[1] / n, -v[0] / n);
 }
 
-void trace_one(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
+void ray_clear(orc_ray* out) {
     std::memset(out, 0, sizeof(*out));
     out->r_disk = out->phi_disk = out->g = out->theta_inf = out->phi_inf = NAN;
-    kerr::Constants c;
-    kerr::State s;
-    pinhole(sc, alpha, beta, c, s);
+}
+
+// The reference loop shape from a launched photon.
+void trace_launched(const orc_scene* sc, kerr::Constants c, kerr::State s, orc_ray* out) {
     out->E = c.E, out->L = c.L, out->Q = c.Q;
     const double a = sc->a;
     const double rcap = kerr::horizonRadius(a) * (1.0 + sc->capture_eps);
@@ -111,6 +112,14 @@ void trace_one(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
             return;
         }
     }
+}
+
+void trace_one(const orc_scene* sc, double alpha, double beta, orc_ray* out) {
+    ray_clear(out);
+    kerr::Constants c;
+    kerr::State s;
+    pinhole(sc, alpha, beta, c, s);
+    trace_launched(sc, c, s, out);
 }
 
 }  // namespace
@@ -212,7 +221,45 @@ int ref_trajectory_trace(double a, double r, double th, double ph, const double 
     return static_cast<int>(rep.end);
 }
 
+// trajectory::traceRay with an arbitrary camera frame (16 doubles, e[k][i]): moving cameras and
+// cameras inside the horizon. out[] as ref_trajectory_trace.
+int ref_trajectory_trace_framed(double a, double r, double th, double ph, const double* frame16,
+                                const double look[3], int disk, double r_in, double r_out, double escape,
+                                double out[8]) {
+    trajectory::RayScene scene;
+    scene.disk = disk != 0;
+    scene.diskInner = r_in;
+    scene.diskOuter = r_out;
+    scene.escapeRadius = escape;
+    kerr::Frame f;
+    for (int k = 0; k < 4; ++k)
+        for (int i = 0; i < 4; ++i) f.e[k][i] = frame16[4 * k + i];
+    const trajectory::RayReport rep = trajectory::traceRay(a, r, th, ph, f, look, scene);
+    out[0] = rep.rEnd, out[1] = rep.g, out[2] = rep.skyDirection[0], out[3] = rep.skyDirection[1];
+    out[4] = rep.skyDirection[2], out[5] = rep.rMin, out[6] = rep.turns, out[7] = rep.energy;
+    return static_cast<int>(rep.end);
+}
+
 void ref_trace_ray(const orc_scene* sc, double alpha, double beta, orc_ray* out) { trace_one(sc, alpha, beta, out); }
+
+// The same loop for a camera with any frame (16 doubles e[k][i]) at the scene's position, with
+// trajectory::traceRay's inside-horizon rule (src/trajectory.cpp:236-244).
+void ref_trace_framed(const orc_scene* sc, const double* frame16, const double look[3], orc_ray* out) {
+    ray_clear(out);
+    kerr::Frame f;
+    for (int k = 0; k < 4; ++k)
+        for (int i = 0; i < 4; ++i) f.e[k][i] = frame16[4 * k + i];
+    kerr::Constants c;
+    kerr::State s;
+    kerr::photonFromFrame(sc->a, sc->r_obs, sc->theta_obs, sc->phi_obs, f, look, c, s);
+    const double rh = kerr::horizonRadius(sc->a);
+    if (sc->r_obs < rh && 2.0 * rh * c.E - sc->a * c.L < 0.0) {
+        out->E = c.E, out->L = c.L, out->Q = c.Q;
+        out->outcome = ORC_CAPTURED;
+        return;
+    }
+    trace_launched(sc, c, s, out);
+}
 
 // Whole frame on nthreads std::threads with an atomic row counter (src/eht.cpp:321-347).
 void ref_trace_frame(const orc_scene* sc, int w, int h, double alo, double ahi, double blo, double bhi, int nthreads,

@@ -15,9 +15,15 @@ Fixtures (all produced by the reference's own functions, never by this project's
                       ISCO..20, escape 1000, capture r_+(1+1e-6): the reference RK4 loop at tolerance 1e-4
   c2_rk4_1e-4.npz     96x54 frame with the 1080p geometry (a=0.998, r_obs=1000, theta=60 deg,
                       alpha in +-20, beta in +-11.25, disk ISCO..30) at tolerance 1e-4
+  framed_ref.npz      cameras with arbitrary frames -- ZAMO, boosted from the ZAMO (Camera::frame's
+                      drift recipe, src/camera.cpp:23-36) and free-falling inside the horizon
+                      (kerr::fourVelocity) -- frames from kerr::observerFrame, 40 look directions each:
+                      trajectory::traceRay's end/rEnd/g (src/trajectory.cpp:214-396) and the reference
+                      loop at tolerance 1e-4 from kerr::photonFromFrame with traceRay's inside-horizon rule
 """
 from __future__ import annotations
 
+import ctypes as C
 import os
 import sys
 import time
@@ -117,6 +123,82 @@ def trajectory_fixture(R: po.Oracle) -> dict:
     return dict(a=a, r=r, theta=th, look=look, r_in=r_in, end=end, values=vals)
 
 
+FRAMED_CAMERAS = (
+    # (a, r, theta, phi, kind, parameters)
+    (0.9, 50.0, np.deg2rad(80.0), 0.0, "zamo", ()),
+    (0.9, 20.0, np.deg2rad(60.0), 0.3, "boost", (0.0, 0.0, 0.5)),
+    (0.9, 15.0, np.deg2rad(100.0), 1.0, "boost", (-0.6, 0.1, 0.0)),
+    (0.998, 8.0, np.deg2rad(45.0), 0.0, "boost", (0.2, -0.3, 0.4)),
+    (0.9, 1.3, np.deg2rad(70.0), 0.0, "fall", (1.0, 0.0, 0.0)),      # inside r_+ = 1.436: E, L, extra Q
+    (0.5, 1.6, np.deg2rad(30.0), 2.0, "fall", (1.0, 0.5, 0.1)),      # inside r_+ = 1.866
+)
+
+
+def framed_camera(R: po.Oracle, a, r, th, kind, par):
+    """The camera frame (4 x 4) the reference builds for one of FRAMED_CAMERAS."""
+    u = np.zeros(4)
+    R.zamo_four_velocity_raw(a, r, th, po._ptr(u))
+    if kind == "boost":
+        z = po.Frame()
+        R.observer_frame_raw(a, r, th, po._ptr(u), C.byref(z))
+        e = np.ctypeslib.as_array(z.e)
+        v = np.array(par)
+        gamma = 1.0 / np.sqrt(1.0 - v @ v)
+        u = gamma * (e[0] + v[0] * e[1] + v[1] * e[2] + v[2] * e[3])
+    elif kind == "fall":  # a massive geodesic observer (mu = 1), falling inward
+        E, L, dq = par
+        c = po.Constants(E, L, 0.0, 1.0)
+        st, ct = np.sin(th), np.cos(th)
+        c.Q = ct * ct * (a * a * (1.0 - E * E) + L * L / (st * st)) + dq
+        Rr = R.radial_potential_raw(a, C.byref(c), r)
+        Th = R.polar_potential_raw(a, C.byref(c), th)
+        s = po.State(0.0, r, th, 0.0, -np.sqrt(max(Rr, 0.0)), np.sqrt(max(Th, 0.0)))
+        d = po.Derivs()
+        R.derivatives_raw(a, C.byref(c), C.byref(s), C.byref(d))
+        sigma = r * r + a * a * ct * ct
+        u = np.array([d.dt, d.dr, d.dtheta, d.dphi]) / sigma
+    f = po.Frame()
+    R.observer_frame_raw(a, r, th, po._ptr(np.ascontiguousarray(u)), C.byref(f))
+    return np.ctypeslib.as_array(f.e).copy()
+
+
+def fibonacci_looks(n):
+    k = np.arange(n) + 0.5
+    z = 1.0 - 2.0 * k / n
+    ph = np.pi * (1.0 + 5.0 ** 0.5) * k
+    rr = np.sqrt(1.0 - z * z)
+    return np.stack([z, rr * np.cos(ph), rr * np.sin(ph)], 1)  # (l_r, l_theta, l_phi)
+
+
+def framed_fixture(R: po.Oracle) -> dict:
+    looks = fibonacci_looks(40)
+    cams, frames = [], []
+    tr_end, tr_val = [], []
+    keys = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf", "steps")
+    rk = {k: [] for k in keys}
+    for a, r, th, ph, kind, par in FRAMED_CAMERAS:
+        f = framed_camera(R, a, r, th, kind, par)
+        r_in = R.isco_radius_raw(a, 1)
+        frames.append(f)
+        cams.append([a, r, th, ph, r_in])
+        sc = po.Scene(a, r, th, ph, r_in, 20.0, 1000.0, 1e-6, 1e-4, 5_000_000, po.RK4)
+        for lk in looks:
+            out = np.zeros(8)
+            tr_end.append(R.trajectory_trace_framed_raw(a, r, th, ph, po._ptr(np.ascontiguousarray(f.reshape(16))),
+                                                        po._ptr(np.ascontiguousarray(lk)), 1, r_in, 20.0, 250.0,
+                                                        po._ptr(out)))
+            tr_val.append(out)
+            ray = R.trace_framed(sc, f, lk)
+            for k in keys:
+                rk[k].append(getattr(ray, k))
+    out = dict(cameras=np.array(cams), frames=np.array(frames), looks=looks, tr_end=np.array(tr_end, np.int32),
+               tr_values=np.array(tr_val))
+    out.update({k: np.array(v) for k, v in rk.items()})
+    print("  framed outcomes", np.bincount(out["outcome"].astype(int), minlength=4), "traceRay ends",
+          np.bincount(out["tr_end"], minlength=5))
+    return out
+
+
 def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
     t = time.time()
     out = R.trace_frame(sc, w, h, *ext)
@@ -135,6 +217,10 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "steps_ref.npz"), **steps_fixture(R))
     print("trajectory_ref.npz")
     np.savez_compressed(os.path.join(HERE, "trajectory_ref.npz"), **trajectory_fixture(R))
+    print("framed_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "framed_ref.npz"), **framed_fixture(R))
+    if os.environ.get("FRAMED_ONLY"):
+        return
     print("c1_rk4_1e-4.npz")
     sc1 = po.scene(a=0.9, r_obs=50.0, theta_obs_deg=80.0, r_disk_out=20.0, tol=1e-4, method=po.RK4,
                    max_steps=5_000_000)

@@ -183,3 +183,46 @@ def test_restatement_bit_exact_against_reference_library(oracle):
     o2 = R.trace_frame(sc, 24, 24, -15, 15, -15, 15)
     for k in o1:
         np.testing.assert_array_equal(o1[k], o2[k])
+
+
+def test_framed_launch_reproduces_reference_loop(oracle, golden):
+    """Cameras with arbitrary frames (ZAMO, boosted, free-falling inside the horizon): the oracle's
+    photonFromFrame launch, inside-horizon rule and RK4 loop at tolerance 1e-4 give the reference's
+    numbers bit for bit."""
+    g = golden("framed_ref.npz")
+    looks = g["looks"]
+    i = 0
+    for cam, fr in zip(g["cameras"], g["frames"]):
+        a, r, th, ph, r_in = cam
+        sc = po.Scene(a, r, th, ph, r_in, 20.0, 1000.0, 1e-6, 1e-4, 5_000_000, po.RK4)
+        for lk in looks:
+            ray = oracle.trace_framed(sc, fr, lk)
+            assert ray.outcome == g["outcome"][i], (i, ray.outcome, g["outcome"][i])
+            for k in ("r_disk", "phi_disk", "g", "theta_inf", "phi_inf"):
+                want = g[k][i]
+                got = getattr(ray, k)
+                assert (np.isnan(want) and np.isnan(got)) or got == want, (i, k, got, want)
+            i += 1
+
+
+def test_framed_rk4_reproduces_reference_traceRay(oracle, golden):
+    """With traceRay's own settings the oracle ends every framed ray as src/trajectory.cpp:214-396
+    does -- including cameras inside the horizon (its dead-zone rule and the rise through r_+)."""
+    g = golden("framed_ref.npz")
+    end_map = {1: po.CAPTURED, 2: po.DISK, 0: po.ESCAPED}
+    i = 0
+    inside = 0
+    for cam, fr in zip(g["cameras"], g["frames"]):
+        a, r, th, ph, r_in = cam
+        rp = oracle.horizon_radius_raw(a)
+        inside += r < rp
+        sc = po.Scene(a, r, th, ph, r_in, 20.0, 250.0, 0.01 / rp, 0.01, 200000, po.RK4)
+        for lk in g["looks"]:
+            ray = oracle.trace_framed(sc, fr, lk)
+            want = end_map[int(g["tr_end"][i])]
+            assert ray.outcome == want, (i, ray.outcome, want)
+            if want == po.DISK:
+                assert abs(ray.r_disk - g["tr_values"][i][0]) < 1e-9 * max(1.0, g["tr_values"][i][0])
+                assert abs(ray.g - g["tr_values"][i][1]) < 1e-9
+            i += 1
+    assert inside == 2
