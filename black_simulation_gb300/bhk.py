@@ -62,6 +62,15 @@ class StatsC(C.Structure):
                 ("kernel_ms", C.c_double)]
 
 
+class EhtViewC(C.Structure):
+    _fields_ = [("a", C.c_double), ("inclination", C.c_double), ("half_width", C.c_double), ("size", C.c_int32),
+                ("pad", C.c_int32), ("frequency", C.c_double), ("mass_solar", C.c_double)]
+
+
+class EhtFlowC(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("n0", "T0", "beta", "keplerian", "height", "sin_theta_b")]
+
+
 class RenderOptsC(C.Structure):
     _fields_ = [("p_min", C.c_double), ("band", C.c_double), ("fallback", C.c_int32), ("cluster", C.c_int32)]
 
@@ -179,6 +188,9 @@ def lib() -> C.CDLL:
                                        C.POINTER(RaysOutC), vp]),
         "bhk_trace_rays_framed": (C.c_int, [vp, i64, vp, vp, vp, vp, vp, vp, d, d, C.POINTER(TraceOptsC),
                                             C.POINTER(RaysOutC), vp]),
+        "bhk_eht_render": (C.c_int, [C.POINTER(EhtViewC), C.POINTER(EhtFlowC), C.c_int32, vp, vp, vp, vp]),
+        "bhk_eht_flux": (d, [vp, C.c_int32, d, d]),
+        "bhk_eht_calibrate": (C.c_int, [C.POINTER(EhtViewC), C.POINTER(EhtFlowC), d, d, C.POINTER(d)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -479,6 +491,50 @@ class Context:
         s = StatsC()
         check(lib().bhk_autotune(self.h, arr, nf, C.byref(oc), C.byref(s)))
         return {k: getattr(s, k) for k, _ in StatsC._fields_}
+
+
+# ------------------------------------------------------------------------------ eht::render ----
+
+EHT_FLOW_DEFAULTS = dict(n0=1e5, T0=4e11, beta=10.0, keplerian=0.9, height=1.0, sin_theta_b=0.8165)
+
+
+def eht_view(a=0.9, inclination=0.3, half_width=16.0, size=128, frequency=230e9, mass_solar=6.5e9) -> EhtViewC:
+    """eht::View (defaults as the reference's, src/eht.h)."""
+    return EhtViewC(a, inclination, half_width, size, 0, frequency, mass_solar)
+
+
+def eht_flow(**kw) -> EhtFlowC:
+    """eht::Flow (defaults as the reference's, src/eht.h)."""
+    v = dict(EHT_FLOW_DEFAULTS)
+    v.update(kw)
+    return EhtFlowC(*[v[k] for k in ("n0", "T0", "beta", "keplerian", "height", "sin_theta_b")])
+
+
+def eht_render(view: EhtViewC, flow: EhtFlowC, with_light: bool = True, device="cuda", stream=None):
+    """eht::render on the GPU: (intensity float64 (size, size), shadow uint8 (size, size), steps int32)
+    CUDA tensors, row-major from beta = +half_width."""
+    import torch
+    n = view.size * view.size
+    inten = torch.empty(n, dtype=torch.float64, device=device)
+    shadow = torch.empty(n, dtype=torch.uint8, device=device)
+    steps = torch.empty(n, dtype=torch.int32, device=device)
+    check(lib().bhk_eht_render(C.byref(view), C.byref(flow), 1 if with_light else 0, _ptr(inten), _ptr(shadow),
+                               _ptr(steps), _stream(stream)))
+    sh = (view.size, view.size)
+    return inten.view(sh), shadow.view(sh), steps.view(sh)
+
+
+def eht_flux(intensity, half_width: float, theta_g_uas: float) -> float:
+    """eht::flux (Jy) of an intensity image (host array or tensor)."""
+    arr = np.ascontiguousarray(intensity.cpu().numpy() if hasattr(intensity, "cpu") else intensity, dtype=np.float64)
+    return float(lib().bhk_eht_flux(arr.ctypes.data, arr.shape[0], half_width, theta_g_uas))
+
+
+def eht_calibrate(view: EhtViewC, flow: EhtFlowC, target_jy: float, theta_g_uas: float) -> float:
+    """eht::calibrate: the density n0 that gives target_jy."""
+    n0 = C.c_double(0.0)
+    check(lib().bhk_eht_calibrate(C.byref(view), C.byref(flow), target_jy, theta_g_uas, C.byref(n0)))
+    return n0.value
 
 
 # ------------------------------------------------------------------------ standard workloads ----

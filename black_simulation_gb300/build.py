@@ -3,8 +3,9 @@
     python -m black_simulation_gb300.build            # or build() from Python
 
 Translation units are compiled in parallel into _build/ and linked into
-black_simulation_gb300/libbhk.so. bhk_steps.cu (the per-step mirrors) is compiled with
---fmad=false so its FP64 results track the reference's C++ to rounding.
+black_simulation_gb300/libbhk.so. bhk_steps.cu (the per-step mirrors) and bhk_eht.cu (the EHT
+image, a sum over the integrator's steps) are compiled with --fmad=false so their FP64 results
+track the reference's C++ to rounding.
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ UNITS = {
     "bhk_diag.cu": [],
     "bhk_static.cu": [],
     "bhk_surrogate.cu": [],
+    "bhk_eht.cu": ["--fmad=false"],
 }
 EXTRA_UNITS: dict[str, list[str]] = {}
 

@@ -204,6 +204,30 @@ bhk_status bhk_critical_curve(double a, double r_obs, double theta_obs, int32_t 
 bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int32_t nframes, const bhk_trace_opts* opts,
                                    const bhk_rays_out* out, void* stream);
 
+/* ---- eht::render (src/eht.h:100-160): the shadow and the synchrotron image of a hot flow ---- */
+typedef struct bhk_eht_view {      /* eht::View */
+    double a, inclination;         /* spin; inclination (rad) */
+    double half_width;             /* the field's half-width (M) */
+    int32_t size, pad;             /* pixels across */
+    double frequency;              /* Hz */
+    double mass_solar;             /* sets the plasma's path lengths */
+} bhk_eht_view;
+typedef struct bhk_eht_flow {      /* eht::Flow */
+    double n0, T0, beta, keplerian, height, sin_theta_b;
+} bhk_eht_flow;
+/* eht::render: size x size pixels, row-major from beta = +half_width; intensity I_nu (device,
+ * double) and shadow (device, 1 where the ray fell in), either may be NULL; steps (device, int32,
+ * may be NULL): integration steps per ray. with_light = 0 only follows the rays (the shadow).
+ * Asynchronous on `stream` (NULL: the legacy default stream). The image is a sum over eht::traceRay's
+ * own steps (src/eht.cpp:260-319), restated in FP64. */
+bhk_status bhk_eht_render(const bhk_eht_view* view, const bhk_eht_flow* flow, int32_t with_light, double* intensity,
+                          uint8_t* shadow, int32_t* steps, void* stream);
+/* eht::flux of a host intensity image: Jy for a source whose M subtends theta_g_uas. */
+double bhk_eht_flux(const double* intensity, int32_t size, double half_width, double theta_g_uas);
+/* eht::calibrate: the density n0 giving target_jy (secant in log n0 on 48-pixel GPU renders). */
+bhk_status bhk_eht_calibrate(const bhk_eht_view* view, const bhk_eht_flow* flow, double target_jy,
+                             double theta_g_uas, double* n0);
+
 /* FLOPs one accepted FP32 Dormand-Prince step costs in the mixed tracer, counted from its source. */
 double bhk_flops_per_step(void);
 

@@ -240,6 +240,44 @@ int ref_trajectory_trace_framed(double a, double r, double th, double ph, const 
     return static_cast<int>(rep.end);
 }
 
+// eht::render (src/eht.cpp:321-347) of View{a, inclination, halfWidth, size, frequency, massSolar}
+// and Flow{n0, T0, beta, keplerian, height, sinThetaB}: intensity and shadow, row-major.
+void ref_eht_render(double a, double inclination, double half_width, int size, double frequency, double mass_solar,
+                    const double* flow6, int threads, double* intensity, unsigned char* shadow) {
+    eht::View v;
+    v.a = a, v.inclination = inclination, v.halfWidth = half_width, v.size = size, v.frequency = frequency;
+    v.massSolar = mass_solar;
+    eht::Flow f;
+    f.n0 = flow6[0], f.T0 = flow6[1], f.beta = flow6[2], f.keplerian = flow6[3], f.height = flow6[4];
+    f.sinThetaB = flow6[5];
+    const eht::Image img = eht::render(v, f, threads);
+    for (size_t k = 0; k < img.intensity.size(); ++k) {
+        intensity[k] = img.intensity[k];
+        shadow[k] = img.shadow[k];
+    }
+}
+
+double ref_eht_calibrate(double a, double inclination, double half_width, int size, double frequency, double mass_solar,
+                         const double* flow6, double target_jy, double theta_g_uas, int threads) {
+    eht::View v;
+    v.a = a, v.inclination = inclination, v.halfWidth = half_width, v.size = size, v.frequency = frequency;
+    v.massSolar = mass_solar;
+    eht::Flow f;
+    f.n0 = flow6[0], f.T0 = flow6[1], f.beta = flow6[2], f.keplerian = flow6[3], f.height = flow6[4];
+    f.sinThetaB = flow6[5];
+    return eht::calibrate(v, f, target_jy, theta_g_uas, threads);
+}
+
+double ref_eht_angular_scale(double mass_solar, double distance_pc) { return eht::angularScale(mass_solar, distance_pc); }
+
+double ref_eht_flux(const double* intensity, int size, double half_width, double theta_g_uas) {
+    eht::Image img;
+    img.size = size;
+    img.halfWidth = half_width;
+    img.intensity.assign(intensity, intensity + static_cast<size_t>(size) * size);
+    return eht::flux(img, theta_g_uas);
+}
+
 void ref_trace_ray(const orc_scene* sc, double alpha, double beta, orc_ray* out) { trace_one(sc, alpha, beta, out); }
 
 // The same loop for a camera with any frame (16 doubles e[k][i]) at the scene's position, with

@@ -20,6 +20,9 @@ Fixtures (all produced by the reference's own functions, never by this project's
                       (kerr::fourVelocity) -- frames from kerr::observerFrame, 40 look directions each:
                       trajectory::traceRay's end/rEnd/g (src/trajectory.cpp:214-396) and the reference
                       loop at tolerance 1e-4 from kerr::photonFromFrame with traceRay's inside-horizon rule
+  eht_ref.npz         eht::render images (src/eht.cpp:260-347): the M87* view of the reference's
+                      calibration test (a = 0.9 at 60 deg, 48 px, density from eht::calibrate at 0.5 Jy),
+                      a = 0.5 at 163 deg (32 px) and a = 0.99 at 30 deg (40 px), default flow
 """
 from __future__ import annotations
 
@@ -199,6 +202,53 @@ def framed_fixture(R: po.Oracle) -> dict:
     return out
 
 
+EHT_VIEWS = (  # (a, inclination deg, half width, size), frequency 230 GHz, M87* mass
+    (0.9, 60.0, 16.0, 48),
+    (0.5, 163.0, 16.0, 32),
+    (0.99, 30.0, 16.0, 40),
+)
+EHT_FLOW = (1e5, 4e11, 10.0, 0.9, 1.0, 0.8165)  # eht::Flow defaults (src/eht.h)
+M87_MASS, M87_DISTANCE_PC, M87_FLUX_JY = 6.5e9, 16.8e6, 0.5
+
+
+def eht_fixture(R: po.Oracle) -> dict:
+    lib = R.lib
+    dp = C.POINTER(C.c_double)
+    lib.ref_eht_render.argtypes = [C.c_double] * 3 + [C.c_int] + [C.c_double] * 2 + [dp, C.c_int, dp,
+                                                                                        C.POINTER(C.c_ubyte)]
+    lib.ref_eht_render.restype = None
+    lib.ref_eht_calibrate.argtypes = [C.c_double] * 3 + [C.c_int] + [C.c_double] * 2 + [dp] + [C.c_double] * 2 + [C.c_int]
+    lib.ref_eht_calibrate.restype = C.c_double
+    lib.ref_eht_angular_scale.argtypes = [C.c_double, C.c_double]
+    lib.ref_eht_angular_scale.restype = C.c_double
+    lib.ref_eht_flux.argtypes = [dp, C.c_int, C.c_double, C.c_double]
+    lib.ref_eht_flux.restype = C.c_double
+    threads = os.cpu_count() or 1
+    theta_g = lib.ref_eht_angular_scale(M87_MASS, M87_DISTANCE_PC)
+    flow = np.array(EHT_FLOW)
+    t = time.time()
+    n0 = lib.ref_eht_calibrate(0.9, np.deg2rad(60.0), 16.0, 40, 230e9, M87_MASS, po._ptr(flow), M87_FLUX_JY, theta_g,
+                               threads)
+    print(f"  calibrated n0 = {n0:.6g} in {time.time() - t:.1f} s")
+    out = dict(views=np.array(EHT_VIEWS), flow=flow, n0_calibrated=n0, theta_g=theta_g, mass=M87_MASS,
+               target_jy=M87_FLUX_JY)
+    for i, (a, inc, hw, size) in enumerate(EHT_VIEWS):
+        fl = flow.copy()
+        if i == 0:
+            fl[0] = n0
+        inten = np.zeros(size * size)
+        shadow = np.zeros(size * size, np.uint8)
+        t = time.time()
+        lib.ref_eht_render(a, np.deg2rad(inc), hw, size, 230e9, M87_MASS, po._ptr(fl), threads, po._ptr(inten),
+                           shadow.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        out[f"intensity_{i}"] = inten
+        out[f"shadow_{i}"] = shadow
+        out[f"flux_{i}"] = lib.ref_eht_flux(po._ptr(inten), size, hw, theta_g)
+        print(f"  view {i}: {size}x{size} in {time.time() - t:.1f} s, flux {out[f'flux_{i}']:.4g} Jy, "
+              f"shadow px {shadow.sum()}")
+    return out
+
+
 def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
     t = time.time()
     out = R.trace_frame(sc, w, h, *ext)
@@ -219,6 +269,8 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "trajectory_ref.npz"), **trajectory_fixture(R))
     print("framed_ref.npz")
     np.savez_compressed(os.path.join(HERE, "framed_ref.npz"), **framed_fixture(R))
+    print("eht_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "eht_ref.npz"), **eht_fixture(R))
     if os.environ.get("FRAMED_ONLY"):
         return
     print("c1_rk4_1e-4.npz")
