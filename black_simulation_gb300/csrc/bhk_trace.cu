@@ -475,31 +475,78 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     constexpr bool F64 = sizeof(T) == 8;
     const T h = s.h;
     T t[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a21) * s.k[0][i]);
-    rhs(s.c, t, s.k[1]);
-#pragma unroll
-    for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a31) * s.k[0][i] + T(DP::a32) * s.k[1][i]);
-    rhs(s.c, t, s.k[2]);
-#pragma unroll
-    for (int i = 0; i < 5; ++i)
-        t[i] = s.y[i] + h * (T(DP::a41) * s.k[0][i] + T(DP::a42) * s.k[1][i] + T(DP::a43) * s.k[2][i]);
-    rhs(s.c, t, s.k[3]);
-#pragma unroll
-    for (int i = 0; i < 5; ++i)
-        t[i] = s.y[i] + h * (T(DP::a51) * s.k[0][i] + T(DP::a52) * s.k[1][i] + T(DP::a53) * s.k[2][i] +
-                             T(DP::a54) * s.k[3][i]);
-    rhs(s.c, t, s.k[4]);
-#pragma unroll
-    for (int i = 0; i < 5; ++i)
-        t[i] = s.y[i] + h * (T(DP::a61) * s.k[0][i] + T(DP::a62) * s.k[1][i] + T(DP::a63) * s.k[2][i] +
-                             T(DP::a64) * s.k[3][i] + T(DP::a65) * s.k[4][i]);
-    rhs(s.c, t, s.k[5]);
     T y5[5];
+    if constexpr (F64) {  // the oracle's operation order
 #pragma unroll
-    for (int i = 0; i < 5; ++i)
-        y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
-                              T(DP::b5) * s.k[4][i] + T(DP::b6) * s.k[5][i]);
+        for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a21) * s.k[0][i]);
+        rhs(s.c, t, s.k[1]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a31) * s.k[0][i] + T(DP::a32) * s.k[1][i]);
+        rhs(s.c, t, s.k[2]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            t[i] = s.y[i] + h * (T(DP::a41) * s.k[0][i] + T(DP::a42) * s.k[1][i] + T(DP::a43) * s.k[2][i]);
+        rhs(s.c, t, s.k[3]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            t[i] = s.y[i] + h * (T(DP::a51) * s.k[0][i] + T(DP::a52) * s.k[1][i] + T(DP::a53) * s.k[2][i] +
+                                 T(DP::a54) * s.k[3][i]);
+        rhs(s.c, t, s.k[4]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            t[i] = s.y[i] + h * (T(DP::a61) * s.k[0][i] + T(DP::a62) * s.k[1][i] + T(DP::a63) * s.k[2][i] +
+                                 T(DP::a64) * s.k[3][i] + T(DP::a65) * s.k[4][i]);
+        rhs(s.c, t, s.k[5]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
+                                  T(DP::b5) * s.k[4][i] + T(DP::b6) * s.k[5][i]);
+    } else {
+        // FP32: each stage's tableau row scaled by h once (shared by the 5 components, computed
+        // where it is used so that it is not held across stages), so that every stage sum is a pure
+        // chain of fused multiply-adds starting from y.
+        {
+            const T b1 = h * T(DP::a21);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = fmaf(b1, s.k[0][i], s.y[i]);
+        }
+        rhs(s.c, t, s.k[1]);
+        {
+            const T b1 = h * T(DP::a31), b2 = h * T(DP::a32);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i]));
+        }
+        rhs(s.c, t, s.k[2]);
+        {
+            const T b1 = h * T(DP::a41), b2 = h * T(DP::a42), b3 = h * T(DP::a43);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i])));
+        }
+        rhs(s.c, t, s.k[3]);
+        {
+            const T b1 = h * T(DP::a51), b2 = h * T(DP::a52), b3 = h * T(DP::a53), b4 = h * T(DP::a54);
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                t[i] = fmaf(b4, s.k[3][i], fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i]))));
+        }
+        rhs(s.c, t, s.k[4]);
+        {
+            const T b1 = h * T(DP::a61), b2 = h * T(DP::a62), b3 = h * T(DP::a63), b4 = h * T(DP::a64),
+                    b5 = h * T(DP::a65);
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                t[i] = fmaf(b5, s.k[4][i],
+                            fmaf(b4, s.k[3][i], fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i])))));
+        }
+        rhs(s.c, t, s.k[5]);
+        {
+            const T c1 = h * T(DP::b1), c3 = h * T(DP::b3), c4 = h * T(DP::b4), c5 = h * T(DP::b5), c6 = h * T(DP::b6);
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                y5[i] = fmaf(c6, s.k[5][i],
+                             fmaf(c5, s.k[4][i], fmaf(c4, s.k[3][i], fmaf(c3, s.k[2][i], fmaf(c1, s.k[0][i], s.y[i])))));
+        }
+    }
     Proj<T> pj;
     rhs<T, !F64>(s.c, y5, s.k[6], &pj);
     T rtol;
@@ -508,8 +555,16 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     T acc = T(0);
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        const T e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] +
-                         T(DP::e5) * s.k[4][i] + T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
+        T e;
+        if constexpr (F64) {
+            e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] + T(DP::e5) * s.k[4][i] +
+                     T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
+        } else {
+            e = h * fmaf(T(DP::e7), s.k[6][i],
+                         fmaf(T(DP::e6), s.k[5][i],
+                              fmaf(T(DP::e5), s.k[4][i],
+                                   fmaf(T(DP::e4), s.k[3][i], fmaf(T(DP::e3), s.k[2][i], T(DP::e1) * s.k[0][i])))));
+        }
         const T sc = rtol + rtol * fmax(fabs(s.y[i]), fabs(y5[i]));
         const T q = Math<T>::div(e, sc);
         acc += q * q;
