@@ -52,7 +52,8 @@ class TraceOptsC(C.Structure):
 class RaysOutC(C.Structure):
     _fields_ = [("outcome", C.c_void_p), ("r_disk", C.c_void_p), ("phi_disk", C.c_void_p), ("g", C.c_void_p),
                 ("theta_inf", C.c_void_p), ("phi_inf", C.c_void_p), ("steps", C.c_void_p),
-                ("rejected", C.c_void_p)]
+                ("rejected", C.c_void_p), ("energy", C.c_void_p), ("g_camera", C.c_void_p), ("b", C.c_void_p),
+                ("q", C.c_void_p), ("r_min", C.c_void_p), ("delay", C.c_void_p), ("turns", C.c_void_p)]
 
 
 class StatsC(C.Structure):
@@ -362,19 +363,23 @@ def fp32_fma_peak_tflops(device: int = 0) -> float:
 # ----------------------------------------------------------------------------- batch tracer ----
 
 FIELDS = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf", "steps", "rejected")
+# The rest of trajectory::RayReport, allocated on request (56 more bytes per ray).
+EXTRA_FIELDS = ("energy", "g_camera", "b", "q", "r_min", "delay", "turns")
 
 
-def alloc_outputs(n: int, device="cuda"):
+def alloc_outputs(n: int, device="cuda", extras: bool = False):
     import torch
     out = {k: torch.empty(n, dtype=torch.float64, device=device) for k in FIELDS[1:6]}
     out["outcome"] = torch.empty(n, dtype=torch.uint8, device=device)
     out["steps"] = torch.empty(n, dtype=torch.int32, device=device)
     out["rejected"] = torch.empty(n, dtype=torch.int32, device=device)
+    if extras:
+        out.update({k: torch.empty(n, dtype=torch.float64, device=device) for k in EXTRA_FIELDS})
     return out
 
 
 def _out_c(out: dict) -> RaysOutC:
-    return RaysOutC(*[_ptr(out.get(k)) for k in FIELDS])
+    return RaysOutC(*[_ptr(out.get(k)) for k in FIELDS + EXTRA_FIELDS])
 
 
 class Context:
@@ -432,7 +437,7 @@ class Context:
         arr, nf = self._frames(frames)
         oc = opts.c()
         ptrs = []
-        for k in FIELDS:
+        for k in FIELDS + EXTRA_FIELDS:
             v = out.get(k)
             ptrs.append(None if v is None else (v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data))
         outc = RaysOutC(*ptrs)

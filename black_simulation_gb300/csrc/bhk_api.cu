@@ -104,9 +104,9 @@ struct bhk_context {
     bool timed_last = false;
 
     // library-owned outputs for the host-buffer entry point and the autotuner
-    size_t cap_out = 0, cap_o8 = 0, cap_od[5] = {0, 0, 0, 0, 0}, cap_os = 0, cap_or = 0;
+    size_t cap_out = 0, cap_o8 = 0, cap_od[12] = {}, cap_os = 0, cap_or = 0;
     uint8_t* o_outcome = nullptr;
-    double* o_d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    double* o_d[12] = {};  // r_disk, phi_disk, g, theta_inf, phi_inf, then the optional seven
     int32_t* o_steps = nullptr;
     int32_t* o_rej = nullptr;
 
@@ -245,6 +245,7 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
                  r.block, r.grid, s);
     if (!r.fp64) launch_rescue(L, c->geom, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, s);
     if (timed) BHK_CUDA(cudaEventRecord(c->ev1, s));
+    launch_constants_out(L, out, c->ctl, lgrid, s);
     BHK_CUDA(cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Control), cudaMemcpyDeviceToHost, s));
     BHK_CUDA(cudaGetLastError());
     return BHK_OK;
@@ -291,6 +292,8 @@ Outputs to_outputs(const bhk_rays_out* o) {
     if (!o) return r;
     r.outcome = o->outcome; r.r_disk = o->r_disk; r.phi_disk = o->phi_disk; r.g = o->g;
     r.theta_inf = o->theta_inf; r.phi_inf = o->phi_inf; r.steps = o->steps; r.rejected = o->rejected;
+    r.energy = o->energy; r.g_camera = o->g_camera; r.b = o->b; r.q = o->q; r.r_min = o->r_min;
+    r.delay = o->delay; r.turns = o->turns;
     return r;
 }
 
@@ -334,9 +337,9 @@ bhk_status finish_call(bhk_context* c, const Resolved& r, int64_t n, bool timed,
     return BHK_OK;
 }
 
-bhk_status ensure_outputs(bhk_context* c, size_t n) {
+bhk_status ensure_outputs(bhk_context* c, size_t n, bool extras = false) {
     cudaError_t e = grow(&c->o_outcome, &c->cap_o8, n);
-    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = grow(&c->o_d[i], &c->cap_od[i], n);
+    for (int i = 0; i < (extras ? 12 : 5) && e == cudaSuccess; ++i) e = grow(&c->o_d[i], &c->cap_od[i], n);
     if (e == cudaSuccess) e = grow(&c->o_steps, &c->cap_os, n);
     if (e == cudaSuccess) e = grow(&c->o_rej, &c->cap_or, n);
     if (e != cudaSuccess) return fail(BHK_ENOMEM, "output allocation");
@@ -344,7 +347,11 @@ bhk_status ensure_outputs(bhk_context* c, size_t n) {
 }
 
 bhk_rays_out own_outputs(bhk_context* c) {
-    return bhk_rays_out{c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2], c->o_d[3], c->o_d[4], c->o_steps, c->o_rej};
+    bhk_rays_out o{};
+    o.outcome = c->o_outcome;
+    o.r_disk = c->o_d[0]; o.phi_disk = c->o_d[1]; o.g = c->o_d[2]; o.theta_inf = c->o_d[3]; o.phi_inf = c->o_d[4];
+    o.steps = c->o_steps; o.rejected = c->o_rej;
+    return o;
 }
 
 cudaStream_t pick(bhk_context* c, void* stream) { return stream ? static_cast<cudaStream_t>(stream) : c->stream; }
@@ -455,9 +462,10 @@ bhk_status bhk_destroy(bhk_context* c) {
     if (c->exec) cudaGraphExecDestroy(c->exec);
     if (c->graph) cudaGraphDestroy(c->graph);
     void* dev[] = {c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf, c->order, c->rescue, c->geom,
-                   c->frames_dev, c->ctl, c->hist, c->offs, c->o_outcome, c->o_d[0], c->o_d[1], c->o_d[2],
-                   c->o_d[3], c->o_d[4], c->o_steps, c->o_rej};
+                   c->frames_dev, c->ctl, c->hist, c->offs, c->o_outcome, c->o_steps, c->o_rej};
     for (void* p : dev)
+        if (p) cudaFree(p);
+    for (double* p : c->o_d)
         if (p) cudaFree(p);
     if (c->frames_host) cudaFreeHost(c->frames_host);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
@@ -555,10 +563,16 @@ bhk_status bhk_trace_frames_host(bhk_context* c, const bhk_frame_desc* frames, i
     int64_t total = 0;
     bhk_status st = check_frames(frames, nframes, &total);
     if (st != BHK_OK) return st;
-    st = ensure_outputs(c, static_cast<size_t>(total));
+    double* hx[7] = {host_out->energy, host_out->g_camera, host_out->b, host_out->q, host_out->r_min, host_out->delay,
+                     host_out->turns};
+    bool extras = false;
+    for (double* p : hx) extras = extras || p;
+    st = ensure_outputs(c, static_cast<size_t>(total), extras);
     if (st != BHK_OK) return st;
     const bhk_rays_out dev = own_outputs(c);
     bhk_rays_out use{};
+    double** ux[7] = {&use.energy, &use.g_camera, &use.b, &use.q, &use.r_min, &use.delay, &use.turns};
+    for (int i = 0; i < 7; ++i) *ux[i] = hx[i] ? c->o_d[5 + i] : nullptr;
     use.outcome = host_out->outcome ? dev.outcome : nullptr;
     use.r_disk = host_out->r_disk ? dev.r_disk : nullptr;
     use.phi_disk = host_out->phi_disk ? dev.phi_disk : nullptr;
@@ -580,6 +594,8 @@ bhk_status bhk_trace_frames_host(bhk_context* c, const bhk_frame_desc* frames, i
         BHK_CUDA(cudaMemcpyAsync(host_out->steps, use.steps, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     if (host_out->rejected)
         BHK_CUDA(cudaMemcpyAsync(host_out->rejected, use.rejected, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    for (int i = 0; i < 7; ++i)
+        if (hx[i]) BHK_CUDA(cudaMemcpyAsync(hx[i], *ux[i], n * sizeof(double), cudaMemcpyDeviceToHost, s));
     BHK_CUDA(cudaStreamSynchronize(s));
     return c->ctl_host->stats[2] ? fail(BHK_EUNFINISHED, "some rays reached the step cap") : BHK_OK;
 }

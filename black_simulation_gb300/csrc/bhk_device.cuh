@@ -433,10 +433,11 @@ struct Proj {
 };
 
 // Right-hand side of the 5-component Mino system y = (r, theta, phi, vr, vtheta), photon (mu = 0):
-// kerr::derivatives restated (src/kerr.cpp:331-351) without dt. With kProj it also returns the
-// potentials for the null-constraint re-projection, sharing sin, cos, P and Delta.
+// kerr::derivatives restated (src/kerr.cpp:331-351). With kProj it also returns the potentials for
+// the null-constraint re-projection, sharing sin, cos, P and Delta; with dt (FP64) also dt/dlambda,
+// the Kerr-Schild time, which the step carries as a passive extra component.
 template <typename T, bool kProj = false>
-__device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj<T>* pj = nullptr) {
+__device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj<T>* pj = nullptr, T* dt = nullptr) {
     const T r = y[0];
     T sn, cs;
     Math<T>::sc(y[1], &sn, &cs);
@@ -465,6 +466,7 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj
         inv2 = T(1) / sn2;
         k[4] = sn * cs * c.nA2E2 + c.L2 * cs / ssc;
         k[2] = c.a * inflow - c.aE + c.L / sn2;
+        if (dt) *dt = rra * inflow - c.a * (c.aE * sn * sn - c.L) - y[3];
     }
     if constexpr (kProj) {
         const T P2 = P * P;
@@ -482,6 +484,17 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     float y;
     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// Dense output of a passive component (its stage derivatives kt[0..6]) at fraction sg of a step.
+__device__ __forceinline__ double dense1(double y0, double y1, const double kt[7], double h, double sg) {
+    const double yd = y1 - y0;
+    const double b = h * kt[0] - yd;
+    const double c4 = yd - h * kt[6] - b;
+    const double c5 = h * (DP::d1 * kt[0] + DP::d3 * kt[2] + DP::d4 * kt[3] + DP::d5 * kt[4] + DP::d6 * kt[5] +
+                           DP::d7 * kt[6]);
+    const double s1 = 1.0 - sg;
+    return y0 + sg * (yd + s1 * (b + sg * (c4 + s1 * c5)));
 }
 
 // Dense output of one component at fraction sg of a step (continuous extension above).

@@ -66,6 +66,7 @@ struct SortScratch {
 struct Rescue {
     double y[5];
     double h;
+    double r_min;                 // closest approach so far
     int64_t ray;
     int32_t accepted, rejected;
     int32_t from_launch, pad;
@@ -84,6 +85,7 @@ struct Outputs {
     double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
     int32_t* steps;
     int32_t* rejected;
+    double *energy, *g_camera, *b, *q, *r_min, *delay, *turns;  // optional (NULL: not written)
 };
 
 // ---- launchers (bhk_trace.cu) ----
@@ -104,6 +106,8 @@ void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
                   cudaStream_t s);
+// energy, g_camera, b, q of every ray from its FP64 launch constants (if any is requested).
+void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s);
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
                    const TraceParams& p, Control* ctl, cudaStream_t s);
 int trace_blocks_per_sm(bool fp64, int regcap, int block);  // 0 when the pair is not allowed

@@ -168,8 +168,9 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     SortScratch S{reinterpret_cast<unsigned*>(base + kLayout.hist), reinterpret_cast<unsigned*>(base + kLayout.offs),
                   reinterpret_cast<int32_t*>(base + kLayout.order)};
     Rescue* rescue = reinterpret_cast<Rescue*>(base + kLayout.rescue);
-    Outputs outs{out->outcome, out->r_disk, out->phi_disk, out->g, out->theta_inf, out->phi_inf, out->steps,
-                 out->rejected};
+    Outputs outs{out->outcome, out->r_disk,   out->phi_disk, out->g, out->theta_inf, out->phi_inf, out->steps,
+                 out->rejected, out->energy, out->g_camera, out->b,        out->q, out->r_min,     out->delay,
+                 out->turns};
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     FrameBatch batch;
@@ -189,6 +190,7 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     }
     launch_trace(fp64, regcap, L, geom, order, outs, rescue, kStaticRescue, p, ctl, block, grid, s);
     if (!fp64) launch_rescue(L, geom, outs, rescue, kStaticRescue, p, ctl, s);
+    launch_constants_out(L, outs, ctl, 152 * 8, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
     return BHK_OK;

@@ -350,7 +350,23 @@ struct Lane {
     // The Kerr metric is symmetric under theta -> pi - theta, so the equations are unchanged, and
     // both poles are approached with the full relative precision of a small angle.
     bool south;
+    T rmin;          // closest approach so far (RayReport::rMin)
+    // FP64 mode: Kerr-Schild time t as a passive extra component (its stage derivatives kt) and the
+    // angle the position has swept (RayReport::delay, turns); `track` is false for FP32 lanes and for
+    // the FP64 continuation of a mixed-precision ray, whose history is not known.
+    bool track;
+    double t, swept, kt[7], pos[3];
 };
+
+// Kerr-Schild Cartesian position (kerr::toCartesian, src/kerr.cpp:638-641).
+__device__ __forceinline__ void ks_position(double a, double r, double th, double ph, double out[3]) {
+    double st, ct, sp, cp;
+    sincos(th, &st, &ct);
+    sincos(ph, &sp, &cp);
+    out[0] = (r * cp - a * sp) * st;
+    out[1] = (r * sp + a * cp) * st;
+    out[2] = r * ct;
+}
 
 // kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
 // first step of the backward march.
@@ -392,7 +408,17 @@ __device__ __forceinline__ void lane_begin_launch(Lane<T>& s, const RayGeom& g, 
         s.y[0] = g.r0; s.y[1] = g.th0; s.y[2] = g.ph0; s.y[3] = L.vr[ray]; s.y[4] = L.vth[ray];
     }
     lane_radii(s, g);
-    rhs(s.c, s.y, s.k[0]);
+    s.rmin = s.y[0];
+    s.t = 0.0;
+    s.swept = 0.0;
+    if constexpr (sizeof(T) == 8) {
+        s.track = true;
+        rhs(s.c, s.y, s.k[0], static_cast<Proj<T>*>(nullptr), &s.kt[0]);
+        ks_position(g.a, s.y[0], s.y[1], s.y[2], s.pos);
+    } else {
+        s.track = false;
+        rhs(s.c, s.y, s.k[0]);
+    }
     if constexpr (sizeof(T) == 4) s.h = first_step<T>(s.y, s.k[0], p.tol0_f);
     else s.h = first_step<T>(s.y, s.k[0], p.tol0);
     s.acc = 0; s.rej = 0; s.last_rej = false;
@@ -423,10 +449,21 @@ __device__ __forceinline__ T nan_t() {
     else return nan_d();
 }
 
+// The path outputs of a finished ray: closest approach (r_+(1 + eps) once captured), and in FP64 mode
+// the time the light travelled (t runs backward from 0 at the camera) and the turns swept.
+template <typename T>
+__device__ __forceinline__ void write_path(const Lane<T>& s, const Outputs& o, long long ray, double t_end,
+                                           bool captured) {
+    if (o.r_min) o.r_min[ray] = captured ? fmin(double(s.rmin), double(s.r_cap)) : double(s.rmin);
+    if (o.delay) o.delay[ray] = s.track ? -t_end : nan_d();
+    if (o.turns) o.turns[ray] = s.track ? s.swept / (2.0 * kPi) : nan_d();
+}
+
 template <typename T>
 __device__ __forceinline__ int finish(const Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl) {
     const T n = nan_t<T>();
     write_out_t<T>(o, ray, outcome, n, n, n, n, n, s.acc, s.rej);
+    write_path(s, o, ray, s.t, outcome == BHK_RAY_CAPTURED);
     if (outcome == BHK_RAY_UNFINISHED) atomicAdd(&ctl->stats[2], 1ull);
     return kFinished;
 }
@@ -479,24 +516,24 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     if constexpr (F64) {  // the oracle's operation order
 #pragma unroll
         for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a21) * s.k[0][i]);
-        rhs(s.c, t, s.k[1]);
+        rhs(s.c, t, s.k[1], static_cast<Proj<T>*>(nullptr), &s.kt[1]);
 #pragma unroll
         for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a31) * s.k[0][i] + T(DP::a32) * s.k[1][i]);
-        rhs(s.c, t, s.k[2]);
+        rhs(s.c, t, s.k[2], static_cast<Proj<T>*>(nullptr), &s.kt[2]);
 #pragma unroll
         for (int i = 0; i < 5; ++i)
             t[i] = s.y[i] + h * (T(DP::a41) * s.k[0][i] + T(DP::a42) * s.k[1][i] + T(DP::a43) * s.k[2][i]);
-        rhs(s.c, t, s.k[3]);
+        rhs(s.c, t, s.k[3], static_cast<Proj<T>*>(nullptr), &s.kt[3]);
 #pragma unroll
         for (int i = 0; i < 5; ++i)
             t[i] = s.y[i] + h * (T(DP::a51) * s.k[0][i] + T(DP::a52) * s.k[1][i] + T(DP::a53) * s.k[2][i] +
                                  T(DP::a54) * s.k[3][i]);
-        rhs(s.c, t, s.k[4]);
+        rhs(s.c, t, s.k[4], static_cast<Proj<T>*>(nullptr), &s.kt[4]);
 #pragma unroll
         for (int i = 0; i < 5; ++i)
             t[i] = s.y[i] + h * (T(DP::a61) * s.k[0][i] + T(DP::a62) * s.k[1][i] + T(DP::a63) * s.k[2][i] +
                                  T(DP::a64) * s.k[3][i] + T(DP::a65) * s.k[4][i]);
-        rhs(s.c, t, s.k[5]);
+        rhs(s.c, t, s.k[5], static_cast<Proj<T>*>(nullptr), &s.kt[5]);
 #pragma unroll
         for (int i = 0; i < 5; ++i)
             y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
@@ -548,7 +585,8 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         }
     }
     Proj<T> pj;
-    rhs<T, !F64>(s.c, y5, s.k[6], &pj);
+    if constexpr (F64) rhs<T, false>(s.c, y5, s.k[6], &pj, &s.kt[6]);
+    else rhs<T, true>(s.c, y5, s.k[6], &pj);
     T rtol;
     if constexpr (F64) rtol = p.rtol;
     else rtol = p.rtol_f;
@@ -602,6 +640,26 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if constexpr (F64) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
         else return kRestart;
     }
+    // Closest approach: the step's end, or inside it where vr changes sign (the turning point, from
+    // the dense output).
+    if (prev[3] * s.y[3] < T(0)) {
+        const T sv = locate(prev, s.y, s.k, h, 3, T(0));
+        s.rmin = fmin(s.rmin, dense(prev[0], s.y[0], s.k, h, 0, sv));
+    }
+    s.rmin = fmin(s.rmin, s.y[0]);
+    double t_prev = 0.0;
+    if constexpr (F64) {
+        t_prev = s.t;
+        s.t += h * (DP::b1 * s.kt[0] + DP::b3 * s.kt[2] + DP::b4 * s.kt[3] + DP::b5 * s.kt[4] + DP::b6 * s.kt[5]);
+        // The angle swept between the step's ends, as trajectory::traceRay sums it (src/trajectory.cpp:299).
+        double x1[3];
+        ks_position(s.c.a, s.y[0], s.y[1], s.y[2], x1);
+        const double n0 = sqrt(s.pos[0] * s.pos[0] + s.pos[1] * s.pos[1] + s.pos[2] * s.pos[2]);
+        const double n1 = sqrt(x1[0] * x1[0] + x1[1] * x1[1] + x1[2] * x1[2]);
+        const double cang = (s.pos[0] * x1[0] + s.pos[1] * x1[1] + s.pos[2] * x1[2]) / fmax(n0 * n1, 1e-300);
+        s.swept += acos(fmin(fmax(cang, -1.0), 1.0));
+        s.pos[0] = x1[0]; s.pos[1] = x1[1]; s.pos[2] = x1[2];
+    }
     const T hp = T(0.5 * kPi);
     // Thin disk: theta crosses pi/2 inside [r_in, r_out].
     if ((prev[1] - hp) * (s.y[1] - hp) < T(0)) {
@@ -613,6 +671,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
                     const double ph = wrap_2pi(dense(prev[2], s.y[2], s.k, h, 2, sg));
                     write_out(out, ray, BHK_RAY_DISK, rc, ph, g, nan_d(), nan_d(), s.acc, s.rej);
+                    write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
                     return kFinished;
                 }
             } else {
@@ -620,6 +679,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
                     const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
                     write_out_t<float>(out, ray, BHK_RAY_DISK, rc, ph, g, nan_f(), nan_f(), s.acc, s.rej);
+                    write_path(s, out, ray, 0.0, false);
                     return kFinished;
                 }
             }
@@ -657,6 +717,8 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
         const T n = nan_t<T>();
         write_out_t<T>(out, ray, BHK_RAY_ESCAPED, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
+        if constexpr (F64) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
+        else write_path(s, out, ray, 0.0, false);
         return kFinished;
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
@@ -700,6 +762,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     for (int i = 0; i < 5; ++i) s.k[0][i] = s.k[6][i];
     s.k[0][0] = s.y[3];
     s.k[0][1] = s.y[4];
+    if constexpr (F64) s.kt[0] = s.kt[6];
     T fac;
     if constexpr (F64) fac = err > 0.0 ? 0.9 * pow(err, -0.2) : 5.0;
     else fac = e2 > 0.0f ? 0.9f * exp2f(-0.1f * __log2f(e2)) : 5.0f;
@@ -721,13 +784,15 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
 }
 
 __device__ __forceinline__ void push_rescue(Rescue* rescue, unsigned cap, Control* ctl, long long ray, const double y[5],
-                                            double h, int acc, int rej, int from_launch, const Outputs& out) {
+                                            double h, double r_min, int acc, int rej, int from_launch,
+                                            const Outputs& out) {
     const unsigned idx = atomicAdd(&ctl->rescue_count, 1u);
     atomicAdd(&ctl->stats[3], 1ull);
     if (idx < cap) {
         Rescue r;
         for (int i = 0; i < 5; ++i) r.y[i] = y[i];
-        r.h = h; r.ray = ray; r.accepted = acc; r.rejected = rej; r.from_launch = from_launch; r.pad = 0;
+        r.h = h; r.r_min = r_min; r.ray = ray; r.accepted = acc; r.rejected = rej; r.from_launch = from_launch;
+        r.pad = 0;
         rescue[idx] = r;
     } else {
         write_out(out, ray, BHK_RAY_UNFINISHED, nan_d(), nan_d(), nan_d(), nan_d(), nan_d(), acc, rej);
@@ -802,7 +867,8 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                             y[4] = -y[4];
                         }
                     }
-                    push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? 0.0 : double(s.h), restart ? 0 : s.acc,
+                    push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? 0.0 : double(s.h),
+                                restart ? y[0] : fmin(double(s.rmin), y[0]), restart ? 0 : s.acc,
                                 restart ? 0 : s.rej, restart ? 1 : 0, out);
                 }
                 ray = -1;
@@ -845,10 +911,28 @@ __global__ void rescue_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, Out
         }
         s.acc = r.accepted;
         s.rej = r.rejected;
+        s.rmin = r.r_min;
+        s.track = false;  // the FP32 part kept no time or swept angle
+        s.t = 0.0;
+        s.swept = 0.0;
         int res = kContinue;
         while (res == kContinue) res = attempt<double>(s, p, r.ray, out, false, ctl, L, geom);
         atomicAdd(&ctl->stats[0], static_cast<unsigned long long>(s.acc - r.accepted));
         atomicAdd(&ctl->stats[1], static_cast<unsigned long long>(s.rej - r.rejected));
+    }
+}
+
+// trajectory::traceRay's energy, gCamera, b, q (src/trajectory.cpp:219-224) from the FP64 launch.
+__global__ void constants_out_kernel(LaunchSoA L, Outputs out, const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double E = L.E[i];
+        const double invE = fabs(E) > 1e-12 ? 1.0 / E : 0.0;
+        if (out.energy) out.energy[i] = E;
+        if (out.g_camera) out.g_camera[i] = invE;
+        if (out.b) out.b[i] = L.L[i] * invE;
+        if (out.q) out.q[i] = L.Q[i] * invE * invE;
     }
 }
 
@@ -920,6 +1004,10 @@ void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
                   cudaStream_t s) {
     trace_variant(fp64, regcap)<<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
+}
+
+void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s) {
+    if (out.energy || out.g_camera || out.b || out.q) constants_out_kernel<<<grid, 128, 0, s>>>(L, out, ctl);
 }
 
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,

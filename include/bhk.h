@@ -136,6 +136,17 @@ typedef struct {
     double* phi_inf;     /*                                                 atan2(d_y, d_x) */
     int32_t* steps;      /* accepted integration steps */
     int32_t* rejected;   /* rejected integration steps */
+    /* The rest of trajectory::RayReport (src/trajectory.h:95-113); NULL pointers are not written. */
+    double* energy;      /* E for unit energy at the camera (RayReport::energy) */
+    double* g_camera;    /* 1 / E (RayReport::gCamera) */
+    double* b;           /* L / E (RayReport::b) */
+    double* q;           /* Q / E^2 (RayReport::q) */
+    double* r_min;       /* closest approach (RayReport::rMin): refined at the radial turning point by the
+                            dense output; r_+(1 + eps) for captured rays */
+    double* delay;       /* Kerr-Schild time the light spent travelling (RayReport::delay); FP64 mode only
+                            (NaN in the mixed mode) */
+    double* turns;       /* angle swept by the position around the hole / 2 pi (RayReport::turns), as the
+                            reference sums it over the steps; FP64 mode only (NaN in the mixed mode) */
 } bhk_rays_out;
 
 /* Statistics of the last trace call on a context (filled at the end of that call's stream work). */

@@ -209,7 +209,7 @@ double ref_bending_angle(double R, double alpha) { return central::bendingAngle(
 // The reference's own trajectory::traceRay (tolerance 0.01, horizon r_+ + 0.01, escape
 // max(escapeRadius, 1.5 r)) from a ZAMO at (a, r, theta, phi). Returns the RayEnd code.
 int ref_trajectory_trace(double a, double r, double th, double ph, const double look[3], int disk, double r_in,
-                         double r_out, double escape, double out[8]) {
+                         double r_out, double escape, double out[9]) {
     trajectory::RayScene scene;
     scene.disk = disk != 0;
     scene.diskInner = r_in;
@@ -217,7 +217,7 @@ int ref_trajectory_trace(double a, double r, double th, double ph, const double 
     scene.escapeRadius = escape;
     const trajectory::RayReport rep = trajectory::traceRay(a, r, th, ph, zamo_frame(a, r, th), look, scene);
     out[0] = rep.rEnd, out[1] = rep.g, out[2] = rep.skyDirection[0], out[3] = rep.skyDirection[1];
-    out[4] = rep.skyDirection[2], out[5] = rep.rMin, out[6] = rep.turns, out[7] = rep.energy;
+    out[4] = rep.skyDirection[2], out[5] = rep.rMin, out[6] = rep.turns, out[7] = rep.energy, out[8] = rep.delay;
     return static_cast<int>(rep.end);
 }
 
@@ -225,7 +225,7 @@ int ref_trajectory_trace(double a, double r, double th, double ph, const double 
 // cameras inside the horizon. out[] as ref_trajectory_trace.
 int ref_trajectory_trace_framed(double a, double r, double th, double ph, const double* frame16,
                                 const double look[3], int disk, double r_in, double r_out, double escape,
-                                double out[8]) {
+                                double out[9]) {
     trajectory::RayScene scene;
     scene.disk = disk != 0;
     scene.diskInner = r_in;
@@ -236,7 +236,7 @@ int ref_trajectory_trace_framed(double a, double r, double th, double ph, const 
         for (int i = 0; i < 4; ++i) f.e[k][i] = frame16[4 * k + i];
     const trajectory::RayReport rep = trajectory::traceRay(a, r, th, ph, f, look, scene);
     out[0] = rep.rEnd, out[1] = rep.g, out[2] = rep.skyDirection[0], out[3] = rep.skyDirection[1];
-    out[4] = rep.skyDirection[2], out[5] = rep.rMin, out[6] = rep.turns, out[7] = rep.energy;
+    out[4] = rep.skyDirection[2], out[5] = rep.rMin, out[6] = rep.turns, out[7] = rep.energy, out[8] = rep.delay;
     return static_cast<int>(rep.end);
 }
 

@@ -9,7 +9,8 @@ Fixtures (all produced by the reference's own functions, never by this project's
   steps_ref.npz       per-step vectors: derivatives, stepMino, photonStepSize, enforceConstraints,
                       normalizeAngles, ZAMO frames + photonFromFrame, launchFromZamo, radii, critical
                       curves, central::bendingAngle (src/kerr.cpp, src/eht.cpp, src/central.cpp)
-  trajectory_ref.npz  trajectory::traceRay end/rEnd/g/skyDirection for ZAMO cameras with a disk
+  trajectory_ref.npz  trajectory::traceRay end and values (rEnd, g, skyDirection, rMin, turns, energy,
+                      delay) for ZAMO cameras with a disk
                       (src/trajectory.cpp:214-396), to pin the loop shape of the oracle
   c1_rk4_1e-4.npz     128x128 frame, a=0.9, r_obs=50, theta=80 deg, alpha,beta in [-15,15], disk
                       ISCO..20, escape 1000, capture r_+(1+1e-6): the reference RK4 loop at tolerance 1e-4
@@ -116,10 +117,10 @@ def trajectory_fixture(R: po.Oracle) -> dict:
     look = np.stack([-np.ones(n), rng.uniform(-0.35, 0.35, n), rng.uniform(-0.35, 0.35, n)], 1)
     look /= np.linalg.norm(look, axis=1, keepdims=True)
     end = np.zeros(n, np.int32)
-    vals = np.zeros((n, 8))
+    vals = np.zeros((n, 9))
     r_in = np.array([R.isco_radius_raw(x, 1) for x in a])
     for i in range(n):
-        out = np.zeros(8)
+        out = np.zeros(9)
         end[i] = R.trajectory_trace_raw(a[i], r[i], th[i], 0.0, po._ptr(np.ascontiguousarray(look[i])), 1, r_in[i],
                                         20.0, 250.0, po._ptr(out))
         vals[i] = out
@@ -186,7 +187,7 @@ def framed_fixture(R: po.Oracle) -> dict:
         cams.append([a, r, th, ph, r_in])
         sc = po.Scene(a, r, th, ph, r_in, 20.0, 1000.0, 1e-6, 1e-4, 5_000_000, po.RK4)
         for lk in looks:
-            out = np.zeros(8)
+            out = np.zeros(9)
             tr_end.append(R.trajectory_trace_framed_raw(a, r, th, ph, po._ptr(np.ascontiguousarray(f.reshape(16))),
                                                         po._ptr(np.ascontiguousarray(lk)), 1, r_in, 20.0, 250.0,
                                                         po._ptr(out)))

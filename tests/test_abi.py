@@ -30,7 +30,7 @@ def test_version_and_flop_count(libbhk):
 
 def test_struct_layouts_match_header():
     assert ctypes.sizeof(bhk.FrameDescC) == 4 * 8 + 2 * 4 + 6 * 8
-    assert ctypes.sizeof(bhk.RaysOutC) == 8 * 8
+    assert ctypes.sizeof(bhk.RaysOutC) == 15 * 8  # 8 core + 7 optional RayReport fields
 
 
 def test_no_cpu_fallback_without_gpu(libbhk):
