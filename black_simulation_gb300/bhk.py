@@ -72,6 +72,12 @@ class EhtFlowC(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("n0", "T0", "beta", "keplerian", "height", "sin_theta_b")]
 
 
+class PathOutC(C.Structure):
+    _fields_ = [("fate", C.c_void_p), ("duration", C.c_void_p), ("r_min", C.c_void_p), ("r_max", C.c_void_p),
+                ("periapses", C.c_void_p), ("precession_deg", C.c_void_p), ("points", C.c_void_p),
+                ("n_points", C.c_void_p)]
+
+
 class RenderOptsC(C.Structure):
     _fields_ = [("p_min", C.c_double), ("band", C.c_double), ("fallback", C.c_int32), ("cluster", C.c_int32)]
 
@@ -190,6 +196,7 @@ def lib() -> C.CDLL:
         "bhk_trace_rays_framed": (C.c_int, [vp, i64, vp, vp, vp, vp, vp, vp, d, d, C.POINTER(TraceOptsC),
                                             C.POINTER(RaysOutC), vp]),
         "bhk_eht_render": (C.c_int, [C.POINTER(EhtViewC), C.POINTER(EhtFlowC), C.c_int32, vp, vp, vp, vp]),
+        "bhk_predict": (C.c_int, [d, vp, vp, i64, d, d, C.c_int32, d, d, vp, C.POINTER(PathOutC), vp]),
         "bhk_eht_flux": (d, [vp, C.c_int32, d, d]),
         "bhk_eht_calibrate": (C.c_int, [C.POINTER(EhtViewC), C.POINTER(EhtFlowC), d, d, C.POINTER(d)]),
     }
@@ -337,6 +344,32 @@ def critical_curve(a: float, r_obs: float, theta_obs: float, samples: int = 400)
     n = C.c_int32(0)
     check(lib().bhk_critical_curve(a, r_obs, theta_obs, samples, al.ctypes.data, be.ctypes.data, cap, C.byref(n)))
     return al[:n.value].copy(), be[:n.value].copy()
+
+
+FATES = ("bound", "circular", "plunges", "escapes", "hits_surface")  # trajectory::Fate
+
+
+def predict(a: float, c, s, max_time: float, min_spacing: float = 0.5, max_points: int = 4000,
+            surface: float = 0.0, escape_radius: float = 2000.0, points: bool = True, stream=None) -> dict:
+    """trajectory::predict for n massive particles at once: constants (n, 4) and states (n, 6) float64
+    CUDA tensors -> dict of per-particle fate, duration, r_min, r_max, periapses, precession_deg,
+    n_points, points ((n, max_points + 1, 3), if asked) and the final states."""
+    import torch
+    n = _n(c, 4)
+    if _n(s, 6) != n:
+        raise ValueError("constants and states differ in length")
+    dev = c.device
+    out = {"fate": torch.empty(n, dtype=torch.int32, device=dev), "periapses": torch.empty(n, dtype=torch.int32, device=dev),
+           "n_points": torch.empty(n, dtype=torch.int32, device=dev), "state": torch.empty((n, 6), dtype=torch.float64, device=dev)}
+    for k in ("duration", "r_min", "r_max", "precession_deg"):
+        out[k] = torch.empty(n, dtype=torch.float64, device=dev)
+    if points:
+        out["points"] = torch.empty((n, max_points + 1, 3), dtype=torch.float64, device=dev)
+    po = PathOutC(*[_ptr(out.get(k)) for k in ("fate", "duration", "r_min", "r_max", "periapses", "precession_deg",
+                                                 "points", "n_points")])
+    check(lib().bhk_predict(a, _ptr(c.contiguous()), _ptr(s.contiguous()), n, max_time, min_spacing, max_points, surface,
+                            escape_radius, _ptr(out["state"]), C.byref(po), _stream(stream)))
+    return out
 
 
 def flops_per_step() -> float:

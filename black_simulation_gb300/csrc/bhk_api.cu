@@ -544,6 +544,18 @@ bhk_status bhk_cartesian_velocity(double a, const bhk_constants* c, const bhk_st
     BHK_STEP_RUN(steps_cartesian_velocity(a, c, s, out, n, static_cast<cudaStream_t>(stream)));
 }
 
+bhk_status bhk_predict(double a, const bhk_constants* c, const bhk_state* s, int64_t n, double max_time,
+                       double min_spacing, int32_t max_points, double surface, double escape_radius,
+                       bhk_state* s_out, const bhk_path_out* out, void* stream) {
+    if (!c || !s || !out || n < 0 || max_points < 1 || !(max_time >= 0.0) || !(std::fabs(a) < 1.0))
+        return fail(BHK_EINVAL, "bhk_predict: bad arguments (|a| < 1, n >= 0, max_points >= 1)");
+    if (n == 0) return BHK_OK;
+    const cudaError_t e = steps_predict(a, c, s, n, max_time, min_spacing, max_points, surface, escape_radius, s_out,
+                                        *out, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "bhk_predict");
+    return BHK_OK;
+}
+
 // ------------------------------------------------------------------------- batch tracer ----
 
 bhk_status bhk_trace_frames(bhk_context* c, const bhk_frame_desc* frames, int32_t nframes,

@@ -145,6 +145,9 @@ cudaError_t steps_photon_from_frame(double a, double r, double th, double ph, co
                                     bhk_constants* c, bhk_state* s, int64_t n, cudaStream_t st);
 cudaError_t steps_launch_from_zamo(double a, double r, double th, double ph, const double* v, double mu,
                                    bhk_constants* c, bhk_state* s, int64_t n, cudaStream_t st);
+cudaError_t steps_predict(double a, const bhk_constants* c, const bhk_state* s, int64_t n, double max_time,
+                          double min_spacing, int32_t max_points, double surface, double escape_radius,
+                          bhk_state* s_out, const bhk_path_out& out, cudaStream_t st);
 cudaError_t steps_cartesian_velocity(double a, const bhk_constants* c, const bhk_state* s, double* out, int64_t n,
                                      cudaStream_t st);
 

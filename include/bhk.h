@@ -178,6 +178,28 @@ bhk_status bhk_trace_rays(bhk_context* ctx, int64_t n, const double* a, const do
  * the reference, whose renderers always trace every pixel). */
 bhk_status bhk_trace_pixels(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes, const int32_t* pixels,
                             int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
+/* ---- trajectory::predict (src/trajectory.h:45-57): massive particles (mu = 1) in coordinate time ---- */
+enum { BHK_FATE_BOUND = 0, BHK_FATE_CIRCULAR = 1, BHK_FATE_PLUNGES = 2, BHK_FATE_ESCAPES = 3,
+       BHK_FATE_HITS_SURFACE = 4 };  /* trajectory::Fate */
+typedef struct bhk_path_out {       /* trajectory::Path per particle; NULL members are not written */
+    int32_t* fate;                  /* BHK_FATE_* within the time simulated */
+    double* duration;               /* coordinate time covered */
+    double *r_min, *r_max;
+    int32_t* periapses;             /* periapsis passages seen */
+    double* precession_deg;         /* periapsis advance per radial period (if periapses >= 2), else 0 */
+    double* points;                 /* (max_points + 1) x 3 Kerr-Schild Cartesian points per particle */
+    int32_t* n_points;              /* points written (at most max_points + 1: the last is the end) */
+} bhk_path_out;
+/* trajectory::predict batched: n particles (constants c[i], states s[i], device memory) integrated
+ * forward in coordinate time with the reference's own scheme (kerr::stepCoordinateTime at
+ * kerr::suggestedTimeStep tolerance 0.01, src/trajectory.cpp:130-185) up to max_time, or until they
+ * plunge (horizon, or the surface of radius `surface` if nonzero) or escape past escape_radius;
+ * path points at least min_spacing apart (max_points >= 1; the start and the end always count, so a
+ * particle writes at most max_points + 1). s_out (may be NULL) receives the final states. FP64. */
+bhk_status bhk_predict(double a, const bhk_constants* c, const bhk_state* s, int64_t n, double max_time,
+                       double min_spacing, int32_t max_points, double surface, double escape_radius,
+                       bhk_state* s_out, const bhk_path_out* out, void* stream);
+
 /* Per-ray cameras with arbitrary frames -- the call shape of trajectory::traceRay(a, r, theta, phi,
  * frame, look, scene) (src/trajectory.h:118-119), batched: camera position (a, r, theta, phi), its
  * frame (kerr::observerFrame of any 4-velocity: ZAMO, boosted, geodesic; bhk_observer_frame builds

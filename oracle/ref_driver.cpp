@@ -268,6 +268,19 @@ double ref_eht_calibrate(double a, double inclination, double half_width, int si
     return eht::calibrate(v, f, target_jy, theta_g_uas, threads);
 }
 
+// trajectory::predict (src/trajectory.cpp:130-185) of one particle: scalars into out[7] (fate,
+// duration, rMin, rMax, periapses, precessionDeg, number of points) and up to cap points (x, y, z).
+void ref_predict(double a, const orc_constants* c, const orc_state* s, double max_time, double min_spacing,
+                 int max_points, double surface, double escape_radius, double out[7], double* points, int cap) {
+    const trajectory::Path p = trajectory::predict(a, kc(c), ks(s), max_time, min_spacing,
+                                                   static_cast<size_t>(max_points), surface, escape_radius);
+    out[0] = static_cast<double>(static_cast<int>(p.fate));
+    out[1] = p.duration, out[2] = p.rMin, out[3] = p.rMax, out[4] = p.periapses, out[5] = p.precessionDeg;
+    out[6] = static_cast<double>(p.points.size());
+    for (size_t k = 0; k < p.points.size() && static_cast<int>(k) < cap; ++k)
+        for (int j = 0; j < 3; ++j) points[3 * k + j] = p.points[k][j];
+}
+
 double ref_eht_angular_scale(double mass_solar, double distance_pc) { return eht::angularScale(mass_solar, distance_pc); }
 
 double ref_eht_flux(const double* intensity, int size, double half_width, double theta_g_uas) {

@@ -21,6 +21,8 @@ Fixtures (all produced by the reference's own functions, never by this project's
                       (kerr::fourVelocity) -- frames from kerr::observerFrame, 40 look directions each:
                       trajectory::traceRay's end/rEnd/g (src/trajectory.cpp:214-396) and the reference
                       loop at tolerance 1e-4 from kerr::photonFromFrame with traceRay's inside-horizon rule
+  predict_ref.npz     trajectory::predict paths of massive particles launched from ZAMOs (bound and
+                      precessing, near-circular, plunging, escaping; src/trajectory.cpp:130-185)
   eht_ref.npz         eht::render images (src/eht.cpp:260-347): the M87* view of the reference's
                       calibration test (a = 0.9 at 60 deg, 48 px, density from eht::calibrate at 0.5 Jy),
                       a = 0.5 at 163 deg (32 px) and a = 0.99 at 30 deg (40 px), default flow
@@ -250,6 +252,39 @@ def eht_fixture(R: po.Oracle) -> dict:
     return out
 
 
+PREDICT_CASES = (  # (a, r, theta deg, ZAMO-frame velocity (r, theta, phi)), mu = 1
+    (0.9, 12.0, 90.0, (0.0, 0.0, 0.38)),     # eccentric, equatorial: precesses
+    (0.9, 10.0, 70.0, (0.05, 0.1, 0.36)),    # inclined, eccentric
+    (0.5, 8.0, 90.0, (0.0, 0.0, 0.42)),      # near circular
+    (0.9, 6.0, 80.0, (-0.3, 0.0, 0.2)),      # plunges
+    (0.3, 20.0, 60.0, (0.7, 0.0, 0.2)),      # escapes
+    (0.998, 4.0, 90.0, (0.0, 0.0, 0.55)),    # close to the hole
+)
+
+
+def predict_fixture(R: po.Oracle) -> dict:
+    lib = R.lib
+    lib.ref_predict.argtypes = [C.c_double, C.POINTER(po.Constants), C.POINTER(po.State), C.c_double, C.c_double,
+                                C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
+    lib.ref_predict.restype = None
+    cap = 2001
+    cons, states, scal, pts = [], [], [], []
+    for a, r, th, v in PREDICT_CASES:
+        c, s = R.launch_from_zamo(a, r, np.deg2rad(th), 0.0, np.array(v, dtype=np.float64), 1.0)
+        out = np.zeros(7)
+        p = np.zeros((cap, 3))
+        lib.ref_predict(a, C.byref(c), C.byref(s), 3000.0, 0.5, cap - 1, 0.0, 2000.0, po._ptr(out), po._ptr(p), cap)
+        cons.append([c.E, c.L, c.Q, c.mu])
+        states.append([s.t, s.r, s.theta, s.phi, s.vr, s.vtheta])
+        scal.append(out)
+        pts.append(p)
+        print(f"  a={a} r={r}: fate {int(out[0])}, {int(out[4])} periapses, precession {out[5]:.3f} deg, "
+              f"{int(out[6])} points")
+    return dict(cases=np.array([[a, r, th] for a, r, th, _ in PREDICT_CASES]), constants=np.array(cons),
+                states=np.array(states), scalars=np.array(scal), points=np.array(pts), max_time=3000.0,
+                min_spacing=0.5, max_points=cap - 1, escape_radius=2000.0)
+
+
 def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
     t = time.time()
     out = R.trace_frame(sc, w, h, *ext)
@@ -270,6 +305,8 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "trajectory_ref.npz"), **trajectory_fixture(R))
     print("framed_ref.npz")
     np.savez_compressed(os.path.join(HERE, "framed_ref.npz"), **framed_fixture(R))
+    print("predict_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "predict_ref.npz"), **predict_fixture(R))
     print("eht_ref.npz")
     np.savez_compressed(os.path.join(HERE, "eht_ref.npz"), **eht_fixture(R))
     if os.environ.get("FRAMED_ONLY"):

@@ -204,3 +204,44 @@ def test_near_axis_photons_leave_together(cuda):
     for k in range(1, 6):
         eps = 1e-6 * 10.0 ** k
         assert np.linalg.norm(d[k] - d[k - 1]) < 2e-3 + 2 * eps
+
+
+def test_predict_matches_reference_paths(cuda, golden):
+    """trajectory::predict batched on the GPU against the reference's own paths (bound and precessing,
+    near-circular, plunging, escaping; tests/golden/predict_ref.npz)."""
+    import torch
+    g = golden("predict_ref.npz")
+    sc = g["scalars"]
+    for i, (a, r, th) in enumerate(g["cases"]):
+        c = torch.tensor(g["constants"][i:i + 1], dtype=torch.float64, device="cuda")
+        s = torch.tensor(g["states"][i:i + 1], dtype=torch.float64, device="cuda")
+        o = bhk.predict(float(a), c, s, float(g["max_time"]), float(g["min_spacing"]), int(g["max_points"]),
+                        escape_radius=float(g["escape_radius"]))
+        torch.cuda.synchronize()
+        assert int(o["fate"][0]) == int(sc[i, 0]), (i, int(o["fate"][0]), sc[i, 0])
+        assert int(o["periapses"][0]) == int(sc[i, 4])
+        assert abs(float(o["duration"][0]) / sc[i, 1] - 1.0) < 1e-9
+        assert abs(float(o["r_min"][0]) / sc[i, 2] - 1.0) < 1e-8
+        assert abs(float(o["r_max"][0]) / sc[i, 3] - 1.0) < 1e-8
+        assert abs(float(o["precession_deg"][0]) - sc[i, 5]) < 1e-5
+        npts = int(o["n_points"][0])
+        assert npts == int(sc[i, 6])
+        pts = o["points"][0, :npts].cpu().numpy()
+        want = g["points"][i, :npts]
+        assert np.abs(pts - want).max() <= 1e-6 * max(1.0, np.abs(want).max())
+
+
+def test_predict_batch_equals_single_particles(cuda, golden):
+    import torch
+    g = golden("predict_ref.npz")
+    # the same particles, several spins in one call are not possible (one a per call): batch per spin
+    idx = [i for i, row in enumerate(g["cases"]) if row[0] == 0.9]
+    c = torch.tensor(g["constants"][idx], dtype=torch.float64, device="cuda")
+    s = torch.tensor(g["states"][idx], dtype=torch.float64, device="cuda")
+    o = bhk.predict(0.9, c, s, 3000.0, 0.5, 2000, points=False)
+    torch.cuda.synchronize()
+    for j, i in enumerate(idx):
+        assert int(o["fate"][j]) == int(g["scalars"][i, 0])
+        assert int(o["n_points"][j]) == int(g["scalars"][i, 6])
+    with pytest.raises(bhk.BhkError):
+        bhk.predict(1.5, c, s, 10.0)
