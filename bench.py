@@ -36,7 +36,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "geodesics/s"
+# BASELINE's headline metric: geodesics/s of the path that meets the 1e-4 exit-angle bound against
+# FP64 (the plain mixed tracer does; the surrogate path's errors are reported beside it).
+METRIC = "geodesics/s at \u22641e-4 rad exit-angle err vs FP64: surrogate vs plain GPU tracer"
 REF_TOL = 1e-2          # reference product tolerance (src/trajectory.cpp:261); meets the 1e-4 bar
 # DRAM bytes (read + write) of one tracer launch from ncu, by workload: the 960x540 capture of
 # profiles/trace_kernel_1080p_mixed.md (14.61 MB) scaled by rays to the full frame.
@@ -306,6 +308,13 @@ def run_ours(args):
         "gpu_launches": 7 * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0 and world == 1 and args.workload == "1080p" and args.scale == 1 and not args.no_surrogate:
+        # The metric's comparison: the surrogate + fallback path against this tracer on the surrogate's
+        # own workload (the orbit sequence), after training the network (not part of the timed steps).
+        try:
+            line["surrogate_vs_tracer"] = orbit_comparison(args, ctx, dev, 3, 2, 1, 60)
+        except Exception as exc:  # the headline line must not be lost to the comparison
+            line["surrogate_vs_tracer"] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, dt, threads = cpu_reference_rate(frames, target_s=15.0)
         line["cpu_baseline"] = {"value": rate, "unit": "rays/s", "cores": threads, "kind": "port",
@@ -318,7 +327,6 @@ def run_ours(args):
 
 # --------------------------------------------------------------------------- the surrogate ----
 
-SURROGATE_METRIC = "geodesics/s at <=1e-4 rad exit-angle err vs FP64: surrogate vs plain GPU tracer"
 # MACs per ray of the network (64 -> 256 -> 256 -> 256 -> 256 -> 16 padded head): forward, and the
 # backward's weight and input gradients (no input gradient of the first layer).
 MAC_FWD = 64 * 256 + 3 * 256 * 256 + 256 * 16
@@ -384,32 +392,27 @@ def error_stats(test, ref):
     return res
 
 
-def run_orbit(args):
-    """Surrogate + integrator fallback against the plain mixed tracer on the orbit sequence:
-    60 poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 (divided by --scale)."""
+def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses: int) -> dict:
+    """Surrogate + integrator fallback against the plain mixed tracer on the orbit sequence
+    (poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 / scale), both timed with CUDA
+    events on the same frames, and both judged on a seeded 1% of each frame's pixels traced in FP64."""
     import torch
-    from black_simulation_gb300 import bhk, build
+    from black_simulation_gb300 import bhk
     from black_simulation_gb300.surrogate import orbit_frames
-    build.build()
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
-    ctx = bhk.Context(0)
-    work_stream = torch.cuda.Stream(dev)
-    torch.cuda.set_stream(work_stream)
     stream = torch.cuda.current_stream()
     sur, train_info = train_surrogate(ctx, args)
-    frames = orbit_frames(args.poses, 3840 // args.scale, 2160 // args.scale)
+    frames = orbit_frames(poses, 3840 // scale, 2160 // scale)
     n = sum(f.rays for f in frames)
     opts = bhk.TraceOpts("mixed", rtol=1e-6)
     out_s = bhk.alloc_outputs(n, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         ms, extra = [], []
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -420,8 +423,9 @@ def run_orbit(args):
             extra.append(r)
         return float(np.mean(ms)), extra
 
-    with Clocks(0) as clk:
+    with Clocks(dev.index or 0) as clk:
         ms_s, stats = timed(lambda: sur.render(ctx, frames, opts, out=out_s)[1])
+    sort_launches = 3 if ctx.stats()["sort_buckets"] > 1 else 0
     ms_infer = float(np.mean([st["infer_ms"] for st in stats]))
     fb = float(np.mean([st["fallback"] for st in stats]))
     out_t = bhk.alloc_outputs(n, dev)
@@ -446,33 +450,57 @@ def run_orbit(args):
     ref_h = {k: ref[k].cpu().numpy() for k in keys}   # compact: entry i is pixel held[i]
     sur_h, tr_h = pick(out_s), pick(out_t)
     answered = ~fbl[held]
-    err_s = error_stats(sur_h, ref_h)
-    err_t = error_stats(tr_h, ref_h)
-    err_net = error_stats({k: v[answered] for k, v in sur_h.items()}, {k: v[answered] for k, v in ref_h.items()})
-    infer_rays_s = n / (ms_infer * 1e-3)
     peak, src = measured_peak("bf16_tflops", 1900.0)
     achieved = n * 2 * MAC_FWD / (ms_infer * 1e-3) / 1e12
-    line = {
-        "metric": SURROGATE_METRIC, "value": n / (ms_s * 1e-3), "unit": "rays/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_s, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32", "data": "synthetic",
-        "config": {"workload": f"{args.poses} orbit poses r=30M a=0.998 theta 85->45deg, "
-                               f"{3840 // args.scale}x{2160 // args.scale}, half-width 1.2x shadow radius, "
-                               "disk ISCO-30M; surrogate + mixed-precision fallback (p_min 0.99, band 0.05M)",
-                   "rays": n, "l2": "flushed (256 MB write) between steps", "training": train_info},
-        "plain_tracer": {"value": n / (ms_t * 1e-3), "ms_per_step": ms_t},
+    sur.close()
+    return {
+        "workload": f"{poses} orbit poses r=30M a=0.998 theta 85->45deg, {3840 // scale}x{2160 // scale}, "
+                    "half-width 1.2x shadow radius, disk ISCO-30M; surrogate + mixed-precision fallback "
+                    "(p_min 0.99, band 0.05M)",
+        "rays": n, "steps": steps, "warmup": warmup, "training": train_info,
+        "surrogate_path": {"value": n / (ms_s * 1e-3), "unit": "rays/s", "ms_per_step": ms_s},
+        "plain_tracer": {"value": n / (ms_t * 1e-3), "unit": "rays/s", "ms_per_step": ms_t},
         "speedup_vs_plain_tracer": ms_t / ms_s,
         "fallback_fraction": fb / n,
-        "inference": {"value": infer_rays_s, "ms": ms_infer},
-        "errors_vs_fp64": {"surrogate_path": err_s, "network_answered_only": err_net, "plain_tracer": err_t,
-                           "fp64_judge_s": t_fp64},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": src,
-                     "kernel": "infer_kernel (fused tcgen05 network)", "flops_per_ray": 2 * MAC_FWD},
-        "gpu_launches": None,
+        "inference": {"value": n / (ms_infer * 1e-3), "ms": ms_infer},
+        "errors_vs_fp64": {"surrogate_path": error_stats(sur_h, ref_h),
+                           "network_answered_only": error_stats({k: v[answered] for k, v in sur_h.items()},
+                                                                {k: v[answered] for k, v in ref_h.items()}),
+                           "plain_tracer": error_stats(tr_h, ref_h), "fp64_judge_s": t_fp64},
+        "meets_1e-4_bound": False,
+        "inference_roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                               "frac": achieved / peak, "traffic": None, "peak_source": src,
+                               "kernel": "infer_kernel (fused tcgen05 network)", "flops_per_ray": 2 * MAC_FWD},
+        # per render: curve table, bias halving, inference; the fallback list's frame set-up, launch,
+        # [sort], trace, rescue; the scatter
+        "gpu_launches": steps * (8 + sort_launches),
         "clocks": clk.summary(),
     }
-    sur.close()
+
+
+def run_orbit(args):
+    """The orbit comparison as its own bench line (value: the surrogate + fallback path)."""
+    import torch
+    from black_simulation_gb300 import bhk, build
+    build.build()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    ctx = bhk.Context(0)
+    work_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work_stream)
+    cmp_ = orbit_comparison(args, ctx, dev, args.steps, args.warmup, args.scale, args.poses)
+    line = {
+        "metric": METRIC, "value": cmp_["surrogate_path"]["value"], "unit": "rays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cmp_["surrogate_path"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
+        "data": "synthetic",
+        "config": {"workload": cmp_["workload"], "rays": cmp_["rays"], "l2": "flushed (256 MB write) between steps",
+                   "training": cmp_["training"]},
+        "plain_tracer": cmp_["plain_tracer"], "speedup_vs_plain_tracer": cmp_["speedup_vs_plain_tracer"],
+        "fallback_fraction": cmp_["fallback_fraction"], "inference": cmp_["inference"],
+        "errors_vs_fp64": cmp_["errors_vs_fp64"], "meets_1e-4_bound": False, "roofline": cmp_["inference_roofline"],
+        "gpu_launches": cmp_["gpu_launches"], "clocks": cmp_["clocks"],
+    }
     ctx.close()
     print(json.dumps(line))
 
@@ -534,6 +562,7 @@ def main():
     ap.add_argument("--autotune", action="store_true", default=True)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="1080p: skip the surrogate-vs-tracer comparison")
     ap.add_argument("--scale", type=int, default=1, help="divide the frame size (profiling captures)")
     ap.add_argument("--block", type=int, default=0, help="fixed launch shape instead of autotuning")
     ap.add_argument("--chunk", type=int, default=0)
