@@ -26,6 +26,8 @@ LIB_PATH = os.path.join(PKG, "libbhk.so")
 
 OK, EINVAL, ECUDA, EUNFINISHED, ENOMEM = 0, 1, 2, 3, 4
 UNFINISHED, CAPTURED, DISK, ESCAPED = 0, 1, 2, 3
+# Past |a| = 1 (naked singularity, no horizon): the sky of the r < 0 region, and the ring singularity.
+ESCAPED_BEYOND, RING = 4, 5
 PREC_FP64, PREC_MIXED = 0, 1
 
 

@@ -302,9 +302,12 @@ bhk_status check_frames(const bhk_frame_desc* f, int32_t nframes, int64_t* total
     int64_t t = 0;
     for (int i = 0; i < nframes; ++i) {
         if (f[i].width <= 0 || f[i].height <= 0) return fail(BHK_EINVAL, "frame with non-positive size");
-        if (!(std::fabs(f[i].a) < 1.0)) return fail(BHK_EINVAL, "spin must satisfy |a| < 1");
-        if (!(f[i].r_obs > 1.0 + std::sqrt(1.0 - f[i].a * f[i].a)))
-            return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole)");
+        // |a| > 1 is a naked singularity (no horizon); the extremal |a| = 1 is refused.
+        const double aa = std::fabs(f[i].a);
+        if (!(aa < 1.0 || aa > 1.0)) return fail(BHK_EINVAL, "spin must be finite and |a| != 1");
+        const double rp = aa < 1.0 ? 1.0 + std::sqrt(1.0 - f[i].a * f[i].a) : 0.0;
+        if (!(f[i].r_obs > rp))
+            return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole; r_obs > 0 past |a| = 1)");
         if (!(f[i].theta_obs > 0.0 && f[i].theta_obs < M_PI)) return fail(BHK_EINVAL, "theta_obs outside (0, pi)");
         if (!(f[i].r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
         t += static_cast<int64_t>(f[i].width) * f[i].height;

@@ -75,16 +75,70 @@ struct Der { double dt, dr, dtheta, dphi, dvr, dvtheta; };
 __host__ __device__ __forceinline__ double dmaxd(double x, double y) { return x > y ? x : y; }
 __host__ __device__ __forceinline__ double dmind(double x, double y) { return x < y ? x : y; }
 
-__device__ __forceinline__ bool naked(double a) { return fabs(a) > 1.0; }
+__host__ __device__ __forceinline__ bool naked(double a) { return fabs(a) > 1.0; }
 
 // r_+ (src/kerr.cpp:157-160).
-__device__ __forceinline__ double horizon_radius(double a) {
+__host__ __device__ __forceinline__ double horizon_radius(double a) {
     return naked(a) ? 0.0 : 1.0 + sqrt(dmaxd(0.0, 1.0 - a * a));
 }
 
-// Prograde/retrograde ISCO, Bardeen-Press-Teukolsky (src/kerr.cpp:179-190); NaN past a = 1.
-__device__ __forceinline__ double isco_radius(double a, bool prograde) {
-    if (naked(a)) return __longlong_as_double(0x7ff8000000000000ULL);
+// Energy per unit mass of the circular equatorial orbit at r (Bardeen, Press & Teukolsky 1972), 1e30
+// where there is none (src/kerr.cpp:122-129).
+__host__ __device__ __forceinline__ double circular_energy(double a, double r, bool prograde) {
+    const double sg = prograde ? 1.0 : -1.0, q = sqrt(r);
+    const double den = r * q - 3.0 * q + 2.0 * sg * a;
+    if (den <= 0.0) return 1e30;
+    return (r * q - 2.0 * q + sg * a) / (pow(r, 0.75) * sqrt(den));
+}
+
+// The radius of least circular-orbit energy in [lo, hi]: the best of 4001 points of a geometric grid,
+// then 80 golden-section steps between its neighbours (src/kerr.cpp:131-153). Out of line: on the
+// device it runs once per frame (or per explicit ray past a = 1) and should not weigh on its callers'
+// registers.
+static __host__ __device__ __noinline__ double least_energy_radius(double a, bool prograde, double lo, double hi) {
+    const int n = 4000;
+    int best = 0;
+    double best_e = 1e30;
+    for (int k = 0; k <= n; ++k) {
+        const double e = circular_energy(a, lo * pow(hi / lo, static_cast<double>(k) / n), prograde);
+        if (e < best_e) {
+            best_e = e;
+            best = k;
+        }
+    }
+    double x0 = lo * pow(hi / lo, (best > 1 ? best - 1 : 0) / static_cast<double>(n));
+    double x1 = lo * pow(hi / lo, (best + 1 < n ? best + 1 : n) / static_cast<double>(n));
+    const double gr = 0.5 * (sqrt(5.0) - 1.0);
+    for (int k = 0; k < 80; ++k) {
+        const double u = x1 - gr * (x1 - x0), v = x0 + gr * (x1 - x0);
+        if (circular_energy(a, u, prograde) < circular_energy(a, v, prograde)) x1 = v;
+        else x0 = u;
+    }
+    return 0.5 * (x0 + x1);
+}
+
+// Circular equatorial photon orbit (src/kerr.cpp:192-206): 2 (1 + cos(2/3 acos(-+a))); past a = 1 the
+// retrograde root of r (r - 3)^2 = 4 a^2 by bisection, and no prograde one (0).
+__host__ __device__ __forceinline__ double photon_orbit_radius(double a, bool prograde) {
+    if (naked(a)) {
+        if (prograde) return 0.0;
+        double lo = 3.0, hi = 3.0 + 2.0 * fabs(a);
+        for (int k = 0; k < 100; ++k) {
+            const double m = 0.5 * (lo + hi);
+            if (m * (m - 3.0) * (m - 3.0) < 4.0 * a * a) lo = m; else hi = m;
+        }
+        return 0.5 * (lo + hi);
+    }
+    return 2.0 * (1.0 + cos(2.0 / 3.0 * acos((prograde ? -1.0 : 1.0) * a)));
+}
+
+// Prograde/retrograde ISCO, Bardeen-Press-Teukolsky (src/kerr.cpp:179-190); past a = 1 the least
+// energy of circular orbits, prograde over [1e-3, 30], retrograde from just outside the retrograde
+// photon orbit to 60 (src/kerr.cpp:180-185).
+__host__ __device__ __forceinline__ double isco_radius(double a, bool prograde) {
+    if (naked(a))
+        return prograde ? least_energy_radius(a, true, 1e-3, 30.0)
+                        : least_energy_radius(a, false, photon_orbit_radius(a, false) * 1.0001, 60.0);
     const double z1 = 1.0 + cbrt(1.0 - a * a) * (cbrt(1.0 + a) + cbrt(1.0 - a));
     const double z2 = sqrt(3.0 * a * a + z1 * z1);
     const double w = sqrt(dmaxd(0.0, (3.0 - z1) * (3.0 + z1 + 2.0 * z2)));

@@ -257,9 +257,8 @@ __device__ void trace_pixel(const bhk_eht_view& v, const bhk_eht_flow& f, double
 
 // One thread per pixel (grid-stride), the image row-major from beta = +half_width
 // (src/eht.cpp:321-347).
-__global__ void render_kernel(bhk_eht_view v, bhk_eht_flow f, int with_light, double* intensity, uint8_t* shadow,
-                              int32_t* steps) {
-    const double rp = horizon_radius(v.a), isco = isco_radius(v.a, true);
+__global__ void render_kernel(bhk_eht_view v, bhk_eht_flow f, int with_light, double rp, double isco,
+                              double* intensity, uint8_t* shadow, int32_t* steps) {
     const long long n = static_cast<long long>(v.size) * v.size;
     const double pixel = 2.0 * v.half_width / v.size;
     for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < n;
@@ -278,7 +277,9 @@ __global__ void render_kernel(bhk_eht_view v, bhk_eht_flow f, int with_light, do
 }
 
 bool valid(const bhk_eht_view* v, const bhk_eht_flow* f) {
-    return v && f && v->size > 0 && v->size <= 16384 && std::fabs(v->a) < 1.0 && v->half_width > 0.0 &&
+    // |a| > 1 (no horizon): eht::traceRay's capture radius r_+ (1 + 1e-4) is then 0 (src/eht.cpp:274-287).
+    return v && f && v->size > 0 && v->size <= 16384 && (std::fabs(v->a) < 1.0 || std::fabs(v->a) > 1.0) &&
+           v->half_width > 0.0 &&
            v->frequency > 0.0 && v->mass_solar > 0.0 && f->T0 > 0.0 && f->beta > 0.0;
 }
 
@@ -290,14 +291,16 @@ extern "C" {
 bhk_status bhk_eht_render(const bhk_eht_view* view, const bhk_eht_flow* flow, int32_t with_light, double* intensity,
                           uint8_t* shadow, int32_t* steps, void* stream) {
     if (!bhk::eht::valid(view, flow)) {
-        bhk::set_last_error("bhk_eht_render: invalid view or flow (size 1..16384, |a| < 1, positive scales)");
+        bhk::set_last_error("bhk_eht_render: invalid view or flow (size 1..16384, finite |a| != 1, positive scales)");
         return BHK_EINVAL;
     }
     const long long n = static_cast<long long>(view->size) * view->size;
     const int block = 128;
     const int grid = static_cast<int>(std::min<long long>((n + block - 1) / block, 152LL * 16));
-    bhk::eht::render_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(*view, *flow, with_light, intensity,
-                                                                                    shadow, steps);
+    // Horizon and prograde ISCO once on the host (past |a| = 1 the ISCO is a 4000-point search).
+    const double rp = bhk::horizon_radius(view->a), isco = bhk::isco_radius(view->a, true);
+    bhk::eht::render_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(*view, *flow, with_light, rp, isco,
+                                                                                    intensity, shadow, steps);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         bhk::set_last_error(std::string("bhk_eht_render: ") + cudaGetErrorString(e));

@@ -21,6 +21,9 @@ struct RayGeom {
     int32_t south0;               // camera below the equator: th0f holds pi - theta_obs
     int32_t dead;                 // per-ray geometry only: a camera inside the horizon sees the hole
                                   // (trajectory::traceRay's rule, src/trajectory.cpp:236-244)
+    int32_t naked;                // |a| > 1: no horizon (r_cap, zone_top at -1e30); the ring and the
+                                  // sky beyond it end rays instead (shaders/trace.frag:1772-1787)
+    int32_t pad;
 };
 
 // Frame descriptor after set-up: pixel mapping, frame tetrad, ray offset, and the per-camera

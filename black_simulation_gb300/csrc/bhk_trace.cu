@@ -16,7 +16,9 @@
 //
 // The reference's ray semantics (src/trajectory.cpp:259-392): backward march in Mino time; disk
 // where theta crosses pi/2 with r in [r_in, r_out] and g from prograde circular gas; captured when
-// falling below r_+(1 + eps); escaped when rising past max(r_escape, 1.5 r_obs).
+// falling below r_+(1 + eps); escaped when rising past max(r_escape, 1.5 r_obs). Past |a| = 1 (no
+// horizon) the renderer's rules (shaders/trace.frag:1768-1787): the ring singularity where
+// Sigma < 4e-4, and the sky of the r < 0 region when falling past -max(r_escape, 1.5 r_obs).
 #include "bhk_device.cuh"
 #include "bhk_internal.h"
 
@@ -51,6 +53,11 @@ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, doub
     g.r_in = r_in_opt > 0.0 ? r_in_opt : isco_radius(a, true);
     g.r_out = r_out;
     g.zone_top = g.rp + dmind(0.05, 0.5 * (g.r_in - g.rp));
+    g.naked = naked(a) ? 1 : 0;
+    if (g.naked) {  // no horizon: nothing is captured (the ring and the far sky are tested instead)
+        g.r_cap = -1e30;
+        g.zone_top = -1e30;
+    }
     // FP32 copies; the launch polar angle is stored relative to the camera's hemisphere (the FP32
     // tracer integrates pi - theta in the south).
     g.south0 = th > 0.5 * kPi ? 1 : 0;
@@ -58,6 +65,7 @@ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, doub
     g.r_capf = float(g.r_cap); g.r_escf = float(g.r_esc); g.r_inf = float(g.r_in); g.r_outf = float(g.r_out);
     g.zone_topf = float(g.zone_top); g.rpf = float(g.rp);
     g.dead = 0;
+    g.pad = 0;
     return g;
 }
 
@@ -369,13 +377,13 @@ __device__ __forceinline__ void ks_position(double a, double r, double th, doubl
 }
 
 // kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
-// first step of the backward march.
+// first step of the backward march. Lengths are r, or past |a| = 1 max(sqrt(Sigma), 0.02).
 template <typename T>
-__device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol) {
+__device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol, T a2, bool nkd) {
     T sn, cs;
     Math<T>::sc(y[1], &sn, &cs);
     sn = fabs(sn);
-    const T rs = y[0];
+    const T rs = nkd ? fmax(sqrt(y[0] * y[0] + a2 * cs * cs), T(0.02)) : y[0];
     const T t = tol * fmin(fmax(rs / T(8), T(1)), T(4));
     T h = t / (fabs(k[0]) / rs + fabs(k[1]) / fmax(sn, T(1e-4)) + fabs(k[2]) + T(1e-6));
     h = fmin(h, sqrt(t * rs / (fabs(k[3]) + T(1e-6))));
@@ -419,8 +427,8 @@ __device__ __forceinline__ void lane_begin_launch(Lane<T>& s, const RayGeom& g, 
         s.track = false;
         rhs(s.c, s.y, s.k[0]);
     }
-    if constexpr (sizeof(T) == 4) s.h = first_step<T>(s.y, s.k[0], p.tol0_f);
-    else s.h = first_step<T>(s.y, s.k[0], p.tol0);
+    if constexpr (sizeof(T) == 4) s.h = first_step<T>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
+    else s.h = first_step<T>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
@@ -501,6 +509,31 @@ __device__ __forceinline__ T locate(const T* y0, const T* y1, const T k[7][5], T
         if (done) break;
     }
     return s;
+}
+
+// A ray that left through r = target within the step just taken: the escape direction is the
+// backward tangent there (dense output), as (theta_inf, phi_inf).
+template <typename T>
+__device__ __forceinline__ int escape(const Lane<T>& s, const T prev[5], T h, T target, int outcome, const Outputs& out,
+                                   long long ray, double t_prev) {
+    const T sg = locate(prev, s.y, s.k, h, 0, target);
+    T x[5], kk[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
+    rhs(s.c, x, kk);
+    T v[3];
+    if (s.south) {  // back to the physical angle: cos(pi - t) = -cos t, d(pi - t) = -dt
+        x[1] = T(kPi) - x[1];
+        x[4] = -x[4];
+    }
+    cartesian_velocity<T>(s.c.a, x[0], x[1], x[2], x[3], x[4], kk[2], v);
+    const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
+    const T n = nan_t<T>();
+    write_out_t<T>(out, ray, outcome, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
+    if constexpr (sizeof(T) == 8) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
+    else write_path(s, out, ray, 0.0, false);
+    return kFinished;
 }
 
 // One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
@@ -686,7 +719,17 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         }
     }
     const bool falling = s.y[0] < prev[0];
+    // Past |a| = 1 only (r stays above r_+ > 1 around a hole): the ring singularity, where
+    // Sigma = r^2 + a^2 cos^2(theta) vanishes (shaders/trace.frag:1773-1778; cos^2 is the same in either
+    // hemisphere representation).
+    if (fabs(s.y[0]) < T(0.02)) {
+        T sn, cs;
+        Math<T>::sc(s.y[1], &sn, &cs);
+        if (s.y[0] * s.y[0] + s.c.a2 * cs * cs < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
+    }
     if (falling) {
+        // Past |a| = 1: gone far out into the r < 0 region, beyond the ring (shaders/trace.frag:1779-1786).
+        if (s.y[0] < -s.r_esc) return escape(s, prev, h, -s.r_esc, BHK_RAY_ESCAPED_BEYOND, out, ray, t_prev);
         if (s.y[0] < s.r_cap) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
         if (s.y[0] < s.zone_top) {
             if constexpr (F64) {
@@ -702,24 +745,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
             }
         }
     } else if (s.y[0] > s.r_esc) {
-        const T sg = locate(prev, s.y, s.k, h, 0, s.r_esc);
-        T x[5], kk[5];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
-        rhs(s.c, x, kk);
-        T v[3];
-        if (s.south) {  // back to the physical angle: cos(pi - t) = -cos t, d(pi - t) = -dt
-            x[1] = T(kPi) - x[1];
-            x[4] = -x[4];
-        }
-        cartesian_velocity<T>(s.c.a, x[0], x[1], x[2], x[3], x[4], kk[2], v);
-        const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
-        const T n = nan_t<T>();
-        write_out_t<T>(out, ray, BHK_RAY_ESCAPED, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
-        if constexpr (F64) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
-        else write_path(s, out, ray, 0.0, false);
-        return kFinished;
+        return escape(s, prev, h, s.r_esc, BHK_RAY_ESCAPED, out, ray, t_prev);
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
     // carrying the FSAL derivative: under theta -> -theta (or 2 pi - theta) Theta'(theta) changes sign.
@@ -773,8 +799,9 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         // the tolerance allows shrinks geometrically and the error-per-step controller, which only
         // looks back, overshoots into a rejection every other step. Cap the step at a fixed fraction
         // of the Mino time left to the pole, ~ r / |vr|.
-        if (p.pole_frac > 0.0f && s.h * s.y[3] > 0.0f) {
-            const float cap = p.pole_frac * s.y[0] * rcp_approx(fabsf(s.y[3]));
+        // (|r| grows on either side of r = 0: past |a| = 1 the r < 0 region has the same pole.)
+        if (p.pole_frac > 0.0f && s.h * s.y[3] * s.y[0] > 0.0f) {
+            const float cap = p.pole_frac * fabsf(s.y[0]) * rcp_approx(fabsf(s.y[3]));
             s.h = copysignf(fminf(fabsf(s.h), cap), s.h);
         }
     }

@@ -34,8 +34,14 @@ typedef enum {
     BHK_ENOMEM = 4        /* device allocation failed */
 } bhk_status;
 
-/* Ray outcomes (trajectory::RayEnd, src/trajectory.h:85, restricted to a bare hole + thin disk). */
-enum { BHK_RAY_UNFINISHED = 0, BHK_RAY_CAPTURED = 1, BHK_RAY_DISK = 2, BHK_RAY_ESCAPED = 3 };
+/* Ray outcomes (trajectory::RayEnd, src/trajectory.h:85, restricted to a bare hole + thin disk).
+ * Past |a| = 1 (a naked singularity, no horizon) nothing is captured; as the renderer has it
+ * (shaders/trace.frag:1768-1787) a ray may instead strike the ring singularity (Sigma =
+ * r^2 + a^2 cos^2 theta < 4e-4: BHK_RAY_RING) or pass through the ring's disk to the r < 0 region
+ * and leave to that region's sky below r = -max(r_escape, 1.5 r_obs) (BHK_RAY_ESCAPED_BEYOND, with
+ * theta_inf, phi_inf like BHK_RAY_ESCAPED). */
+enum { BHK_RAY_UNFINISHED = 0, BHK_RAY_CAPTURED = 1, BHK_RAY_DISK = 2, BHK_RAY_ESCAPED = 3,
+       BHK_RAY_ESCAPED_BEYOND = 4, BHK_RAY_RING = 5 };
 
 /* Layout-identical to kerr::Constants, kerr::State, kerr::Derivatives, kerr::Frame
  * (src/kerr.h:81-99, 143-145). */

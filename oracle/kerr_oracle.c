@@ -35,10 +35,45 @@ double orc_horizon_radius(double a) {
     return 1.0 + sqrt(dmax(0.0, 1.0 - a * a));
 }
 
-/* Bardeen-Press-Teukolsky ISCO (src/kerr.cpp:179-190); the naked-spin numeric search is not
- * restated (spins past 1 are outside this path). */
+/* Energy per unit mass of the circular equatorial orbit at r (Bardeen, Press & Teukolsky 1972), 1e30
+ * where there is none (src/kerr.cpp:122-129). */
+static double circular_energy(double a, double r, int prograde) {
+    const double sg = prograde ? 1.0 : -1.0, q = sqrt(r);
+    const double den = r * q - 3.0 * q + 2.0 * sg * a;
+    if (den <= 0.0) return 1e30;
+    return (r * q - 2.0 * q + sg * a) / (pow(r, 0.75) * sqrt(den));
+}
+
+/* The radius of least circular-orbit energy in [lo, hi]: the best of 4001 points of a geometric
+ * grid, then 80 golden-section steps between its neighbours (src/kerr.cpp:131-153). */
+static double least_energy_radius(double a, int prograde, double lo, double hi) {
+    const int n = 4000;
+    int best = 0;
+    double best_e = 1e30;
+    for (int k = 0; k <= n; ++k) {
+        const double e = circular_energy(a, lo * pow(hi / lo, (double)k / n), prograde);
+        if (e < best_e) {
+            best_e = e;
+            best = k;
+        }
+    }
+    double x0 = lo * pow(hi / lo, (best > 1 ? best - 1 : 0) / (double)n);
+    double x1 = lo * pow(hi / lo, (best + 1 < n ? best + 1 : n) / (double)n);
+    const double gr = 0.5 * (sqrt(5.0) - 1.0);
+    for (int k = 0; k < 80; ++k) {
+        const double u = x1 - gr * (x1 - x0), v = x0 + gr * (x1 - x0);
+        if (circular_energy(a, u, prograde) < circular_energy(a, v, prograde)) x1 = v;
+        else x0 = u;
+    }
+    return 0.5 * (x0 + x1);
+}
+
+/* ISCO: Bardeen-Press-Teukolsky (src/kerr.cpp:179-190); past a = 1 the least-energy search, prograde
+ * over [1e-3, 30], retrograde from just outside the retrograde photon orbit to 60 (src/kerr.cpp:180-185). */
 double orc_isco_radius(double a, int prograde) {
-    if (is_naked(a)) return NAN;
+    if (is_naked(a))
+        return prograde ? least_energy_radius(a, 1, 1e-3, 30.0)
+                        : least_energy_radius(a, 0, orc_photon_orbit_radius(a, 0) * 1.0001, 60.0);
     const double z1 = 1.0 + cbrt(1.0 - a * a) * (cbrt(1.0 + a) + cbrt(1.0 - a));
     const double z2 = sqrt(3.0 * a * a + z1 * z1);
     const double w = sqrt(dmax(0.0, (3.0 - z1) * (3.0 + z1 + 2.0 * z2)));
@@ -511,6 +546,9 @@ static void ray_init(orc_ray* out) {
     out->r_disk = out->phi_disk = out->g = out->theta_inf = out->phi_inf = NAN;
 }
 
+/* Sigma below which a ray has struck the ring singularity (shaders/trace.frag:1773-1778). */
+#define ORC_RING_SIGMA 4e-4
+
 static double effective_escape(const orc_scene* sc) { return dmax(sc->r_escape, 1.5 * sc->r_obs); }
 static double disk_inner(const orc_scene* sc) {
     return sc->r_disk_in > 0.0 ? sc->r_disk_in : orc_isco_radius(sc->a, 1);
@@ -521,6 +559,7 @@ static double disk_inner(const orc_scene* sc) {
 static void trace_rk4(const orc_scene* sc, orc_constants c, orc_state s, orc_ray* out) {
     out->E = c.E, out->L = c.L, out->Q = c.Q;
     const double a = sc->a;
+    const int naked = is_naked(a);
     const double r_cap = orc_horizon_radius(a) * (1.0 + sc->capture_eps);
     const double r_esc = effective_escape(sc);
     const double r_in = disk_inner(sc), r_out = sc->r_disk_out;
@@ -544,21 +583,29 @@ static void trace_rk4(const orc_scene* sc, orc_constants c, orc_state s, orc_ray
                 return;
             }
         }
-        if (s.r < r_cap && s.r < prev.r) {
+        if (naked) {
+            const double cs = cos(s.theta);
+            if (s.r * s.r + a * a * cs * cs < ORC_RING_SIGMA) {
+                out->outcome = ORC_RING;
+                return;
+            }
+        } else if (s.r < r_cap && s.r < prev.r) {
             out->outcome = ORC_CAPTURED;
             return;
         }
-        if (s.r > r_esc && s.r > prev.r) {
+        const double r_far = naked ? -r_esc : -INFINITY;
+        if ((s.r > r_esc && s.r > prev.r) || (s.r < r_far && s.r < prev.r)) {
+            const double target = s.r > 0.0 ? r_esc : r_far;
             orc_state x = s;
             if (fabs(s.theta - prev.theta) < 1.0) {
-                const double f = (r_esc - prev.r) / (s.r - prev.r);
-                x.r = r_esc;
+                const double f = (target - prev.r) / (s.r - prev.r);
+                x.r = target;
                 x.theta = prev.theta + f * (s.theta - prev.theta);
                 x.phi = prev.phi + f * (s.phi - prev.phi);
                 x.vr = prev.vr + f * (s.vr - prev.vr);
                 x.vtheta = prev.vtheta + f * (s.vtheta - prev.vtheta);
             }
-            out->outcome = ORC_ESCAPED;
+            out->outcome = s.r > 0.0 ? ORC_ESCAPED : ORC_ESCAPED_BEYOND;
             escape_direction(a, &c, &x, &out->theta_inf, &out->phi_inf);
             return;
         }
@@ -625,6 +672,8 @@ static void trace_dp5(const orc_scene* sc, orc_constants c, orc_state s, orc_ray
     const double r_esc = effective_escape(sc);
     const double r_in = disk_inner(sc), r_out = sc->r_disk_out;
     const double zone = dmin(0.05, 0.5 * (r_in - rp));
+    const int naked = is_naked(a);
+    const double r_far = naked ? -r_esc : -INFINITY;
     const double rtol = sc->tol, atol = sc->tol;
     const double half_pi = 0.5 * ORC_PI;
 
@@ -686,20 +735,28 @@ static void trace_dp5(const orc_scene* sc, orc_constants c, orc_state s, orc_ray
             }
         }
         const int falling = y.v[0] < prev.v[0];
-        if (falling && (y.v[0] < r_cap || (y.v[0] < rp + zone &&
-                                           orc_no_radial_root_below(a, c.E, c.L, c.Q, y.v[0], sc->capture_eps)))) {
+        if (naked) {
+            const double cs = cos(y.v[1]);
+            if (y.v[0] * y.v[0] + a * a * cs * cs < ORC_RING_SIGMA) {
+                out->outcome = ORC_RING;
+                return;
+            }
+        } else if (falling && (y.v[0] < r_cap || (y.v[0] < rp + zone &&
+                                                  orc_no_radial_root_below(a, c.E, c.L, c.Q, y.v[0],
+                                                                           sc->capture_eps)))) {
             out->outcome = ORC_CAPTURED;
             return;
         }
-        if (!falling && y.v[0] > r_esc) {
-            const double sg = locate(prev.v, y.v, k, h, 0, r_esc);
+        if ((!falling && y.v[0] > r_esc) || (falling && y.v[0] < r_far)) {
+            const double target = falling ? r_far : r_esc;
+            const double sg = locate(prev.v, y.v, k, h, 0, target);
             orc_state x = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
             x.r = dense(prev.v, y.v, k, h, 0, sg);
             x.theta = dense(prev.v, y.v, k, h, 1, sg);
             x.phi = dense(prev.v, y.v, k, h, 2, sg);
             x.vr = dense(prev.v, y.v, k, h, 3, sg);
             x.vtheta = dense(prev.v, y.v, k, h, 4, sg);
-            out->outcome = ORC_ESCAPED;
+            out->outcome = falling ? ORC_ESCAPED_BEYOND : ORC_ESCAPED;
             escape_direction(a, &c, &x, &out->theta_inf, &out->phi_inf);
             return;
         }

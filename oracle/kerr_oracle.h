@@ -60,7 +60,11 @@ int orc_critical_curve_finite(double a, double r_obs, double theta_obs, int samp
                               double* beta, int cap);
 
 /* ---- ray-level tracer ---- */
-enum { ORC_UNFINISHED = 0, ORC_CAPTURED = 1, ORC_DISK = 2, ORC_ESCAPED = 3 };
+/* Past a = 1 (no horizon; shaders/trace.frag:1552-1554, 1768-1787): no capture; a ray whose Sigma
+ * falls below 4e-4 has struck the ring singularity (ORC_RING), and one that passed through the
+ * ring's disk and leaves below r = -max(r_escape, 1.5 r_obs) escaped to the sky of the r < 0
+ * region (ORC_ESCAPED_BEYOND, with its direction like ORC_ESCAPED). */
+enum { ORC_UNFINISHED = 0, ORC_CAPTURED = 1, ORC_DISK = 2, ORC_ESCAPED = 3, ORC_ESCAPED_BEYOND = 4, ORC_RING = 5 };
 enum { ORC_METHOD_RK4 = 0, ORC_METHOD_DP5 = 1 };
 
 typedef struct {

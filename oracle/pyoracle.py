@@ -20,6 +20,7 @@ LIB_ORACLE = os.path.join(HERE, "liboracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libkerr_ref.so")
 
 UNFINISHED, CAPTURED, DISK, ESCAPED = 0, 1, 2, 3
+ESCAPED_BEYOND, RING = 4, 5  # past |a| = 1: the sky of the r < 0 region, the ring singularity
 RK4, DP5 = 0, 1
 
 

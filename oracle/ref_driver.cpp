@@ -64,6 +64,7 @@ void ray_clear(orc_ray* out) {
 void trace_launched(const orc_scene* sc, kerr::Constants c, kerr::State s, orc_ray* out) {
     out->E = c.E, out->L = c.L, out->Q = c.Q;
     const double a = sc->a;
+    const bool naked = std::abs(a) > 1.0;
     const double rcap = kerr::horizonRadius(a) * (1.0 + sc->capture_eps);
     const double resc = std::max(sc->r_escape, 1.5 * sc->r_obs);
     const double rin = sc->r_disk_in > 0.0 ? sc->r_disk_in : kerr::iscoRadius(a, true);
@@ -93,21 +94,31 @@ void trace_launched(const orc_scene* sc, kerr::Constants c, kerr::State s, orc_r
                 }
             }
         }
-        if (s.r < rcap && s.r < prev.r) {
+        // Past a = 1 there is no horizon: the renderer's rules (shaders/trace.frag:1772-1787) -- the
+        // ring singularity where Sigma < 4e-4, and the sky of the r < 0 region beyond r = -resc.
+        if (naked) {
+            const double cs = std::cos(s.theta);
+            if (s.r * s.r + a * a * cs * cs < 4e-4) {
+                out->outcome = ORC_RING;
+                return;
+            }
+        } else if (s.r < rcap && s.r < prev.r) {
             out->outcome = ORC_CAPTURED;
             return;
         }
-        if (s.r > resc && s.r > prev.r) {
+        const bool far = naked && s.r < -resc && s.r < prev.r;
+        if ((s.r > resc && s.r > prev.r) || far) {
+            const double target = far ? -resc : resc;
             kerr::State x = s;
             if (std::abs(s.theta - prev.theta) < 1.0) {
-                const double f = (resc - prev.r) / (s.r - prev.r);
-                x.r = resc;
+                const double f = (target - prev.r) / (s.r - prev.r);
+                x.r = target;
                 x.theta = prev.theta + f * (s.theta - prev.theta);
                 x.phi = prev.phi + f * (s.phi - prev.phi);
                 x.vr = prev.vr + f * (s.vr - prev.vr);
                 x.vtheta = prev.vtheta + f * (s.vtheta - prev.vtheta);
             }
-            out->outcome = ORC_ESCAPED;
+            out->outcome = far ? ORC_ESCAPED_BEYOND : ORC_ESCAPED;
             sky(a, c, x, &out->theta_inf, &out->phi_inf);
             return;
         }

@@ -23,6 +23,10 @@ Fixtures (all produced by the reference's own functions, never by this project's
                       loop at tolerance 1e-4 from kerr::photonFromFrame with traceRay's inside-horizon rule
   predict_ref.npz     trajectory::predict paths of massive particles launched from ZAMOs (bound and
                       precessing, near-circular, plunging, escaping; src/trajectory.cpp:130-185)
+  naked_ref.npz       past |a| = 1 (no horizon): kerr::iscoRadius / photonOrbitRadius of naked spins;
+                      frames traced by the reference loop at tolerance 1e-4 with the renderer's rules
+                      for naked singularities (ring where Sigma < 4e-4, the sky of the r < 0 region;
+                      shaders/trace.frag:1768-1787); an eht::render image at a = 1.2
   eht_ref.npz         eht::render images (src/eht.cpp:260-347): the M87* view of the reference's
                       calibration test (a = 0.9 at 60 deg, 48 px, density from eht::calibrate at 0.5 Jy),
                       a = 0.5 at 163 deg (32 px) and a = 0.99 at 30 deg (40 px), default flow
@@ -285,10 +289,48 @@ def predict_fixture(R: po.Oracle) -> dict:
                 min_spacing=0.5, max_points=cap - 1, escape_radius=2000.0)
 
 
+NAKED_SPINS = (1.02, 1.05, 1.2, 1.5, 2.0, -1.3)
+NAKED_FRAMES = (  # (a, r_obs, theta_obs deg, r_disk_out, width, height, (alpha_lo, alpha_hi, beta_lo, beta_hi))
+    (1.2, 100.0, 30.0, 20.0, 64, 64, (-4.0, 4.0, -4.0, 4.0)),        # through the ring's disk, disk from ISCO < 1
+    (1.05, 50.0, 75.0, 20.0, 48, 27, (-12.0, 12.0, -6.75, 6.75)),   # near edge-on
+    (1.5, 30.0, 60.0, 0.0, 40, 40, (-6.0, 6.0, -6.0, 6.0)),         # no disk: both skies
+)
+NAKED_EHT = (1.2, 60.0, 16.0, 24)  # (a, inclination deg, half width, size)
+
+
+def naked_fixture(R: po.Oracle) -> dict:
+    lib = R.lib
+    lib.ref_isco_radius.argtypes = [C.c_double, C.c_int]
+    lib.ref_isco_radius.restype = C.c_double
+    lib.ref_photon_orbit_radius.argtypes = [C.c_double, C.c_int]
+    lib.ref_photon_orbit_radius.restype = C.c_double
+    out = dict(spins=np.array(NAKED_SPINS),
+               isco=np.array([[lib.ref_isco_radius(a, p) for p in (1, 0)] for a in NAKED_SPINS]),
+               photon_orbit=np.array([[lib.ref_photon_orbit_radius(a, p) for p in (1, 0)] for a in NAKED_SPINS]))
+    for i, (a, r, th, rout, w, h, ext) in enumerate(NAKED_FRAMES):
+        sc = po.scene(a=a, r_obs=r, theta_obs_deg=th, r_disk_out=rout, tol=1e-4, method=po.RK4, max_steps=5_000_000)
+        for k, v in frame_fixture(R, sc, w, h, ext).items():
+            out[f"f{i}_{k}"] = v
+    dp = C.POINTER(C.c_double)
+    lib.ref_eht_render.argtypes = [C.c_double] * 3 + [C.c_int] + [C.c_double] * 2 + [dp, C.c_int, dp,
+                                                                                        C.POINTER(C.c_ubyte)]
+    lib.ref_eht_render.restype = None
+    a, inc, hw, size = NAKED_EHT
+    flow = np.array(EHT_FLOW)
+    inten = np.zeros(size * size)
+    shadow = np.zeros(size * size, np.uint8)
+    t = time.time()
+    lib.ref_eht_render(a, np.deg2rad(inc), hw, size, 230e9, M87_MASS, po._ptr(flow), os.cpu_count() or 1,
+                       po._ptr(inten), shadow.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    print(f"  eht {size}x{size} at a = {a} in {time.time() - t:.1f} s, shadow px {shadow.sum()}")
+    out.update(eht_view=np.array(NAKED_EHT), eht_flow=flow, eht_intensity=inten, eht_shadow=shadow)
+    return out
+
+
 def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
     t = time.time()
     out = R.trace_frame(sc, w, h, *ext)
-    print(f"  traced {w}x{h} in {time.time() - t:.1f} s, outcomes {np.bincount(out['outcome'], minlength=4)}")
+    print(f"  traced {w}x{h} in {time.time() - t:.1f} s, outcomes {np.bincount(out['outcome'], minlength=6)}")
     return dict(outcome=out["outcome"].astype(np.uint8), r_disk=out["r_disk"], phi_disk=out["phi_disk"],
                 g=out["g"], theta_inf=out["theta_inf"], phi_inf=out["phi_inf"], steps=out["steps"],
                 width=w, height=h, extents=np.array(ext),
@@ -299,6 +341,10 @@ def frame_fixture(R: po.Oracle, sc: po.Scene, w, h, ext) -> dict:
 def main() -> None:
     po.build(reference=True)
     R = po.Oracle(reference=True)
+    print("naked_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "naked_ref.npz"), **naked_fixture(R))
+    if os.environ.get("NAKED_ONLY"):
+        return
     print("steps_ref.npz")
     np.savez_compressed(os.path.join(HERE, "steps_ref.npz"), **steps_fixture(R))
     print("trajectory_ref.npz")

