@@ -85,7 +85,9 @@ struct bhk_context {
     uint16_t* key = nullptr;
     float4* cf = nullptr;
     float2* vf = nullptr;
-    size_t cap_cf = 0, cap_vf = 0;
+    float4* kf = nullptr;
+    float2* khf = nullptr;
+    size_t cap_cf = 0, cap_vf = 0, cap_kf = 0, cap_khf = 0;
     int32_t* order = nullptr;
     Rescue* rescue = nullptr;
     RayGeom* geom = nullptr;
@@ -153,6 +155,7 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.p.tol0_f = static_cast<float>(r.p.tol0);
     r.block = o->block > 0 ? o->block : (ctx->tuned_block[pi] ? ctx->tuned_block[pi] : 128);
     r.chunk = o->chunk > 0 ? o->chunk : (ctx->tuned_chunk[pi] ? ctx->tuned_chunk[pi] : 32);
+    r.chunk = (std::max(r.chunk, 32) + 31) / 32 * 32;  // whole batches of 32 (one per lane)
     r.buckets = o->sort_buckets > 0 ? o->sort_buckets : (ctx->tuned_buckets[pi] ? ctx->tuned_buckets[pi] : 64);
     r.buckets = std::min(r.buckets, kMaxBuckets);
     r.p.chunk = r.chunk;
@@ -179,12 +182,14 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     if (e == cudaSuccess) e = grow(&c->key, &c->cap_key, rays);
     if (e == cudaSuccess) e = grow(&c->cf, &c->cap_cf, rays);
     if (e == cudaSuccess) e = grow(&c->vf, &c->cap_vf, rays);
+    if (e == cudaSuccess) e = grow(&c->kf, &c->cap_kf, rays);
+    if (e == cudaSuccess) e = grow(&c->khf, &c->cap_khf, rays);
     if (e == cudaSuccess) e = grow(&c->order, &c->cap_order, rays);
     if (e == cudaSuccess) e = grow(&c->rescue, &c->cap_rescue, rc);
     if (e == cudaSuccess) e = grow(&c->geom, &c->cap_geom, geoms);
     if (e == cudaSuccess) e = grow(&c->frames_dev, &c->cap_frames, frames);
     if (e != cudaSuccess) return fail(BHK_ENOMEM, std::string("scratch allocation: ") + cudaGetErrorString(e));
-    c->cap_rays = std::min({c->cap_E, c->cap_order, c->cap_key, c->cap_cf, c->cap_vf});
+    c->cap_rays = std::min({c->cap_E, c->cap_order, c->cap_key, c->cap_cf, c->cap_vf, c->cap_kf, c->cap_khf});
     if (frames > c->cap_frames_host) {
         if (c->frames_host) cudaFreeHost(c->frames_host);
         c->frames_host = nullptr;
@@ -195,7 +200,9 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     return BHK_OK;
 }
 
-LaunchSoA soa(bhk_context* c) { return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf}; }
+LaunchSoA soa(bhk_context* c) {
+    return LaunchSoA{c->E, c->L, c->Q, c->vr, c->vth, c->gid, c->key, c->cf, c->vf, c->kf, c->khf};
+}
 
 struct Batch {
     int mode;  // 0 frames, 1 explicit, 2 a list of pixels of the frames (ex[0] = the device list),
@@ -206,12 +213,18 @@ struct Batch {
     double r_in, r_out;
 };
 
+constexpr bool kTileOrder = true;
+
 // Enqueues the whole pipeline on stream s (also used while capturing a graph).
 bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outputs& out, bool timed,
                    cudaStream_t s) {
     BHK_CUDA(cudaMemsetAsync(c->ctl, 0, sizeof(Control), s));
     const int lgrid = c->num_sms * 8;
     LaunchSoA L = soa(c);
+    if (r.fp64) {  // the FP32 start is for the FP32 tracer only
+        L.kf = nullptr;
+        L.khf = nullptr;
+    }
     if (b.mode == 0) {
         BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
                                  s));
@@ -223,8 +236,8 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
         // The set-up writes the frames' pixel total; the batch is the list.
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
-        launch_rays_list(c->frames_dev, b.nframes, static_cast<const int32_t*>(static_cast<const void*>(b.ex[0])), L,
-                         r.p, c->ctl, lgrid, s);
+        launch_rays_list(c->frames_dev, c->geom, b.nframes,
+                         static_cast<const int32_t*>(static_cast<const void*>(b.ex[0])), L, r.p, c->ctl, lgrid, s);
     } else if (b.mode == 3) {
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
         launch_rays_framed(b.ex[0], b.ex[1], b.ex[2], b.ex[3], reinterpret_cast<const bhk_frame*>(b.ex[4]), b.ex[5],
@@ -238,6 +251,9 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
     if (r.buckets > 1) {
         BHK_CUDA(cudaMemsetAsync(c->hist, 0, sizeof(unsigned) * kMaxBuckets, s));
         launch_sort(L, SortScratch{c->hist, c->offs, c->order}, r.p, c->ctl, lgrid, s);
+        order = c->order;
+    } else if (b.mode == 0 && kTileOrder) {  // frames: warps take compact 8 x 4 patches of pixels
+        launch_tile_order(c->frames_dev, b.nframes, c->order, c->ctl, lgrid, s);
         order = c->order;
     }
     if (timed) BHK_CUDA(cudaEventRecord(c->ev0, s));
@@ -697,7 +713,7 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
     o.use_graph = 0;
     const int pi = o.precision == BHK_PREC_FP64 ? 0 : 1;
     const int blocks[] = {64, 128, 256};
-    const int chunks[] = {1, 32, 256};
+    const int chunks[] = {32, 256};
     const int buckets[] = {1, 64, 512};
     const int budgets[] = {3, 1, 2};
     const bhk_rays_out out = own_outputs(c);

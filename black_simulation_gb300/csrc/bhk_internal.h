@@ -46,6 +46,11 @@ struct LaunchSoA {
     uint16_t* key;                // cost bucket for the pre-sort
     float4* cf;
     float2* vf;
+    // FP32 runs only (nullptr otherwise): the FP32 tracer's first step, prepared by the launch kernel
+    // so that a lane picking up a ray does no arithmetic on its own -- the right-hand side at the
+    // launch point (k[0..3] in kf, k[4] and the first step h in khf).
+    float4* kf;
+    float2* khf;
 };
 
 // Small control block reset at the start of every batch.
@@ -96,7 +101,8 @@ void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int
                         Control* ctl, cudaStream_t s);
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s);
-void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, LaunchSoA L, const TraceParams& p,
+void launch_rays_list(const FrameDev* frames, const RayGeom* geom, int nframes, const int32_t* list, LaunchSoA L,
+                      const TraceParams& p,
                       const Control* ctl, int grid, cudaStream_t s);
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
                           const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
@@ -106,6 +112,8 @@ void launch_rays_framed(const double* a, const double* r, const double* th, cons
                         const double* look, double r_in, double r_out, RayGeom* geom, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s);
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
+void launch_tile_order(const FrameDev* frames, int nframes, int32_t* order, const Control* ctl, int grid,
+                       cudaStream_t s);
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
                   cudaStream_t s);

@@ -33,7 +33,7 @@ constexpr int kMaxDevices = 64;
 
 // Layout of the working memory inside the static array (offsets, 256-byte aligned).
 struct Layout {
-    size_t ctl, hist, offs, frames, geom, E, L, Q, vr, vth, gid, key, order, cf, vf, rescue, total;
+    size_t ctl, hist, offs, frames, geom, E, L, Q, vr, vth, gid, key, order, cf, vf, kf, khf, rescue, total;
 };
 
 constexpr size_t up256(size_t x) { return (x + 255) / 256 * 256; }
@@ -56,6 +56,8 @@ constexpr Layout make_layout() {
     l.order = o; o = up256(o + sizeof(int32_t) * kStaticMaxRays);
     l.cf = o; o = up256(o + sizeof(float4) * kStaticMaxRays);
     l.vf = o; o = up256(o + sizeof(float2) * kStaticMaxRays);
+    l.kf = o; o = up256(o + sizeof(float4) * kStaticMaxRays);
+    l.khf = o; o = up256(o + sizeof(float2) * kStaticMaxRays);
     l.rescue = o; o = up256(o + sizeof(Rescue) * kStaticRescue);
     l.total = o;
     return l;
@@ -150,7 +152,7 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
                   : (o.pole_step_frac < 0.0 ? 0.0f
                      : static_cast<float>(std::fmin(0.5, 0.1 * std::pow(p.rtol / 1e-6, 0.2))));
     int block = o.block > 0 ? std::min(o.block, 256) : 128;
-    p.chunk = o.chunk > 0 ? o.chunk : 32;
+    p.chunk = ((o.chunk > 32 ? o.chunk : 32) + 31) / 32 * 32;  // whole batches of 32 (one per lane)
     p.buckets = std::min(o.sort_buckets > 0 ? o.sort_buckets : 1, kMaxBuckets);
     const int rb = o.reg_budget > 0 ? o.reg_budget : 2;
     const int regcap = (fp64 || rb >= 3) ? 0 : rb;
@@ -164,7 +166,9 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
                 reinterpret_cast<double*>(base + kLayout.Q), reinterpret_cast<double*>(base + kLayout.vr),
                 reinterpret_cast<double*>(base + kLayout.vth), reinterpret_cast<int32_t*>(base + kLayout.gid),
                 reinterpret_cast<uint16_t*>(base + kLayout.key), reinterpret_cast<float4*>(base + kLayout.cf),
-                reinterpret_cast<float2*>(base + kLayout.vf)};
+                reinterpret_cast<float2*>(base + kLayout.vf),
+                fp64 ? nullptr : reinterpret_cast<float4*>(base + kLayout.kf),
+                fp64 ? nullptr : reinterpret_cast<float2*>(base + kLayout.khf)};
     SortScratch S{reinterpret_cast<unsigned*>(base + kLayout.hist), reinterpret_cast<unsigned*>(base + kLayout.offs),
                   reinterpret_cast<int32_t*>(base + kLayout.order)};
     Rescue* rescue = reinterpret_cast<Rescue*>(base + kLayout.rescue);

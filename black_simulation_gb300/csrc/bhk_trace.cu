@@ -28,12 +28,6 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ unsigned lanemask_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
 __device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ULL); }
 
 __device__ __forceinline__ double wrap_2pi(double x) {
@@ -79,15 +73,44 @@ __device__ __forceinline__ uint16_t cost_key(double E, double L, double Q, int b
     return static_cast<uint16_t>(k < 0 ? 0 : (k >= buckets ? buckets - 1 : k));
 }
 
-__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, double a, double E, double Lz, double Q,
-                                             double vr, double vth, int32_t gid, int buckets) {
+// kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
+// first step of the backward march. Lengths are r, or past |a| = 1 max(sqrt(Sigma), 0.02).
+template <typename T>
+__device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol, T a2, bool nkd) {
+    T sn, cs;
+    Math<T>::sc(y[1], &sn, &cs);
+    sn = fabs(sn);
+    const T rs = nkd ? fmax(sqrt(y[0] * y[0] + a2 * cs * cs), T(0.02)) : y[0];
+    const T t = tol * fmin(fmax(rs / T(8), T(1)), T(4));
+    T h = t / (fabs(k[0]) / rs + fabs(k[1]) / fmax(sn, T(1e-4)) + fabs(k[2]) + T(1e-6));
+    h = fmin(h, sqrt(t * rs / (fabs(k[3]) + T(1e-6))));
+    h = fmin(h, sqrt(t * fmax(sn, T(1e-4)) / (fabs(k[4]) + T(1e-6))));
+    return -h;
+}
+
+// The launch record of ray i. For FP32 runs also the FP32 tracer's start: the right-hand side at the
+// launch point and the first step, from exactly the FP32 values the tracer starts from.
+__device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, const RayGeom& g, double E, double Lz, double Q,
+                                             double vr, double vth, int32_t gid, const TraceParams& p) {
     L.E[i] = E; L.L[i] = Lz; L.Q[i] = Q;
     L.vr[i] = vr; L.vth[i] = vth;
     L.geom_id[i] = gid;
-    L.key[i] = cost_key(E, Lz, Q, buckets);
-    const double x = Lz - a * E;
-    L.cf[i] = make_float4(float(E), float(Lz), float(Q), float(x * x + Q));
-    L.vf[i] = make_float2(float(vr), float(vth));
+    L.key[i] = cost_key(E, Lz, Q, p.buckets);
+    const double x = Lz - g.a * E;
+    const float4 cf = make_float4(float(E), float(Lz), float(Q), float(x * x + Q));
+    const float2 vf = make_float2(float(vr), float(vth));
+    L.cf[i] = cf;
+    L.vf[i] = vf;
+    if (L.kf) {
+        RayC<float> c;
+        c.set_t(g.af, cf.x, cf.y, cf.z, cf.w);
+        const float y[5] = {g.r0f, g.th0f, g.ph0f, vf.x, g.south0 ? -vf.y : vf.y};
+        float k[5];
+        rhs(c, y, k);
+        const float h = first_step<float>(y, k, p.tol0_f, c.a2, g.naked != 0);
+        L.kf[i] = make_float4(k[0], k[1], k[2], k[3]);
+        L.khf[i] = make_float2(k[4], h);
+    }
 }
 
 // ------------------------------------------------------------------------- set-up kernels ----
@@ -141,8 +164,9 @@ __device__ __forceinline__ double rsqrt_newton(double x) {
 // kerr::photonFromFrame for pixel (alpha, beta) of a ZAMO pinhole, with the camera's metric
 // contractions precomputed: p_mu = (g e_0)_mu - look^i (g e_i)_mu, p^r = e_0^r - look^i e_i^r.
 // Launch record i for global pixel `pix` of the frame table (binary search over frame offsets).
-__device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, int nframes, long long pix,
-                                             long long i, LaunchSoA& L, const TraceParams& p) {
+__device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
+                                             int nframes, long long pix, long long i, LaunchSoA& L,
+                                             const TraceParams& p) {
     int lo = 0, hi = nframes - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -171,24 +195,25 @@ __device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames
         Lz = 0.0;
         Q = vth * vth - f.cs2 * a2E2;
     }
-    store_launch(L, i, f.d.a, E, Lz, Q, vr, vth, lo, p.buckets);
+    store_launch(L, i, geom[lo], E, Lz, Q, vr, vth, lo, p);
 }
 
-__global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, int nframes, LaunchSoA L, TraceParams p,
-                                     const Control* __restrict__ ctl) {
+__global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
+                                     int nframes, LaunchSoA L, TraceParams p, const Control* __restrict__ ctl) {
     const long long n = ctl->n_rays;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x)
-        launch_pixel(frames, nframes, i, i, L, p);
+        launch_pixel(frames, geom, nframes, i, i, L, p);
 }
 
 // Launch records for a list of global pixel indices (record i traces pixel list[i]).
-__global__ void launch_list_kernel(const FrameDev* __restrict__ frames, int nframes, const int32_t* __restrict__ list,
-                                   LaunchSoA L, TraceParams p, const Control* __restrict__ ctl) {
+__global__ void launch_list_kernel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom, int nframes,
+                                   const int32_t* __restrict__ list, LaunchSoA L, TraceParams p,
+                                   const Control* __restrict__ ctl) {
     const long long n = ctl->n_rays;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x)
-        launch_pixel(frames, nframes, list[i], i, L, p);
+        launch_pixel(frames, geom, nframes, list[i], i, L, p);
 }
 
 __global__ void launch_explicit_kernel(const double* __restrict__ a, const double* __restrict__ r_obs,
@@ -208,8 +233,9 @@ __global__ void launch_explicit_kernel(const double* __restrict__ a, const doubl
         Cons c;
         St s;
         photon_from_frame(ai, ri, ti, 0.0, e, look, c, s);
-        geom[i] = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
-        store_launch(L, i, ai, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
+        const RayGeom g = make_geom(ai, ri, ti, 0.0, r_in, r_out, p);
+        geom[i] = g;
+        store_launch(L, i, g, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p);
     }
 }
 
@@ -235,7 +261,7 @@ __global__ void launch_framed_kernel(const double* __restrict__ a, const double*
         RayGeom g = make_geom(ai, ri, ti, pi, r_in, r_out, p);
         g.dead = (ri < g.rp && 2.0 * g.rp * c.E - ai * c.L < 0.0) ? 1 : 0;
         geom[i] = g;
-        store_launch(L, i, ai, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p.buckets);
+        store_launch(L, i, g, c.E, c.L, c.Q, s.vr, s.vtheta, static_cast<int32_t>(i), p);
     }
 }
 
@@ -376,21 +402,6 @@ __device__ __forceinline__ void ks_position(double a, double r, double th, doubl
     out[2] = r * ct;
 }
 
-// kerr::photonStepSize (src/kerr.cpp:563-575) from derivatives already evaluated, negated: the
-// first step of the backward march. Lengths are r, or past |a| = 1 max(sqrt(Sigma), 0.02).
-template <typename T>
-__device__ __forceinline__ T first_step(const T y[5], const T k[5], T tol, T a2, bool nkd) {
-    T sn, cs;
-    Math<T>::sc(y[1], &sn, &cs);
-    sn = fabs(sn);
-    const T rs = nkd ? fmax(sqrt(y[0] * y[0] + a2 * cs * cs), T(0.02)) : y[0];
-    const T t = tol * fmin(fmax(rs / T(8), T(1)), T(4));
-    T h = t / (fabs(k[0]) / rs + fabs(k[1]) / fmax(sn, T(1e-4)) + fabs(k[2]) + T(1e-6));
-    h = fmin(h, sqrt(t * rs / (fabs(k[3]) + T(1e-6))));
-    h = fmin(h, sqrt(t * fmax(sn, T(1e-4)) / (fabs(k[4]) + T(1e-6))));
-    return -h;
-}
-
 template <typename T>
 __device__ __forceinline__ void lane_radii(Lane<T>& s, const RayGeom& g) {
     if constexpr (sizeof(T) == 4) {
@@ -398,6 +409,28 @@ __device__ __forceinline__ void lane_radii(Lane<T>& s, const RayGeom& g) {
     } else {
         s.r_cap = g.r_cap; s.r_esc = g.r_esc; s.r_in = g.r_in; s.r_out = g.r_out; s.zone_top = g.zone_top;
     }
+}
+
+// Starts an FP32 lane at its launch point from its launch record; the right-hand side there and the
+// first step come prepared by the launch kernel when `have_k`, else are computed here.
+__device__ __forceinline__ void lane_begin_f32(Lane<float>& s, const RayGeom& g, float4 cf, float2 vf, float4 k,
+                                               float2 kh, bool have_k, const TraceParams& p) {
+    s.c.set_t(g.af, cf.x, cf.y, cf.z, cf.w);
+    s.south = g.south0 != 0;
+    s.y[0] = g.r0f; s.y[1] = g.th0f; s.y[2] = g.ph0f; s.y[3] = vf.x; s.y[4] = s.south ? -vf.y : vf.y;
+    lane_radii(s, g);
+    s.rmin = s.y[0];
+    s.t = 0.0;
+    s.swept = 0.0;
+    s.track = false;
+    if (have_k) {
+        s.k[0][0] = k.x; s.k[0][1] = k.y; s.k[0][2] = k.z; s.k[0][3] = k.w; s.k[0][4] = kh.x;
+        s.h = kh.y;
+    } else {
+        rhs(s.c, s.y, s.k[0]);
+        s.h = first_step<float>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
+    }
+    s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
 // Starts a lane on ray `ray` at its launch point, first step from kerr::photonStepSize.
@@ -423,12 +456,19 @@ __device__ __forceinline__ void lane_begin_launch(Lane<T>& s, const RayGeom& g, 
         s.track = true;
         rhs(s.c, s.y, s.k[0], static_cast<Proj<T>*>(nullptr), &s.kt[0]);
         ks_position(g.a, s.y[0], s.y[1], s.y[2], s.pos);
+        s.h = first_step<T>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
     } else {
         s.track = false;
-        rhs(s.c, s.y, s.k[0]);
+        if (L.kf) {  // prepared by the launch kernel
+            const float4 k = L.kf[ray];
+            const float2 kh = L.khf[ray];
+            s.k[0][0] = k.x; s.k[0][1] = k.y; s.k[0][2] = k.z; s.k[0][3] = k.w; s.k[0][4] = kh.x;
+            s.h = kh.y;
+        } else {
+            rhs(s.c, s.y, s.k[0]);
+            s.h = first_step<T>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
+        }
     }
-    if constexpr (sizeof(T) == 4) s.h = first_step<T>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
-    else s.h = first_step<T>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
@@ -719,17 +759,22 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         }
     }
     const bool falling = s.y[0] < prev[0];
-    // Past |a| = 1 only (r stays above r_+ > 1 around a hole): the ring singularity, where
-    // Sigma = r^2 + a^2 cos^2(theta) vanishes (shaders/trace.frag:1773-1778; cos^2 is the same in either
-    // hemisphere representation).
+    // Past |a| = 1 only (around a hole r stays above r_+ > 1): the ring singularity, where
+    // Sigma = r^2 + a^2 cos^2(theta) < 4e-4 (shaders/trace.frag:1773-1778). That needs |r| < 0.02 and
+    // |cos theta| < 0.02 / |a|, where cos theta = sin d, d = pi/2 - theta, is d - d^3/6 to 3e-11 (the
+    // same in either hemisphere representation).
     if (fabs(s.y[0]) < T(0.02)) {
-        T sn, cs;
-        Math<T>::sc(s.y[1], &sn, &cs);
-        if (s.y[0] * s.y[0] + s.c.a2 * cs * cs < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
+        const T d = T(0.5 * kPi) - s.y[1];
+        const T c = d - d * d * d * T(1.0 / 6.0);
+        if (s.y[0] * s.y[0] + s.c.a2 * c * c < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
     }
+    // Escaped: rising past r_esc, or past |a| = 1 falling past -r_esc into the sky of the r < 0 region,
+    // beyond the ring (shaders/trace.frag:1779-1792).
+    const bool beyond = falling && s.y[0] < -s.r_esc;
+    if (beyond || (!falling && s.y[0] > s.r_esc))
+        return escape(s, prev, h, beyond ? -s.r_esc : s.r_esc, beyond ? BHK_RAY_ESCAPED_BEYOND : BHK_RAY_ESCAPED, out,
+                      ray, t_prev);
     if (falling) {
-        // Past |a| = 1: gone far out into the r < 0 region, beyond the ring (shaders/trace.frag:1779-1786).
-        if (s.y[0] < -s.r_esc) return escape(s, prev, h, -s.r_esc, BHK_RAY_ESCAPED_BEYOND, out, ray, t_prev);
         if (s.y[0] < s.r_cap) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
         if (s.y[0] < s.zone_top) {
             if constexpr (F64) {
@@ -744,8 +789,6 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 return kRescue;
             }
         }
-    } else if (s.y[0] > s.r_esc) {
-        return escape(s, prev, h, s.r_esc, BHK_RAY_ESCAPED, out, ray, t_prev);
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
     // carrying the FSAL derivative: under theta -> -theta (or 2 pi - theta) Theta'(theta) changes sign.
@@ -836,16 +879,19 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
              Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl) {
     const int lane = threadIdx.x & 31;
     const long long n = ctl->n_rays;
-    const unsigned lt = lanemask_lt();
     Lane<T> s;
     long long ray = -1;
     bool exhausted = false;
-    long long pool_pos = 0, pool_end = 0;
+    int pool_pos = 0, pool_end = 0;  // this warp's chunk of the queue (a batch holds < 2^31 rays)
     unsigned long long n_acc = 0, n_rej = 0;
     int iter = 0;
     for (;;) {
-        unsigned need = __ballot_sync(kFull, ray < 0);
-        while (need && !exhausted) {
+        // A warp traces its rays in batches of 32 queue-adjacent rays -- neighbouring pixels, or rays
+        // of one cost bucket -- and takes the next batch only when every lane's ray has ended. Rays
+        // that start together stay alike (similar step sizes, events and branches) for their whole
+        // path; refilling lanes one by one mixes rays at different stages within the warp, and the
+        // divergence that follows costs more than the lanes that wait for their batch's last ray.
+        while (!exhausted && !__any_sync(kFull, ray >= 0)) {
             if (pool_pos >= pool_end) {
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(&ctl->queue, static_cast<unsigned long long>(p.chunk));
@@ -854,24 +900,26 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                     exhausted = true;
                     break;
                 }
-                pool_pos = static_cast<long long>(base);
-                pool_end = pool_pos + p.chunk < n ? pool_pos + p.chunk : n;
+                pool_pos = static_cast<int>(base);
+                pool_end = static_cast<int>(base + p.chunk < static_cast<unsigned long long>(n) ? base + p.chunk : n);
             }
-            const int avail = static_cast<int>(pool_end - pool_pos);
-            const int rank = __popc(need & lt);
-            if (((need >> lane) & 1u) && rank < avail) {
-                const long long q = pool_pos + rank;
+            const int q = pool_pos + lane;
+            if (q < pool_end) {
                 ray = order ? order[q] : q;
                 const RayGeom& G = geom[L.geom_id[ray]];
-                lane_begin_launch(s, G, L, ray, p);
+                if constexpr (sizeof(T) == 4) {
+                    const float4 k = L.kf ? L.kf[ray] : float4{};
+                    const float2 kh = L.khf ? L.khf[ray] : float2{};
+                    lane_begin_f32(s, G, L.cf[ray], L.vf[ray], k, kh, L.kf != nullptr, p);
+                } else {
+                    lane_begin_launch(s, G, L, ray, p);
+                }
                 if (G.dead) {  // seen from inside the horizon: the hole, with no step taken
                     finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
                     ray = -1;
                 }
             }
-            const int served = __popc(need) < avail ? __popc(need) : avail;
-            pool_pos += served;
-            need = __ballot_sync(kFull, ray < 0);
+            pool_pos = pool_pos + 32 < pool_end ? pool_pos + 32 : pool_end;
         }
         if (!__any_sync(kFull, ray >= 0)) break;
         ++iter;
@@ -987,8 +1035,7 @@ void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int
 
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s) {
-    (void)geom;
-    launch_frames_kernel<<<grid, 128, 0, s>>>(frames, nframes, L, p, ctl);
+    launch_frames_kernel<<<grid, 128, 0, s>>>(frames, geom, nframes, L, p, ctl);
 }
 
 void launch_rays_framed(const double* a, const double* r, const double* th, const double* ph, const bhk_frame* frames,
@@ -997,9 +1044,9 @@ void launch_rays_framed(const double* a, const double* r, const double* th, cons
     launch_framed_kernel<<<grid, 128, 0, s>>>(a, r, th, ph, frames, look, r_in, r_out, geom, L, p, ctl);
 }
 
-void launch_rays_list(const FrameDev* frames, int nframes, const int32_t* list, LaunchSoA L, const TraceParams& p,
-                      const Control* ctl, int grid, cudaStream_t s) {
-    launch_list_kernel<<<grid, 128, 0, s>>>(frames, nframes, list, L, p, ctl);
+void launch_rays_list(const FrameDev* frames, const RayGeom* geom, int nframes, const int32_t* list, LaunchSoA L,
+                      const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
+    launch_list_kernel<<<grid, 128, 0, s>>>(frames, geom, nframes, list, L, p, ctl);
 }
 
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
@@ -1007,6 +1054,37 @@ void launch_rays_explicit(const double* a, const double* r_obs, const double* th
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
     (void)r_escape;
     launch_explicit_kernel<<<grid, 128, 0, s>>>(a, r_obs, th_obs, alpha, beta, r_in, r_out, geom, L, p, ctl);
+}
+
+// Queue order of the frames' pixels by tiles of 8 x 4 (ragged at the right and bottom edges), so that
+// a warp's batch of 32 rays is a compact patch of the image rather than a strip of one row:
+// order[q(p)] = p with q(p) = 4 ty W + hh 8 tx + (y - 4 ty) ww + (x - 8 tx) for pixel p = (x, y) of a
+// W x H frame, tile (tx, ty) = (x / 8, y / 4), hh and ww its height and width.
+__global__ void tile_order_kernel(const FrameDev* __restrict__ frames, int nframes, int32_t* order,
+                                  const Control* __restrict__ ctl) {
+    const long long n = ctl->n_rays;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = nframes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
+        }
+        const FrameDev& f = frames[lo];
+        const int W = f.d.width, H = f.d.height;
+        const int local = static_cast<int>(i - f.offset);
+        const int y = local / W, x = local - y * W;
+        const int ty = y >> 2, tx = x >> 3;
+        const int hh = H - 4 * ty < 4 ? H - 4 * ty : 4;
+        const int ww = W - 8 * tx < 8 ? W - 8 * tx : 8;
+        const long long q = f.offset + 4LL * ty * W + static_cast<long long>(hh) * 8 * tx + (y - 4 * ty) * ww + (x - 8 * tx);
+        order[q] = static_cast<int32_t>(i);
+    }
+}
+
+void launch_tile_order(const FrameDev* frames, int nframes, int32_t* order, const Control* ctl, int grid,
+                       cudaStream_t s) {
+    tile_order_kernel<<<grid, 256, 0, s>>>(frames, nframes, order, ctl);
 }
 
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {

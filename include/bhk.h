@@ -122,7 +122,9 @@ typedef struct {
     int32_t reproject_every;/* mixed: besides the FP32 re-projection every step, an FP64 radial one every N
                                iterations of a warp (results then depend on the launch shape); 0 = off */
     int32_t block;          /* threads per block of the tracer; 0 -> autotuned or 128 */
-    int32_t chunk;          /* rays a warp takes from the queue at a time; 0 -> autotuned or 32 */
+    int32_t chunk;          /* rays a warp takes from the queue at a time, traced in batches of 32 (one
+                               per lane; the next batch starts when all 32 have ended); rounded up to a
+                               multiple of 32; 0 -> autotuned or 32 */
     int32_t sort_buckets;   /* rays pre-sorted into this many cost buckets; 0 -> autotuned or 64; 1 = none */
     int32_t use_graph;      /* 1: replay the whole batch as one captured CUDA graph */
     int32_t reg_budget;     /* mixed tracer variant: 0 autotuned (else uncapped), 1: <= 102 registers per
