@@ -59,12 +59,12 @@ struct GraphKey {
 };
 
 // FP32 FLOPs of one Dormand-Prince attempt of the mixed tracer, counted from the source (an FMA is 2):
-//   right-hand side (bhk_device.cuh rhs<float>): sine/cosine 27 (12 FMA, 2 MUL, 1 ADD), Delta and
-//     r^2 + a^2 4, P 2, inflow 5, R'/2 5, 1/sin powers 2, Theta'/2 5, dphi 4 -> 55, x 6 stages = 330;
-//     the FSAL stage's constraint potentials 18;
-//   stage sums y + h sum a_ij k_j over 5 components: 15 + 25 + 35 + 45 + 55 + 55 = 230;
-//   error estimate and weighted norm: 5 x 17 = 85;  step control and pole cap: 8.
-constexpr double kFlopsPerStep = 671.0;
+//   right-hand side (bhk_device.cuh rhs<float>): sine/cosine 23 (10 FMA, 2 MUL, 1 ADD), Delta and
+//     r^2 + a^2 4, P 2, inflow 4, 1/sin powers 2, dphi 3, R'/2 4, Theta'/2 4 -> 46, x 6 stages = 276;
+//     the FSAL stage's constraint potentials 15;
+//   stage sums y + h sum a_ij k_j over 5 components: 20 products h a_ij and 100 FMA = 220;
+//   error estimate and weighted norm: 5 x 16 + 2 = 82;  step control and pole cap: 8.
+constexpr double kFlopsPerStep = 601.0;
 
 }  // namespace
 
@@ -213,8 +213,6 @@ struct Batch {
     double r_in, r_out;
 };
 
-constexpr bool kTileOrder = true;
-
 // Enqueues the whole pipeline on stream s (also used while capturing a graph).
 bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outputs& out, bool timed,
                    cudaStream_t s) {
@@ -252,7 +250,7 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         BHK_CUDA(cudaMemsetAsync(c->hist, 0, sizeof(unsigned) * kMaxBuckets, s));
         launch_sort(L, SortScratch{c->hist, c->offs, c->order}, r.p, c->ctl, lgrid, s);
         order = c->order;
-    } else if (b.mode == 0 && kTileOrder) {  // frames: warps take compact 8 x 4 patches of pixels
+    } else if (b.mode == 0) {  // frames: warps take compact 4 x 8 patches of pixels
         launch_tile_order(c->frames_dev, b.nframes, c->order, c->ctl, lgrid, s);
         order = c->order;
     }

@@ -670,11 +670,11 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if constexpr (F64) {
             e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] + T(DP::e5) * s.k[4][i] +
                      T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
-        } else {
-            e = h * fmaf(T(DP::e7), s.k[6][i],
-                         fmaf(T(DP::e6), s.k[5][i],
-                              fmaf(T(DP::e5), s.k[4][i],
-                                   fmaf(T(DP::e4), s.k[3][i], fmaf(T(DP::e3), s.k[2][i], T(DP::e1) * s.k[0][i])))));
+        } else {  // without the factor h, applied once to the sum below
+            e = fmaf(T(DP::e7), s.k[6][i],
+                     fmaf(T(DP::e6), s.k[5][i],
+                          fmaf(T(DP::e5), s.k[4][i],
+                               fmaf(T(DP::e4), s.k[3][i], fmaf(T(DP::e3), s.k[2][i], T(DP::e1) * s.k[0][i])))));
         }
         const T sc = rtol + rtol * fmax(fabs(s.y[i]), fabs(y5[i]));
         const T q = Math<T>::div(e, sc);
@@ -688,7 +688,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         e2 = err;
         ok = err <= T(1);
     } else {
-        e2 = acc * T(0.2);
+        e2 = acc * (T(0.2) * h * h);
         err = e2;
         ok = e2 <= T(1);
     }
@@ -1056,10 +1056,12 @@ void launch_rays_explicit(const double* a, const double* r_obs, const double* th
     launch_explicit_kernel<<<grid, 128, 0, s>>>(a, r_obs, th_obs, alpha, beta, r_in, r_out, geom, L, p, ctl);
 }
 
-// Queue order of the frames' pixels by tiles of 8 x 4 (ragged at the right and bottom edges), so that
+// Queue order of the frames' pixels by tiles of 4 x 8 (ragged at the right and bottom edges), so that
 // a warp's batch of 32 rays is a compact patch of the image rather than a strip of one row:
-// order[q(p)] = p with q(p) = 4 ty W + hh 8 tx + (y - 4 ty) ww + (x - 8 tx) for pixel p = (x, y) of a
-// W x H frame, tile (tx, ty) = (x / 8, y / 4), hh and ww its height and width.
+// order[q(p)] = p with q(p) = 8 ty W + hh 4 tx + (y - 8 ty) ww + (x - 4 tx) for pixel p = (x, y) of a
+// W x H frame, tile (tx, ty) = (x / 4, y / 8), hh and ww its height and width.
+constexpr int kTileW = 4, kTileH = 8;  // one warp's batch
+
 __global__ void tile_order_kernel(const FrameDev* __restrict__ frames, int nframes, int32_t* order,
                                   const Control* __restrict__ ctl) {
     const long long n = ctl->n_rays;
@@ -1074,10 +1076,11 @@ __global__ void tile_order_kernel(const FrameDev* __restrict__ frames, int nfram
         const int W = f.d.width, H = f.d.height;
         const int local = static_cast<int>(i - f.offset);
         const int y = local / W, x = local - y * W;
-        const int ty = y >> 2, tx = x >> 3;
-        const int hh = H - 4 * ty < 4 ? H - 4 * ty : 4;
-        const int ww = W - 8 * tx < 8 ? W - 8 * tx : 8;
-        const long long q = f.offset + 4LL * ty * W + static_cast<long long>(hh) * 8 * tx + (y - 4 * ty) * ww + (x - 8 * tx);
+        const int ty = y / kTileH, tx = x / kTileW;
+        const int hh = H - kTileH * ty < kTileH ? H - kTileH * ty : kTileH;
+        const int ww = W - kTileW * tx < kTileW ? W - kTileW * tx : kTileW;
+        const long long q = f.offset + static_cast<long long>(kTileH) * ty * W + static_cast<long long>(hh) * kTileW * tx +
+                            (y - kTileH * ty) * ww + (x - kTileW * tx);
         order[q] = static_cast<int32_t>(i);
     }
 }
