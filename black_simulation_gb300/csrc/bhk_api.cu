@@ -227,7 +227,8 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
                                  s));
         launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
-        launch_rays_frames(c->frames_dev, c->geom, b.nframes, L, r.p, c->ctl, lgrid, s);
+        // With the cost sort the keys are needed first; otherwise the trace kernel launches the rays.
+        if (r.buckets > 1) launch_rays_frames(c->frames_dev, c->geom, b.nframes, L, r.p, c->ctl, lgrid, s);
     } else if (b.mode == 2) {
         BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
                                  s));
@@ -255,8 +256,9 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         order = c->order;
     }
     if (timed) BHK_CUDA(cudaEventRecord(c->ev0, s));
+    const bool fused = b.mode == 0 && r.buckets <= 1;
     launch_trace(r.fp64, r.regcap, L, c->geom, order, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl,
-                 r.block, r.grid, s);
+                 r.block, r.grid, s, fused ? c->frames_dev : nullptr, fused ? b.nframes : 0);
     if (!r.fp64) launch_rescue(L, c->geom, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, s);
     if (timed) BHK_CUDA(cudaEventRecord(c->ev1, s));
     launch_constants_out(L, out, c->ctl, lgrid, s);

@@ -114,9 +114,12 @@ void launch_rays_framed(const double* a, const double* r, const double* th, cons
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
 void launch_tile_order(const FrameDev* frames, int nframes, int32_t* order, const Control* ctl, int grid,
                        cudaStream_t s);
+// With frames (frame batches traced in queue order without the cost sort), the trace kernel makes
+// each ray's launch record itself when it takes the ray; otherwise the records come from a launch
+// kernel run before it.
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
-                  cudaStream_t s);
+                  cudaStream_t s, const FrameDev* frames = nullptr, int nframes = 0);
 // energy, g_camera, b, q of every ray from its FP64 launch constants (if any is requested).
 void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s);
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,

@@ -876,7 +876,8 @@ __device__ __forceinline__ void push_rescue(Rescue* rescue, unsigned cap, Contro
 template <typename T, int kMinBlocks>
 __global__ void __launch_bounds__(kMinBlocks > 0 ? 128 : 256, kMinBlocks > 0 ? kMinBlocks : 1)
 trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __restrict__ order,
-             Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl) {
+             Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl,
+             const FrameDev* __restrict__ frames, int nframes) {
     const int lane = threadIdx.x & 31;
     const long long n = ctl->n_rays;
     Lane<T> s;
@@ -906,6 +907,10 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             const int q = pool_pos + lane;
             if (q < pool_end) {
                 ray = order ? order[q] : q;
+                // Frames: the launch record is made here, by the whole warp at once, so that its FP64
+                // arithmetic overlaps other warps' FP32 integration instead of taking a kernel of
+                // its own.
+                if (frames) launch_pixel(frames, geom, nframes, ray, ray, L, p);
                 const RayGeom& G = geom[L.geom_id[ray]];
                 if constexpr (sizeof(T) == 4) {
                     const float4 k = L.kf ? L.kf[ray] : float4{};
@@ -1097,7 +1102,8 @@ void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control
 }
 
 namespace {
-using TraceFn = void (*)(LaunchSoA, const RayGeom*, const int32_t*, Outputs, Rescue*, unsigned, TraceParams, Control*);
+using TraceFn = void (*)(LaunchSoA, const RayGeom*, const int32_t*, Outputs, Rescue*, unsigned, TraceParams, Control*,
+                         const FrameDev*, int);
 
 // Variant by precision and register cap (see trace_kernel).
 TraceFn trace_variant(bool fp64, int regcap) {
@@ -1110,8 +1116,9 @@ TraceFn trace_variant(bool fp64, int regcap) {
 
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
-                  cudaStream_t s) {
-    trace_variant(fp64, regcap)<<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl);
+                  cudaStream_t s, const FrameDev* frames, int nframes) {
+    trace_variant(fp64, regcap)<<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl, frames,
+                                                        nframes);
 }
 
 void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s) {
