@@ -600,6 +600,49 @@ bhk_status bhk_trace_frames_host(bhk_context* c, const bhk_frame_desc* frames, i
     for (double* p : hx) extras = extras || p;
     st = ensure_outputs(c, static_cast<size_t>(total), extras);
     if (st != BHK_OK) return st;
+    // Page-locked (or registered) host outputs are written by the kernels themselves, over the host
+    // link while the rays are traced; other host memory goes through device buffers and copies.
+    {
+        void* hp[15] = {host_out->outcome, host_out->r_disk, host_out->phi_disk, host_out->g, host_out->theta_inf,
+                        host_out->phi_inf, host_out->steps, host_out->rejected, hx[0], hx[1], hx[2], hx[3], hx[4],
+                        hx[5], hx[6]};
+        void* dp[15] = {};
+        bool all_mapped = true;
+        for (int i = 0; i < 15 && all_mapped; ++i) {
+            if (!hp[i]) continue;
+            cudaPointerAttributes a{};
+            if (cudaPointerGetAttributes(&a, hp[i]) != cudaSuccess) {
+                cudaGetLastError();
+                all_mapped = false;
+            } else if (a.type != cudaMemoryTypeHost || !a.devicePointer) {
+                all_mapped = false;
+            } else {
+                dp[i] = a.devicePointer;
+            }
+        }
+        if (all_mapped) {
+            bhk_rays_out direct{};
+            direct.outcome = static_cast<uint8_t*>(dp[0]);
+            direct.r_disk = static_cast<double*>(dp[1]);
+            direct.phi_disk = static_cast<double*>(dp[2]);
+            direct.g = static_cast<double*>(dp[3]);
+            direct.theta_inf = static_cast<double*>(dp[4]);
+            direct.phi_inf = static_cast<double*>(dp[5]);
+            direct.steps = static_cast<int32_t*>(dp[6]);
+            direct.rejected = static_cast<int32_t*>(dp[7]);
+            direct.energy = static_cast<double*>(dp[8]);
+            direct.g_camera = static_cast<double*>(dp[9]);
+            direct.b = static_cast<double*>(dp[10]);
+            direct.q = static_cast<double*>(dp[11]);
+            direct.r_min = static_cast<double*>(dp[12]);
+            direct.delay = static_cast<double*>(dp[13]);
+            direct.turns = static_cast<double*>(dp[14]);
+            st = trace_frames_locked(c, frames, nframes, opts, &direct, c->stream, true);
+            if (st != BHK_OK) return st;
+            BHK_CUDA(cudaStreamSynchronize(c->stream));
+            return c->ctl_host->stats[2] ? fail(BHK_EUNFINISHED, "some rays reached the step cap") : BHK_OK;
+        }
+    }
     const bhk_rays_out dev = own_outputs(c);
     bhk_rays_out use{};
     double** ux[7] = {&use.energy, &use.g_camera, &use.b, &use.q, &use.r_min, &use.delay, &use.turns};

@@ -177,6 +177,21 @@ def test_host_buffer_entry_point_and_step_cap(ctx):
     assert ctx.stats()["unfinished"] == np.sum(capped["outcome"] == bhk.UNFINISHED)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_host_entry_point_writes_pinned_buffers_directly(ctx, prec):
+    """Page-locked host outputs are written by the kernels themselves (no staging copies): the same
+    values as the device-buffer call, with and without the optional RayReport outputs."""
+    f = bhk.frame_c1(40, 24)
+    dev = host(ctx.trace_frames([f], bhk.TraceOpts(prec), out=bhk.alloc_outputs(f.rays, "cuda", extras=True)))
+    for extras in (False, True):
+        keys = bhk.FIELDS + (bhk.EXTRA_FIELDS if extras else ())
+        pinned = {k: torch.empty(f.rays, dtype=torch.from_numpy(dev[k]).dtype, pin_memory=True) for k in keys}
+        _, st = ctx.trace_frames_host([f], bhk.TraceOpts(prec), out=pinned)
+        assert st == bhk.OK
+        for k in keys:
+            np.testing.assert_array_equal(pinned[k].numpy(), dev[k], err_msg=k)
+
+
 def test_invalid_frames_are_rejected(ctx):
     with pytest.raises(bhk.BhkError) as e:
         ctx.trace_frames([bhk.Frame(1.0, 50, 1.0, 4, 4, -1, 1, -1, 1)], bhk.TraceOpts())  # extremal spin
