@@ -35,13 +35,13 @@ __device__ __forceinline__ float rcp_approx(float x) {
 __device__ __forceinline__ void sincos_fast(float x, float* s, float* c) {
     const float shifted = fmaf(x, 0.636619772367581343f, 12582912.0f);
     const int q = __float_as_int(shifted);
-    const float k = shifted - 12582912.0f;
+    const float k = __fsub_rn(shifted, 12582912.0f);
     float r = fmaf(k, -1.57079637050628662109375f, x);
     r = fmaf(k, 4.37113900018624283e-8f, r);
-    const float r2 = r * r;
+    const float r2 = __fmul_rn(r, r);
     float ps = fmaf(r2, -1.9515282645509862e-4f, 8.332160757714382e-3f);     // s7, s5
     ps = fmaf(r2, ps, -1.6666654609479015e-1f);                               // s3
-    const float sr = fmaf(r * r2, ps, r);
+    const float sr = fmaf(__fmul_rn(r, r2), ps, r);
     float pc = fmaf(r2, 2.4383566768620477e-5f, -1.3886681641998991e-3f);    // c8, c6
     pc = fmaf(r2, pc, 4.166662035693103e-2f);                                 // c4
     pc = fmaf(r2, pc, -4.9999999694474034e-1f);                               // c2
@@ -499,33 +499,35 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj
         //   dphi = a inflow - a E + L / sin^2,  Theta'/2 = cos (sin (-a^2 E^2) + sgn(sin) L^2 / |sin|^3).
         // Delta is not clamped away from 0: the FP32 tracer stays outside the capture zone, and a zero
         // there turns the state non-finite, which hands the ray to the FP64 continuation.
+        // Every operation is spelled out (fmaf or a rounded intrinsic) so that no compilation of this
+        // function contracts differently: the frame path and the launch kernel must agree bit for bit.
         const float r = y[0];
         float sn, cs;
         sincos_fast(y[1], &sn, &cs);
         const float rra = fmaf(r, r, c.a2);
         const float delta = fmaf(-2.0f, r, rra);
         const float P = fmaf(c.E, rra, -c.aL);
-        const bool opposite = P * y[3] < 0.0f;
-        const float num = opposite ? c.K : P + y[3];
-        const float den = opposite ? P - y[3] : delta;
-        const float inflow = num * rcp_approx(den);
+        const bool opposite = __fmul_rn(P, y[3]) < 0.0f;
+        const float num = opposite ? c.K : __fadd_rn(P, y[3]);
+        const float den = opposite ? __fsub_rn(P, y[3]) : delta;
+        const float inflow = __fmul_rn(num, rcp_approx(den));
         const float inv = rcp_approx(fmaxf(fabsf(sn), 1e-9f));
-        const float li = c.L * inv;    // L / |sin|
-        const float li2 = li * inv;    // L / sin^2
+        const float li = __fmul_rn(c.L, inv);    // L / |sin|
+        const float li2 = __fmul_rn(li, inv);    // L / sin^2
         k[0] = y[3];
         k[1] = y[4];
-        k[2] = fmaf(c.a, inflow, li2 - c.aE);
+        k[2] = fmaf(c.a, inflow, fmaf(li, inv, -c.aE));
         k[3] = fmaf(r, fmaf(c.twoE, P, -c.K), c.K);
-        k[4] = cs * fmaf(sn, c.nA2E2, copysignf(li * li2, sn));
+        k[4] = __fmul_rn(cs, fmaf(sn, c.nA2E2, copysignf(__fmul_rn(li, li2), sn)));
         if constexpr (kProj) {
-            const float P2 = P * P;
+            const float P2 = __fmul_rn(P, P);
             pj->R = fmaf(-delta, c.K, P2);
-            pj->Rz = 0.05f * fmaf(fabsf(delta), c.K, P2);
-            const float cs2 = cs * cs;
-            const float l2cot2 = cs2 * (li * li);  // L^2 cot^2
-            const float pm = c.nA2E2 * cs2;
-            pj->Th = c.Q - pm - l2cot2;
-            pj->Thz = 0.05f * (fabsf(c.Q) + fabsf(pm) + l2cot2);
+            pj->Rz = __fmul_rn(0.05f, fmaf(fabsf(delta), c.K, P2));
+            const float cs2 = __fmul_rn(cs, cs);
+            const float l2cot2 = __fmul_rn(cs2, __fmul_rn(li, li));  // L^2 cot^2
+            const float pm = __fmul_rn(c.nA2E2, cs2);
+            pj->Th = __fsub_rn(fmaf(-c.nA2E2, cs2, c.Q), l2cot2);
+            pj->Thz = __fmul_rn(0.05f, __fadd_rn(__fadd_rn(fabsf(c.Q), fabsf(pm)), l2cot2));
         }
         (void)dt;
     } else {

@@ -164,9 +164,12 @@ __device__ __forceinline__ double rsqrt_newton(double x) {
 // kerr::photonFromFrame for pixel (alpha, beta) of a ZAMO pinhole, with the camera's metric
 // contractions precomputed: p_mu = (g e_0)_mu - look^i (g e_i)_mu, p^r = e_0^r - look^i e_i^r.
 // Launch record i for global pixel `pix` of the frame table (binary search over frame offsets).
-__device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
-                                             int nframes, long long pix, long long i, LaunchSoA& L,
-                                             const TraceParams& p) {
+struct Launched {
+    double E, L, Q, vr, vth;
+    int32_t gid;  // frame (geometry record) of the pixel
+};
+
+__device__ __forceinline__ Launched photon_of_pixel(const FrameDev* __restrict__ frames, int nframes, long long pix) {
     int lo = 0, hi = nframes - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -195,7 +198,14 @@ __device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames
         Lz = 0.0;
         Q = vth * vth - f.cs2 * a2E2;
     }
-    store_launch(L, i, geom[lo], E, Lz, Q, vr, vth, lo, p);
+    return Launched{E, Lz, Q, vr, vth, lo};
+}
+
+__device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
+                                             int nframes, long long pix, long long i, LaunchSoA& L,
+                                             const TraceParams& p) {
+    const Launched x = photon_of_pixel(frames, nframes, pix);
+    store_launch(L, i, geom[x.gid], x.E, x.L, x.Q, x.vr, x.vth, x.gid, p);
 }
 
 __global__ void launch_frames_kernel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
@@ -907,18 +917,30 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             const int q = pool_pos + lane;
             if (q < pool_end) {
                 ray = order ? order[q] : q;
-                // Frames: the launch record is made here, by the whole warp at once, so that its FP64
-                // arithmetic overlaps other warps' FP32 integration instead of taking a kernel of
-                // its own.
-                if (frames) launch_pixel(frames, geom, nframes, ray, ray, L, p);
-                const RayGeom& G = geom[L.geom_id[ray]];
+                // Frames: the launch is made here, by the whole warp at once, so that its FP64
+                // arithmetic overlaps other warps' FP32 integration instead of taking a kernel of its
+                // own; only the FP64 record (for the FP64 continuation and the RayReport constants)
+                // is stored.
                 if constexpr (sizeof(T) == 4) {
-                    const float4 k = L.kf ? L.kf[ray] : float4{};
-                    const float2 kh = L.khf ? L.khf[ray] : float2{};
-                    lane_begin_f32(s, G, L.cf[ray], L.vf[ray], k, kh, L.kf != nullptr, p);
+                    if (frames) {
+                        const Launched x = photon_of_pixel(frames, nframes, ray);
+                        L.E[ray] = x.E; L.L[ray] = x.L; L.Q[ray] = x.Q; L.vr[ray] = x.vr; L.vth[ray] = x.vth;
+                        L.geom_id[ray] = x.gid;
+                        const RayGeom& G = geom[x.gid];
+                        const double xk = x.L - G.a * x.E;
+                        lane_begin_f32(s, G, make_float4(float(x.E), float(x.L), float(x.Q), float(xk * xk + x.Q)),
+                                       make_float2(float(x.vr), float(x.vth)), float4{}, float2{}, false, p);
+                    } else {
+                        const RayGeom& G = geom[L.geom_id[ray]];
+                        const float4 k = L.kf ? L.kf[ray] : float4{};
+                        const float2 kh = L.khf ? L.khf[ray] : float2{};
+                        lane_begin_f32(s, G, L.cf[ray], L.vf[ray], k, kh, L.kf != nullptr, p);
+                    }
                 } else {
-                    lane_begin_launch(s, G, L, ray, p);
+                    if (frames) launch_pixel(frames, geom, nframes, ray, ray, L, p);
+                    lane_begin_launch(s, geom[L.geom_id[ray]], L, ray, p);
                 }
+                const RayGeom& G = geom[L.geom_id[ray]];
                 if (G.dead) {  // seen from inside the horizon: the hole, with no step taken
                     finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
                     ray = -1;
