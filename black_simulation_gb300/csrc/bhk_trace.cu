@@ -443,42 +443,21 @@ __device__ __forceinline__ void lane_begin_f32(Lane<float>& s, const RayGeom& g,
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
-// Starts a lane on ray `ray` at its launch point, first step from kerr::photonStepSize.
-template <typename T>
-__device__ __forceinline__ void lane_begin_launch(Lane<T>& s, const RayGeom& g, const LaunchSoA& L, long long ray,
+// Starts an FP64 lane on ray `ray` at its launch point, first step from kerr::photonStepSize (the
+// FP32 tracer starts its lanes with lane_begin_f32).
+__device__ __forceinline__ void lane_begin_launch(Lane<double>& s, const RayGeom& g, const LaunchSoA& L, long long ray,
                                                   const TraceParams& p) {
-    if constexpr (sizeof(T) == 4) {
-        const float4 cf = L.cf[ray];
-        const float2 vf = L.vf[ray];
-        s.c.set_t(g.af, cf.x, cf.y, cf.z, cf.w);
-        s.south = g.south0 != 0;
-        s.y[0] = g.r0f; s.y[1] = g.th0f; s.y[2] = g.ph0f; s.y[3] = vf.x; s.y[4] = s.south ? -vf.y : vf.y;
-    } else {
-        s.c.set(g.a, L.E[ray], L.L[ray], L.Q[ray]);
-        s.south = false;
-        s.y[0] = g.r0; s.y[1] = g.th0; s.y[2] = g.ph0; s.y[3] = L.vr[ray]; s.y[4] = L.vth[ray];
-    }
+    s.c.set(g.a, L.E[ray], L.L[ray], L.Q[ray]);
+    s.south = false;
+    s.y[0] = g.r0; s.y[1] = g.th0; s.y[2] = g.ph0; s.y[3] = L.vr[ray]; s.y[4] = L.vth[ray];
     lane_radii(s, g);
     s.rmin = s.y[0];
     s.t = 0.0;
     s.swept = 0.0;
-    if constexpr (sizeof(T) == 8) {
-        s.track = true;
-        rhs(s.c, s.y, s.k[0], static_cast<Proj<T>*>(nullptr), &s.kt[0]);
-        ks_position(g.a, s.y[0], s.y[1], s.y[2], s.pos);
-        s.h = first_step<T>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
-    } else {
-        s.track = false;
-        if (L.kf) {  // prepared by the launch kernel
-            const float4 k = L.kf[ray];
-            const float2 kh = L.khf[ray];
-            s.k[0][0] = k.x; s.k[0][1] = k.y; s.k[0][2] = k.z; s.k[0][3] = k.w; s.k[0][4] = kh.x;
-            s.h = kh.y;
-        } else {
-            rhs(s.c, s.y, s.k[0]);
-            s.h = first_step<T>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
-        }
-    }
+    s.track = true;
+    rhs(s.c, s.y, s.k[0], static_cast<Proj<double>*>(nullptr), &s.kt[0]);
+    ks_position(g.a, s.y[0], s.y[1], s.y[2], s.pos);
+    s.h = first_step<double>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
     s.acc = 0; s.rej = 0; s.last_rej = false;
 }
 
@@ -723,13 +702,15 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if constexpr (F64) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
         else return kRestart;
     }
-    // Closest approach: the step's end, or inside it where vr changes sign (the turning point, from
-    // the dense output).
-    if (prev[3] * s.y[3] < T(0)) {
-        const T sv = locate(prev, s.y, s.k, h, 3, T(0));
-        s.rmin = fmin(s.rmin, dense(prev[0], s.y[0], s.k, h, 0, sv));
+    // Closest approach (when asked for): the step's end, or inside it where vr changes sign (the
+    // turning point, from the dense output).
+    if (out.r_min) {
+        if (prev[3] * s.y[3] < T(0)) {
+            const T sv = locate(prev, s.y, s.k, h, 3, T(0));
+            s.rmin = fmin(s.rmin, dense(prev[0], s.y[0], s.k, h, 0, sv));
+        }
+        s.rmin = fmin(s.rmin, s.y[0]);
     }
-    s.rmin = fmin(s.rmin, s.y[0]);
     double t_prev = 0.0;
     if constexpr (F64) {
         t_prev = s.t;
@@ -852,8 +833,9 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         // the tolerance allows shrinks geometrically and the error-per-step controller, which only
         // looks back, overshoots into a rejection every other step. Cap the step at a fixed fraction
         // of the Mino time left to the pole, ~ r / |vr|.
-        // (|r| grows on either side of r = 0: past |a| = 1 the r < 0 region has the same pole.)
-        if (p.pole_frac > 0.0f && s.h * s.y[3] * s.y[0] > 0.0f) {
+        // Outgoing: |r| grew over the step just taken (past |a| = 1 the r < 0 region has the same
+        // pole); not within 2 M of r = 0, where the cap would vanish.
+        if (p.pole_frac > 0.0f && falling == (s.y[0] < 0.0f) && fabsf(s.y[0]) > 2.0f) {
             const float cap = p.pole_frac * fabsf(s.y[0]) * rcp_approx(fabsf(s.y[3]));
             s.h = copysignf(fminf(fabsf(s.h), cap), s.h);
         }
