@@ -4,14 +4,16 @@
 //   frame_setup   1 block, FP64: per-frame ZAMO tetrad (kerr::observerFrame), its lowered vectors,
 //                 horizon, ISCO, capture and escape radii
 //   launch        FP64, one thread per ray: pinhole (alpha, beta) -> look -> kerr::photonFromFrame
-//                 -> E, L, Q, vr, vtheta (the axis snap included); cost bucket
-//   sort          bucket histogram / scan / block-aggregated scatter: queue order, costliest first
-//   trace         persistent grid; every lane owns one ray and pulls a new one from its warp's chunk
-//                 of the device queue as soon as its ray ends (step counts vary ~100x near the
-//                 photon ring, so lanes never wait for a warp's slowest ray). Dormand-Prince 5(4)
-//                 with FSAL and dense-output event location, in FP64 (parity mode) or FP32 (mixed
-//                 mode: FP64 for the launch constants, the disk g, the analytic capture test near
-//                 the horizon and the optional periodic radial re-projection)
+//                 -> E, L, Q, vr, vtheta (the axis snap included); cost bucket. For frames traced
+//                 without the cost sort the trace kernel does this itself as it takes the rays.
+//   order         frames: 4 x 8 pixel tiles (tile_order_kernel); or with the cost sort, bucket
+//                 histogram / scan / block-aggregated scatter: queue order, costliest first
+//   trace         persistent grid; every lane owns one ray; a warp takes 32 queue-adjacent rays
+//                 from the device queue and traces them to completion before it takes the next 32
+//                 (rays that start together stay alike, so the warp's lanes take the same branches).
+//                 Dormand-Prince 5(4) with FSAL and dense-output event location, in FP64 (parity
+//                 mode) or FP32 (mixed mode: FP64 for the launch constants, the disk g, the analytic
+//                 capture test near the horizon and the optional periodic radial re-projection)
 //   rescue        FP64 continuation of the rare rays the FP32 kernel hands over
 //
 // The reference's ray semantics (src/trajectory.cpp:259-392): backward march in Mino time; disk
