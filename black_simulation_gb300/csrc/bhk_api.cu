@@ -98,6 +98,7 @@ struct bhk_context {
 
     // pinned staging
     FrameDev* frames_host = nullptr;
+    RayGeom* geom_host = nullptr;  // the frames' geometries, set up on the host with the frame table
     size_t cap_frames_host = 0;
     Control* ctl_host = nullptr;
     long long* n_host = nullptr;
@@ -192,8 +193,12 @@ bhk_status ensure_scratch(bhk_context* c, size_t rays, size_t geoms, size_t fram
     c->cap_rays = std::min({c->cap_E, c->cap_order, c->cap_key, c->cap_cf, c->cap_vf, c->cap_kf, c->cap_khf});
     if (frames > c->cap_frames_host) {
         if (c->frames_host) cudaFreeHost(c->frames_host);
+        if (c->geom_host) cudaFreeHost(c->geom_host);
         c->frames_host = nullptr;
+        c->geom_host = nullptr;
+        c->cap_frames_host = 0;
         e = cudaMallocHost(reinterpret_cast<void**>(&c->frames_host), frames * sizeof(FrameDev));
+        if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&c->geom_host), frames * sizeof(RayGeom));
         if (e != cudaSuccess) return fail(BHK_ENOMEM, "pinned staging allocation");
         c->cap_frames_host = frames;
     }
@@ -223,18 +228,16 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         L.kf = nullptr;
         L.khf = nullptr;
     }
-    if (b.mode == 0) {
+    if (b.mode == 0 || b.mode == 2) {  // the frame table, its geometries and the ray count, set up on the host
         BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
                                  s));
-        launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
+        BHK_CUDA(cudaMemcpyAsync(c->geom, c->geom_host, sizeof(RayGeom) * b.nframes, cudaMemcpyHostToDevice, s));
+        BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    }
+    if (b.mode == 0) {
         // With the cost sort the keys are needed first; otherwise the trace kernel launches the rays.
         if (r.buckets > 1) launch_rays_frames(c->frames_dev, c->geom, b.nframes, L, r.p, c->ctl, lgrid, s);
-    } else if (b.mode == 2) {
-        BHK_CUDA(cudaMemcpyAsync(c->frames_dev, c->frames_host, sizeof(FrameDev) * b.nframes, cudaMemcpyHostToDevice,
-                                 s));
-        launch_frame_setup(c->frames_dev, c->frames_dev, c->geom, b.nframes, r.p, c->ctl, s);
-        // The set-up writes the frames' pixel total; the batch is the list.
-        BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    } else if (b.mode == 2) {  // the batch is the list (its length staged as the ray count)
         launch_rays_list(c->frames_dev, c->geom, b.nframes,
                          static_cast<const int32_t*>(static_cast<const void*>(b.ex[0])), L, r.p, c->ctl, lgrid, s);
     } else if (b.mode == 3) {
@@ -333,13 +336,17 @@ bhk_status check_frames(const bhk_frame_desc* f, int32_t nframes, int64_t* total
     return BHK_OK;
 }
 
-bhk_status stage_frames(bhk_context* c, const bhk_frame_desc* f, int32_t nframes) {
-    // The previous batch's H2D copy may still read the staging buffer.
+// Fills the pinned frame table, the frames' geometries and the ray count (the FP64 per-frame set-up
+// runs here, on the host, while the previous batch may still be tracing).
+bhk_status stage_frames(bhk_context* c, const bhk_frame_desc* f, int32_t nframes, const TraceParams& p) {
+    // The previous batch's H2D copy may still read the staging buffers.
     if (c->staging_free) BHK_CUDA(cudaEventSynchronize(c->staging_free));
     for (int i = 0; i < nframes; ++i) {
         std::memset(&c->frames_host[i], 0, sizeof(FrameDev));
+        std::memset(&c->geom_host[i], 0, sizeof(RayGeom));
         c->frames_host[i].d = f[i];
     }
+    *c->n_host = setup_frames_host(c->frames_host, c->geom_host, nframes, p);
     return BHK_OK;
 }
 
@@ -384,7 +391,7 @@ bhk_status trace_frames_locked(bhk_context* c, const bhk_frame_desc* frames, int
     st = ensure_scratch(c, static_cast<size_t>(total), static_cast<size_t>(nframes), static_cast<size_t>(nframes));
     if (st != BHK_OK) return st;
     const Resolved r = resolve(c, opts);
-    st = stage_frames(c, frames, nframes);
+    st = stage_frames(c, frames, nframes, r.p);
     if (st != BHK_OK) return st;
     Batch b{0, nframes, total, {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}, 0.0, 0.0};
     st = run_batch(c, b, r, to_outputs(out), timed, s);
@@ -415,7 +422,7 @@ bhk_status bhk::trace_pixel_list(bhk_context* c, const bhk_frame_desc* frames, i
     st = ensure_scratch(c, static_cast<size_t>(n), static_cast<size_t>(nframes), static_cast<size_t>(nframes));
     if (st != BHK_OK) return st;
     const Resolved r = resolve(c, opts);
-    st = stage_frames(c, frames, nframes);  // also waits until the pinned ray count is free
+    st = stage_frames(c, frames, nframes, r.p);  // also waits until the pinned ray count is free
     if (st != BHK_OK) return st;
     *c->n_host = n;
     Batch b{2, nframes, n, {reinterpret_cast<const double*>(list), nullptr, nullptr, nullptr, nullptr, nullptr},
@@ -487,6 +494,7 @@ bhk_status bhk_destroy(bhk_context* c) {
     for (double* p : c->o_d)
         if (p) cudaFree(p);
     if (c->frames_host) cudaFreeHost(c->frames_host);
+    if (c->geom_host) cudaFreeHost(c->geom_host);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     if (c->n_host) cudaFreeHost(c->n_host);
     if (c->staging_free) cudaEventDestroy(c->staging_free);

@@ -153,7 +153,7 @@ __device__ __forceinline__ double circular_omega(double a, double r, bool progra
 }
 
 // Covariant Kerr-Schild metric (src/kerr.cpp:238-254).
-__device__ __forceinline__ void metric_tensor(double a, double r, double theta, double g[4][4]) {
+__host__ __device__ __forceinline__ void metric_tensor(double a, double r, double theta, double g[4][4]) {
     double sn, cs;
     sincos(theta, &sn, &cs);
     const double sn2 = sn * sn;
@@ -174,7 +174,7 @@ __device__ __forceinline__ void metric_tensor(double a, double r, double theta, 
     g[3][3] = A * sn2 / sigma;
 }
 
-__device__ __forceinline__ double metric_dot(const double g[4][4], const double* x, const double* y) {
+__host__ __device__ __forceinline__ double metric_dot(const double g[4][4], const double* x, const double* y) {
     double acc = 0.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -186,7 +186,7 @@ __device__ __forceinline__ double metric_dot(const double g[4][4], const double*
 struct MetricAt { double sigma, delta, A, omega; };
 
 // (src/kerr.cpp:227-236)
-__device__ __forceinline__ MetricAt metric_at(double a, double r, double theta) {
+__host__ __device__ __forceinline__ MetricAt metric_at(double a, double r, double theta) {
     double sn, cs;
     sincos(theta, &sn, &cs);
     MetricAt m;
@@ -312,14 +312,14 @@ __device__ __forceinline__ bool normalize_angles(St& s) {
 }
 
 // ZAMO 4-velocity (src/kerr.cpp:424-430).
-__device__ __forceinline__ void zamo_four_velocity(double a, double r, double theta, double u[4]) {
+__host__ __device__ __forceinline__ void zamo_four_velocity(double a, double r, double theta, double u[4]) {
     const MetricAt m = metric_at(a, r, theta);
     const double ut = sqrt(m.A / (m.sigma * m.delta));
     u[0] = ut; u[1] = 0.0; u[2] = 0.0; u[3] = m.omega * ut;
 }
 
 // Gram-Schmidt observer frame: slots filled in the order theta, phi, r (src/kerr.cpp:432-456).
-__device__ __forceinline__ void observer_frame(double a, double r, double theta, const double u[4], double e[4][4]) {
+__host__ __device__ __forceinline__ void observer_frame(double a, double r, double theta, const double u[4], double e[4][4]) {
     double g[4][4];
     metric_tensor(a, r, theta, g);
 #pragma unroll

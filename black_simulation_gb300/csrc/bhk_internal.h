@@ -99,6 +99,8 @@ struct Outputs {
 // ---- launchers (bhk_trace.cu) ----
 void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p,
                         Control* ctl, cudaStream_t s);
+// The same set-up on the host (the frame table's offsets, tetrads and geometries); returns the rays.
+long long setup_frames_host(FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p);
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s);
 void launch_rays_list(const FrameDev* frames, const RayGeom* geom, int nframes, const int32_t* list, LaunchSoA L,

@@ -39,8 +39,8 @@ __device__ __forceinline__ double wrap_2pi(double x) {
     return y;
 }
 
-__device__ __forceinline__ RayGeom make_geom(double a, double r, double th, double ph, double r_in_opt, double r_out,
-                                             const TraceParams& p) {
+__host__ __device__ __forceinline__ RayGeom make_geom(double a, double r, double th, double ph, double r_in_opt,
+                                                      double r_out, const TraceParams& p) {
     RayGeom g;
     g.a = a; g.r0 = r; g.th0 = th; g.ph0 = ph;
     g.rp = horizon_radius(a);
@@ -117,6 +117,35 @@ __device__ __forceinline__ void store_launch(LaunchSoA L, int64_t i, const RayGe
 
 // ------------------------------------------------------------------------- set-up kernels ----
 
+// Per-frame set-up in FP64: the ZAMO tetrad at the camera (kerr::observerFrame), its vectors
+// lowered with the camera's metric, the pieces of kerr::photonFromFrame that do not depend on the
+// pixel, and the frame's ray geometry (horizon, ISCO, capture and escape radii). The API's batches
+// do this on the host while staging the frame table; the allocation-free entry point on the device.
+__host__ __device__ inline void setup_frame(FrameDev& fr, RayGeom& geom, const TraceParams& p) {
+    const bhk_frame_desc d = fr.d;
+    double u[4], e[4][4], g[4][4];
+    zamo_four_velocity(d.a, d.r_obs, d.theta_obs, u);
+    observer_frame(d.a, d.r_obs, d.theta_obs, u, e);
+    metric_tensor(d.a, d.r_obs, d.theta_obs, g);
+    for (int k = 0; k < 4; ++k)
+        for (int i = 0; i < 4; ++i) {
+            fr.e[k][i] = e[k][i];
+            double acc = 0.0;
+            for (int j = 0; j < 4; ++j) acc += g[i][j] * e[k][j];
+            fr.el[k][i] = acc;
+        }
+    double sn, cs;
+    sincos(d.theta_obs, &sn, &cs);
+    fr.sigma = metric_at(d.a, d.r_obs, d.theta_obs).sigma;
+    fr.cs2 = cs * cs;
+    fr.inv_sn2 = 1.0 / dmaxd(sn * sn, 1e-18);
+    fr.a2 = d.a * d.a;
+    fr.inv_r = 1.0 / d.r_obs;
+    fr.px = (d.alpha_hi - d.alpha_lo) / d.width;
+    fr.py = (d.beta_hi - d.beta_lo) / d.height;
+    geom = make_geom(d.a, d.r_obs, d.theta_obs, d.phi_obs, d.r_disk_in, d.r_disk_out, p);
+}
+
 __global__ void frame_setup_kernel(FrameDev* frames, RayGeom* geom, int nframes, TraceParams p, Control* ctl) {
     if (threadIdx.x == 0) {
         long long off = 0;
@@ -126,30 +155,7 @@ __global__ void frame_setup_kernel(FrameDev* frames, RayGeom* geom, int nframes,
         }
         ctl->n_rays = off;
     }
-    for (int f = threadIdx.x; f < nframes; f += blockDim.x) {
-        const bhk_frame_desc d = frames[f].d;
-        double u[4], e[4][4], g[4][4];
-        zamo_four_velocity(d.a, d.r_obs, d.theta_obs, u);
-        observer_frame(d.a, d.r_obs, d.theta_obs, u, e);
-        metric_tensor(d.a, d.r_obs, d.theta_obs, g);
-        for (int k = 0; k < 4; ++k)
-            for (int i = 0; i < 4; ++i) {
-                frames[f].e[k][i] = e[k][i];
-                double acc = 0.0;
-                for (int j = 0; j < 4; ++j) acc += g[i][j] * e[k][j];
-                frames[f].el[k][i] = acc;
-            }
-        double sn, cs;
-        sincos(d.theta_obs, &sn, &cs);
-        frames[f].sigma = metric_at(d.a, d.r_obs, d.theta_obs).sigma;
-        frames[f].cs2 = cs * cs;
-        frames[f].inv_sn2 = 1.0 / dmaxd(sn * sn, 1e-18);
-        frames[f].a2 = d.a * d.a;
-        frames[f].inv_r = 1.0 / d.r_obs;
-        frames[f].px = (d.alpha_hi - d.alpha_lo) / d.width;
-        frames[f].py = (d.beta_hi - d.beta_lo) / d.height;
-        geom[f] = make_geom(d.a, d.r_obs, d.theta_obs, d.phi_obs, d.r_disk_in, d.r_disk_out, p);
-    }
+    for (int f = threadIdx.x; f < nframes; f += blockDim.x) setup_frame(frames[f], geom[f], p);
 }
 
 // 1/sqrt(x) in FP64 for x in [1, ~10]: FP32 seed (rsqrt.approx, ~2^-22 relative) refined by two Newton
@@ -1042,6 +1048,16 @@ void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int
                         Control* ctl, cudaStream_t s) {
     (void)in;
     frame_setup_kernel<<<1, 128, 0, s>>>(frames, geom, nframes, p, ctl);
+}
+
+long long setup_frames_host(FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p) {
+    long long off = 0;
+    for (int f = 0; f < nframes; ++f) {
+        frames[f].offset = off;
+        off += static_cast<long long>(frames[f].d.width) * frames[f].d.height;
+        setup_frame(frames[f], geom[f], p);
+    }
+    return off;
 }
 
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
