@@ -305,7 +305,7 @@ def run_ours(args):
                      "traffic": NCU_TRAFFIC.get(args.workload) if args.scale == 1 else None,
                      "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run",
                      "kernel_ms": k_ms, "flops_per_step": fps},
-        "gpu_launches": 3 * args.steps,  # per step: tile order, trace (with the launch), rescue
+        "gpu_launches": 2 * args.steps,  # per step: trace (with the launch and the tile order), rescue
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and args.workload == "1080p" and args.scale == 1 and not args.no_surrogate:

@@ -114,8 +114,6 @@ void launch_rays_framed(const double* a, const double* r, const double* th, cons
                         const double* look, double r_in, double r_out, RayGeom* geom, LaunchSoA L, const TraceParams& p,
                         const Control* ctl, int grid, cudaStream_t s);
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
-void launch_tile_order(const FrameDev* frames, int nframes, int32_t* order, const Control* ctl, int grid,
-                       cudaStream_t s);
 // With frames (frame batches traced in queue order without the cost sort), the trace kernel makes
 // each ray's launch record itself when it takes the ray; otherwise the records come from a launch
 // kernel run before it.

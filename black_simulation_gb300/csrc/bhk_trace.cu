@@ -6,8 +6,8 @@
 //   launch        FP64, one thread per ray: pinhole (alpha, beta) -> look -> kerr::photonFromFrame
 //                 -> E, L, Q, vr, vtheta (the axis snap included); cost bucket. For frames traced
 //                 without the cost sort the trace kernel does this itself as it takes the rays.
-//   order         frames: 4 x 8 pixel tiles (tile_order_kernel); or with the cost sort, bucket
-//                 histogram / scan / block-aggregated scatter: queue order, costliest first
+//   order         frames: by 4 x 8 pixel tiles, mapped in the trace kernel; or the cost sort: bucket
+//                 histogram / scan / block-aggregated scatter, costliest first
 //   trace         persistent grid; every lane owns one ray; a warp takes 32 queue-adjacent rays
 //                 from the device queue and traces them to completion before it takes the next 32
 //                 (rays that start together stay alike, so the warp's lanes take the same branches).
@@ -177,15 +177,35 @@ struct Launched {
     int32_t gid;  // frame (geometry record) of the pixel
 };
 
-__device__ __forceinline__ Launched photon_of_pixel(const FrameDev* __restrict__ frames, int nframes, long long pix) {
+// The frame of global ray index i (binary search over the frame offsets).
+__device__ __forceinline__ int frame_of(const FrameDev* __restrict__ frames, int nframes, long long i) {
     int lo = 0, hi = nframes - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (frames[mid].offset <= pix) lo = mid; else hi = mid - 1;
+        if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
     }
-    const FrameDev& f = frames[lo];
-    const int local = static_cast<int>(pix - f.offset);  // < 2^31 rays per batch
-    const int row = local / f.d.width, col = local - row * f.d.width;
+    return lo;
+}
+
+// A warp's batch of 32 rays is a 4 x 8 tile of pixels (ragged at the right and bottom edges): queue
+// position q of a W x H frame is pixel (x, y) with q = 8 ty W + hh 4 tx + (y - 8 ty) ww + (x - 4 tx),
+// tile (tx, ty) = (x / 4, y / 8), hh and ww the tile's height and width.
+constexpr int kTileW = 4, kTileH = 8;
+
+__device__ __forceinline__ void tile_pixel(int W, int H, int lq, int* row, int* col) {
+    const int ty = lq / (kTileH * W);
+    const int rem = lq - ty * kTileH * W;
+    const int hh = H - kTileH * ty < kTileH ? H - kTileH * ty : kTileH;
+    const int tx = rem / (hh * kTileW);
+    const int rem2 = rem - tx * hh * kTileW;
+    const int ww = W - kTileW * tx < kTileW ? W - kTileW * tx : kTileW;
+    const int dy = rem2 / ww;
+    *row = kTileH * ty + dy;
+    *col = kTileW * tx + (rem2 - dy * ww);
+}
+
+__device__ __forceinline__ Launched photon_at(const FrameDev& f, int fi, int row, int col) {
+    const int lo = fi;
     const double alpha = f.d.alpha_lo + (col + 0.5) * f.px;
     const double beta = f.d.beta_hi - (row + 0.5) * f.py;
     const double lt = -beta * f.inv_r, lp = alpha * f.inv_r;
@@ -207,6 +227,14 @@ __device__ __forceinline__ Launched photon_of_pixel(const FrameDev* __restrict__
         Q = vth * vth - f.cs2 * a2E2;
     }
     return Launched{E, Lz, Q, vr, vth, lo};
+}
+
+__device__ __forceinline__ Launched photon_of_pixel(const FrameDev* __restrict__ frames, int nframes, long long pix) {
+    const int fi = frame_of(frames, nframes, pix);
+    const FrameDev& f = frames[fi];
+    const int local = static_cast<int>(pix - f.offset);  // < 2^31 rays per batch
+    const int row = local / f.d.width;
+    return photon_at(f, fi, row, local - row * f.d.width);
 }
 
 __device__ __forceinline__ void launch_pixel(const FrameDev* __restrict__ frames, const RayGeom* __restrict__ geom,
@@ -906,14 +934,23 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             }
             const int q = pool_pos + lane;
             if (q < pool_end) {
-                ray = order ? order[q] : q;
+                // Frames: queue position -> pixel by 4 x 8 tiles (the frame is the same for both).
+                int fi = 0, prow = 0, pcol = 0;
+                if (frames) {
+                    fi = frame_of(frames, nframes, q);
+                    const FrameDev& f = frames[fi];
+                    tile_pixel(f.d.width, f.d.height, static_cast<int>(q - f.offset), &prow, &pcol);
+                    ray = f.offset + static_cast<long long>(prow) * f.d.width + pcol;
+                } else {
+                    ray = order ? order[q] : q;
+                }
                 // Frames: the launch is made here, by the whole warp at once, so that its FP64
                 // arithmetic overlaps other warps' FP32 integration instead of taking a kernel of its
                 // own; only the FP64 record (for the FP64 continuation and the RayReport constants)
                 // is stored.
                 if constexpr (sizeof(T) == 4) {
                     if (frames) {
-                        const Launched x = photon_of_pixel(frames, nframes, ray);
+                        const Launched x = photon_at(frames[fi], fi, prow, pcol);
                         L.E[ray] = x.E; L.L[ray] = x.L; L.Q[ray] = x.Q; L.vr[ray] = x.vr; L.vth[ray] = x.vth;
                         L.geom_id[ray] = x.gid;
                         const RayGeom& G = geom[x.gid];
@@ -1081,40 +1118,6 @@ void launch_rays_explicit(const double* a, const double* r_obs, const double* th
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
     (void)r_escape;
     launch_explicit_kernel<<<grid, 128, 0, s>>>(a, r_obs, th_obs, alpha, beta, r_in, r_out, geom, L, p, ctl);
-}
-
-// Queue order of the frames' pixels by tiles of 4 x 8 (ragged at the right and bottom edges), so that
-// a warp's batch of 32 rays is a compact patch of the image rather than a strip of one row:
-// order[q(p)] = p with q(p) = 8 ty W + hh 4 tx + (y - 8 ty) ww + (x - 4 tx) for pixel p = (x, y) of a
-// W x H frame, tile (tx, ty) = (x / 4, y / 8), hh and ww its height and width.
-constexpr int kTileW = 4, kTileH = 8;  // one warp's batch
-
-__global__ void tile_order_kernel(const FrameDev* __restrict__ frames, int nframes, int32_t* order,
-                                  const Control* __restrict__ ctl) {
-    const long long n = ctl->n_rays;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        int lo = 0, hi = nframes - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (frames[mid].offset <= i) lo = mid; else hi = mid - 1;
-        }
-        const FrameDev& f = frames[lo];
-        const int W = f.d.width, H = f.d.height;
-        const int local = static_cast<int>(i - f.offset);
-        const int y = local / W, x = local - y * W;
-        const int ty = y / kTileH, tx = x / kTileW;
-        const int hh = H - kTileH * ty < kTileH ? H - kTileH * ty : kTileH;
-        const int ww = W - kTileW * tx < kTileW ? W - kTileW * tx : kTileW;
-        const long long q = f.offset + static_cast<long long>(kTileH) * ty * W + static_cast<long long>(hh) * kTileW * tx +
-                            (y - kTileH * ty) * ww + (x - kTileW * tx);
-        order[q] = static_cast<int32_t>(i);
-    }
-}
-
-void launch_tile_order(const FrameDev* frames, int nframes, int32_t* order, const Control* ctl, int grid,
-                       cudaStream_t s) {
-    tile_order_kernel<<<grid, 256, 0, s>>>(frames, nframes, order, ctl);
 }
 
 void launch_sort(LaunchSoA L, SortScratch S, const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
