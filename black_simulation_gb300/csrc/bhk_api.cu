@@ -157,12 +157,12 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.block = o->block > 0 ? o->block : (ctx->tuned_block[pi] ? ctx->tuned_block[pi] : 128);
     r.chunk = o->chunk > 0 ? o->chunk : (ctx->tuned_chunk[pi] ? ctx->tuned_chunk[pi] : 32);
     r.chunk = (std::max(r.chunk, 32) + 31) / 32 * 32;  // whole batches of 32 (one per lane)
-    r.buckets = o->sort_buckets > 0 ? o->sort_buckets : (ctx->tuned_buckets[pi] ? ctx->tuned_buckets[pi] : 64);
+    r.buckets = o->sort_buckets > 0 ? o->sort_buckets : (ctx->tuned_buckets[pi] ? ctx->tuned_buckets[pi] : 1);
     r.buckets = std::min(r.buckets, kMaxBuckets);
     r.p.chunk = r.chunk;
     r.p.buckets = r.buckets;
     r.graph = o->use_graph != 0;
-    const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 3);
+    const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 2);
     r.regcap = (r.fp64 || rb >= 3) ? 0 : rb;
     if (r.regcap > 0 && r.block > 128) r.block = 128;
     r.block = std::min(r.block, 256);
@@ -766,7 +766,7 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
     const int budgets[] = {3, 1, 2};
     const bhk_rays_out out = own_outputs(c);
     float best = 1e30f;
-    int bb = 128, bc = 32, bk = 64, br = 3;
+    int bb = 128, bc = 32, bk = 1, br = 2;
     cudaEvent_t t0, t1;
     BHK_CUDA(cudaEventCreate(&t0));
     BHK_CUDA(cudaEventCreate(&t1));
