@@ -207,7 +207,8 @@ def run_reference(args):
     cfg = {k: v for k, v in cfg.items() if k not in ("precision", "rtol")}
     rates = []
     for i in range(args.warmup + args.steps):
-        rate, n, dt, threads = cpu_reference_rate(frames, target_s=max(2.0, 30.0 / (args.warmup + args.steps)))
+        target = args.ref_sample_s if args.ref_sample_s else max(2.0, 30.0 / (args.warmup + args.steps))
+        rate, n, dt, threads = cpu_reference_rate(frames, target_s=target)
         if i >= args.warmup:
             rates.append((rate, n, dt))
     value = float(np.mean([r[0] for r in rates]))
@@ -563,6 +564,8 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="1080p: skip the surrogate-vs-tracer comparison")
+    ap.add_argument("--ref-sample-s", type=float, default=0.0,
+                    help="--impl reference: seconds of CPU work per step (0: 30 s over all steps, at least 2 s)")
     ap.add_argument("--scale", type=int, default=1, help="divide the frame size (profiling captures)")
     ap.add_argument("--block", type=int, default=0, help="fixed launch shape instead of autotuning")
     ap.add_argument("--chunk", type=int, default=0)
