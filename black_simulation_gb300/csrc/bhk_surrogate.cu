@@ -228,12 +228,25 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int i = threadIdx.x; i < BN; i += blockDim.x) scol[i] = 0.0f;
             __syncthreads();
         }
-#pragma unroll 1
-        for (int j = 0; j < BN / 16; ++j) {
+        // The accumulator is read 16 columns at a time, the next load in flight while the current
+        // columns are processed (kDsilu: the pre-activations of both also loaded ahead).
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * warp) << 16);
+        auto zload = [&](int j, uint4 (&zp)[2]) {
+            if constexpr (EPI == kDsilu) {
+                const int nb = n0 + 16 * j;
+                if (live && nb < ea.N) {
+                    const uint4* zs = reinterpret_cast<const uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
+                    zp[0] = zs[0];
+                    zp[1] = zs[1];
+                }
+            }
+        };
+        auto process = [&](int j, const uint32_t (&r)[16], const uint4 (&zpre)[2]) {
             float v[16];
-            tc::tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + 16 * j, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
             const int nb = n0 + 16 * j;
-            if (nb >= ea.N) continue;
+            if (nb >= ea.N) return;
             if constexpr (EPI == kStoreF32) {
                 if (live)
                     for (int i = 0; i < 16; ++i)
@@ -257,8 +270,15 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             } else if constexpr (EPI == kBiasSilu) {
                 __align__(16) bf16 zb[16], ab[16];
                 if (live) {
+                    float bb[16];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float4 b = __ldg(reinterpret_cast<const float4*>(ea.bias + nb) + q);
+                        bb[4 * q] = b.x; bb[4 * q + 1] = b.y; bb[4 * q + 2] = b.z; bb[4 * q + 3] = b.w;
+                    }
+#pragma unroll
                     for (int i = 0; i < 16; i += 2) {
-                        const float z0 = v[i] + ea.bias[nb + i], z1 = v[i + 1] + ea.bias[nb + i + 1];
+                        const float z0 = v[i] + bb[i], z1 = v[i + 1] + bb[i + 1];
                         zb[i] = __float2bfloat16_rn(z0);
                         zb[i + 1] = __float2bfloat16_rn(z1);
                         const uint32_t a2 = silu2_half(0.5f * z0, 0.5f * z1);
@@ -279,9 +299,8 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 __align__(16) bf16 ob[16];
                 if (live) {
                     __align__(16) bf16 zin[16];
-                    const uint4* zs = reinterpret_cast<const uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
-                    reinterpret_cast<uint4*>(zin)[0] = zs[0];
-                    reinterpret_cast<uint4*>(zin)[1] = zs[1];
+                    reinterpret_cast<uint4*>(zin)[0] = zpre[0];
+                    reinterpret_cast<uint4*>(zin)[1] = zpre[1];
                     for (int i = 0; i < 16; ++i) {
                         const float z = __bfloat162float(zin[i]);
                         const float sg = sigmoidf(z);
@@ -304,6 +323,28 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                     if (!(lane & 1)) atomicAdd(&scol[16 * j + col], tot);
                 }
             }
+                };
+        constexpr int kJ = BN / 16;
+        uint32_t ra[16], rb[16];
+        uint4 za[2] = {}, zb2[2] = {};
+        tc::tmem_ld16_issue(trow, ra);
+        zload(0, za);
+        tc::tmem_wait16(ra);
+#pragma unroll 1
+        for (int j = 0; j < kJ; j += 2) {
+            if (j + 1 < kJ) {
+                tc::tmem_ld16_issue(trow + 16 * (j + 1), rb);
+                zload(j + 1, zb2);
+            }
+            process(j, ra, za);
+            if (j + 1 >= kJ) break;
+            tc::tmem_wait16(rb);
+            if (j + 2 < kJ) {
+                tc::tmem_ld16_issue(trow + 16 * (j + 2), ra);
+                zload(j + 2, za);
+            }
+            process(j + 1, rb, zb2);
+            if (j + 2 < kJ) tc::tmem_wait16(ra);
         }
         if constexpr (EPI == kDsilu) {
             __syncthreads();
