@@ -761,8 +761,12 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         s.pos[0] = x1[0]; s.pos[1] = x1[1]; s.pos[2] = x1[2];
     }
     const T hp = T(0.5 * kPi);
-    // Thin disk: theta crosses pi/2 inside [r_in, r_out].
-    if ((prev[1] - hp) * (s.y[1] - hp) < T(0)) {
+    // Thin disk: theta crosses pi/2 inside [r_in, r_out]. (FP32: the hemisphere representation keeps
+    // theta at or below pi/2 at a step's start, so a crossing is theta above pi/2 at its end.)
+    bool crossed;
+    if constexpr (F64) crossed = (prev[1] - hp) * (s.y[1] - hp) < T(0);
+    else crossed = prev[1] < hp && s.y[1] > hp;
+    if (crossed) {
         const T sg = locate(prev, s.y, s.k, h, 1, hp);
         const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
         if (rc >= s.r_in && rc <= s.r_out) {
