@@ -48,7 +48,8 @@ __host__ __device__ __forceinline__ RayGeom make_geom(double a, double r, double
     g.r_esc = fmax(p.r_escape, 1.5 * r);
     g.r_in = r_in_opt > 0.0 ? r_in_opt : isco_radius(a, true);
     g.r_out = r_out;
-    g.zone_top = g.rp + dmind(0.05, 0.5 * (g.r_in - g.rp));
+    // The analytic capture zone's top, never below the capture radius (a disk reaching inside r_+).
+    g.zone_top = fmax(g.rp + dmind(0.05, 0.5 * (g.r_in - g.rp)), g.r_cap);
     g.naked = naked(a) ? 1 : 0;
     if (g.naked) {  // no horizon: nothing is captured (the ring and the far sky are tested instead)
         g.r_cap = -1e30;
@@ -800,25 +801,26 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         if (s.y[0] * s.y[0] + s.c.a2 * c * c < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
     }
     // Escaped: rising past r_esc, or past |a| = 1 falling past -r_esc into the sky of the r < 0 region,
-    // beyond the ring (shaders/trace.frag:1779-1792).
-    const bool beyond = falling && s.y[0] < -s.r_esc;
-    if (beyond || (!falling && s.y[0] > s.r_esc))
+    // beyond the ring (shaders/trace.frag:1779-1792). Rays start inside |r| < r_esc (the camera sits
+    // within r_esc / 1.5), so |r| first exceeds r_esc on the step that leaves.
+    if (fabs(s.y[0]) > s.r_esc) {
+        const bool beyond = s.y[0] < T(0);
         return escape(s, prev, h, beyond ? -s.r_esc : s.r_esc, beyond ? BHK_RAY_ESCAPED_BEYOND : BHK_RAY_ESCAPED, out,
                       ray, t_prev);
-    if (falling) {
+    }
+    // Captured (zone_top lies above r_cap; both are -1e30 past |a| = 1).
+    if (s.y[0] < s.zone_top && falling) {
         if (s.y[0] < s.r_cap) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
-        if (s.y[0] < s.zone_top) {
-            if constexpr (F64) {
-                if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
-                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
-            } else {
-                if (no_radial_root_below_f(s.c, s.r_cap, s.y[0])) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
-                // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
-                const RayGeom& G = geom[L.geom_id[ray]];
-                if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
-                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
-                return kRescue;
-            }
+        if constexpr (F64) {
+            if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
+                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+        } else {
+            if (no_radial_root_below_f(s.c, s.r_cap, s.y[0])) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+            // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
+            const RayGeom& G = geom[L.geom_id[ray]];
+            if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
+                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+            return kRescue;
         }
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
