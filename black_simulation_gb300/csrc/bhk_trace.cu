@@ -424,7 +424,7 @@ struct Lane {
     T y[5];
     T k[7][5];
     T h;
-    T r_cap, r_esc, r_in, r_out, zone_top;
+    T r_cap, r_esc, zone_top;  // (the disk's radii are read from the geometry at an equator crossing)
     int acc, rej;
     bool last_rej;
     // FP32 only: the ray is in the southern hemisphere and y[1], y[4] hold pi - theta and -vtheta.
@@ -452,9 +452,9 @@ __device__ __forceinline__ void ks_position(double a, double r, double th, doubl
 template <typename T>
 __device__ __forceinline__ void lane_radii(Lane<T>& s, const RayGeom& g) {
     if constexpr (sizeof(T) == 4) {
-        s.r_cap = g.r_capf; s.r_esc = g.r_escf; s.r_in = g.r_inf; s.r_out = g.r_outf; s.zone_top = g.zone_topf;
+        s.r_cap = g.r_capf; s.r_esc = g.r_escf; s.zone_top = g.zone_topf;
     } else {
-        s.r_cap = g.r_cap; s.r_esc = g.r_esc; s.r_in = g.r_in; s.r_out = g.r_out; s.zone_top = g.zone_top;
+        s.r_cap = g.r_cap; s.r_esc = g.r_esc; s.zone_top = g.zone_top;
     }
 }
 
@@ -770,7 +770,10 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     if (crossed) {
         const T sg = locate(prev, s.y, s.k, h, 1, hp);
         const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
-        if (rc >= s.r_in && rc <= s.r_out) {
+        const RayGeom& G = geom[L.geom_id[ray]];
+        T r_in, r_out;
+        if constexpr (F64) { r_in = G.r_in; r_out = G.r_out; } else { r_in = G.r_inf; r_out = G.r_outf; }
+        if (rc >= r_in && rc <= r_out) {
             if constexpr (F64) {
                 double g;
                 if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
