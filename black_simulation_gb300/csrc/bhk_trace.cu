@@ -424,7 +424,7 @@ struct Lane {
     T y[5];
     T k[7][5];
     T h;
-    T r_cap, r_esc, zone_top;  // (the disk's radii are read from the geometry at an equator crossing)
+    T r_esc, zone_top;  // (the capture and disk radii are read from the geometry where they are needed)
     int acc, rej;
     bool last_rej;
     // FP32 only: the ray is in the southern hemisphere and y[1], y[4] hold pi - theta and -vtheta.
@@ -452,9 +452,9 @@ __device__ __forceinline__ void ks_position(double a, double r, double th, doubl
 template <typename T>
 __device__ __forceinline__ void lane_radii(Lane<T>& s, const RayGeom& g) {
     if constexpr (sizeof(T) == 4) {
-        s.r_cap = g.r_capf; s.r_esc = g.r_escf; s.zone_top = g.zone_topf;
+        s.r_esc = g.r_escf; s.zone_top = g.zone_topf;
     } else {
-        s.r_cap = g.r_cap; s.r_esc = g.r_esc; s.zone_top = g.zone_top;
+        s.r_esc = g.r_esc; s.zone_top = g.zone_top;
     }
 }
 
@@ -527,17 +527,19 @@ __device__ __forceinline__ T nan_t() {
 // the time the light travelled (t runs backward from 0 at the camera) and the turns swept.
 template <typename T>
 __device__ __forceinline__ void write_path(const Lane<T>& s, const Outputs& o, long long ray, double t_end,
-                                           bool captured) {
-    if (o.r_min) o.r_min[ray] = captured ? fmin(double(s.rmin), double(s.r_cap)) : double(s.rmin);
+                                           double r_cap = INFINITY) {
+    if (o.r_min) o.r_min[ray] = fmin(double(s.rmin), r_cap);
     if (o.delay) o.delay[ray] = s.track ? -t_end : nan_d();
     if (o.turns) o.turns[ray] = s.track ? s.swept / (2.0 * kPi) : nan_d();
 }
 
 template <typename T>
-__device__ __forceinline__ int finish(const Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl) {
+// r_cap: the capture radius of a captured ray (its closest approach is at most that).
+__device__ __forceinline__ int finish(const Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl,
+                                      double r_cap = INFINITY) {
     const T n = nan_t<T>();
     write_out_t<T>(o, ray, outcome, n, n, n, n, n, s.acc, s.rej);
-    write_path(s, o, ray, s.t, outcome == BHK_RAY_CAPTURED);
+    write_path(s, o, ray, s.t, r_cap);
     if (outcome == BHK_RAY_UNFINISHED) atomicAdd(&ctl->stats[2], 1ull);
     return kFinished;
 }
@@ -597,8 +599,8 @@ __device__ __forceinline__ int escape(const Lane<T>& s, const T prev[5], T h, T 
     const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
     const T n = nan_t<T>();
     write_out_t<T>(out, ray, outcome, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
-    if constexpr (sizeof(T) == 8) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
-    else write_path(s, out, ray, 0.0, false);
+    if constexpr (sizeof(T) == 8) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
+    else write_path(s, out, ray, 0.0);
     return kFinished;
 }
 
@@ -779,7 +781,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
                     const double ph = wrap_2pi(dense(prev[2], s.y[2], s.k, h, 2, sg));
                     write_out(out, ray, BHK_RAY_DISK, rc, ph, g, nan_d(), nan_d(), s.acc, s.rej);
-                    write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg), false);
+                    write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
                     return kFinished;
                 }
             } else {
@@ -787,7 +789,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
                     const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
                     write_out_t<float>(out, ray, BHK_RAY_DISK, rc, ph, g, nan_f(), nan_f(), s.acc, s.rej);
-                    write_path(s, out, ray, 0.0, false);
+                    write_path(s, out, ray, 0.0);
                     return kFinished;
                 }
             }
@@ -811,18 +813,20 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         return escape(s, prev, h, beyond ? -s.r_esc : s.r_esc, beyond ? BHK_RAY_ESCAPED_BEYOND : BHK_RAY_ESCAPED, out,
                       ray, t_prev);
     }
-    // Captured (zone_top lies above r_cap; both are -1e30 past |a| = 1).
+    // Captured (zone_top lies above r_cap; both are -1e30 past |a| = 1; r_cap is read from the
+    // geometry here rather than held in a register).
     if (s.y[0] < s.zone_top && falling) {
-        if (s.y[0] < s.r_cap) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+        const RayGeom& G = geom[L.geom_id[ray]];
+        if (s.y[0] < (F64 ? T(G.r_cap) : T(G.r_capf))) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
         if constexpr (F64) {
             if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
-                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
         } else {
-            if (no_radial_root_below_f(s.c, s.r_cap, s.y[0])) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+            if (no_radial_root_below_f(s.c, G.r_capf, s.y[0]))
+                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
             // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
-            const RayGeom& G = geom[L.geom_id[ray]];
             if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
-                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
             return kRescue;
         }
     }
@@ -978,7 +982,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                 }
                 const RayGeom& G = geom[L.geom_id[ray]];
                 if (G.dead) {  // seen from inside the horizon: the hole, with no step taken
-                    finish(s, out, ray, BHK_RAY_CAPTURED, ctl);
+                    finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
                     ray = -1;
                 }
             }
