@@ -60,7 +60,8 @@ struct GraphKey {
 
 // FP32 FLOPs of one Dormand-Prince attempt of the mixed tracer, counted from the source (an FMA is 2):
 //   right-hand side (bhk_device.cuh rhs<float>): sine/cosine 23 (10 FMA, 2 MUL, 1 ADD), Delta and
-//     r^2 + a^2 4, P 2, inflow 4, 1/sin powers 2, dphi 4, R'/2 4, Theta'/2 4 -> 47, x 6 stages = 282;
+//     r^2 + a^2 4, P 2, inflow 4, sin cos, sin^2 and L / sin^2 3, dphi 4, R'/2 4, Theta'/2 3 -> 47,
+//     x 6 stages = 282;
 //     the FSAL stage's constraint potentials 15;
 //   stage sums y + h sum a_ij k_j over 5 components: 20 products h a_ij and 100 FMA = 220;
 //   error estimate and weighted norm: 5 x 16 + 2 = 82;  step control and pole cap: 8.

@@ -23,7 +23,8 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return y;
 }
 
-// sin and cos of x for |x| below a few thousand. Reduction x = k pi/2 + r with a two-constant
+// sin r and cos r of the reduced argument of x (|x| below a few thousand), and the quadrant k (its
+// low bits). Reduction x = k pi/2 + r with a two-constant
 // Cody-Waite split of pi/2 (hi = pi/2 rounded to float, lo = the remainder), then polynomials on
 // |r| <= pi/4: sin r = r + r^3 (s3 + s5 r^2 + s7 r^4), cos r = 1 + r^2 (c2 + c4 r^2 + c6 r^4 + c8 r^6),
 // whose coefficients were fitted for this file to the least maximum relative error by Lawson's
@@ -32,7 +33,7 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // k is rounded by adding 1.5 * 2^23 (the integer lands in the low mantissa bits, which also give
 // the quadrant): no float/int conversion instructions, which on this part issue to the narrow
 // FP64 pipe.
-__device__ __forceinline__ void sincos_fast(float x, float* s, float* c) {
+__device__ __forceinline__ int sincos_reduced(float x, float* sr, float* cr) {
     const float shifted = fmaf(x, 0.636619772367581343f, 12582912.0f);
     const int q = __float_as_int(shifted);
     const float k = __fsub_rn(shifted, 12582912.0f);
@@ -41,11 +42,19 @@ __device__ __forceinline__ void sincos_fast(float x, float* s, float* c) {
     const float r2 = __fmul_rn(r, r);
     float ps = fmaf(r2, -1.9515282645509862e-4f, 8.332160757714382e-3f);     // s7, s5
     ps = fmaf(r2, ps, -1.6666654609479015e-1f);                               // s3
-    const float sr = fmaf(__fmul_rn(r, r2), ps, r);
+    *sr = fmaf(__fmul_rn(r, r2), ps, r);
     float pc = fmaf(r2, 2.4383566768620477e-5f, -1.3886681641998991e-3f);    // c8, c6
     pc = fmaf(r2, pc, 4.166662035693103e-2f);                                 // c4
     pc = fmaf(r2, pc, -4.9999999694474034e-1f);                               // c2
-    const float cr = fmaf(r2, pc, 1.0f);
+    *cr = fmaf(r2, pc, 1.0f);
+    return q;
+}
+
+// sin x and cos x from the reduced pair: quadrant k mod 4 = 0, 1, 2, 3 gives
+// (sin, cos) = (sr, cr), (cr, -sr), (-sr, -cr), (-cr, sr).
+__device__ __forceinline__ void sincos_fast(float x, float* s, float* c) {
+    float sr, cr;
+    const int q = sincos_reduced(x, &sr, &cr);
     const float s0 = (q & 1) ? cr : sr;
     const float c0 = (q & 1) ? sr : cr;
     *s = (q & 2) ? -s0 : s0;
@@ -496,14 +505,20 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj
     if constexpr (sizeof(T) == 4) {
         // The FP32 form, arranged for fused multiply-adds (the same terms, regrouped):
         //   Delta = (r^2 + a^2) - 2 r,  R'/2 = r (2 E P - K) + K,
-        //   dphi = a inflow - a E + L / sin^2,  Theta'/2 = cos (sin (-a^2 E^2) + sgn(sin) L^2 / |sin|^3).
+        //   dphi = a inflow - a E + L / sin^2,  Theta'/2 = sin cos (-a^2 E^2 + (L / sin^2)^2).
+        // theta enters only through sin^2, cos^2 and sin cos, so the quadrant's signs reduce to one:
+        // with the reduced pair (sr, cr), sin^2 = (odd ? cr : sr)^2 and sin cos = (odd ? -1 : 1) sr cr.
         // Delta is not clamped away from 0: the FP32 tracer stays outside the capture zone, and a zero
         // there turns the state non-finite, which hands the ray to the FP64 continuation.
         // Every operation is spelled out (fmaf or a rounded intrinsic) so that no compilation of this
         // function contracts differently: the frame path and the launch kernel must agree bit for bit.
         const float r = y[0];
-        float sn, cs;
-        sincos_fast(y[1], &sn, &cs);
+        float sr, cr;
+        const bool odd = (sincos_reduced(y[1], &sr, &cr) & 1) != 0;
+        const float m = odd ? cr : sr;                          // +-sin
+        const float sc = __fmul_rn(odd ? -sr : sr, cr);         // sin cos
+        const float inv2 = rcp_approx(fmaxf(__fmul_rn(m, m), 1e-16f));
+        const float li2 = __fmul_rn(c.L, inv2);                 // L / sin^2
         const float rra = fmaf(r, r, c.a2);
         const float delta = fmaf(-2.0f, r, rra);
         const float P = fmaf(c.E, rra, -c.aL);
@@ -511,20 +526,18 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj
         const float num = opposite ? c.K : __fadd_rn(P, y[3]);
         const float den = opposite ? __fsub_rn(P, y[3]) : delta;
         const float inflow = __fmul_rn(num, rcp_approx(den));
-        const float inv = rcp_approx(fmaxf(fabsf(sn), 1e-9f));
-        const float li = __fmul_rn(c.L, inv);    // L / |sin|
-        const float li2 = __fmul_rn(li, inv);    // L / sin^2
         k[0] = y[3];
         k[1] = y[4];
-        k[2] = fmaf(c.a, inflow, fmaf(li, inv, -c.aE));
+        k[2] = fmaf(c.a, inflow, fmaf(c.L, inv2, -c.aE));
         k[3] = fmaf(r, fmaf(c.twoE, P, -c.K), c.K);
-        k[4] = __fmul_rn(cs, fmaf(sn, c.nA2E2, copysignf(__fmul_rn(li, li2), sn)));
+        k[4] = __fmul_rn(sc, fmaf(li2, li2, c.nA2E2));
         if constexpr (kProj) {
             const float P2 = __fmul_rn(P, P);
             pj->R = fmaf(-delta, c.K, P2);
             pj->Rz = __fmul_rn(0.05f, fmaf(fabsf(delta), c.K, P2));
-            const float cs2 = __fmul_rn(cs, cs);
-            const float l2cot2 = __fmul_rn(cs2, __fmul_rn(li, li));  // L^2 cot^2
+            const float cm = odd ? sr : cr;                     // +-cos
+            const float cs2 = __fmul_rn(cm, cm);
+            const float l2cot2 = __fmul_rn(cs2, __fmul_rn(c.L, li2));  // L^2 cot^2
             const float pm = __fmul_rn(c.nA2E2, cs2);
             pj->Th = __fsub_rn(fmaf(-c.nA2E2, cs2, c.Q), l2cot2);
             pj->Thz = __fmul_rn(0.05f, __fadd_rn(__fadd_rn(fabsf(c.Q), fabsf(pm)), l2cot2));
