@@ -922,11 +922,12 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
     const int lane = threadIdx.x & 31;
     const long long n = ctl->n_rays;
     Lane<T> s;
-    long long ray = -1;
+    // A batch holds < 2^31 rays (the API refuses more), so queue positions and ray indices fit 32 bits.
+    int ray = -1;
     bool exhausted = false;
-    int pool_pos = 0, pool_end = 0;  // this warp's chunk of the queue (a batch holds < 2^31 rays)
-    unsigned long long n_acc = 0, n_rej = 0;
-    int iter = 0;
+    int pool_pos = 0, pool_end = 0;  // this warp's chunk of the queue
+    // Per-lane step counts, flushed to the 64-bit totals before they can wrap (a ray adds < 2^31).
+    unsigned n_acc = 0, n_rej = 0;
     for (;;) {
         // A warp traces its rays in batches of 32 queue-adjacent rays -- neighbouring pixels, or rays
         // of one cost bucket -- and takes the next batch only when every lane's ray has ended. Rays
@@ -953,7 +954,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                     fi = frame_of(frames, nframes, q);
                     const FrameDev& f = frames[fi];
                     tile_pixel(f.d.width, f.d.height, static_cast<int>(q - f.offset), &prow, &pcol);
-                    ray = f.offset + static_cast<long long>(prow) * f.d.width + pcol;
+                    ray = static_cast<int>(f.offset) + prow * f.d.width + pcol;
                 } else {
                     ray = order ? order[q] : q;
                 }
@@ -989,13 +990,19 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
             pool_pos = pool_pos + 32 < pool_end ? pool_pos + 32 : pool_end;
         }
         if (!__any_sync(kFull, ray >= 0)) break;
-        ++iter;
-        const bool reproject = p.reproject_every > 0 && (iter % p.reproject_every) == 0;
         if (ray >= 0) {
+            // The optional FP64 re-projection on every reproject_every-th attempt of the ray.
+            const bool reproject = p.reproject_every > 0 && (s.acc + s.rej + 1) % p.reproject_every == 0;
             const int r = attempt<T>(s, p, ray, out, reproject, ctl, L, geom);
             if (r != kContinue) {
-                n_acc += s.acc;
-                n_rej += s.rej;
+                n_acc += static_cast<unsigned>(s.acc);
+                n_rej += static_cast<unsigned>(s.rej);
+                if ((n_acc | n_rej) >= (1u << 30)) {
+                    atomicAdd(&ctl->stats[0], static_cast<unsigned long long>(n_acc));
+                    atomicAdd(&ctl->stats[1], static_cast<unsigned long long>(n_rej));
+                    n_acc = 0;
+                    n_rej = 0;
+                }
                 if (r == kRescue || r == kRestart) {
                     double y[5];
                     const bool restart = r == kRestart;
@@ -1018,13 +1025,14 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
         }
     }
     // Step statistics: one atomic per warp.
+    unsigned long long t_acc = n_acc, t_rej = n_rej;
     for (int o = 16; o > 0; o >>= 1) {
-        n_acc += __shfl_down_sync(kFull, n_acc, o);
-        n_rej += __shfl_down_sync(kFull, n_rej, o);
+        t_acc += __shfl_down_sync(kFull, t_acc, o);
+        t_rej += __shfl_down_sync(kFull, t_rej, o);
     }
     if (lane == 0) {
-        atomicAdd(&ctl->stats[0], n_acc);
-        atomicAdd(&ctl->stats[1], n_rej);
+        atomicAdd(&ctl->stats[0], t_acc);
+        atomicAdd(&ctl->stats[1], t_rej);
     }
 }
 

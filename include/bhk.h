@@ -119,8 +119,8 @@ typedef struct {
     int32_t max_steps;      /* accepted-step cap per ray; 0 -> 20000 */
     double r_escape;        /* escaped once r > max(r_escape, 1.5 r_obs) while rising; 0 -> 1000 */
     double capture_eps;     /* captured once r < r_+(1 + capture_eps) while falling; 0 -> 1e-6 */
-    int32_t reproject_every;/* mixed: besides the FP32 re-projection every step, an FP64 radial one every N
-                               iterations of a warp (results then depend on the launch shape); 0 = off */
+    int32_t reproject_every;/* mixed: besides the FP32 re-projection every step, an FP64 radial one on every
+                               N-th step attempt of a ray; 0 = off */
     int32_t block;          /* threads per block of the tracer; 0 -> autotuned or 128 */
     int32_t chunk;          /* rays a warp takes from the queue at a time, traced in batches of 32 (one
                                per lane; the next batch starts when all 32 have ended); rounded up to a

@@ -134,6 +134,24 @@ def test_launch_shape_and_order_do_not_change_results(ctx, prec, rb):
             np.testing.assert_array_equal(got[k], base[k], err_msg=f"{k} {blk} {ch} {bu} {graph}")
 
 
+def test_fp64_reprojection_cadence_is_per_ray(ctx, oracle):
+    """reproject_every counts a ray's own step attempts, so the optional FP64 radial re-projection
+    keeps results independent of the launch shape, and changes them only at FP32 integration error."""
+    f = bhk.frame_c1(48, 40)
+    base = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", reproject_every=3, block=128, chunk=32)))
+    for blk, ch in ((64, 1), (128, 256)):
+        got = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", reproject_every=3, block=blk, chunk=ch)))
+        for k in bhk.FIELDS[:-1]:  # (all but the rejected-step count, as above)
+            np.testing.assert_array_equal(got[k], base[k], err_msg=f"{k} {blk} {ch}")
+    off = host(ctx.trace_frames([f], bhk.TraceOpts("mixed")))
+    al, be = po.pixel_grid(f.width, f.height, f.alpha_lo, f.alpha_hi, f.beta_lo, f.beta_hi)
+    ca, cb = oracle.critical_curve_finite(f.a, f.r_obs, f.theta_obs, 800)
+    outside = po.band_distance(al, be, ca, cb) > 1e-2
+    np.testing.assert_array_equal(base["outcome"][outside], off["outcome"][outside])
+    err = errors(base, off, outside)
+    assert max(err.values()) < 2e-4, err
+
+
 def test_register_budget_variants_agree_within_fp32_error(ctx, oracle):
     """The register-capped FP32 variants are separate compilations (their floating-point
     contraction may differ in the last bit), so they agree to FP32 integration error, not bits."""
