@@ -426,6 +426,11 @@ struct Lane {
     T h;
     T r_esc, zone_top;  // (the capture and disk radii are read from the geometry where they are needed)
     int acc, rej;
+    // FP32 lanes: the outcome of a ray that has ended (-1 while it is traced). Its results wait in the
+    // lane's state (y, s.h) and are written with the rest of the warp's batch by flush_f32: a warp's
+    // rays end on different steps, and writing each as it ends runs that code once per step on which
+    // any lane ended.
+    int pend;
     bool last_rej;
     // FP32 only: the ray is in the southern hemisphere and y[1], y[4] hold pi - theta and -vtheta.
     // The Kerr metric is symmetric under theta -> pi - theta, so the equations are unchanged, and
@@ -477,7 +482,7 @@ __device__ __forceinline__ void lane_begin_f32(Lane<float>& s, const RayGeom& g,
         rhs(s.c, s.y, s.k[0]);
         s.h = first_step<float>(s.y, s.k[0], p.tol0_f, s.c.a2, g.naked != 0);
     }
-    s.acc = 0; s.rej = 0; s.last_rej = false;
+    s.acc = 0; s.rej = 0; s.last_rej = false; s.pend = -1;
 }
 
 // Starts an FP64 lane on ray `ray` at its launch point, first step from kerr::photonStepSize (the
@@ -495,7 +500,7 @@ __device__ __forceinline__ void lane_begin_launch(Lane<double>& s, const RayGeom
     rhs(s.c, s.y, s.k[0], static_cast<Proj<double>*>(nullptr), &s.kt[0]);
     ks_position(g.a, s.y[0], s.y[1], s.y[2], s.pos);
     s.h = first_step<double>(s.y, s.k[0], p.tol0, s.c.a2, g.naked != 0);
-    s.acc = 0; s.rej = 0; s.last_rej = false;
+    s.acc = 0; s.rej = 0; s.last_rej = false; s.pend = -1;
 }
 
 __device__ __forceinline__ void write_out(const Outputs& o, long long ray, int outcome, double rd, double pd, double g,
@@ -533,14 +538,19 @@ __device__ __forceinline__ void write_path(const Lane<T>& s, const Outputs& o, l
     if (o.turns) o.turns[ray] = s.track ? s.swept / (2.0 * kPi) : nan_d();
 }
 
+// A ray that ends without a disk or sky result. r_cap: the capture radius of a captured ray (its
+// closest approach is at most that; FP32 lanes read it again when their batch is written).
 template <typename T>
-// r_cap: the capture radius of a captured ray (its closest approach is at most that).
-__device__ __forceinline__ int finish(const Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl,
+__device__ __forceinline__ int finish(Lane<T>& s, const Outputs& o, long long ray, int outcome, Control* ctl,
                                       double r_cap = INFINITY) {
-    const T n = nan_t<T>();
-    write_out_t<T>(o, ray, outcome, n, n, n, n, n, s.acc, s.rej);
-    write_path(s, o, ray, s.t, r_cap);
-    if (outcome == BHK_RAY_UNFINISHED) atomicAdd(&ctl->stats[2], 1ull);
+    if constexpr (sizeof(T) == 4) {
+        s.pend = outcome;
+    } else {
+        const T n = nan_t<T>();
+        write_out_t<T>(o, ray, outcome, n, n, n, n, n, s.acc, s.rej);
+        write_path(s, o, ray, s.t, r_cap);
+        if (outcome == BHK_RAY_UNFINISHED) atomicAdd(&ctl->stats[2], 1ull);
+    }
     return kFinished;
 }
 
@@ -579,29 +589,69 @@ __device__ __forceinline__ T locate(const T* y0, const T* y1, const T k[7][5], T
     return s;
 }
 
-// A ray that left through r = target within the step just taken: the escape direction is the
-// backward tangent there (dense output), as (theta_inf, phi_inf).
+// The escape direction at the exit point x (the state in the lane's hemisphere representation):
+// the backward tangent there, as (theta_inf, phi_inf).
 template <typename T>
-__device__ __forceinline__ int escape(const Lane<T>& s, const T prev[5], T h, T target, int outcome, const Outputs& out,
-                                   long long ray, double t_prev) {
-    const T sg = locate(prev, s.y, s.k, h, 0, target);
+__device__ __forceinline__ void exit_direction(const RayC<T>& c, bool south, const T x_in[5], T* theta_inf,
+                                               T* phi_inf) {
     T x[5], kk[5];
 #pragma unroll
-    for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
-    rhs(s.c, x, kk);
+    for (int i = 0; i < 5; ++i) x[i] = x_in[i];
+    rhs(c, x, kk);
     T v[3];
-    if (s.south) {  // back to the physical angle: cos(pi - t) = -cos t, d(pi - t) = -dt
+    if (south) {  // back to the physical angle: cos(pi - t) = -cos t, d(pi - t) = -dt
         x[1] = T(kPi) - x[1];
         x[4] = -x[4];
     }
-    cartesian_velocity<T>(s.c.a, x[0], x[1], x[2], x[3], x[4], kk[2], v);
+    cartesian_velocity<T>(c.a, x[0], x[1], x[2], x[3], x[4], kk[2], v);
     const T nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     const T dz = fmin(fmax(-v[2] / nrm, T(-1)), T(1));
-    const T n = nan_t<T>();
-    write_out_t<T>(out, ray, outcome, n, n, n, acos(dz), atan2(-v[1] / nrm, -v[0] / nrm), s.acc, s.rej);
-    if constexpr (sizeof(T) == 8) write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
-    else write_path(s, out, ray, 0.0);
+    *theta_inf = acos(dz);
+    *phi_inf = atan2(-v[1] / nrm, -v[0] / nrm);
+}
+
+// A ray that left through r = target within the step just taken: the exit point from the dense
+// output. FP32 lanes keep it in y and work out the direction when their batch is written.
+template <typename T>
+__device__ __forceinline__ int escape(Lane<T>& s, const T prev[5], T h, T target, int outcome, const Outputs& out,
+                                   long long ray, double t_prev) {
+    const T sg = locate(prev, s.y, s.k, h, 0, target);
+    T x[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) x[i] = dense(prev[i], s.y[i], s.k, h, i, sg);
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) s.y[i] = x[i];
+        s.pend = outcome;
+    } else {
+        T ti, pi;
+        exit_direction(s.c, s.south, x, &ti, &pi);
+        const T n = nan_t<T>();
+        write_out_t<T>(out, ray, outcome, n, n, n, ti, pi, s.acc, s.rej);
+        write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
+    }
     return kFinished;
+}
+
+// Writes the results of an FP32 lane whose ray has ended (s.pend): disk r, g, phi in y[0..2], the
+// exit point in y for the skies; r_min, the steps and the capture radius as in finish().
+__device__ __forceinline__ void flush_f32(const Lane<float>& s, const Outputs& o, long long ray, Control* ctl,
+                                          const RayGeom* __restrict__ geom, const LaunchSoA& L) {
+    const float n = nan_f();
+    float rd = n, pd = n, g = n, ti = n, pi = n;
+    double r_cap = INFINITY;
+    const int oc = s.pend;
+    if (oc == BHK_RAY_DISK) {
+        rd = s.y[0]; g = s.y[1]; pd = s.y[2];
+    } else if (oc == BHK_RAY_ESCAPED || oc == BHK_RAY_ESCAPED_BEYOND) {
+        exit_direction(s.c, s.south, s.y, &ti, &pi);
+    } else if (oc == BHK_RAY_CAPTURED) {
+        r_cap = geom[L.geom_id[ray]].r_cap;
+    } else if (oc == BHK_RAY_UNFINISHED) {
+        atomicAdd(&ctl->stats[2], 1ull);
+    }
+    write_out_t<float>(o, ray, oc, rd, pd, g, ti, pi, s.acc, s.rej);
+    write_path(s, o, ray, 0.0, r_cap);
 }
 
 // One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
@@ -788,8 +838,8 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 float g;
                 if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
                     const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
-                    write_out_t<float>(out, ray, BHK_RAY_DISK, rc, ph, g, nan_f(), nan_f(), s.acc, s.rej);
-                    write_path(s, out, ray, 0.0);
+                    s.y[0] = rc; s.y[1] = g; s.y[2] = ph;  // written with the batch (flush_f32)
+                    s.pend = BHK_RAY_DISK;
                     return kFinished;
                 }
             }
@@ -934,7 +984,15 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
         // that start together stay alike (similar step sizes, events and branches) for their whole
         // path; refilling lanes one by one mixes rays at different stages within the warp, and the
         // divergence that follows costs more than the lanes that wait for their batch's last ray.
-        while (!exhausted && !__any_sync(kFull, ray >= 0)) {
+        // A lane traces while its ray has not ended (FP64 lanes drop the ray as it ends).
+        const bool active = ray >= 0 && s.pend < 0;
+        if (!__any_sync(kFull, active)) {
+            // The batch is over: its FP32 results are written together, then the next one is taken.
+            if constexpr (sizeof(T) == 4) {
+                if (ray >= 0) flush_f32(s, out, ray, ctl, geom, L);
+            }
+            ray = -1;
+            if (exhausted) break;
             if (pool_pos >= pool_end) {
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(&ctl->queue, static_cast<unsigned long long>(p.chunk));
@@ -984,13 +1042,13 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                 const RayGeom& G = geom[L.geom_id[ray]];
                 if (G.dead) {  // seen from inside the horizon: the hole, with no step taken
                     finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
-                    ray = -1;
+                    if constexpr (sizeof(T) == 8) ray = -1;
                 }
             }
             pool_pos = pool_pos + 32 < pool_end ? pool_pos + 32 : pool_end;
+            continue;
         }
-        if (!__any_sync(kFull, ray >= 0)) break;
-        if (ray >= 0) {
+        if (active) {
             // The optional FP64 re-projection on every reproject_every-th attempt of the ray.
             const bool reproject = p.reproject_every > 0 && (s.acc + s.rej + 1) % p.reproject_every == 0;
             const int r = attempt<T>(s, p, ray, out, reproject, ctl, L, geom);
@@ -1019,8 +1077,10 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
                     push_rescue(rescue, rescue_cap, ctl, ray, y, restart ? 0.0 : double(s.h),
                                 restart ? y[0] : fmin(double(s.rmin), y[0]), restart ? 0 : s.acc,
                                 restart ? 0 : s.rej, restart ? 1 : 0, out);
+                    ray = -1;
+                } else if constexpr (sizeof(T) == 8) {
+                    ray = -1;  // written as it ended
                 }
-                ray = -1;
             }
         }
     }
