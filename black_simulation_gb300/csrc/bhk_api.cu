@@ -255,7 +255,7 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
         BHK_CUDA(cudaMemsetAsync(c->hist, 0, sizeof(unsigned) * kMaxBuckets, s));
         launch_sort(L, SortScratch{c->hist, c->offs, c->order}, r.p, c->ctl, lgrid, s);
         order = c->order;
-    }  // frames without the sort: the trace kernel takes its rays by 4 x 8 pixel tiles itself
+    }  // frames without the sort: the trace kernel takes its rays by 8 x 4 pixel tiles itself
     if (timed) BHK_CUDA(cudaEventRecord(c->ev0, s));
     const bool fused = b.mode == 0 && r.buckets <= 1;
     launch_trace(r.fp64, r.regcap, L, c->geom, order, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl,

@@ -126,7 +126,7 @@ typedef struct {
                                per lane; the next batch starts when all 32 have ended); rounded up to a
                                multiple of 32; 0 -> autotuned or 32 */
     int32_t sort_buckets;   /* rays pre-sorted into this many cost buckets; 0 -> autotuned or 1; 1 = none
-                               (frames are then taken by 4 x 8 pixel tiles and launched in the kernel) */
+                               (frames are then taken by 8 x 4 pixel tiles and launched in the kernel) */
     int32_t use_graph;      /* 1: replay the whole batch as one captured CUDA graph */
     int32_t reg_budget;     /* mixed tracer variant: 0 autotuned (else 2), 1: <= 102 registers per
                                thread (20 warps/SM, blocks <= 128), 2: <= 85 (24 warps/SM), 3: uncapped */

@@ -183,7 +183,7 @@ def test_ragged_multi_frame_batch_equals_single_frames(ctx):
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_tile_order_covers_every_pixel_of_ragged_frames(ctx, prec):
-    """Frames are traced in 4 x 8 pixel tiles (ragged at the right and bottom edges) with the launch
+    """Frames are traced in 8 x 4 pixel tiles (ragged at the right and bottom edges) with the launch
     made inside the trace kernel; tracing every pixel through the pixel-list path (row order, launch
     kernel) gives the same bits, and no pixel is left untraced."""
     frames = [bhk.Frame(0.9, 40.0, 1.1, 13, 7, -9, 9, -5, 5, 0.0, 20.0),
