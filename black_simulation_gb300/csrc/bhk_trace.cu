@@ -790,9 +790,8 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         prev[i] = s.y[i];
         s.y[i] = y5[i];
     }
-    if (!isfinite(s.y[0])) {
-        if constexpr (F64) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
-        else return kRestart;
+    if constexpr (F64) {
+        if (!isfinite(s.y[0])) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
     }
     // Closest approach (when asked for): the step's end, or inside it where vr changes sign (the
     // turning point, from the dense output).
@@ -816,71 +815,101 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         s.swept += acos(fmin(fmax(cang, -1.0), 1.0));
         s.pos[0] = x1[0]; s.pos[1] = x1[1]; s.pos[2] = x1[2];
     }
-    const T hp = T(0.5 * kPi);
-    // Thin disk: theta crosses pi/2 inside [r_in, r_out]. (FP32: the hemisphere representation keeps
-    // theta at or below pi/2 at a step's start, so a crossing is theta above pi/2 at its end.)
-    bool crossed;
-    if constexpr (F64) crossed = (prev[1] - hp) * (s.y[1] - hp) < T(0);
-    else crossed = prev[1] < hp && s.y[1] > hp;
-    if (crossed) {
-        const T sg = locate(prev, s.y, s.k, h, 1, hp);
-        const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
-        const RayGeom& G = geom[L.geom_id[ray]];
-        T r_in, r_out;
-        if constexpr (F64) { r_in = G.r_in; r_out = G.r_out; } else { r_in = G.r_inf; r_out = G.r_outf; }
-        if (rc >= r_in && rc <= r_out) {
-            if constexpr (F64) {
-                double g;
-                if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
-                    const double ph = wrap_2pi(dense(prev[2], s.y[2], s.k, h, 2, sg));
-                    write_out(out, ray, BHK_RAY_DISK, rc, ph, g, nan_d(), nan_d(), s.acc, s.rej);
-                    write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
-                    return kFinished;
-                }
-            } else {
-                float g;
-                if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
-                    const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
-                    s.y[0] = rc; s.y[1] = g; s.y[2] = ph;  // written with the batch (flush_f32)
-                    s.pend = BHK_RAY_DISK;
-                    return kFinished;
+    const bool falling = s.y[0] < prev[0];
+    // The rare events of a step, tested at once for FP32 lanes: a non-finite state, the ring's
+    // neighbourhood, escape, the capture zone, and a pole or the equator crossed (a disk crossing is
+    // one). Most steps meet none and pass all of their code with one branch.
+    bool rare = true;
+    if constexpr (!F64) {
+        const T a0 = fabs(s.y[0]);
+        rare = !(a0 >= T(0.02) && a0 <= s.r_esc) || (s.y[0] < s.zone_top && falling) || s.y[1] < T(0) ||
+               s.y[1] > T(0.5 * kPi);
+    }
+    if (rare) {
+        if constexpr (!F64) {
+            if (!isfinite(s.y[0])) return kRestart;
+        }
+        const T hp = T(0.5 * kPi);
+        // Thin disk: theta crosses pi/2 inside [r_in, r_out]. (FP32: the hemisphere representation keeps
+        // theta at or below pi/2 at a step's start, so a crossing is theta above pi/2 at its end.)
+        bool crossed;
+        if constexpr (F64) crossed = (prev[1] - hp) * (s.y[1] - hp) < T(0);
+        else crossed = prev[1] < hp && s.y[1] > hp;
+        if (crossed) {
+            const T sg = locate(prev, s.y, s.k, h, 1, hp);
+            const T rc = dense(prev[0], s.y[0], s.k, h, 0, sg);
+            const RayGeom& G = geom[L.geom_id[ray]];
+            T r_in, r_out;
+            if constexpr (F64) { r_in = G.r_in; r_out = G.r_out; } else { r_in = G.r_inf; r_out = G.r_outf; }
+            if (rc >= r_in && rc <= r_out) {
+                if constexpr (F64) {
+                    double g;
+                    if (disk_redshift(s.c.a, s.c.E, s.c.L, rc, &g)) {
+                        const double ph = wrap_2pi(dense(prev[2], s.y[2], s.k, h, 2, sg));
+                        write_out(out, ray, BHK_RAY_DISK, rc, ph, g, nan_d(), nan_d(), s.acc, s.rej);
+                        write_path(s, out, ray, dense1(t_prev, s.t, s.kt, h, sg));
+                        return kFinished;
+                    }
+                } else {
+                    float g;
+                    if (disk_redshift_f(s.c.a, s.c.E, s.c.L, rc, &g)) {
+                        const float ph = wrap_2pi_f(dense(prev[2], s.y[2], s.k, h, 2, sg));
+                        s.y[0] = rc; s.y[1] = g; s.y[2] = ph;  // written with the batch (flush_f32)
+                        s.pend = BHK_RAY_DISK;
+                        return kFinished;
+                    }
                 }
             }
         }
-    }
-    const bool falling = s.y[0] < prev[0];
-    // Past |a| = 1 only (around a hole r stays above r_+ > 1): the ring singularity, where
-    // Sigma = r^2 + a^2 cos^2(theta) < 4e-4 (shaders/trace.frag:1773-1778). That needs |r| < 0.02 and
-    // |cos theta| < 0.02 / |a|, where cos theta = sin d, d = pi/2 - theta, is d - d^3/6 to 3e-11 (the
-    // same in either hemisphere representation).
-    if (fabs(s.y[0]) < T(0.02)) {
-        const T d = T(0.5 * kPi) - s.y[1];
-        const T c = d - d * d * d * T(1.0 / 6.0);
-        if (s.y[0] * s.y[0] + s.c.a2 * c * c < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
-    }
-    // Escaped: rising past r_esc, or past |a| = 1 falling past -r_esc into the sky of the r < 0 region,
-    // beyond the ring (shaders/trace.frag:1779-1792). Rays start inside |r| < r_esc (the camera sits
-    // within r_esc / 1.5), so |r| first exceeds r_esc on the step that leaves.
-    if (fabs(s.y[0]) > s.r_esc) {
-        const bool beyond = s.y[0] < T(0);
-        return escape(s, prev, h, beyond ? -s.r_esc : s.r_esc, beyond ? BHK_RAY_ESCAPED_BEYOND : BHK_RAY_ESCAPED, out,
-                      ray, t_prev);
-    }
-    // Captured (zone_top lies above r_cap; both are -1e30 past |a| = 1; r_cap is read from the
-    // geometry here rather than held in a register).
-    if (s.y[0] < s.zone_top && falling) {
-        const RayGeom& G = geom[L.geom_id[ray]];
-        if (s.y[0] < (F64 ? T(G.r_cap) : T(G.r_capf))) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
-        if constexpr (F64) {
-            if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
-                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
-        } else {
-            if (no_radial_root_below_f(s.c, G.r_capf, s.y[0]))
-                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
-            // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
-            if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
-                return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
-            return kRescue;
+        // Past |a| = 1 only (around a hole r stays above r_+ > 1): the ring singularity, where
+        // Sigma = r^2 + a^2 cos^2(theta) < 4e-4 (shaders/trace.frag:1773-1778). That needs |r| < 0.02 and
+        // |cos theta| < 0.02 / |a|, where cos theta = sin d, d = pi/2 - theta, is d - d^3/6 to 3e-11 (the
+        // same in either hemisphere representation).
+        if (fabs(s.y[0]) < T(0.02)) {
+            const T d = T(0.5 * kPi) - s.y[1];
+            const T c = d - d * d * d * T(1.0 / 6.0);
+            if (s.y[0] * s.y[0] + s.c.a2 * c * c < T(4e-4)) return finish(s, out, ray, BHK_RAY_RING, ctl);
+        }
+        // Escaped: rising past r_esc, or past |a| = 1 falling past -r_esc into the sky of the r < 0 region,
+        // beyond the ring (shaders/trace.frag:1779-1792). Rays start inside |r| < r_esc (the camera sits
+        // within r_esc / 1.5), so |r| first exceeds r_esc on the step that leaves.
+        if (fabs(s.y[0]) > s.r_esc) {
+            const bool beyond = s.y[0] < T(0);
+            return escape(s, prev, h, beyond ? -s.r_esc : s.r_esc,
+                          beyond ? BHK_RAY_ESCAPED_BEYOND : BHK_RAY_ESCAPED, out, ray, t_prev);
+        }
+        // Captured (zone_top lies above r_cap; both are -1e30 past |a| = 1; r_cap is read from the
+        // geometry here rather than held in a register).
+        if (s.y[0] < s.zone_top && falling) {
+            const RayGeom& G = geom[L.geom_id[ray]];
+            if (s.y[0] < (F64 ? T(G.r_cap) : T(G.r_capf))) return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
+            if constexpr (F64) {
+                if (no_radial_root_below(s.c.a, s.c.E, s.c.L, s.c.Q, s.y[0], p.eps))
+                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
+            } else {
+                if (no_radial_root_below_f(s.c, G.r_capf, s.y[0]))
+                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
+                // Not proven in FP32: decide in FP64 (src/kerr.h:167-172 -- R near a turning point).
+                if (no_radial_root_below(G.a, L.E[ray], L.L[ray], L.Q[ray], double(s.y[0]), p.eps))
+                    return finish(s, out, ray, BHK_RAY_CAPTURED, ctl, G.r_cap);
+                return kRescue;
+            }
+        }
+        if constexpr (!F64) {
+            // Pole reflection (kerr::normalizeAngles) in the hemisphere representation, carrying the
+            // FSAL derivative: under theta -> -theta Theta'(theta) changes sign.
+            if (s.y[1] < T(0)) {  // over the pole of this hemisphere
+                s.y[1] = -s.y[1];
+                s.y[2] += T(kPi);
+                s.y[4] = -s.y[4];
+                s.k[6][4] = -s.k[6][4];
+            }
+            if (s.y[1] > T(0.5 * kPi)) {  // across the equator: the other hemisphere's representation
+                s.y[1] = T(kPi) - s.y[1];
+                s.y[4] = -s.y[4];
+                s.k[6][4] = -s.k[6][4];
+                s.south = !s.south;
+            }
         }
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
@@ -892,18 +921,6 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         enforce_constraints(s.c.a, cc, st);
         s.y[1] = st.theta; s.y[2] = st.phi; s.y[3] = st.vr; s.y[4] = st.vtheta;
     } else {
-        if (s.y[1] < T(0)) {  // over the pole of this hemisphere
-            s.y[1] = -s.y[1];
-            s.y[2] += T(kPi);
-            s.y[4] = -s.y[4];
-            s.k[6][4] = -s.k[6][4];
-        }
-        if (s.y[1] > T(0.5 * kPi)) {  // across the equator: the other hemisphere's representation
-            s.y[1] = T(kPi) - s.y[1];
-            s.y[4] = -s.y[4];
-            s.k[6][4] = -s.k[6][4];
-            s.south = !s.south;
-        }
         // Every step, from the FSAL stage's potentials: keeps the FP32 rounding of vr ~ r^2 made
         // far out from becoming an O(1) error near the hole.
         if (pj.R > pj.Rz) s.y[3] = copysignf(sqrt_approx(pj.R), s.y[3]);
