@@ -42,7 +42,7 @@ METRIC = "geodesics/s at \u22641e-4 rad exit-angle err vs FP64: surrogate vs pla
 REF_TOL = 1e-2          # reference product tolerance (src/trajectory.cpp:261); meets the 1e-4 bar
 # DRAM bytes (read + write) of one tracer launch from ncu, by workload: the 960x540 capture of
 # profiles/trace_kernel_1080p_mixed.md (14.61 MB) scaled by rays to the full frame.
-NCU_TRAFFIC = {"1080p": 5.2e6}  # DRAM read + write of one trace launch: ncu at half size, x4 rays
+NCU_TRAFFIC = {"1080p": 6.6e6}  # DRAM read + write of one trace launch: ncu at half size, x4 rays
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
