@@ -517,7 +517,10 @@ __device__ __forceinline__ void rhs(const RayC<T>& c, const T y[5], T k[5], Proj
         const bool odd = (sincos_reduced(y[1], &sr, &cr) & 1) != 0;
         const float m = odd ? cr : sr;                          // +-sin
         const float sc = __fmul_rn(odd ? -sr : sr, cr);         // sin cos
-        const float inv2 = rcp_approx(fmaxf(__fmul_rn(m, m), 1e-16f));
+        // No clamp on sin^2: it is 0 only with theta exactly on a pole, where L / sin^2 is not finite
+        // (0 * inf for the L = 0 rays that cross the axis; rays with L != 0 turn before the pole), so
+        // such a stage makes the step's error non-finite and the step is rejected and retried shorter.
+        const float inv2 = rcp_approx(__fmul_rn(m, m));
         const float li2 = __fmul_rn(c.L, inv2);                 // L / sin^2
         const float rra = fmaf(r, r, c.a2);
         const float delta = fmaf(-2.0f, r, rra);

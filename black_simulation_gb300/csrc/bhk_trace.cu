@@ -817,13 +817,13 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     }
     const bool falling = s.y[0] < prev[0];
     // The rare events of a step, tested at once for FP32 lanes: a non-finite state, the ring's
-    // neighbourhood, escape, the capture zone, and a pole or the equator crossed (a disk crossing is
-    // one). Most steps meet none and pass all of their code with one branch.
+    // neighbourhood, escape, the capture zone, a pole or the equator crossed (a disk crossing is one)
+    // and the step limit. Most steps meet none and pass all of their code with one branch.
     bool rare = true;
     if constexpr (!F64) {
         const T a0 = fabs(s.y[0]);
         rare = !(a0 >= T(0.02) && a0 <= s.r_esc) || (s.y[0] < s.zone_top && falling) || s.y[1] < T(0) ||
-               s.y[1] > T(0.5 * kPi);
+               s.y[1] > T(0.5 * kPi) || s.acc >= p.max_steps;
     }
     if (rare) {
         if constexpr (!F64) {
@@ -910,6 +910,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
                 s.k[6][4] = -s.k[6][4];
                 s.south = !s.south;
             }
+            if (s.acc >= p.max_steps) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
         }
     }
     // Pole reflection (kerr::normalizeAngles) and constraint re-projection (kerr::enforceConstraints),
@@ -960,7 +961,9 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         }
     }
     s.last_rej = false;
-    if (s.acc >= p.max_steps) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
+    if constexpr (F64) {
+        if (s.acc >= p.max_steps) return finish(s, out, ray, BHK_RAY_UNFINISHED, ctl);
+    }
     return kContinue;
 }
 
