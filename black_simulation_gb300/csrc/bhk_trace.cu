@@ -430,9 +430,9 @@ struct Lane {
     T r_esc, zone_top;  // (the capture and disk radii are read from the geometry where they are needed)
     int acc, rej;
     // FP32 lanes: the outcome of a ray that has ended (-1 while it is traced). Its results wait in the
-    // lane's state (y, s.h) and are written with the rest of the warp's batch by flush_f32: a warp's
-    // rays end on different steps, and writing each as it ends runs that code once per step on which
-    // any lane ended.
+    // lane's state (y) and are written with the rest of the warp's batch by flush_f32: a warp's rays
+    // end on different steps, and writing each as it ends runs that code once per step on which any
+    // lane ended.
     int pend;
     bool last_rej;
     // FP32 only: the ray is in the southern hemisphere and y[1], y[4] hold pi - theta and -vtheta.
