@@ -197,18 +197,24 @@ def test_tile_order_covers_every_pixel_of_ragged_frames(ctx, prec):
         np.testing.assert_array_equal(full[k], listed[k], err_msg=k)
 
 
-def test_host_buffer_entry_point_and_step_cap(ctx):
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_host_buffer_entry_point_and_step_cap(ctx, prec):
+    """The host-buffer call equals the device one; a step cap ends rays as unfinished once that many
+    steps were accepted (or rejected), with NaN results, and the statistics count them."""
     f = bhk.frame_c1(16, 16)
-    dev = host(ctx.trace_frames([f], bhk.TraceOpts("fp64")))
-    out, st = ctx.trace_frames_host([f], bhk.TraceOpts("fp64"))
+    dev = host(ctx.trace_frames([f], bhk.TraceOpts(prec)))
+    out, st = ctx.trace_frames_host([f], bhk.TraceOpts(prec))
     assert st == bhk.OK
     for k in bhk.FIELDS:
         np.testing.assert_array_equal(out[k], dev[k])
-    capped, st = ctx.trace_frames_host([f], bhk.TraceOpts("fp64", max_steps=5))
+    capped, st = ctx.trace_frames_host([f], bhk.TraceOpts(prec, max_steps=5))
     assert st == bhk.EUNFINISHED
     assert np.all(capped["outcome"][capped["steps"] >= 5] != bhk.ESCAPED)
-    assert np.any(capped["outcome"] == bhk.UNFINISHED)
-    assert ctx.stats()["unfinished"] == np.sum(capped["outcome"] == bhk.UNFINISHED)
+    unf = capped["outcome"] == bhk.UNFINISHED
+    assert np.any(unf)
+    assert np.all((capped["steps"][unf] == 5) | (capped["rejected"][unf] == 5))  # either count can end it
+    assert np.all(np.isnan(capped["r_disk"][unf]))
+    assert ctx.stats()["unfinished"] == np.sum(unf)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
