@@ -1148,6 +1148,7 @@ __global__ void rescue_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, Out
         s.track = false;  // the FP32 part kept no time or swept angle
         s.t = 0.0;
         s.swept = 0.0;
+        s.pend = -1;
         int res = kContinue;
         while (res == kContinue) res = attempt<double>(s, p, r.ray, out, false, ctl, L, geom);
         atomicAdd(&ctl->stats[0], static_cast<unsigned long long>(s.acc - r.accepted));
