@@ -61,6 +61,57 @@ def test_frames_and_photon_launches_match_reference(cuda, golden):
         close(s.cpu().numpy()[0], g["zamo_state"][i], rtol=1e-11, atol=1e-11)
 
 
+def _ks_metric(a, r, th):
+    """The Kerr-Schild metric g_mn at (r, theta) (kerr::metricTensor, src/kerr.cpp:238-254) and Sigma."""
+    sn, cs = math.sin(th), math.cos(th)
+    sigma = r * r + a * a * cs * cs
+    A = (r * r + a * a) ** 2 - a * a * (r * r - 2 * r + a * a) * sn * sn
+    f = 2 * r / sigma
+    gm = np.zeros((4, 4))
+    gm[0, 0] = -(1 - f); gm[0, 1] = gm[1, 0] = f; gm[0, 3] = gm[3, 0] = -f * a * sn * sn
+    gm[1, 1] = 1 + f; gm[1, 3] = gm[3, 1] = -a * sn * sn * (1 + f); gm[2, 2] = sigma; gm[3, 3] = A * sn * sn / sigma
+    return gm, sigma
+
+
+def _observed_photon(a, r, th, v, look):
+    """kerr::observedPhoton (src/kerr.cpp:485-500) composed from the GPU mirrors: the observer moving
+    with 3-velocity v relative to the ZAMO (launchFromZamo with mu = 1, its 4-velocity as
+    kerr::fourVelocity forms it, src/kerr.cpp:418-422), its frame, the photon seen along look,
+    normalised to E = 1. Returns the frequency the observer measures (1 / E before normalising),
+    the constants, the state and the observer's 4-velocity."""
+    oc, os_ = bhk.launch_from_zamo(a, r, th, 0.0, dev([v]), 1.0)
+    d = bhk.derivatives(a, oc, os_).cpu().numpy()[0]
+    _, sigma = _ks_metric(a, r, th)
+    u = d[:4] / sigma
+    f = bhk.observer_frame(a, dev([r]), dev([th]), dev([u]))
+    c, s = bhk.photon_from_frame(a, r, th, 0.0, f[0], dev([look]))
+    cv, sv = c.cpu().numpy()[0].copy(), s.cpu().numpy()[0].copy()
+    inv = 1.0 / cv[0]
+    cv[1] *= inv; cv[2] *= inv * inv; sv[4] *= inv; sv[5] *= inv; cv[0] = 1.0
+    return inv, cv, sv, u
+
+
+def test_moving_observer(cuda):
+    """testMovingObserver (tests/test_kerr.cpp:349-381): a boosted observer measures the energy the
+    boost predicts (1e-10), the aberrated photon is null (1e-9), flying at 0.6 c straight at what it
+    looks at blueshifts it by sqrt(1.6 / 0.4) = 2 (1e-12), and an observer at rest is deterministic."""
+    a, r, th = 0.9, 7.0, 1.2
+    look = [-0.6, 0.48, 0.64]
+    g0, _, _, _ = _observed_photon(a, r, th, [0.0, 0.0, 0.0], look)
+    g, c, s, u = _observed_photon(a, r, th, [-0.3, 0.2, 0.5], look)
+    cd, sd = dev([c]), dev([s])
+    d = bhk.derivatives(a, cd, sd).cpu().numpy()[0]
+    gm, sigma = _ks_metric(a, r, th)
+    assert abs(-(d[:4] / sigma) @ gm @ u - g) < 1e-10
+    R, Th = bhk.potentials(a, cd, sd)
+    assert abs(s[4] ** 2 - R.item()) < 1e-9
+    assert abs(s[5] ** 2 - Th.item()) < 1e-9
+    still, _, _, _ = _observed_photon(a, r, th, [0.0, 0.0, 0.0], [-1.0, 0.0, 0.0])
+    moving, _, _, _ = _observed_photon(a, r, th, [-0.6, 0.0, 0.0], [-1.0, 0.0, 0.0])
+    assert abs(moving / still - 2.0) < 1e-12
+    assert _observed_photon(a, r, th, [0.0, 0.0, 0.0], look)[0] == g0
+
+
 def test_observer_frames_orthonormal_and_photons_null(cuda):
     """testObserverFrames (tests/test_kerr.cpp:703-800): ZAMO frames orthonormal to 1e-12, photons
     from them null to 1e-9, and a ZAMO photon equals launchFromZamo to 1e-12."""
@@ -69,14 +120,7 @@ def test_observer_frames_orthonormal_and_photons_null(cuda):
     ths = dev([1.1, 1.2, 0.3, 2.9])
     F = bhk.observer_frame(a, rs, ths).cpu().numpy()
     for k in range(4):
-        r, th = float(rs[k]), float(ths[k])
-        sn, cs = math.sin(th), math.cos(th)
-        sigma = r * r + a * a * cs * cs
-        A = (r * r + a * a) ** 2 - a * a * (r * r - 2 * r + a * a) * sn * sn
-        f = 2 * r / sigma
-        gm = np.zeros((4, 4))
-        gm[0, 0] = -(1 - f); gm[0, 1] = gm[1, 0] = f; gm[0, 3] = gm[3, 0] = -f * a * sn * sn
-        gm[1, 1] = 1 + f; gm[1, 3] = gm[3, 1] = -a * sn * sn * (1 + f); gm[2, 2] = sigma; gm[3, 3] = A * sn * sn / sigma
+        gm, _ = _ks_metric(a, float(rs[k]), float(ths[k]))
         G = F[k] @ gm @ F[k].T
         assert np.max(np.abs(G - np.diag([-1.0, 1, 1, 1]))) < 1e-12
     look = np.array([[-0.48, 0.6, 0.64]])
