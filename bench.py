@@ -36,7 +36,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# BASELINE's headline metric: geodesics/s of the path that meets the 1e-4 exit-angle bound against
+# The headline metric: geodesics/s of the path that meets the 1e-4 exit-angle bound against
 # FP64 (the plain mixed tracer does; the surrogate path's errors are reported beside it).
 METRIC = "geodesics/s at \u22641e-4 rad exit-angle err vs FP64: surrogate vs plain GPU tracer"
 REF_TOL = 1e-2          # reference product tolerance (src/trajectory.cpp:261); meets the 1e-4 bar
@@ -396,7 +396,7 @@ def error_stats(test, ref):
 def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses: int) -> dict:
     """Surrogate + integrator fallback against the plain mixed tracer on the orbit sequence
     (poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 / scale), both timed with CUDA
-    events on the same frames, and both judged on a seeded 1% of each frame's pixels traced in FP64."""
+    events on the same frames, and both checked against a seeded 1% of each frame's pixels traced in FP64."""
     import torch
     from black_simulation_gb300 import bhk
     from black_simulation_gb300.surrogate import orbit_frames
@@ -431,7 +431,7 @@ def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses:
     fb = float(np.mean([st["fallback"] for st in stats]))
     out_t = bhk.alloc_outputs(n, dev)
     ms_t, _ = timed(lambda: ctx.trace_frames(frames, opts, out=out_t))
-    # 1% held-out pixels per frame (seeded), traced in FP64 as the judge
+    # 1% held-out pixels per frame (seeded), traced in FP64 as the yardstick
     rng = np.random.default_rng(args.seed + 1)
     held, off = [], 0
     for f in frames:
@@ -467,7 +467,7 @@ def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses:
         "errors_vs_fp64": {"surrogate_path": error_stats(sur_h, ref_h),
                            "network_answered_only": error_stats({k: v[answered] for k, v in sur_h.items()},
                                                                 {k: v[answered] for k, v in ref_h.items()}),
-                           "plain_tracer": error_stats(tr_h, ref_h), "fp64_judge_s": t_fp64},
+                           "plain_tracer": error_stats(tr_h, ref_h), "fp64_check_s": t_fp64},
         "meets_1e-4_bound": False,
         "inference_roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                                "frac": achieved / peak, "traffic": None, "peak_source": src,

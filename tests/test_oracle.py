@@ -167,11 +167,11 @@ def test_capture_zone_test_agrees_with_sampling(oracle):
         E, L, Q = 1.0, rng.uniform(-7, 7), rng.uniform(-1, 30)
         rp = oracle.horizon_radius_raw(a)
         r = rp + rng.uniform(0.001, 0.05)
-        verdict = oracle.no_radial_root_below_raw(a, E, L, Q, r, 1e-6)
+        proven = oracle.no_radial_root_below_raw(a, E, L, Q, r, 1e-6)
         xs = np.linspace(rp * (1 + 1e-6), r, 2001)
         c = po.Constants(E, L, Q, 0.0)
         Rs = np.array([oracle.radial_potential_raw(a, c, x) for x in xs])
-        if verdict:  # a "no root" verdict must never be wrong
+        if proven:  # a "no root" answer must never be wrong
             assert Rs.min() > 0
 
 
