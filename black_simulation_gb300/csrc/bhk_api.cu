@@ -247,8 +247,8 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
                            b.r_in, b.r_out, c->geom, L, r.p, c->ctl, lgrid, s);
     } else {
         BHK_CUDA(cudaMemcpyAsync(&c->ctl->n_rays, c->n_host, sizeof(long long), cudaMemcpyHostToDevice, s));
-        launch_rays_explicit(b.ex[0], b.ex[1], b.ex[2], b.ex[3], b.ex[4], b.r_in, b.r_out, r.p.r_escape, c->geom, L,
-                             r.p, c->ctl, lgrid, s);
+        launch_rays_explicit(b.ex[0], b.ex[1], b.ex[2], b.ex[3], b.ex[4], b.r_in, b.r_out, c->geom, L, r.p, c->ctl,
+                             lgrid, s);
     }
     const int32_t* order = nullptr;
     if (r.buckets > 1) {

@@ -97,8 +97,8 @@ struct Outputs {
 };
 
 // ---- launchers (bhk_trace.cu) ----
-void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p,
-                        Control* ctl, cudaStream_t s);
+void launch_frame_setup(FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p, Control* ctl,
+                        cudaStream_t s);
 // The same set-up on the host (the frame table's offsets, tetrads and geometries); returns the rays.
 long long setup_frames_host(FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p);
 void launch_rays_frames(const FrameDev* frames, const RayGeom* geom, int nframes, LaunchSoA L, const TraceParams& p,
@@ -107,7 +107,7 @@ void launch_rays_list(const FrameDev* frames, const RayGeom* geom, int nframes, 
                       const TraceParams& p,
                       const Control* ctl, int grid, cudaStream_t s);
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
-                          const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
+                          const double* beta, double r_in, double r_out, RayGeom* geom, LaunchSoA L,
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s);
 // Per-ray cameras with arbitrary frames (moving, or inside the horizon): kerr::photonFromFrame.
 void launch_rays_framed(const double* a, const double* r, const double* th, const double* ph, const bhk_frame* frames,

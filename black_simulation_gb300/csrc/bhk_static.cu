@@ -185,7 +185,7 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     if (e == cudaSuccess && p.buckets > 1) e = cudaMemsetAsync(S.hist, 0, sizeof(unsigned) * kMaxBuckets, s);
     if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("clearing the control block: ") + cudaGetErrorString(e));
     stage_frames_kernel<<<1, 64, 0, s>>>(batch, fdev);
-    launch_frame_setup(fdev, fdev, geom, nframes, p, ctl, s);
+    launch_frame_setup(fdev, geom, nframes, p, ctl, s);
     launch_rays_frames(fdev, geom, nframes, L, p, ctl, sms * 8, s);
     const int32_t* order = nullptr;
     if (p.buckets > 1) {

@@ -1186,9 +1186,8 @@ __global__ void critical_curve_kernel(double a, double r_obs, double th, int sam
 
 // ------------------------------------------------------------------------------ launchers ----
 
-void launch_frame_setup(const FrameDev* in, FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p,
-                        Control* ctl, cudaStream_t s) {
-    (void)in;
+void launch_frame_setup(FrameDev* frames, RayGeom* geom, int nframes, const TraceParams& p, Control* ctl,
+                        cudaStream_t s) {
     frame_setup_kernel<<<1, 128, 0, s>>>(frames, geom, nframes, p, ctl);
 }
 
@@ -1219,9 +1218,8 @@ void launch_rays_list(const FrameDev* frames, const RayGeom* geom, int nframes, 
 }
 
 void launch_rays_explicit(const double* a, const double* r_obs, const double* th_obs, const double* alpha,
-                          const double* beta, double r_in, double r_out, double r_escape, RayGeom* geom, LaunchSoA L,
+                          const double* beta, double r_in, double r_out, RayGeom* geom, LaunchSoA L,
                           const TraceParams& p, const Control* ctl, int grid, cudaStream_t s) {
-    (void)r_escape;
     launch_explicit_kernel<<<grid, 128, 0, s>>>(a, r_obs, th_obs, alpha, beta, r_in, r_out, geom, L, p, ctl);
 }
 
