@@ -81,12 +81,12 @@ class PathOutC(C.Structure):
 
 
 class RenderOptsC(C.Structure):
-    _fields_ = [("p_min", C.c_double), ("band", C.c_double), ("fallback", C.c_int32), ("cluster", C.c_int32)]
+    _fields_ = [("p_min", C.c_double), ("band", C.c_double), ("fallback", C.c_int32), ("accept", C.c_int32)]
 
 
 class RenderStatsC(C.Structure):
     _fields_ = [("rays", C.c_int64), ("fallback", C.c_int64), ("infer_ms", C.c_double), ("trace_ms", C.c_double),
-                ("cluster", C.c_int32), ("grid", C.c_int32)]
+                ("accept", C.c_int32), ("grid", C.c_int32)]
 
 
 @dataclasses.dataclass

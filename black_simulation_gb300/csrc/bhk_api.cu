@@ -260,7 +260,8 @@ bhk_status enqueue(bhk_context* c, const Batch& b, const Resolved& r, const Outp
     const bool fused = b.mode == 0 && r.buckets <= 1;
     launch_trace(r.fp64, r.regcap, L, c->geom, order, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl,
                  r.block, r.grid, s, fused ? c->frames_dev : nullptr, fused ? b.nframes : 0);
-    if (!r.fp64) launch_rescue(L, c->geom, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, s);
+    if (!r.fp64)
+        launch_rescue(L, c->geom, out, c->rescue, static_cast<unsigned>(c->cap_rescue), r.p, c->ctl, c->num_sms, s);
     if (timed) BHK_CUDA(cudaEventRecord(c->ev1, s));
     launch_constants_out(L, out, c->ctl, lgrid, s);
     BHK_CUDA(cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Control), cudaMemcpyDeviceToHost, s));
@@ -398,6 +399,10 @@ bhk_status trace_frames_locked(bhk_context* c, const bhk_frame_desc* frames, int
 }
 
 }  // namespace
+
+bhk_status bhk::validate_frames(const bhk_frame_desc* f, int32_t nframes, int64_t* total) {
+    return check_frames(f, nframes, total);
+}
 
 bhk_status bhk::trace_pixel_list(bhk_context* c, const bhk_frame_desc* frames, int32_t nframes, const int32_t* list,
                                  int64_t n, const bhk_trace_opts* opts, const bhk_rays_out* out, bhk_rays_out* used,

@@ -296,7 +296,14 @@ bhk_status bhk_eht_render(const bhk_eht_view* view, const bhk_eht_flow* flow, in
     }
     const long long n = static_cast<long long>(view->size) * view->size;
     const int block = 128;
-    const int grid = static_cast<int>(std::min<long long>((n + block - 1) / block, 152LL * 16));
+    int device = 0, sms = 0;
+    if (cudaGetDevice(&device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        bhk::set_last_error("bhk_eht_render: no usable CUDA device");
+        return BHK_ECUDA;
+    }
+    const int grid = static_cast<int>(std::min<long long>((n + block - 1) / block, 16LL * sms));
     // Horizon and prograde ISCO once on the host (past |a| = 1 the ISCO is a 4000-point search).
     const double rp = bhk::horizon_radius(view->a), isco = bhk::isco_radius(view->a, true);
     bhk::eht::render_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(*view, *flow, with_light, rp, isco,

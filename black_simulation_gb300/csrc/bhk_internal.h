@@ -122,14 +122,20 @@ void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const
                   cudaStream_t s, const FrameDev* frames = nullptr, int nframes = 0);
 // energy, g_camera, b, q of every ray from its FP64 launch constants (if any is requested).
 void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s);
+// grid: one block of 64 threads per SM is plenty (rescued rays are rare).
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
-                   const TraceParams& p, Control* ctl, cudaStream_t s);
+                   const TraceParams& p, Control* ctl, int grid, cudaStream_t s);
 int trace_blocks_per_sm(bool fp64, int regcap, int block);  // 0 when the pair is not allowed
 void launch_critical_curve(double a, double r_obs, double theta_obs, int samples, double* alpha, double* beta,
                            int* valid, cudaStream_t s);
 
 // Sets the text bhk_last_error() returns on this thread (bhk_api.cu).
 void set_last_error(const std::string& msg);
+
+// The frame checks of bhk_trace_frames (bhk_api.cu): sizes, spin (|a| != 1; naked singularities
+// allowed), camera outside the horizon, theta_obs in (0, pi), r_disk_out >= 0, < 2^31 rays. Sets the
+// last error and returns BHK_EINVAL on the first bad frame; *total receives the ray count.
+bhk_status validate_frames(const bhk_frame_desc* f, int32_t nframes, int64_t* total);
 
 // ---- context internals for the other translation units (bhk_api.cu) ----
 // Traces pixels list[0..n) (device memory, global pixel indices of the frames) into `out` (compact:

@@ -11,15 +11,23 @@
 //  - the array holds kStaticMaxRays rays and kStaticMaxFrames frames per call (6.1 MB), and
 //    every GPU that loads libbhk keeps it until the process exits;
 //  - all calls share the one array, whose contents persist from the previous call. The control
-//    block (queue counter, statistics) is cleared at the start of each call; everything else is
-//    rewritten before it is read. Calls that overlap on the GPU (two streams, or two host threads
-//    without ordering between them) race on the array: order them on one stream.
+//    block (queue counter, statistics) and, with the cost sort, its bucket histogram are cleared at
+//    the start of each call; everything else is rewritten before it is read. Calls that overlap on
+//    the GPU (two streams, or two host threads without ordering between them) race on the array:
+//    order them on one stream.
 //  - the first call on a device looks up the array's device address (cudaGetSymbolAddress with
-//    that device current) and caches it; make that first call before any stream capture.
+//    that device current) and caches it with the identity of the device's context; make that first
+//    call before any stream capture. A call that finds a different context (after cudaDeviceReset)
+//    looks the address up again, so it too belongs before any capture.
+//  - the call is asynchronous and reports BHK_OK once its work is queued: rays that reach the step
+//    cap show only as BHK_RAY_UNFINISHED in the outcome array (the context entry points synchronise
+//    to return BHK_EUNFINISHED; this one never waits on the GPU).
 #include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
+
+#include <cuda.h>
 
 #include "bhk_internal.h"
 
@@ -73,7 +81,9 @@ bhk_status fail(bhk_status s, const std::string& m) {
     return s;
 }
 
-// Frame descriptors travel as a kernel parameter (well under the 32 KB parameter limit).
+// Frame descriptors travel as a kernel parameter: 64 x 88 + 8 bytes, above the classic 4 KB limit
+// and within the 32,764 bytes that CUDA 12.1 and later allow on Volta and later GPUs (this library is
+// built by CUDA 13 for sm_103a only).
 struct FrameBatch {
     bhk_frame_desc f[kStaticMaxFrames];
     int n;
@@ -90,15 +100,69 @@ __global__ void stage_frames_kernel(FrameBatch batch, FrameDev* frames) {
 
 std::mutex g_addr_mu;
 void* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 
-// Device address of the static array on the current device, looked up once per device.
+// The two driver calls, taken through the runtime's entry-point query so that libbhk does not link
+// libcuda directly (it loads on machines without a driver, where every call reports BHK_ECUDA).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+bool driver_fns(CtxGetCurrentFn* cur, CtxGetIdFn* id) {
+    static CtxGetCurrentFn f_cur = nullptr;
+    static CtxGetIdFn f_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f_cur = reinterpret_cast<CtxGetCurrentFn>(p);
+        else
+            cudaGetLastError();
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f_id = reinterpret_cast<CtxGetIdFn>(p);
+        else
+            cudaGetLastError();
+    });
+    *cur = f_cur;
+    *id = f_id;
+    return f_cur && f_id;
+}
+
+// Unique id of the context the runtime uses on this thread for `device` (its primary context unless
+// the caller made another current). cudaSetDevice binds the primary context where none is current,
+// or after cudaDeviceReset destroyed the one that was.
+bool current_context_id(int device, unsigned long long* id) {
+    CtxGetCurrentFn get_cur;
+    CtxGetIdFn get_id;
+    if (!driver_fns(&get_cur, &get_id)) return false;
+    CUcontext cur = nullptr;
+    if (get_cur(&cur) == CUDA_SUCCESS && cur && get_id(cur, id) == CUDA_SUCCESS) return true;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cur = nullptr;
+    return get_cur(&cur) == CUDA_SUCCESS && cur && get_id(cur, id) == CUDA_SUCCESS;
+}
+
+// Device address of the static array on the current device: looked up (cudaGetSymbolAddress) once per
+// device and context, with that device current.
 bhk_status scratch_address(int device, unsigned char** out) {
+    unsigned long long id = 0;
+    if (!current_context_id(device, &id)) return fail(BHK_ECUDA, "no current CUDA context for the device");
     std::lock_guard<std::mutex> lock(g_addr_mu);
-    if (!g_addr[device]) {
+    if (!g_addr[device] || g_ctx_id[device] != id) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(BHK_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        }
         g_addr[device] = p;
+        g_ctx_id[device] = id;
     }
     *out = static_cast<unsigned char*>(g_addr[device]);
     return BHK_OK;
@@ -114,17 +178,10 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     if (!frames || nframes <= 0 || !out) return fail(BHK_EINVAL, "frames, nframes and out are required");
     if (nframes > kStaticMaxFrames)
         return fail(BHK_EINVAL, "bhk_trace_frames_static takes at most 64 frames per call");
+    // The same frame checks as bhk_trace_frames (naked singularities included), then the array's limits.
     int64_t total = 0;
-    for (int i = 0; i < nframes; ++i) {
-        const bhk_frame_desc& f = frames[i];
-        if (f.width <= 0 || f.height <= 0) return fail(BHK_EINVAL, "frame with non-positive size");
-        if (!(std::fabs(f.a) < 1.0)) return fail(BHK_EINVAL, "spin must satisfy |a| < 1");
-        if (!(f.r_obs > 1.0 + std::sqrt(1.0 - f.a * f.a)))
-            return fail(BHK_EINVAL, "camera must sit outside the horizon (ZAMO pinhole)");
-        if (!(f.theta_obs > 0.0 && f.theta_obs < M_PI)) return fail(BHK_EINVAL, "theta_obs outside (0, pi)");
-        if (!(f.r_disk_out >= 0.0)) return fail(BHK_EINVAL, "r_disk_out must be >= 0 (0: no disk)");
-        total += static_cast<int64_t>(f.width) * f.height;
-    }
+    const bhk_status vs = validate_frames(frames, nframes, &total);
+    if (vs != BHK_OK) return vs;
     if (total > kStaticMaxRays)
         return fail(BHK_EINVAL, "bhk_trace_frames_static takes at most 65536 rays per call (the static scratch)");
     int device = 0;
@@ -193,8 +250,8 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
         order = S.order;
     }
     launch_trace(fp64, regcap, L, geom, order, outs, rescue, kStaticRescue, p, ctl, block, grid, s);
-    if (!fp64) launch_rescue(L, geom, outs, rescue, kStaticRescue, p, ctl, s);
-    launch_constants_out(L, outs, ctl, 152 * 8, s);
+    if (!fp64) launch_rescue(L, geom, outs, rescue, kStaticRescue, p, ctl, sms, s);
+    launch_constants_out(L, outs, ctl, sms * 8, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
     return BHK_OK;

@@ -1273,7 +1273,7 @@ struct InferArgs {
     unsigned long long* n_list;
     float p_min, band;
     int* err;
-    int cl;  // CTAs per cluster sharing each weight chunk by TMA multicast (1, 2 or 4)
+    int accept;  // BHK_ACCEPT_*: which of the network's classes it may answer
 };
 
 // Byte offset of (row, col) in a 128-row x 64-column BF16 tile with the 128-byte swizzle.
@@ -1310,9 +1310,7 @@ __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb,
 // other tile's epilogue warps turn their accumulators into the next layer's operand. Each tile
 // slot owns 256 TMEM columns and a 64 KB activation buffer; the weight ring is shared and filled
 // in the MMA's order (pair of tiles, layer, slot, chunk). Every MMA is 128 x 256 x 16, so each
-// activation slice is read from shared memory once per layer. The CTAs of a cluster (cl of them) walk
-// the same chunk sequence: each loads 1/cl of every weight chunk and multicasts it to all, and each
-// MMA commit releases the ring stage in every CTA, so L2 serves each chunk once per cluster.
+// activation slice is read from shared memory once per layer. CTA b takes tiles b, b + grid, ...
 __global__ void __launch_bounds__(kInfThreads, 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
              const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
@@ -1330,21 +1328,15 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     float* sB = reinterpret_cast<float*>(tmem_slot + 4);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cl = ia.cl;
-    const int rank = cl > 1 ? static_cast<int>(tc::cluster_rank()) : 0;
-    const uint16_t mask = static_cast<uint16_t>((1u << cl) - 1u);
     const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
-    // Cluster-uniform schedule: at step k cluster c takes tile group c + k * ncl, CTA `rank` its tile
-    // group * cl + rank (past the end: an empty tile), so every CTA of a cluster has the same steps.
-    const long long ngroups = (ntiles + cl - 1) / cl;
-    const long long cid = blockIdx.x / cl, ncl = gridDim.x / cl;
-    const long long n_my = cid < ngroups ? (ngroups - cid + ncl - 1) / ncl : 0;
+    const long long cid = blockIdx.x, ncl = gridDim.x;
+    const long long n_my = cid < ntiles ? (ntiles - cid + ncl - 1) / ncl : 0;
     const long long pairs = (n_my + 1) / 2;
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
     if (threadIdx.x == 0) {
         for (int st = 0; st < kInfStages; ++st) {
             tc::mbar_init(&full[st], 1);
-            tc::mbar_init(&empty[st], cl);  // one commit from every CTA of the cluster
+            tc::mbar_init(&empty[st], 1);
         }
         for (int sl = 0; sl < 2; ++sl) {
             tc::mbar_init(&act_ready[sl], 32 * kEpiWarps / 2);
@@ -1362,7 +1354,6 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
     tc::fence_before_sync();
     __syncthreads();
-    if (cl > 1) tc::cluster_sync();  // every CTA's barriers exist before any multicast reaches them
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     auto give_up = [&]() {
@@ -1390,25 +1381,12 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                             const int kc = c;
                             const CUtensorMap* m = l == 0 ? &tW0 : l == 1 ? &tW1 : l == 2 ? &tW2 : l == 3 ? &tW3 : &tW4;
                             tc::mbar_expect_tx(&full[st], l < 4 ? kWChunkBytes : kHeadChunkBytes);
-                            uint8_t* dst = ring + st * kWChunkBytes;
-                            if (cl == 1) {
-                                tc::tma_load_2d(dst, m, kc * 64, 0, &full[st]);
-                            } else if (l < 4) {  // this CTA's 256 / cl rows of the chunk, to all
-                                const int rows = 256 / cl;
-                                tc::tma_load_2d_multicast(dst + rank * rows * 128, m, kc * 64, rank * rows,
-                                                          &full[st], mask);
-                            } else if (rank == 0) {  // the head's 16 rows come from the first CTA
-                                tc::tma_load_2d_multicast(dst, m, kc * 64, 0, &full[st], mask);
-                            }
+                            tc::tma_load_2d(ring + st * kWChunkBytes, m, kc * 64, 0, &full[st]);
                         }
                     }
-            // Before the CTA may exit (bounded): every load of the last ring round has landed here, and
-            // with clusters every CTA's release of those stages has reached this CTA's barriers.
+            // Before the CTA may exit (bounded): every load of the last ring round has landed.
             for (long long r = q - kInfStages; r < q; ++r)
                 if (r >= 0) tc::mbar_wait(&full[r % kInfStages], static_cast<uint32_t>((r / kInfStages) & 1));
-            if (cl > 1 && ok)
-                for (long long r = q - kInfStages; r < q; ++r)
-                    if (r >= 0) tc::mbar_wait(&empty[r % kInfStages], static_cast<uint32_t>((r / kInfStages) & 1));
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---- MMA issuer
@@ -1443,8 +1421,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
 #pragma unroll
                             for (int kk = 0; kk < 4; ++kk)
                                 tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId256 : kId16, (kc | kk) ? 1u : 0u);
-                            if (cl == 1) tc::mma_commit(&empty[st]);
-                            else tc::mma_commit_multicast(&empty[st], mask);  // the stage is free in no CTA until all used it
+                            tc::mma_commit(&empty[st]);
                         }
                         if (ok) tc::mma_commit(&acc_full[sl]);
                     }
@@ -1465,7 +1442,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         // warp-collective).
         for (long long k = slot; k < n_my; k += 2) {
             if (__any_sync(0xffffffffu, *abort_flag)) break;
-            const long long tile = (cid + k * ncl) * cl + rank;
+            const long long tile = cid + k * ncl;
             const long long ray = tile * kTileRays + row;
             const bool live = ray < ia.n;
             int fi = 0;
@@ -1584,7 +1561,10 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                     const int jb = min(kCurveBins - 1, max(0, static_cast<int>(psi * (kCurveBins / 3.14159265f))));
                     band = fabsf(sqrtf(da * da + ab_ * ab_) - f.rho[jb]) * f.kn[jb] < ia.band;
                 }
-                fb = pmax < ia.p_min || band || fabsf(alpha) < f.snap || !(zsum == zsum);
+                // Answers limited to captured rays carry no continuous output, so where the class is
+                // right they are exactly the tracer's (the network's r_disk, g and direction are not used).
+                fb = pmax < ia.p_min || band || fabsf(alpha) < f.snap || !(zsum == zsum) ||
+                     (ia.accept == BHK_ACCEPT_CAPTURED && cls != 0);
                 ia.outcome[ray] = static_cast<uint8_t>(cls + 1);
                 if (ia.r_disk) ia.r_disk[ray] = rd;
                 if (ia.phi_disk) ia.phi_disk[ray] = nan;
@@ -1606,7 +1586,6 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 1) tc::tmem_dealloc(tmem, 512);
-    if (cl > 1) tc::cluster_sync();  // no CTA leaves while another may still deliver to or signal it
 }
 
 __global__ void halve_bias_kernel(const float* b0, const float* b1, const float* b2, const float* b3, float* out) {
@@ -1661,8 +1640,8 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     ro.band = 0.05;
     ro.fallback = 1;
     if (ropts) ro = *ropts;
-    if (ro.cluster != 0 && ro.cluster != 1 && ro.cluster != 2 && ro.cluster != 4) {
-        set_last_error("bhk_surrogate_render: cluster must be 0 (automatic), 1, 2 or 4");
+    if (ro.accept != BHK_ACCEPT_ALL && ro.accept != BHK_ACCEPT_CAPTURED) {
+        set_last_error("bhk_surrogate_render: accept must be BHK_ACCEPT_ALL or BHK_ACCEPT_CAPTURED");
         return BHK_EINVAL;
     }
     std::lock_guard<std::mutex> lock_ctx(bhk::context_mutex(ctx));
@@ -1725,37 +1704,12 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     std::call_once(attr, [] { cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem); });
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    // One CTA per SM (it holds all 512 TMEM columns), optionally in clusters sharing the weight
-    // stream by multicast. Measured on GB300 (60 x 960x540 orbit frames): 1.98 G rays/s without
-    // clusters, 1.91 with pairs, 1.81 with fours -- L2 is not the limit (shared-memory bandwidth is),
-    // so the default is no cluster. The grid is the number of clusters resident at once (a static
-    // schedule must not need a second wave).
-    int cl = 1, resident = sms;
-    const int want = ro.cluster > 0 ? ro.cluster : 1;
-    for (int c : {4, 2, 1}) {
-        if (c != want) continue;
-        cudaLaunchConfig_t q{};
-        cudaLaunchAttribute at{};
-        at.id = cudaLaunchAttributeClusterDimension;
-        at.val.clusterDim.x = c;
-        at.val.clusterDim.y = 1;
-        at.val.clusterDim.z = 1;
-        q.gridDim = dim3((sms / c) * c);
-        q.blockDim = dim3(kInfThreads);
-        q.dynamicSmemBytes = kInfSmem;
-        q.attrs = &at;
-        q.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, infer_kernel, &q) == cudaSuccess && nclusters > 0) {
-            cl = c;
-            resident = nclusters;
-            break;
-        }
-        cudaGetLastError();
-    }
+    // One CTA per SM (it holds all 512 TMEM columns); the grid is the number of CTAs resident at once
+    // (the static tile schedule must not need a second wave).
+    const int resident = sms;
     Maps M;
     CUtensorMap w4;
-    const uint32_t slice = 256u / cl;
+    const uint32_t slice = 256u;
     if (!make_tmap(&M.W[0], s->w_rm[0], kHid, kFeat, slice) || !make_tmap(&M.W[1], s->w_rm[1], kHid, kHid, slice) ||
         !make_tmap(&M.W[2], s->w_rm[2], kHid, kHid, slice) || !make_tmap(&M.W[3], s->w_rm[3], kHid, kHid, slice) ||
         !make_tmap(&w4, s->w_rm[4], kOutPad, kHid, 16)) {
@@ -1763,12 +1717,11 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
         return BHK_ECUDA;
     }
     const long long ntiles = (total + kTileRays - 1) / kTileRays;
-    const long long groups = (ntiles + cl - 1) / cl;
-    const int grid = static_cast<int>(std::min<long long>(groups, resident) * cl);
+    const int grid = static_cast<int>(std::min<long long>(ntiles, resident));
     halve_bias_kernel<<<4, 256, 0, st>>>(s->p + s->L.b[0], s->p + s->L.b[1], s->p + s->L.b[2], s->p + s->L.b[3],
                                          s->half_bias);
     InferArgs ia{};
-    ia.cl = cl;
+    ia.accept = ro.accept;
     ia.half_bias = s->half_bias;
     ia.frames = dframes;
     ia.nframes = nframes;
@@ -1792,21 +1745,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
     if (e != cudaSuccess) return fail_cuda(e, "launch set-up");
-    {
-        cudaLaunchConfig_t q{};
-        cudaLaunchAttribute at{};
-        at.id = cudaLaunchAttributeClusterDimension;
-        at.val.clusterDim.x = cl;
-        at.val.clusterDim.y = 1;
-        at.val.clusterDim.z = 1;
-        q.gridDim = dim3(grid);
-        q.blockDim = dim3(kInfThreads);
-        q.dynamicSmemBytes = kInfSmem;
-        q.stream = st;
-        q.attrs = &at;
-        q.numAttrs = 1;
-        e = cudaLaunchKernelEx(&q, infer_kernel, M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
-    }
+    infer_kernel<<<grid, kInfThreads, kInfSmem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->n_list_host, s->n_list, 8, cudaMemcpyDeviceToHost, st);
@@ -1846,7 +1785,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
         stats->fallback = nfb;
         stats->infer_ms = ms;
         stats->trace_ms = trace_ms;
-        stats->cluster = cl;
+        stats->accept = ro.accept;
         stats->grid = grid;
     }
     return rs;

@@ -1254,8 +1254,8 @@ void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid
 }
 
 void launch_rescue(LaunchSoA L, const RayGeom* geom, Outputs out, Rescue* rescue, unsigned rescue_cap,
-                   const TraceParams& p, Control* ctl, cudaStream_t s) {
-    rescue_kernel<<<152, 64, 0, s>>>(L, geom, out, rescue, rescue_cap, p, ctl);
+                   const TraceParams& p, Control* ctl, int grid, cudaStream_t s) {
+    rescue_kernel<<<grid, 64, 0, s>>>(L, geom, out, rescue, rescue_cap, p, ctl);
 }
 
 int trace_blocks_per_sm(bool fp64, int regcap, int block) {

@@ -22,6 +22,7 @@ from . import bhk
 N_IN, N_OUT = 5, 8
 LAYERS = ((256, 64), (256, 256), (256, 256), (256, 256), (16, 256))  # (fan_out, fan_in), head padded to 16
 R_DISK_SCALE = 30.0
+ACCEPT = {"all": 0, "captured": 1}  # bhk_render_opts.accept (BHK_ACCEPT_ALL, BHK_ACCEPT_CAPTURED)
 
 
 def layer_offsets():
@@ -179,15 +180,18 @@ class Surrogate:
 
 
     def render(self, ctx, frames, opts=None, p_min: float = 0.99, band: float = 0.05, fallback: bool = True,
-               out: Optional[dict] = None, stream=None, cluster: int = 0):
+               out: Optional[dict] = None, stream=None, accept: str = "all"):
         """Surrogate + integrator-fallback render of `frames` (bhk.Frame list) through the fused
-        inference kernel; returns (outputs as bhk.alloc_outputs gives, stats dict)."""
+        inference kernel; returns (outputs as bhk.alloc_outputs gives, stats dict). accept="captured"
+        keeps only the network's captured answers and traces every other ray."""
         n = sum(f.rays for f in frames)
         if out is None:
             out = bhk.alloc_outputs(n, f"cuda:{self.device}")
         arr = (bhk.FrameDescC * len(frames))(*[f.c() for f in frames])
         oc = (opts or bhk.TraceOpts("mixed")).c()
-        ro = bhk.RenderOptsC(p_min, band, 1 if fallback else 0, cluster)
+        if accept not in ACCEPT:
+            raise ValueError(f"accept must be one of {sorted(ACCEPT)}")
+        ro = bhk.RenderOptsC(p_min, band, 1 if fallback else 0, ACCEPT[accept])
         st = bhk.RenderStatsC()
         outc = bhk._out_c(out)
         bhk.check(bhk.lib().bhk_surrogate_render(self._h, ctx.h, arr, len(frames), C.byref(oc), C.byref(ro),

@@ -171,9 +171,10 @@ typedef struct {
  * BHK_EUNFINISHED if any ray hit the step cap (after synchronising the stream), else BHK_OK. */
 bhk_status bhk_trace_frames(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes,
                             const bhk_trace_opts* opts, const bhk_rays_out* out, void* stream);
-/* The same with HOST output buffers: the library traces into its own device buffers and copies the
- * results back before returning (synchronous). This is the eht::render-style call
- * (src/eht.cpp:321-347): frames in, images out, in host memory. */
+/* The same with HOST output buffers, synchronous: the eht::render-style call (src/eht.cpp:321-347),
+ * frames in, images out, in host memory. Page-locked outputs (cudaHostAlloc / cudaHostRegister) are
+ * written by the kernels directly over the host link while the rays are traced; pageable outputs go
+ * through the library's own device buffers and are copied back before the call returns. */
 bhk_status bhk_trace_frames_host(bhk_context* ctx, const bhk_frame_desc* frames, int32_t nframes,
                                  const bhk_trace_opts* opts, const bhk_rays_out* host_out);
 /* Per-ray variant: explicit (a, r_obs, theta_obs, alpha, beta) device arrays of n rays, ZAMO pinhole
@@ -235,14 +236,18 @@ bhk_status bhk_critical_curve(double a, double r_obs, double theta_obs, int32_t 
 /* bhk_trace_frames without any device allocation (no counterpart in the reference). For callers that
  * may not allocate device memory -- a host framework that owns the whole device-memory budget
  * through its own pool, or a per-frame render loop where cudaMalloc/cudaFree would synchronise the
- * device. Outputs are the caller's device buffers; all working memory lives in one fixed array in
- * libbhk's device image (6.1 MB, held by every GPU that loads the library until exit).
+ * device. Outputs are the caller's device buffers (the RayReport extras of bhk_rays_out included);
+ * all working memory lives in one fixed array in libbhk's device image (6.1 MB, held by every GPU
+ * that loads the library until exit).
+ * Frames are checked as bhk_trace_frames checks them (naked singularities, |a| > 1, are traced too).
  * Limits: at most 65536 rays and 64 frames per call; larger requests return BHK_EINVAL. No context:
  * the tracer runs on the current device and on `stream` (NULL = the legacy default stream) with the
- * opts given (0 fields take the context defaults; no autotuning). All calls share the array, which
- * keeps the previous call's contents (the control block is cleared at the start of each call):
- * calls that overlap on the GPU race, so order them on one stream. The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make it before any stream capture. */
+ * opts given (0 fields take the context defaults; no autotuning). Asynchronous: BHK_OK means the work
+ * is queued, and rays that reach the step cap show only as BHK_RAY_UNFINISHED in `outcome` (this call
+ * never returns BHK_EUNFINISHED). All calls share the array, which keeps the previous call's contents
+ * (the control block is cleared at the start of each call): calls that overlap on the GPU race, so
+ * order them on one stream. The first call on a device (and the first after cudaDeviceReset) looks up
+ * the array's device address (cudaGetSymbolAddress); make it before any stream capture. */
 bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int32_t nframes, const bhk_trace_opts* opts,
                                    const bhk_rays_out* out, void* stream);
 
@@ -327,18 +332,24 @@ bhk_status bhk_surrogate_dataset(bhk_context* ctx, int64_t n, uint64_t seed, dou
                                  const bhk_trace_opts* opts, float* x, uint8_t* cls, float* target, double* rays5,
                                  void* stream);
 
+/* Which of the network's answers a render keeps. BHK_ACCEPT_ALL: every confident ray outside the
+ * band (the network's r_disk, g and escape direction are its answers, ~1e-2 accurate). BHK_ACCEPT_CAPTURED:
+ * only rays the network classes captured; every disk or escaping ray is traced. A captured ray has no
+ * continuous output, so each accepted answer is exactly the tracer's wherever the class is right. */
+enum { BHK_ACCEPT_ALL = 0, BHK_ACCEPT_CAPTURED = 1 };
+
 typedef struct bhk_render_opts {
     double p_min;        /* rays whose largest class probability is below this fall back (0.99) */
     double band;         /* rays within this image-plane distance (M) of the critical curve fall back (0.05) */
     int32_t fallback;    /* 1: trace the fallback rays (the product); 0: only list them (measurement) */
-    int32_t cluster;     /* CTAs sharing each weight chunk by TMA multicast: 1, 2 or 4 (0: 1) */
+    int32_t accept;      /* BHK_ACCEPT_ALL (0) or BHK_ACCEPT_CAPTURED */
 } bhk_render_opts;
 
 typedef struct bhk_render_stats {
     int64_t rays, fallback;  /* rays rendered, rays handed to the integrator */
     double infer_ms;         /* fused inference kernel (CUDA events) */
     double trace_ms;         /* fallback trace incl. its launch and the scatter (CUDA events) */
-    int32_t cluster, grid;   /* launch shape of the inference kernel */
+    int32_t accept, grid;    /* the acceptance mode used; CTAs of the inference kernel */
 } bhk_render_stats;
 
 /* Renders frames with the surrogate and integrator fallback: one fused tcgen05 inference kernel over

@@ -6,6 +6,8 @@ unmodified kerr.cpp, trajectory.cpp, central.cpp and eht.cpp through oracle/Make
     python tests/golden/make_golden.py
 
 Fixtures (all produced by the reference's own functions, never by this project's code):
+  steps_blocks_ref.npz  per-step vectors in 8 spin blocks of 64 states (derivatives, stepMino,
+                      photonStepSize, enforceConstraints, radialPotential/polarPotential), for batched checks
   steps_ref.npz       per-step vectors: derivatives, stepMino, photonStepSize, enforceConstraints,
                       normalizeAngles, ZAMO frames + photonFromFrame, launchFromZamo, radii, critical
                       curves, central::bendingAngle (src/kerr.cpp, src/eht.cpp, src/central.cpp)
@@ -43,6 +45,39 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
 import pyoracle as po  # noqa: E402
+
+
+def steps_blocks_fixture(R: po.Oracle) -> dict:
+    """Per-step vectors in spin blocks (8 spins x 64 states), so that each mirror is checked through
+    one batched launch per spin (the reference call shape shares a by the batch)."""
+    rng = np.random.default_rng(20261204)
+    spins = np.array([0.0, 0.3, 0.5, 0.7, 0.9, 0.95, 0.99, 0.998])
+    per = 64
+    n = spins.size * per
+    a = np.repeat(spins, per)
+    cons = np.stack([rng.uniform(0.5, 1.5, n), rng.uniform(-8, 8, n), rng.uniform(-2, 40, n), np.zeros(n)], 1)
+    st = np.stack([rng.uniform(-5, 5, n), rng.uniform(1.2, 1000, n), rng.uniform(-0.3, np.pi + 0.3, n),
+                   rng.uniform(-10, 10, n), rng.uniform(-1e3, 1e3, n), rng.uniform(-10, 10, n)], 1)
+    h = rng.uniform(-0.02, 0.02, n)
+    tol = float(10.0 ** rng.uniform(-4, -1))  # one tolerance per batch, as photonStepSize takes it
+    der = np.zeros((n, 6))
+    stepped = np.zeros((n, 6))
+    hstep = np.zeros(n)
+    enforced = np.zeros((n, 6))
+    pot = np.zeros((n, 2))
+    for i in range(n):
+        c = po.Constants(*cons[i])
+        s = po.State(*st[i])
+        d = R.derivatives(a[i], c, s)
+        der[i] = [d.dt, d.dr, d.dtheta, d.dphi, d.dvr, d.dvtheta]
+        x = R.step_mino(a[i], c, s, h[i])
+        stepped[i] = [x.t, x.r, x.theta, x.phi, x.vr, x.vtheta]
+        hstep[i] = R.photon_step_size(a[i], c, s, tol)
+        x = R.enforce_constraints(a[i], c, s)
+        enforced[i] = [x.t, x.r, x.theta, x.phi, x.vr, x.vtheta]
+        pot[i] = [R.radial_potential_raw(a[i], C.byref(c), st[i][1]), R.polar_potential_raw(a[i], C.byref(c), st[i][2])]
+    return dict(spins=spins, per=np.array(per), a=a, cons=cons, state=st, h=h, tol=np.array(tol), derivatives=der,
+                step_mino=stepped, step_size=hstep, enforced=enforced, potentials=pot)
 
 
 def steps_fixture(R: po.Oracle) -> dict:
@@ -344,6 +379,10 @@ def main() -> None:
     print("naked_ref.npz")
     np.savez_compressed(os.path.join(HERE, "naked_ref.npz"), **naked_fixture(R))
     if os.environ.get("NAKED_ONLY"):
+        return
+    print("steps_blocks_ref.npz")
+    np.savez_compressed(os.path.join(HERE, "steps_blocks_ref.npz"), **steps_blocks_fixture(R))
+    if os.environ.get("BLOCKS_ONLY"):
         return
     print("steps_ref.npz")
     np.savez_compressed(os.path.join(HERE, "steps_ref.npz"), **steps_fixture(R))

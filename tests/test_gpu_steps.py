@@ -23,11 +23,11 @@ def close(got, want, rtol=RTOL, atol=1e-12):
 
 
 def test_per_step_mirrors_match_reference_vectors(cuda, golden):
+    """Every one of the 512 reference rows, each with its own spin (one launch of n = 1 per row)."""
     g = golden("steps_ref.npz")
     n = len(g["a"])
-    for i in range(0, n, 64):
-        sl = slice(i, i + 64)
-        a = float(g["a"][i])  # the batch shares one spin: rerun rows one spin at a time
+    for i in range(n):
+        a = float(g["a"][i])  # the batch shares one spin: rows of different spins go one at a time
         c = dev(g["cons"][i:i + 1])
         s = dev(g["state"][i:i + 1])
         close(bhk.derivatives(a, c, s).cpu().numpy()[0], g["derivatives"][i])
@@ -38,13 +38,35 @@ def test_per_step_mirrors_match_reference_vectors(cuda, golden):
         s3 = s.clone()
         bhk.enforce_constraints(a, c, s3)
         close(s3.cpu().numpy()[0], g["enforced"][i])
-        del sl
     # normalizeAngles is spin-free: the whole table in one launch.
     st = g["state"].copy()
     st[:, 2] *= 3.0
     s = dev(st)
     bhk.normalize_angles(s)
     close(s.cpu().numpy(), g["normalized"])
+
+
+def test_batched_mirrors_match_reference_vectors_per_spin_block(cuda, golden):
+    """The batched launch path (n = 64 rows sharing a spin, as the reference call shape has it): each
+    mirror once per spin over its 64 rows, all 8 x 64 reference rows checked (src/kerr.cpp:331-575)."""
+    g = golden("steps_blocks_ref.npz")
+    per, tol = int(g["per"]), float(g["tol"])
+    for b, a in enumerate(g["spins"]):
+        sl = slice(b * per, (b + 1) * per)
+        assert np.all(g["a"][sl] == a)
+        c, s = dev(g["cons"][sl]), dev(g["state"][sl])
+        close(bhk.derivatives(float(a), c, s).cpu().numpy(), g["derivatives"][sl])
+        s2 = s.clone()
+        bhk.step_mino(float(a), c, s2, dev(g["h"][sl]))
+        close(s2.cpu().numpy(), g["step_mino"][sl])
+        close(bhk.photon_step_size(float(a), c, s, tol).cpu().numpy(), g["step_size"][sl])
+        s3 = s.clone()
+        bhk.enforce_constraints(float(a), c, s3)
+        close(s3.cpu().numpy(), g["enforced"][sl])
+        R, Th = bhk.potentials(float(a), c, s)
+        close(R.cpu().numpy(), g["potentials"][sl, 0])
+        # Theta = Q - cos^2 (...) cancels: absolute tolerance on the scale of its terms
+        close(Th.cpu().numpy(), g["potentials"][sl, 1], atol=1e-10)
 
 
 def test_frames_and_photon_launches_match_reference(cuda, golden):
