@@ -63,9 +63,10 @@ struct GraphKey {
 //     r^2 + a^2 4, P 2, inflow 4, sin cos, sin^2 and L / sin^2 3, dphi 4, R'/2 4, Theta'/2 3 -> 47,
 //     x 6 stages = 282;
 //     the FSAL stage's constraint potentials 15;
-//   stage sums y + h sum a_ij k_j over 5 components: 20 products h a_ij and 100 FMA = 220;
+//   stage sums y + h sum_j a_ij k_j over 5 components (bhk_trace.cu stage_f32): per stage of M terms
+//     and component a product, M - 1 FMA and the FMA by h, 2M + 1 -> 5 x (2 x 20 + 6) = 230;
 //   error estimate and weighted norm: 5 x 16 + 2 = 82;  step control and pole cap: 8.
-constexpr double kFlopsPerStep = 607.0;
+constexpr double kFlopsPerStep = 617.0;
 
 }  // namespace
 
@@ -163,7 +164,7 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.p.chunk = r.chunk;
     r.p.buckets = r.buckets;
     r.graph = o->use_graph != 0;
-    const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 2);
+    const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 1);
     r.regcap = (r.fp64 || rb >= 3) ? 0 : rb;
     if (r.regcap > 0 && r.block > 128) r.block = 128;
     r.block = std::min(r.block, 256);
@@ -772,7 +773,7 @@ bhk_status bhk_autotune(bhk_context* c, const bhk_frame_desc* frames, int32_t nf
     const int budgets[] = {3, 1, 2};
     const bhk_rays_out out = own_outputs(c);
     float best = 1e30f;
-    int bb = 128, bc = 32, bk = 1, br = 2;
+    int bb = 128, bc = 32, bk = 1, br = 1;
     cudaEvent_t t0, t1;
     BHK_CUDA(cudaEventCreate(&t0));
     BHK_CUDA(cudaEventCreate(&t1));

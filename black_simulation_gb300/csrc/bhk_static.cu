@@ -81,21 +81,29 @@ bhk_status fail(bhk_status s, const std::string& m) {
     return s;
 }
 
-// Frame descriptors travel as a kernel parameter: 64 x 88 + 8 bytes, above the classic 4 KB limit
-// and within the 32,764 bytes that CUDA 12.1 and later allow on Volta and later GPUs (this library is
-// built by CUDA 13 for sm_103a only).
-struct FrameBatch {
-    bhk_frame_desc f[kStaticMaxFrames];
-    int n;
+// The frames' set-up (tetrads, lowered vectors, horizon, ISCO, capture and escape radii) is made on the
+// host by the same code as bhk_trace_frames uses, so both entry points trace from identical bits, and
+// travels to the device as kernel parameters: 64 x 408 + 8 bytes of frame records and 64 x 136 + 16
+// bytes of geometries, each above the classic 4 KB limit and within the 32,764 bytes that CUDA 12.1 and
+// later allow on Volta and later GPUs (this library is built by CUDA 13 for sm_103a only).
+struct FrameTable {
+    FrameDev f[kStaticMaxFrames];
+    int n, pad;
 };
+struct GeomTable {
+    RayGeom g[kStaticMaxFrames];
+    long long n_rays;
+    int n, pad;
+};
+static_assert(sizeof(FrameTable) <= 32764 && sizeof(GeomTable) <= 32764, "kernel parameter limit");
 
-__global__ void stage_frames_kernel(FrameBatch batch, FrameDev* frames) {
-    for (int i = threadIdx.x; i < batch.n; i += blockDim.x) {
-        FrameDev fd;
-        memset(&fd, 0, sizeof(fd));
-        fd.d = batch.f[i];
-        frames[i] = fd;
-    }
+__global__ void stage_frames_kernel(FrameTable t, FrameDev* frames) {
+    for (int i = threadIdx.x; i < t.n; i += blockDim.x) frames[i] = t.f[i];
+}
+
+__global__ void stage_geom_kernel(GeomTable t, RayGeom* geom, Control* ctl) {
+    for (int i = threadIdx.x; i < t.n; i += blockDim.x) geom[i] = t.g[i];
+    if (threadIdx.x == 0) ctl->n_rays = t.n_rays;
 }
 
 std::mutex g_addr_mu;
@@ -211,7 +219,7 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     int block = o.block > 0 ? std::min(o.block, 256) : 128;
     p.chunk = ((o.chunk > 32 ? o.chunk : 32) + 31) / 32 * 32;  // whole batches of 32 (one per lane)
     p.buckets = std::min(o.sort_buckets > 0 ? o.sort_buckets : 1, kMaxBuckets);
-    const int rb = o.reg_budget > 0 ? o.reg_budget : 2;
+    const int rb = o.reg_budget > 0 ? o.reg_budget : 1;
     const int regcap = (fp64 || rb >= 3) ? 0 : rb;
     if (regcap > 0) block = std::min(block, 128);
     const int grid = std::max(1, trace_blocks_per_sm(fp64, regcap, block)) * sms;
@@ -234,15 +242,19 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
                  out->turns};
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    FrameBatch batch;
-    std::memset(&batch, 0, sizeof(batch));
-    for (int i = 0; i < nframes; ++i) batch.f[i] = frames[i];
-    batch.n = nframes;
+    // Host-side tables (about 35 KB on this thread's stack; no allocation).
+    FrameTable ft;
+    GeomTable gt;
+    std::memset(static_cast<void*>(&ft), 0, sizeof(ft));
+    std::memset(static_cast<void*>(&gt), 0, sizeof(gt));
+    for (int i = 0; i < nframes; ++i) ft.f[i].d = frames[i];
+    gt.n_rays = setup_frames_host(ft.f, gt.g, nframes, p);
+    ft.n = gt.n = nframes;
     cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(Control), s);
     if (e == cudaSuccess && p.buckets > 1) e = cudaMemsetAsync(S.hist, 0, sizeof(unsigned) * kMaxBuckets, s);
     if (e != cudaSuccess) return fail(BHK_ECUDA, std::string("clearing the control block: ") + cudaGetErrorString(e));
-    stage_frames_kernel<<<1, 64, 0, s>>>(batch, fdev);
-    launch_frame_setup(fdev, geom, nframes, p, ctl, s);
+    stage_frames_kernel<<<1, 64, 0, s>>>(ft, fdev);
+    stage_geom_kernel<<<1, 64, 0, s>>>(gt, geom, ctl);
     launch_rays_frames(fdev, geom, nframes, L, p, ctl, sms * 8, s);
     const int32_t* order = nullptr;
     if (p.buckets > 1) {

@@ -657,6 +657,87 @@ __device__ __forceinline__ void flush_f32(const Lane<float>& s, const Outputs& o
     write_path(s, o, ray, 0.0, r_cap);
 }
 
+// ---- packed FP32 (f32x2) pieces of the FP32 step ----
+// The state's components pair up as (r, theta) = (0, 1) and (vr, vtheta) = (3, 4), with phi (2) alone;
+// the pairs go through Blackwell's packed FP32 instructions, which do two lanes' worth of FP32 work per
+// issued instruction (the tracer is bound by instruction issue, not by the FMA pipe).
+__device__ __forceinline__ float2 pr01(const float v[5]) { return make_float2(v[0], v[1]); }
+__device__ __forceinline__ float2 pr34(const float v[5]) { return make_float2(v[3], v[4]); }
+
+// The Dormand-Prince coefficients the FP32 step multiplies, by position: [0, 20) the stage rows
+// a21; a31 a32; ...; a61 .. a65 and the solution row b1 b3 b4 b5 b6, [20, 26) the error row
+// e1 e3 e4 e5 e6 e7. Each enters a packed instruction as a pair (c, c), made from an immediate.
+__device__ __forceinline__ constexpr float dp_coef(int i) {
+    constexpr double c[26] = {DP::a21, DP::a31, DP::a32, DP::a41, DP::a42, DP::a43, DP::a51, DP::a52, DP::a53,
+                              DP::a54, DP::a61, DP::a62, DP::a63, DP::a64, DP::a65, DP::b1,  DP::b3,  DP::b4,
+                              DP::b5,  DP::b6,  DP::e1,  DP::e3,  DP::e4,  DP::e5,  DP::e6,  DP::e7};
+    return float(c[i]);
+}
+constexpr int kCoefE = 20;
+__device__ __forceinline__ float2 dp_pair(int i) { return make_float2(dp_coef(i), dp_coef(i)); }
+
+// t = y + h sum_m a_m k[j_m] with a_m = dp_coef(O + m): the tableau row's sum first (a chain of fused
+// multiply-adds in the order of m, from a product), then one fused multiply-add by h onto y.
+template <int O, int M>
+__device__ __forceinline__ void stage_f32(const float y[5], const float k[7][5], float2 hh, const int (&j)[M],
+                                          float t[5]) {
+    float2 u0 = __fmul2_rn(dp_pair(O), pr01(k[j[0]]));
+    float2 u1 = __fmul2_rn(dp_pair(O), pr34(k[j[0]]));
+    float u2 = __fmul_rn(dp_coef(O), k[j[0]][2]);
+#pragma unroll
+    for (int m = 1; m < M; ++m) {
+        const float2 am = dp_pair(O + m);
+        u0 = __ffma2_rn(am, pr01(k[j[m]]), u0);
+        u1 = __ffma2_rn(am, pr34(k[j[m]]), u1);
+        u2 = fmaf(am.x, k[j[m]][2], u2);
+    }
+    const float2 p0 = __ffma2_rn(hh, u0, pr01(y)), p1 = __ffma2_rn(hh, u1, pr34(y));
+    t[0] = p0.x; t[1] = p0.y; t[2] = fmaf(hh.x, u2, y[2]); t[3] = p1.x; t[4] = p1.y;
+}
+
+// Sum over the components of (e_i / sc_i)^2, e = the embedded error estimate without its factor h and
+// sc_i = rtol (1 + max(|y_i|, |y5_i|)): the FP32 error norm's sum, in the scalar form's rounding.
+__device__ __forceinline__ float error_norm2_f32(const float y[5], const float y5[5], const float k[7][5], float rtol) {
+    const float2 e1 = dp_pair(kCoefE), e3 = dp_pair(kCoefE + 1), e4 = dp_pair(kCoefE + 2), e5 = dp_pair(kCoefE + 3),
+                 e6 = dp_pair(kCoefE + 4), e7 = dp_pair(kCoefE + 5);
+    const float2 rt = make_float2(rtol, rtol);
+    float2 q[2];
+    float q2;
+#pragma unroll
+    for (int pr = 0; pr < 2; ++pr) {
+        const int i = pr == 0 ? 0 : 3;
+        const float2 k0 = make_float2(k[0][i], k[0][i + 1]), k2 = make_float2(k[2][i], k[2][i + 1]),
+                     k3 = make_float2(k[3][i], k[3][i + 1]), k4 = make_float2(k[4][i], k[4][i + 1]),
+                     k5 = make_float2(k[5][i], k[5][i + 1]), k6 = make_float2(k[6][i], k[6][i + 1]);
+        float2 e = __fmul2_rn(e1, k0);
+        e = __ffma2_rn(e3, k2, e);
+        e = __ffma2_rn(e4, k3, e);
+        e = __ffma2_rn(e5, k4, e);
+        e = __ffma2_rn(e6, k5, e);
+        e = __ffma2_rn(e7, k6, e);
+        const float2 mx = make_float2(fmaxf(fabsf(y[i]), fabsf(y5[i])), fmaxf(fabsf(y[i + 1]), fabsf(y5[i + 1])));
+        const float2 sc = __ffma2_rn(rt, mx, rt);
+        q[pr] = __fmul2_rn(e, make_float2(rcp_approx(sc.x), rcp_approx(sc.y)));
+    }
+    {
+        float e = __fmul_rn(e1.x, k[0][2]);
+        e = fmaf(e3.x, k[2][2], e);
+        e = fmaf(e4.x, k[3][2], e);
+        e = fmaf(e5.x, k[4][2], e);
+        e = fmaf(e6.x, k[5][2], e);
+        e = fmaf(e7.x, k[6][2], e);
+        const float sc = fmaf(rtol, fmaxf(fabsf(y[2]), fabsf(y5[2])), rtol);
+        q2 = __fmul_rn(e, rcp_approx(sc));
+    }
+    // The sum in component order 0 .. 4, as the scalar loop accumulates it.
+    float acc = __fmul_rn(q[0].x, q[0].x);
+    acc = fmaf(q[0].y, q[0].y, acc);
+    acc = fmaf(q2, q2, acc);
+    acc = fmaf(q[1].x, q[1].x, acc);
+    acc = fmaf(q[1].y, q[1].y, acc);
+    return acc;
+}
+
 // One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
 // kRescue (FP32 only: hand the state to FP64) or kRestart (FP32 only: non-finite state).
 template <typename T>
@@ -693,50 +774,20 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
             y5[i] = s.y[i] + h * (T(DP::b1) * s.k[0][i] + T(DP::b3) * s.k[2][i] + T(DP::b4) * s.k[3][i] +
                                   T(DP::b5) * s.k[4][i] + T(DP::b6) * s.k[5][i]);
     } else {
-        // FP32: each stage's tableau row scaled by h once (shared by the 5 components, computed
-        // where it is used so that it is not held across stages), so that every stage sum is a pure
-        // chain of fused multiply-adds starting from y.
-        {
-            const T b1 = h * T(DP::a21);
-#pragma unroll
-            for (int i = 0; i < 5; ++i) t[i] = fmaf(b1, s.k[0][i], s.y[i]);
-        }
+        // FP32: each stage's sum y + h sum_j a_ij k_j with the pairs (r, theta) and (vr, vtheta) on
+        // the packed f32x2 instructions (two components per instruction), phi alone.
+        const float2 hh = make_float2(h, h);
+        stage_f32<0, 1>(s.y, s.k, hh, {0}, t);
         rhs(s.c, t, s.k[1]);
-        {
-            const T b1 = h * T(DP::a31), b2 = h * T(DP::a32);
-#pragma unroll
-            for (int i = 0; i < 5; ++i) t[i] = fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i]));
-        }
+        stage_f32<1, 2>(s.y, s.k, hh, {0, 1}, t);
         rhs(s.c, t, s.k[2]);
-        {
-            const T b1 = h * T(DP::a41), b2 = h * T(DP::a42), b3 = h * T(DP::a43);
-#pragma unroll
-            for (int i = 0; i < 5; ++i) t[i] = fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i])));
-        }
+        stage_f32<3, 3>(s.y, s.k, hh, {0, 1, 2}, t);
         rhs(s.c, t, s.k[3]);
-        {
-            const T b1 = h * T(DP::a51), b2 = h * T(DP::a52), b3 = h * T(DP::a53), b4 = h * T(DP::a54);
-#pragma unroll
-            for (int i = 0; i < 5; ++i)
-                t[i] = fmaf(b4, s.k[3][i], fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i]))));
-        }
+        stage_f32<6, 4>(s.y, s.k, hh, {0, 1, 2, 3}, t);
         rhs(s.c, t, s.k[4]);
-        {
-            const T b1 = h * T(DP::a61), b2 = h * T(DP::a62), b3 = h * T(DP::a63), b4 = h * T(DP::a64),
-                    b5 = h * T(DP::a65);
-#pragma unroll
-            for (int i = 0; i < 5; ++i)
-                t[i] = fmaf(b5, s.k[4][i],
-                            fmaf(b4, s.k[3][i], fmaf(b3, s.k[2][i], fmaf(b2, s.k[1][i], fmaf(b1, s.k[0][i], s.y[i])))));
-        }
+        stage_f32<10, 5>(s.y, s.k, hh, {0, 1, 2, 3, 4}, t);
         rhs(s.c, t, s.k[5]);
-        {
-            const T c1 = h * T(DP::b1), c3 = h * T(DP::b3), c4 = h * T(DP::b4), c5 = h * T(DP::b5), c6 = h * T(DP::b6);
-#pragma unroll
-            for (int i = 0; i < 5; ++i)
-                y5[i] = fmaf(c6, s.k[5][i],
-                             fmaf(c5, s.k[4][i], fmaf(c4, s.k[3][i], fmaf(c3, s.k[2][i], fmaf(c1, s.k[0][i], s.y[i])))));
-        }
+        stage_f32<15, 5>(s.y, s.k, hh, {0, 2, 3, 4, 5}, y5);
     }
     Proj<T> pj;
     if constexpr (F64) rhs<T, false>(s.c, y5, s.k[6], &pj, &s.kt[6]);
@@ -745,21 +796,17 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
     if constexpr (F64) rtol = p.rtol;
     else rtol = p.rtol_f;
     T acc = T(0);
+    if constexpr (F64) {
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        T e;
-        if constexpr (F64) {
-            e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] + T(DP::e5) * s.k[4][i] +
-                     T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
-        } else {  // without the factor h, applied once to the sum below
-            e = fmaf(T(DP::e7), s.k[6][i],
-                     fmaf(T(DP::e6), s.k[5][i],
-                          fmaf(T(DP::e5), s.k[4][i],
-                               fmaf(T(DP::e4), s.k[3][i], fmaf(T(DP::e3), s.k[2][i], T(DP::e1) * s.k[0][i])))));
+        for (int i = 0; i < 5; ++i) {
+            const T e = h * (T(DP::e1) * s.k[0][i] + T(DP::e3) * s.k[2][i] + T(DP::e4) * s.k[3][i] +
+                             T(DP::e5) * s.k[4][i] + T(DP::e6) * s.k[5][i] + T(DP::e7) * s.k[6][i]);
+            const T sc = rtol + rtol * fmax(fabs(s.y[i]), fabs(y5[i]));
+            const T q = Math<T>::div(e, sc);
+            acc += q * q;
         }
-        const T sc = rtol + rtol * fmax(fabs(s.y[i]), fabs(y5[i]));
-        const T q = Math<T>::div(e, sc);
-        acc += q * q;
+    } else {
+        acc = error_norm2_f32(s.y, y5, s.k, rtol);  // without the factor h, applied once below
     }
     // err = sqrt(acc / 5); the FP32 path works with err^2.
     T err, e2;

@@ -128,7 +128,7 @@ typedef struct {
     int32_t sort_buckets;   /* rays pre-sorted into this many cost buckets; 0 -> autotuned or 1; 1 = none
                                (frames are then taken by 8 x 4 pixel tiles and launched in the kernel) */
     int32_t use_graph;      /* 1: replay the whole batch as one captured CUDA graph */
-    int32_t reg_budget;     /* mixed tracer variant: 0 autotuned (else 2), 1: <= 102 registers per
+    int32_t reg_budget;     /* mixed tracer variant: 0 autotuned (else 1), 1: <= 102 registers per
                                thread (20 warps/SM, blocks <= 128), 2: <= 85 (24 warps/SM), 3: uncapped */
     double pole_step_frac;  /* mixed: outgoing steps capped at this fraction of the Mino time left before
                                r runs off to infinity (~ r/|vr|); 0 -> 0.1 (rtol/1e-6)^(1/5), < 0 off */
