@@ -225,6 +225,68 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def batch_measurement(args, ctx, dev, steps: int = 5, warmup: int = 3) -> dict:
+    """The 64-frame batch (uneven sizes, spins and poses; one persistent launch replayed as a CUDA graph,
+    launch shape autotuned) beside the headline frame: rays/s on the device and end to end, the tracer's
+    roofline, and errors against FP64 on a seeded sample of its pixels (it has millions of escaping
+    rays, so the exit-angle bound is exercised here)."""
+    import torch
+    from black_simulation_gb300 import bhk
+    frames, opts, cfg = workload("batch64")
+    n = sum(f.rays for f in frames)
+    tuned = ctx.autotune(frames, opts)
+    opts.block, opts.chunk, opts.sort_buckets, opts.reg_budget = (tuned["block"], tuned["chunk"],
+                                                                  tuned["sort_buckets"], tuned["reg_budget"])
+    out = bhk.alloc_outputs(n, dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        ctx.trace_frames(frames, opts, out=out)
+    torch.cuda.synchronize()
+    ms, kms, acc = [], [], []
+    with Clocks(dev.index or 0) as clk:
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.trace_frames(frames, opts, out=out)
+            b.record(stream)
+            st = ctx.stats()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            kms.append(st["kernel_ms"])
+            acc.append(st["accepted_steps"])
+    errs = fp64_check(ctx, frames, out, dev, 1e-3, 65536, args.seed + 2)
+    counts = {k: int(v) for k, v in zip(*np.unique(out["outcome"].cpu().numpy(), return_counts=True))}
+    del out
+    pinned = {k: v.pin_memory() for k, v in bhk.alloc_outputs(n, "cpu").items()}
+    e2e = []
+    for i in range(1 + steps):
+        t0 = time.perf_counter()
+        ctx.trace_frames_host(frames, opts, out=pinned)
+        if i >= 1:
+            e2e.append(time.perf_counter() - t0)
+    d2h = sum(v.numel() * v.element_size() for v in pinned.values())
+    del pinned
+    peak = bhk.fp32_fma_peak_tflops(dev.index or 0)
+    fps = bhk.flops_per_step()
+    k_ms = float(np.mean(kms))
+    achieved = float(np.mean(acc)) * fps / (k_ms * 1e-3) / 1e12
+    return {"workload": cfg["workload"], "rays": n, "steps": steps, "warmup": warmup, "precision": cfg["precision"],
+            "rtol": opts.rtol, "launch": {**{k: tuned[k] for k in ("block", "chunk", "sort_buckets", "reg_budget")},
+                                          "graph": True, "autotuned": True},
+            "value": n / (float(np.mean(ms)) * 1e-3), "unit": "rays/s", "ms_per_step": float(np.mean(ms)),
+            "e2e": {"value": n / float(np.mean(e2e)), "unit": "rays/s", "h2d_bytes_per_step":
+                    len(frames) * bhk.C.sizeof(bhk.FrameDescC), "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "kernel_ms": k_ms, "flops_per_step": fps,
+                         "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run"},
+            "mean_accepted_steps_per_ray": float(np.mean(acc)) / n,
+            "outcomes": {"captured": counts.get(1, 0), "disk": counts.get(2, 0), "escaped": counts.get(3, 0),
+                         "unfinished": counts.get(0, 0)},
+            "errors_vs_fp64": errs, "gpu_launches": steps * 2, "clocks": clk.summary()}
+
+
 def run_ours(args):
     import torch
     from black_simulation_gb300 import bhk, build
@@ -309,6 +371,17 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,  # per step: trace (with the launch and the tile order), rescue
         "clocks": clk.summary(),
     }
+    if rank == 0 and args.workload in ("1080p", "batch64"):
+        # errors of the timed workload's last step against FP64 on a seeded sample of its pixels
+        if args.workload == "1080p":
+            line["errors_vs_fp64"] = fp64_check(ctx, frames, out, dev, 0.01, 1 << 20, args.seed)
+        else:
+            line["errors_vs_fp64"] = fp64_check(ctx, frames, out, dev, 1e-3, 65536, args.seed + 2)
+    if rank == 0 and world == 1 and args.workload == "1080p" and args.scale == 1 and not args.no_batch:
+        try:
+            line["batch64"] = batch_measurement(args, ctx, dev)
+        except Exception as exc:  # the headline line must not be lost to the extra workload
+            line["batch64"] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and world == 1 and args.workload == "1080p" and args.scale == 1 and not args.no_surrogate:
         # The metric's comparison: the surrogate + fallback path against this tracer on the surrogate's
         # own workload (the orbit sequence), after training the network (not part of the timed steps).
@@ -390,6 +463,152 @@ def error_stats(test, ref):
         res["r_disk_rel"] = {"median": float(np.median(er)), "p99": float(np.quantile(er, 0.99)), "max": float(er.max()),
                              "n": int(disk.sum())}
         res["g_rel"] = {"median": float(np.median(eg)), "p99": float(np.quantile(eg, 0.99)), "max": float(eg.max())}
+        if "phi_disk" in test:
+            ep = np.abs(np.angle(np.exp(1j * (test["phi_disk"][disk] - ref["phi_disk"][disk]))))
+            if np.isfinite(ep).all():
+                res["phi_disk_rad"] = {"median": float(np.median(ep)), "p99": float(np.quantile(ep, 0.99)),
+                                       "max": float(ep.max())}
+    return res
+
+
+def held_out_pixels(frames, per_frame: float, cap: int, seed: int):
+    """A seeded sample of each frame's pixels (global indices, sorted): `per_frame` of its pixels,
+    at most `cap` over all frames (taken in proportion), at least one per frame."""
+    total = sum(f.rays for f in frames)
+    frac = min(per_frame, cap / total)
+    rng = np.random.default_rng(seed)
+    held, off = [], 0
+    for f in frames:
+        held.append(off + rng.choice(f.rays, max(1, int(f.rays * frac)), replace=False))
+        off += f.rays
+    return np.sort(np.concatenate(held)).astype(np.int32)
+
+
+def output_errors(test, ref):
+    """Per pixel and output: r_disk and g relative, phi_disk (rad) for pixels both traces put on the
+    disk, the exit direction (rad) for pixels both send to the same sky; NaN elsewhere."""
+    n = ref["outcome"].size
+    e = {k: np.full(n, np.nan) for k in ("r_disk", "g", "phi_disk", "exit_angle")}
+    disk = (test["outcome"] == 2) & (ref["outcome"] == 2)
+    e["r_disk"][disk] = np.abs(test["r_disk"][disk] / ref["r_disk"][disk] - 1.0)
+    e["g"][disk] = np.abs(test["g"][disk] / ref["g"][disk] - 1.0)
+    e["phi_disk"][disk] = np.abs(np.angle(np.exp(1j * (test["phi_disk"][disk] - ref["phi_disk"][disk]))))
+    esc = np.isin(ref["outcome"], (3, 4)) & (test["outcome"] == ref["outcome"])
+    e["exit_angle"][esc] = angle_between(test["theta_inf"][esc], test["phi_inf"][esc], ref["theta_inf"][esc],
+                                         ref["phi_inf"][esc])
+    return e
+
+
+def per_ray_error(test, ref):
+    """Each pixel's worst error against FP64 over the outputs its outcome defines (r_disk and g
+    relative, phi_disk as an angle; the exit direction as an angle); inf where the outcomes differ."""
+    err = np.zeros(ref["outcome"].size)
+    disk = (test["outcome"] == 2) & (ref["outcome"] == 2)
+    err[disk] = np.fmax.reduce([np.abs(test["r_disk"][disk] / ref["r_disk"][disk] - 1.0),
+                                np.abs(test["g"][disk] / ref["g"][disk] - 1.0),
+                                np.abs(np.angle(np.exp(1j * (test["phi_disk"][disk] - ref["phi_disk"][disk]))))])
+    esc = np.isin(ref["outcome"], (3, 4)) & (test["outcome"] == ref["outcome"])
+    err[esc] = angle_between(test["theta_inf"][esc], test["phi_inf"][esc], ref["theta_inf"][esc], ref["phi_inf"][esc])
+    err[test["outcome"] != ref["outcome"]] = np.inf
+    return err
+
+
+def outlier_causes(test, ref, dist, r_in, r_out, band: float, thr: float, same_tol=None):
+    """Why each pixel whose error exceeds thr does: near the critical curve (image-plane distance below
+    `band`, where a ray's error grows as it winds the photon sphere); at a disk edge (either trace's
+    disk crossing within 1e-3 relative of the pixel's r_in or r_out, so one trace counts a crossing the
+    other misses); a different equator crossing (both on the disk, radii apart by more than 1 %); the
+    integration tolerance (the FP64 trace at the test's own tolerance, `same_tol`, errs above thr on
+    that pixel too: the step-size control, not the FP32 arithmetic); the outcome flips (elsewhere);
+    other (what FP32 arithmetic adds)."""
+    err = per_ray_error(test, ref)
+    bad = err > thr
+    tol_bad = per_ray_error(same_tol, ref) > thr if same_tol is not None else np.zeros(bad.size, bool)
+    causes = {"band": 0, "disk_edge": 0, "different_crossing": 0, "tolerance": 0, "outcome_elsewhere": 0,
+              "other": 0}
+    near = lambda r: (np.abs(r / r_in - 1.0) < 1e-3) | (np.abs(r / r_out - 1.0) < 1e-3)  # noqa: E731
+    edge = near(np.nan_to_num(test["r_disk"], nan=-1.0)) | near(np.nan_to_num(ref["r_disk"], nan=-1.0))
+    both_disk = (test["outcome"] == 2) & (ref["outcome"] == 2)
+    apart = both_disk & (np.abs(np.nan_to_num(test["r_disk"]) / np.where(both_disk, ref["r_disk"], 1.0) - 1.0) > 1e-2)
+    for i in np.nonzero(bad)[0]:
+        if dist[i] < band:
+            causes["band"] += 1
+        elif edge[i]:
+            causes["disk_edge"] += 1
+        elif apart[i]:
+            causes["different_crossing"] += 1
+        elif tol_bad[i]:
+            causes["tolerance"] += 1
+        elif test["outcome"][i] != ref["outcome"][i]:
+            causes["outcome_elsewhere"] += 1
+        else:
+            causes["other"] += 1
+    return int(bad.sum()), causes, err
+
+
+KEYS = ("outcome", "r_disk", "phi_disk", "g", "theta_inf", "phi_inf")
+
+
+def fp64_reference(ctx, frames, held, dev, same_rtol: float = 1e-6) -> dict:
+    """The sampled pixels `held` (global indices) traced in FP64 (rtol 1e-10), with each one's distance
+    to its frame's analytic critical curve and its disk radii; also traced in FP64 at `same_rtol` (the
+    tested path's tolerance), which separates the error of the tolerance from that of FP32 arithmetic."""
+    import torch
+    from black_simulation_gb300 import bhk
+    hd = torch.from_numpy(held).to(dev)
+    t0 = time.perf_counter()
+    ref = ctx.trace_pixels(frames, hd, bhk.TraceOpts("fp64", rtol=1e-10))
+    torch.cuda.synchronize()
+    t_fp64 = time.perf_counter() - t0
+    same = ctx.trace_pixels(frames, hd, bhk.TraceOpts("fp64", rtol=same_rtol))
+    torch.cuda.synchronize()
+    offs = np.cumsum([0] + [f.rays for f in frames])
+    fi = np.searchsorted(offs, held, side="right") - 1
+    dist, r_in, r_out = np.empty(held.size), np.empty(held.size), np.empty(held.size)
+    for j, f in enumerate(frames):
+        m = fi == j
+        if not m.any():
+            continue
+        al, be = bhk.pixel_alpha_beta(f, held[m] - offs[j])
+        ca, cb = bhk.critical_curve(f.a, f.r_obs, f.theta_obs, 400)
+        dist[m] = bhk.curve_distance(al, be, ca, cb)
+        r_in[m] = f.r_disk_in if f.r_disk_in > 0 else bhk.isco_prograde(f.a)
+        r_out[m] = f.r_disk_out
+    return {"held": held, "index": hd, "out": {k: ref[k].cpu().numpy() for k in KEYS}, "dist": dist, "r_in": r_in,
+            "r_out": r_out, "seconds": t_fp64, "same_rtol": same_rtol,
+            "same": {k: same[k].cpu().numpy() for k in KEYS}}
+
+
+def judge(test_h, R, band: float = 1e-2, thr: float = 1e-4, mask=None) -> dict:
+    """Errors of test_h (host arrays on R's pixels) against the FP64 reference R, raw and outside a
+    `band` (M) of the critical curve, with the count of pixels above `thr` and their causes."""
+    ref_h, same_h, dist, r_in, r_out = R["out"], R["same"], R["dist"], R["r_in"], R["r_out"]
+    if mask is not None:
+        test_h = {k: v[mask] for k, v in test_h.items()}
+        ref_h = {k: v[mask] for k, v in ref_h.items()}
+        same_h = {k: v[mask] for k, v in same_h.items()}
+        dist, r_in, r_out = dist[mask], r_in[mask], r_out[mask]
+    outside = dist >= band
+    n_bad, causes, err = outlier_causes(test_h, ref_h, dist, r_in, r_out, band, thr, same_h)
+    n_tol = int(np.sum((per_ray_error(same_h, ref_h) > thr) & outside))
+    oe = output_errors(test_h, ref_h)
+    by_output = {k: int(np.sum((v > thr) & outside)) for k, v in oe.items()}
+    magnitude = {f">{t:g}": int(np.sum((err > t) & outside)) for t in (1e-4, 1e-3, 1e-2, 1e-1)}
+    return {"pixels": int(dist.size), "reference": "FP64 Dormand-Prince, rtol 1e-10", "band_m": band,
+            "raw": error_stats(test_h, ref_h),
+            "outside_band": error_stats({k: v[outside] for k, v in test_h.items()},
+                                        {k: v[outside] for k, v in ref_h.items()}),
+            f"above_{thr:g}": {"count": n_bad, "outside_band": int(((err > thr) & outside).sum()), "by_cause": causes,
+                               f"fp64_at_rtol_{R['same_rtol']:g}_outside_band": n_tol,
+                               "outside_band_by_output": by_output, "outside_band_by_magnitude": magnitude}}
+
+
+def fp64_check(ctx, frames, out, dev, per_frame: float, cap: int, seed: int) -> dict:
+    """judge() of the device outputs `out` (all pixels of `frames`) on a seeded sample of pixels."""
+    R = fp64_reference(ctx, frames, held_out_pixels(frames, per_frame, cap, seed), dev)
+    res = judge({k: out[k][R["index"]].cpu().numpy() for k in KEYS}, R)
+    res["sample"] = f"{per_frame:g} of each frame's pixels, at most {cap} (seed {seed})"
+    res["fp64_check_s"] = R["seconds"]
     return res
 
 
@@ -432,25 +651,13 @@ def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses:
     out_t = bhk.alloc_outputs(n, dev)
     ms_t, _ = timed(lambda: ctx.trace_frames(frames, opts, out=out_t))
     # 1% held-out pixels per frame (seeded), traced in FP64 as the yardstick
-    rng = np.random.default_rng(args.seed + 1)
-    held, off = [], 0
-    for f in frames:
-        held.append(off + rng.choice(f.rays, max(1, f.rays // 100), replace=False))
-        off += f.rays
-    held = np.sort(np.concatenate(held)).astype(np.int32)
-    hd = torch.from_numpy(held).to(dev)
-    t0 = time.perf_counter()
-    ref = ctx.trace_pixels(frames, hd, bhk.TraceOpts("fp64", rtol=1e-10))
-    torch.cuda.synchronize()
-    t_fp64 = time.perf_counter() - t0
+    R = fp64_reference(ctx, frames, held_out_pixels(frames, 0.01, 1 << 40, args.seed + 1), dev)
     fbl = np.zeros(n, bool)
     sur.render(ctx, frames, opts, out=out_s, fallback=True)
     fbl[sur.fallback_list().cpu().numpy()] = True
-    keys = ("outcome", "r_disk", "g", "theta_inf", "phi_inf")
-    pick = lambda o: {k: o[k][hd].cpu().numpy() for k in keys}
-    ref_h = {k: ref[k].cpu().numpy() for k in keys}   # compact: entry i is pixel held[i]
+    pick = lambda o: {k: o[k][R["index"]].cpu().numpy() for k in KEYS}  # noqa: E731
     sur_h, tr_h = pick(out_s), pick(out_t)
-    answered = ~fbl[held]
+    answered = ~fbl[R["held"]]
     peak, src = measured_peak("bf16_tflops", 1900.0)
     achieved = n * 2 * MAC_FWD / (ms_infer * 1e-3) / 1e12
     sur.close()
@@ -464,10 +671,9 @@ def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses:
         "speedup_vs_plain_tracer": ms_t / ms_s,
         "fallback_fraction": fb / n,
         "inference": {"value": n / (ms_infer * 1e-3), "ms": ms_infer},
-        "errors_vs_fp64": {"surrogate_path": error_stats(sur_h, ref_h),
-                           "network_answered_only": error_stats({k: v[answered] for k, v in sur_h.items()},
-                                                                {k: v[answered] for k, v in ref_h.items()}),
-                           "plain_tracer": error_stats(tr_h, ref_h), "fp64_check_s": t_fp64},
+        "errors_vs_fp64": {"surrogate_path": judge(sur_h, R), "network_answered_only": judge(sur_h, R, mask=answered),
+                           "plain_tracer": judge(tr_h, R), "sample": "1% of each frame's pixels (seeded)",
+                           "fp64_check_s": R["seconds"]},
         "meets_1e-4_bound": False,
         "inference_roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                                "frac": achieved / peak, "traffic": None, "peak_source": src,
@@ -564,6 +770,7 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="1080p: skip the surrogate-vs-tracer comparison")
+    ap.add_argument("--no-batch", action="store_true", help="1080p: skip the 64-frame batch beside the headline")
     ap.add_argument("--ref-sample-s", type=float, default=0.0,
                     help="--impl reference: seconds of CPU work per step (0: 30 s over all steps, at least 2 s)")
     ap.add_argument("--scale", type=int, default=1, help="divide the frame size (profiling captures)")

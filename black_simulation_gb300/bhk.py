@@ -348,6 +348,33 @@ def critical_curve(a: float, r_obs: float, theta_obs: float, samples: int = 400)
     return al[:n.value].copy(), be[:n.value].copy()
 
 
+def pixel_alpha_beta(frame: "Frame", local):
+    """Image-plane (alpha, beta) of the frame's pixels with row-major indices `local` (numpy), as the
+    tracer places them: pixel centres, rows from beta_hi down."""
+    local = np.asarray(local, dtype=np.int64)
+    row, col = np.divmod(local, frame.width)
+    alpha = frame.alpha_lo + (col + 0.5) * (frame.alpha_hi - frame.alpha_lo) / frame.width
+    beta = frame.beta_hi - (row + 0.5) * (frame.beta_hi - frame.beta_lo) / frame.height
+    return alpha, beta
+
+
+def curve_distance(alpha, beta, curve_alpha, curve_beta, chunk: int = 2048):
+    """Image-plane distance (M) from each point (alpha, beta) to the closed polyline through
+    (curve_alpha, curve_beta) -- e.g. the analytic critical curve critical_curve() returns."""
+    alpha, beta = np.asarray(alpha, dtype=np.float64), np.asarray(beta, dtype=np.float64)
+    ax, ay = np.asarray(curve_alpha, dtype=np.float64), np.asarray(curve_beta, dtype=np.float64)
+    bx, by = np.roll(ax, -1), np.roll(ay, -1)
+    ex, ey = bx - ax, by - ay
+    ll = np.maximum(ex * ex + ey * ey, 1e-300)
+    out = np.empty(alpha.size)
+    for i in range(0, alpha.size, chunk):
+        px, py = alpha[i:i + chunk, None], beta[i:i + chunk, None]
+        t = np.clip(((px - ax) * ex + (py - ay) * ey) / ll, 0.0, 1.0)
+        dx, dy = px - (ax + t * ex), py - (ay + t * ey)
+        out[i:i + chunk] = np.sqrt(dx * dx + dy * dy).min(axis=1)
+    return out
+
+
 FATES = ("bound", "circular", "plunges", "escapes", "hits_surface")  # trajectory::Fate
 
 

@@ -106,6 +106,80 @@ def test_mixed_precision_errors_vs_fp64(ctx, oracle, golden, name, a, r_obs, deg
     assert st["unfinished"] == 0
 
 
+# Two geometries of the seeded 64-frame batch (frames 37 and 60 of its generator, rounded), at reduced
+# resolution: a distant camera near the pole (a = 0.1411, r_obs = 983.45 M, 13.51 deg, 16:9) and the
+# closest camera of the batch (a = 0.2189, r_obs = 23.35 M, 64.47 deg, square, a wide field). Half-width
+# 1.2 x the largest distance of the analytic critical curve from the image centre; disk ISCO..30 M.
+BATCH_CASES = [(0.1411, 983.45, 13.51, 96, 54), (0.2189, 23.35, 64.47, 64, 64)]
+
+
+def batch_frame(oracle, a, r_obs, deg, w, h):
+    ca, cb = oracle.critical_curve_finite(a, r_obs, math.radians(deg), 200)
+    half = 1.2 * float(np.max(np.hypot(ca, cb)))
+    hb = half * h / w
+    return bhk.Frame(a, r_obs, math.radians(deg), w, h, -half, half, -hb, hb, 0.0, 30.0)
+
+
+def frame_band(oracle, f, width):
+    al, be = po.pixel_grid(f.width, f.height, f.alpha_lo, f.alpha_hi, f.beta_lo, f.beta_hi)
+    ca, cb = oracle.critical_curve_finite(f.a, f.r_obs, f.theta_obs, 800)
+    return po.band_distance(al, be, ca, cb) > width
+
+
+def ray_errors(out, ref):
+    """Per pixel: the largest error of r_disk, g (relative) and phi_disk (rad) for disk rays, of the
+    exit direction (rad) for escaping rays; inf where the outcomes differ."""
+    err = np.zeros(ref["outcome"].size)
+    d = (out["outcome"] == bhk.DISK) & (ref["outcome"] == bhk.DISK)
+    e = (out["outcome"] == bhk.ESCAPED) & (ref["outcome"] == bhk.ESCAPED)
+    ang = lambda x, y: np.abs(np.angle(np.exp(1j * (x - y))))  # noqa: E731
+    err[d] = np.maximum.reduce([np.abs(out["r_disk"][d] / ref["r_disk"][d] - 1), np.abs(out["g"][d] / ref["g"][d] - 1),
+                                ang(out["phi_disk"][d], ref["phi_disk"][d])])
+    c = (np.sin(out["theta_inf"][e]) * np.sin(ref["theta_inf"][e]) * np.cos(out["phi_inf"][e] - ref["phi_inf"][e]) +
+         np.cos(out["theta_inf"][e]) * np.cos(ref["theta_inf"][e]))
+    err[e] = np.arccos(np.clip(c, -1.0, 1.0))
+    err[out["outcome"] != ref["outcome"]] = np.inf
+    return err
+
+
+@pytest.mark.parametrize("a,r_obs,deg,w,h", BATCH_CASES)
+def test_batch_frames_against_oracle_dp5(ctx, oracle, a, r_obs, deg, w, h):
+    """Frames of the 64-frame batch's geometry against the oracle's FP64 Dormand-Prince at rtol 1e-10.
+    FP64 mode: the same outcomes outside 1e-4 M of the critical curve, every output to 1e-8. Mixed mode
+    at the batch's rtol 1e-6, outside 1e-2 M of the curve: the same outcomes; the median ray within
+    1e-6 and the 99th percentile within 2e-5. Its worst rays exceed 1e-4 because of the tolerance, not
+    of FP32: the FP64 integration at the same rtol errs there too (many turns near the photon sphere).
+    So the FP32 arithmetic is judged where the tolerance is not the limit -- wherever the FP64 trace at
+    rtol 1e-6 is within 2.5e-5, the mixed trace is within 1e-4."""
+    f = batch_frame(oracle, a, r_obs, deg, w, h)
+    box = (f.width, f.height, f.alpha_lo, f.alpha_hi, f.beta_lo, f.beta_hi)
+    ref = oracle.trace_frame(po.scene(a=a, r_obs=r_obs, theta_obs_deg=deg, r_disk_out=30.0, tol=1e-10, method=po.DP5),
+                             *box)
+    fp64 = host(ctx.trace_frames([f], bhk.TraceOpts("fp64", rtol=1e-10)))
+    outside = frame_band(oracle, f, 1e-4)
+    np.testing.assert_array_equal(fp64["outcome"][outside], ref["outcome"][outside])
+    err = errors(fp64, ref)
+    print("batch frame", (a, r_obs, deg), "fp64 vs oracle DP5:", err)
+    for k, v in err.items():
+        assert v <= 1e-8, (k, v)
+    mixed = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6)))
+    same = oracle.trace_frame(po.scene(a=a, r_obs=r_obs, theta_obs_deg=deg, r_disk_out=30.0, tol=1e-6, method=po.DP5),
+                              *box)
+    outside = frame_band(oracle, f, 1e-2)
+    assert np.mean(mixed["outcome"][outside] == ref["outcome"][outside]) == 1.0
+    n_esc = int(np.sum((ref["outcome"] == bhk.ESCAPED) & outside))
+    assert n_esc > 0
+    em, es = ray_errors(mixed, ref)[outside], ray_errors(same, ref)[outside]
+    quiet = es < 2.5e-5
+    print("batch frame", (a, r_obs, deg), "mixed vs oracle DP5:", errors(mixed, ref, outside), "escaping rays", n_esc,
+          "median %.2e p99 %.2e max %.2e; FP64 at rtol 1e-6: max %.2e; above 1e-4: mixed %d, FP64 rtol 1e-6 %d; "
+          "max where the tolerance is not the limit %.2e (%d rays)" % (
+              np.median(em), np.quantile(em, 0.99), em.max(), es.max(), np.sum(em > 1e-4), np.sum(es > 1e-4),
+              em[quiet].max(), quiet.sum()))
+    assert np.median(em) < 1e-6 and np.quantile(em, 0.99) < 2e-5
+    assert quiet.mean() > 0.99 and em[quiet].max() < 1e-4
+
+
 def test_per_ray_api_equals_frame_api(ctx):
     f = bhk.frame_c1(20, 12)
     frame_out = host(ctx.trace_frames([f], bhk.TraceOpts("fp64")))
