@@ -40,9 +40,13 @@ sys.path.insert(0, ROOT)
 # FP64 (the plain mixed tracer does; the surrogate path's errors are reported beside it).
 METRIC = "geodesics/s at \u22641e-4 rad exit-angle err vs FP64: surrogate vs plain GPU tracer"
 REF_TOL = 1e-2          # reference product tolerance (src/trajectory.cpp:261); meets the 1e-4 bar
-# DRAM bytes (read + write) of one tracer launch from ncu, by workload: the 960x540 capture of
-# profiles/trace_kernel_1080p_mixed.md (14.61 MB) scaled by rays to the full frame.
-NCU_TRAFFIC = {"1080p": 6.6e6}  # DRAM read + write of one trace launch: ncu at half size, x4 rays
+# DRAM bytes (read + write) of one full-size trace launch from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, one launch after an L2 flush; profiles/trace_kernel_1080p_mixed.md): 0.6 MB read,
+# 136.9 MB written. The algorithmic bytes of a launch are its writes: the outputs (49 B per ray) and the
+# rays' FP64 launch records (E, L, Q, vr, vtheta and the frame index, 44 B per ray); part of them is still
+# in L2 when the kernel ends.
+NCU_TRAFFIC = {"1080p": 137.5e6}
+BYTES_PER_RAY = 49 + 44
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -366,6 +370,7 @@ def run_ours(args):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC.get(args.workload) if args.scale == 1 else None,
+                     "algorithmic_bytes": BYTES_PER_RAY * n_rays,
                      "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run",
                      "kernel_ms": k_ms, "flops_per_step": fps},
         "gpu_launches": 2 * args.steps,  # per step: trace (with the launch and the tile order), rescue
