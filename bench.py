@@ -409,6 +409,11 @@ def run_ours(args):
 # MACs per ray of the network (64 -> 256 -> 256 -> 256 -> 256 -> 16 padded head): forward, and the
 # backward's weight and input gradients (no input gradient of the first layer).
 MAC_FWD = 64 * 256 + 3 * 256 * 256 + 256 * 16
+
+
+def mac_fwd(width: int) -> int:
+    """Multiply-adds per ray of the network's forward pass at a hidden width (head padded to 16)."""
+    return 64 * width + 3 * width * width + width * 16
 MAC_TRAIN = 2 * MAC_FWD + 256 * 16 + 3 * 256 * 256
 
 
@@ -420,31 +425,38 @@ def measured_peak(key: str, fallback: float):
         return fallback, "fallback (no measured peaks file)"
 
 
-def train_surrogate(ctx, args, log=None):
-    """Training set and training run of the surrogate (50M tracer-labelled rays, batch 65,536, Adam,
-    cosine learning rate from 1e-3). Returns (surrogate, info)."""
+def train_surrogates(ctx, args, widths=(256, 64)) -> dict:
+    """Training set (50M tracer-labelled rays) and one training run per hidden width (batch 65,536,
+    Adam, cosine learning rate from 1e-3). Returns {width: (surrogate, info)}."""
     import torch
     from black_simulation_gb300.surrogate import Surrogate, make_dataset
-    s = Surrogate(ctx.device, seed=args.seed, max_batch=65536)
-    if args.surrogate_ckpt and os.path.exists(args.surrogate_ckpt):
-        s.load(args.surrogate_ckpt)
-        return s, {"checkpoint": args.surrogate_ckpt}
-    if args.train_steps == 0:  # untrained network (kernel profiling: the work per ray is the same)
-        return s, {"untrained": True}
-    t0 = time.perf_counter()
-    x, cls, tgt = make_dataset(ctx, args.train_rays, seed=args.seed)
-    torch.cuda.synchronize()
-    t_data = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    hist = s.train(x, cls, tgt, batch=65536, steps=args.train_steps, lr=1e-3)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
-    if args.surrogate_ckpt:
-        s.save(args.surrogate_ckpt)
-    del x, cls, tgt
-    return s, {"train_rays": args.train_rays, "train_steps": args.train_steps, "dataset_s": t_data,
-               "train_s": t_train, "train_rays_per_s": args.train_steps * 65536 / t_train,
-               "final_loss": [float(v) for v in hist[-50:].mean(axis=0)]}
+    nets, data, t_data = {}, None, 0.0
+    for w in widths:
+        s = Surrogate(ctx.device, seed=args.seed, max_batch=65536, width=w)
+        ckpt = args.surrogate_ckpt and (args.surrogate_ckpt if w == 256 else f"{args.surrogate_ckpt}.w{w}.npz")
+        if ckpt and os.path.exists(ckpt):
+            s.load(ckpt)
+            nets[w] = (s, {"checkpoint": ckpt})
+            continue
+        if args.train_steps == 0:  # untrained network (kernel profiling: the work per ray is the same)
+            nets[w] = (s, {"untrained": True})
+            continue
+        if data is None:
+            t0 = time.perf_counter()
+            data = make_dataset(ctx, args.train_rays, seed=args.seed)
+            torch.cuda.synchronize()
+            t_data = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        hist = s.train(*data, batch=65536, steps=args.train_steps, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        if ckpt:
+            s.save(ckpt)
+        nets[w] = (s, {"width": w, "train_rays": args.train_rays, "train_steps": args.train_steps, "dataset_s": t_data,
+                       "train_s": t_train, "train_rays_per_s": args.train_steps * 65536 / t_train,
+                       "final_loss": [float(v) for v in hist[-50:].mean(axis=0)]})
+    del data
+    return nets
 
 
 def angle_between(t1, p1, t2, p2):
@@ -529,25 +541,16 @@ def outlier_causes(test, ref, dist, r_in, r_out, band: float, thr: float, same_t
     err = per_ray_error(test, ref)
     bad = err > thr
     tol_bad = per_ray_error(same_tol, ref) > thr if same_tol is not None else np.zeros(bad.size, bool)
-    causes = {"band": 0, "disk_edge": 0, "different_crossing": 0, "tolerance": 0, "outcome_elsewhere": 0,
-              "other": 0}
     near = lambda r: (np.abs(r / r_in - 1.0) < 1e-3) | (np.abs(r / r_out - 1.0) < 1e-3)  # noqa: E731
     edge = near(np.nan_to_num(test["r_disk"], nan=-1.0)) | near(np.nan_to_num(ref["r_disk"], nan=-1.0))
     both_disk = (test["outcome"] == 2) & (ref["outcome"] == 2)
     apart = both_disk & (np.abs(np.nan_to_num(test["r_disk"]) / np.where(both_disk, ref["r_disk"], 1.0) - 1.0) > 1e-2)
-    for i in np.nonzero(bad)[0]:
-        if dist[i] < band:
-            causes["band"] += 1
-        elif edge[i]:
-            causes["disk_edge"] += 1
-        elif apart[i]:
-            causes["different_crossing"] += 1
-        elif tol_bad[i]:
-            causes["tolerance"] += 1
-        elif test["outcome"][i] != ref["outcome"][i]:
-            causes["outcome_elsewhere"] += 1
-        else:
-            causes["other"] += 1
+    left = bad.copy()
+    causes = {}
+    for name, m in (("band", dist < band), ("disk_edge", edge), ("different_crossing", apart), ("tolerance", tol_bad),
+                    ("outcome_elsewhere", test["outcome"] != ref["outcome"]), ("other", np.ones(bad.size, bool))):
+        causes[name] = int(np.sum(left & m))
+        left &= ~m
     return int(bad.sum()), causes, err
 
 
@@ -619,25 +622,27 @@ def fp64_check(ctx, frames, out, dev, per_frame: float, cap: int, seed: int) -> 
 
 def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses: int) -> dict:
     """Surrogate + integrator fallback against the plain mixed tracer on the orbit sequence
-    (poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 / scale), both timed with CUDA
-    events on the same frames, and both checked against a seeded 1% of each frame's pixels traced in FP64."""
+    (poses at r = 30 M, a = 0.998, theta 85 -> 45 deg, 3840 x 2160 / scale), all timed with CUDA
+    events on the same frames and checked against a seeded 1% of each frame's pixels traced in FP64:
+    networks of hidden width 64 and 256 at the default thresholds (class probability 0.99, band
+    0.05 M), and the speed/error curve over the thresholds and the acceptance modes."""
     import torch
     from black_simulation_gb300 import bhk
     from black_simulation_gb300.surrogate import orbit_frames
     stream = torch.cuda.current_stream()
-    sur, train_info = train_surrogate(ctx, args)
+    nets = train_surrogates(ctx, args)
     frames = orbit_frames(poses, 3840 // scale, 2160 // scale)
     n = sum(f.rays for f in frames)
     opts = bhk.TraceOpts("mixed", rtol=1e-6)
     out_s = bhk.alloc_outputs(n, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def timed(fn):
-        for _ in range(warmup):
+    def timed(fn, n_steps=steps, n_warm=warmup):
+        for _ in range(n_warm):
             fn()
         torch.cuda.synchronize()
         ms, extra = [], []
-        for _ in range(steps):
+        for _ in range(n_steps):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -648,45 +653,74 @@ def orbit_comparison(args, ctx, dev, steps: int, warmup: int, scale: int, poses:
             extra.append(r)
         return float(np.mean(ms)), extra
 
-    with Clocks(dev.index or 0) as clk:
-        ms_s, stats = timed(lambda: sur.render(ctx, frames, opts, out=out_s)[1])
-    sort_launches = 3 if ctx.stats()["sort_buckets"] > 1 else 0
-    ms_infer = float(np.mean([st["infer_ms"] for st in stats]))
-    fb = float(np.mean([st["fallback"] for st in stats]))
     out_t = bhk.alloc_outputs(n, dev)
     ms_t, _ = timed(lambda: ctx.trace_frames(frames, opts, out=out_t))
     # 1% held-out pixels per frame (seeded), traced in FP64 as the yardstick
     R = fp64_reference(ctx, frames, held_out_pixels(frames, 0.01, 1 << 40, args.seed + 1), dev)
-    fbl = np.zeros(n, bool)
-    sur.render(ctx, frames, opts, out=out_s, fallback=True)
-    fbl[sur.fallback_list().cpu().numpy()] = True
     pick = lambda o: {k: o[k][R["index"]].cpu().numpy() for k in KEYS}  # noqa: E731
-    sur_h, tr_h = pick(out_s), pick(out_t)
-    answered = ~fbl[R["held"]]
+    tracer_oc = out_t["outcome"].cpu().numpy()
+
+    def point(w, p_min=0.99, band=0.05, accept="all", n_steps=steps, n_warm=warmup, full=False):
+        sur = nets[w][0]
+        with Clocks(dev.index or 0) as clk:
+            ms, stats = timed(lambda: sur.render(ctx, frames, opts, out=out_s, p_min=p_min, band=band,
+                                                 accept=accept)[1], n_steps, n_warm)
+        fbl = np.zeros(n, bool)
+        fbl[sur.fallback_list().cpu().numpy()] = True
+        h = pick(out_s)
+        res = {"width": w, "p_min": p_min, "band_m": band, "accept": accept, "value": n / (ms * 1e-3),
+               "unit": "rays/s", "ms_per_step": ms, "speedup_vs_plain_tracer": ms_t / ms,
+               "fallback_fraction": float(np.mean([st["fallback"] for st in stats])) / n,
+               "inference_ms": float(np.mean([st["infer_ms"] for st in stats])),
+               "fallback_trace_ms": float(np.mean([st["trace_ms"] for st in stats])),
+               "outcome_agreement_with_tracer": float(np.mean(out_s["outcome"].cpu().numpy() == tracer_oc))}
+        j = judge(h, R)
+        if full:
+            res["errors_vs_fp64"] = j
+            res["errors_vs_fp64_network_answered_only"] = judge(h, R, mask=~fbl[R["held"]])
+            res["clocks"] = clk.summary()
+        else:
+            res["errors_vs_fp64"] = {"outcome_agreement": j["raw"]["outcome_agreement"],
+                                     "r_disk_rel_median": j["raw"].get("r_disk_rel", {}).get("median"),
+                                     "g_rel_median": j["raw"].get("g_rel", {}).get("median"),
+                                     "above_1e-4": j["above_0.0001"]["count"]}
+        return res
+
+    w64 = point(64, full=True)
+    w256 = point(256, full=True)
+    curve = []
+    for w in (64, 256):
+        for p_min in (0.9, 0.99, 0.999):
+            for band in (0.02, 0.05):
+                curve.append(point(w, p_min, band, n_steps=2, n_warm=1))
+    curve.append(point(256, accept="captured", n_steps=2, n_warm=1))
     peak, src = measured_peak("bf16_tflops", 1900.0)
-    achieved = n * 2 * MAC_FWD / (ms_infer * 1e-3) / 1e12
-    sur.close()
+    infer = {}
+    for w, p_ in ((64, w64), (256, w256)):
+        fl = 2 * mac_fwd(w)
+        achieved = n * fl / (p_["inference_ms"] * 1e-3) / 1e12
+        infer[str(w)] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": src,
+                         "kernel": f"infer_kernel<{w}> (fused tcgen05 network)", "flops_per_ray": fl}
+    for s_, _ in nets.values():
+        s_.close()
+    best = max([w64, w256], key=lambda r: r["value"])
     return {
         "workload": f"{poses} orbit poses r=30M a=0.998 theta 85->45deg, {3840 // scale}x{2160 // scale}, "
                     "half-width 1.2x shadow radius, disk ISCO-30M; surrogate + mixed-precision fallback "
-                    "(p_min 0.99, band 0.05M)",
-        "rays": n, "steps": steps, "warmup": warmup, "training": train_info,
-        "surrogate_path": {"value": n / (ms_s * 1e-3), "unit": "rays/s", "ms_per_step": ms_s},
-        "plain_tracer": {"value": n / (ms_t * 1e-3), "unit": "rays/s", "ms_per_step": ms_t},
-        "speedup_vs_plain_tracer": ms_t / ms_s,
-        "fallback_fraction": fb / n,
-        "inference": {"value": n / (ms_infer * 1e-3), "ms": ms_infer},
-        "errors_vs_fp64": {"surrogate_path": judge(sur_h, R), "network_answered_only": judge(sur_h, R, mask=answered),
-                           "plain_tracer": judge(tr_h, R), "sample": "1% of each frame's pixels (seeded)",
-                           "fp64_check_s": R["seconds"]},
-        "meets_1e-4_bound": False,
-        "inference_roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                               "frac": achieved / peak, "traffic": None, "peak_source": src,
-                               "kernel": "infer_kernel (fused tcgen05 network)", "flops_per_ray": 2 * MAC_FWD},
+                    "(p_min 0.99, band 0.05M unless stated)",
+        "rays": n, "steps": steps, "warmup": warmup,
+        "training": {str(w): info for w, (_, info) in nets.items()},
+        "plain_tracer": {"value": n / (ms_t * 1e-3), "unit": "rays/s", "ms_per_step": ms_t,
+                         "errors_vs_fp64": judge(pick(out_t), R)},
+        "surrogate_path": {k: best[k] for k in ("width", "value", "unit", "ms_per_step")},
+        "speedup_vs_plain_tracer": best["speedup_vs_plain_tracer"],
+        "width64": w64, "width256": w256, "speed_error_curve": curve,
+        "meets_1e-4_bound": False, "fp64_check_s": R["seconds"], "sample": "1% of each frame's pixels (seeded)",
+        "inference_roofline": infer,
         # per render: curve table, bias halving, inference; the fallback list's frame set-up, launch,
-        # [sort], trace, rescue; the scatter
-        "gpu_launches": steps * (8 + sort_launches),
-        "clocks": clk.summary(),
+        # trace, rescue; the scatter
+        "gpu_launches_per_render": 8,
     }
 
 
@@ -709,9 +743,9 @@ def run_orbit(args):
         "config": {"workload": cmp_["workload"], "rays": cmp_["rays"], "l2": "flushed (256 MB write) between steps",
                    "training": cmp_["training"]},
         "plain_tracer": cmp_["plain_tracer"], "speedup_vs_plain_tracer": cmp_["speedup_vs_plain_tracer"],
-        "fallback_fraction": cmp_["fallback_fraction"], "inference": cmp_["inference"],
-        "errors_vs_fp64": cmp_["errors_vs_fp64"], "meets_1e-4_bound": False, "roofline": cmp_["inference_roofline"],
-        "gpu_launches": cmp_["gpu_launches"], "clocks": cmp_["clocks"],
+        "width64": cmp_["width64"], "width256": cmp_["width256"], "speed_error_curve": cmp_["speed_error_curve"],
+        "meets_1e-4_bound": False, "roofline": cmp_["inference_roofline"][str(cmp_["surrogate_path"]["width"])],
+        "gpu_launches": cmp_["gpu_launches_per_render"] * args.steps, "clocks": cmp_["width64"]["clocks"],
     }
     ctx.close()
     print(json.dumps(line))

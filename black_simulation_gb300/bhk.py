@@ -181,6 +181,9 @@ def lib() -> C.CDLL:
                                               C.POINTER(RaysOutC), vp]),
         "bhk_surrogate_num_params": (i64, []),
         "bhk_surrogate_create": (C.c_int, [C.c_int, C.c_uint64, C.c_int32, C.POINTER(vp)]),
+        "bhk_surrogate_create_width": (C.c_int, [C.c_int, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(vp)]),
+        "bhk_surrogate_width": (C.c_int32, [vp]),
+        "bhk_surrogate_param_count": (i64, [vp]),
         "bhk_surrogate_destroy": (C.c_int, [vp]),
         "bhk_surrogate_params": (C.c_int, [vp, vp, C.c_int32]),
         "bhk_surrogate_fourier": (C.c_int, [vp, vp, C.c_int32]),

@@ -490,20 +490,24 @@ extern "C" bhk_status bhk_tc_gemm(const void* A, const void* B, float* C, int32_
 namespace bhk {
 namespace sur {
 
-constexpr int kIn = 5, kFreq = 32, kFeat = 64, kHid = 256, kOut = 8, kOutPad = 16, kLayers = 5;
-__host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kFeat : kHid; }
-__host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOutPad : kHid; }
+// The hidden width (kHidden, the four SiLU layers) is a property of each network: 256 (the default) or
+// 64 (a network 12.5 x cheaper to evaluate, for the speed/accuracy trade of the learned path).
+constexpr int kIn = 5, kFreq = 32, kFeat = 64, kOut = 8, kOutPad = 16, kLayers = 5;
+constexpr int kHidDefault = 256;
+__host__ __device__ constexpr bool width_ok(int hid) { return hid == 64 || hid == 256; }
+__host__ __device__ constexpr int fan_in(int l, int hid) { return l == 0 ? kFeat : hid; }
+__host__ __device__ constexpr int fan_out(int l, int hid) { return l == kLayers - 1 ? kOutPad : hid; }
 
 // Flat FP32 parameter vector: W_l (fan_out x fan_in, row-major) then b_l, for l = 1..5.
 struct ParamLayout {
     size_t w[kLayers], b[kLayers], total;
-    ParamLayout() {
+    explicit ParamLayout(int hid = kHidDefault) {
         size_t o = 0;
         for (int l = 0; l < kLayers; ++l) {
             w[l] = o;
-            o += static_cast<size_t>(fan_out(l)) * fan_in(l);
+            o += static_cast<size_t>(fan_out(l, hid)) * fan_in(l, hid);
             b[l] = o;
-            o += fan_out(l);
+            o += fan_out(l, hid);
         }
         total = o;
     }
@@ -629,6 +633,7 @@ struct AdamArgs {
     bf16* w_t[kLayers];
     size_t wofs[kLayers];
     size_t total;
+    int hid;                        // hidden width of the network
     float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
 };
 
@@ -643,13 +648,14 @@ __global__ void adam_kernel(AdamArgs a) {
         const float w = a.p[i] - a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
         a.p[i] = w;
         for (int l = 0; l < kLayers; ++l) {
-            const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+            const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
+            const size_t n = static_cast<size_t>(fo) * fi;
             if (i >= a.wofs[l] && i < a.wofs[l] + n) {
                 const size_t j = i - a.wofs[l];
-                const int o = static_cast<int>(j / fan_in(l)), k = static_cast<int>(j % fan_in(l));
+                const int o = static_cast<int>(j / fi), k = static_cast<int>(j % fi);
                 const bf16 wb = __float2bfloat16_rn(w);
                 a.w_rm[l][j] = wb;
-                a.w_t[l][static_cast<size_t>(k) * fan_out(l) + o] = wb;
+                a.w_t[l][static_cast<size_t>(k) * fo + o] = wb;
             }
         }
     }
@@ -660,13 +666,14 @@ __global__ void refresh_bf16_kernel(AdamArgs a) {
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
          i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         for (int l = 0; l < kLayers; ++l) {
-            const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+            const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
+            const size_t n = static_cast<size_t>(fo) * fi;
             if (i >= a.wofs[l] && i < a.wofs[l] + n) {
                 const size_t j = i - a.wofs[l];
-                const int o = static_cast<int>(j / fan_in(l)), k = static_cast<int>(j % fan_in(l));
+                const int o = static_cast<int>(j / fi), k = static_cast<int>(j % fi);
                 const bf16 wb = __float2bfloat16_rn(a.p[i]);
                 a.w_rm[l][j] = wb;
-                a.w_t[l][static_cast<size_t>(k) * fan_out(l) + o] = wb;
+                a.w_t[l][static_cast<size_t>(k) * fo + o] = wb;
             }
         }
     }
@@ -680,6 +687,7 @@ __global__ void refresh_bf16_kernel(AdamArgs a) {
 struct bhk_surrogate {
     int device = 0;
     int cap = 0;  // batch capacity (rows of every activation buffer)
+    int hid = bhk::sur::kHidDefault;  // hidden width
     bhk::sur::ParamLayout L;
     float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     bhk::sur::bf16* w_rm[bhk::sur::kLayers] = {};
@@ -730,6 +738,7 @@ AdamArgs adam_args(bhk_surrogate* s) {
         a.wofs[l] = s->L.w[l];
     }
     a.total = s->L.total;
+    a.hid = s->hid;
     return a;
 }
 
@@ -743,15 +752,17 @@ struct Maps {
 bool build_maps(bhk_surrogate* s, int n, bool transposed, Maps* M) {
     bool ok = make_tmap(&M->F_rm, s->F_rm, n, kFeat, kTileM) && make_tmap(&M->dy_rm, s->dy_rm, n, kOutPad, kTileM);
     for (int l = 0; l < kLayers && ok; ++l) {
-        ok = make_tmap(&M->W[l], s->w_rm[l], fan_out(l), fan_in(l), box_rows_for(fan_out(l))) &&
-             make_tmap(&M->Wt[l], s->w_t[l], fan_in(l), fan_out(l), box_rows_for(fan_in(l)));
+        const int fi = fan_in(l, s->hid), fo = fan_out(l, s->hid);
+        ok = make_tmap(&M->W[l], s->w_rm[l], fo, fi, box_rows_for(fo)) &&
+             make_tmap(&M->Wt[l], s->w_t[l], fi, fo, box_rows_for(fi));
     }
-    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_rm[i], s->a_rm[i], n, kHid, kTileM);
-    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, kHid, kTileM);
+    const int H = s->hid;
+    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_rm[i], s->a_rm[i], n, H, kTileM);
+    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, H, kTileM);
     if (!transposed) return ok;
     ok = ok && make_tmap(&M->F_t, s->F_t, kFeat, s->cap, 64) && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM);
-    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_t[i], s->a_t[i], kHid, s->cap, 256);
-    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_t[i], s->dz_t[i], kHid, s->cap, kTileM);
+    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_t[i], s->a_t[i], H, s->cap, box_rows_for(H));
+    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_t[i], s->dz_t[i], H, s->cap, kTileM);
     return ok;
 }
 
@@ -765,23 +776,24 @@ EpiArgs epi(int M, int N) {
 // Forward pass of n rows (features already in F): z, activations in both layouts, head into Y.
 cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, bool keep_t, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
+    const int H = s->hid;
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
-        EpiArgs ea = epi(n, kHid);
+        EpiArgs ea = epi(n, H);
         ea.bias = s->p + s->L.b[l];
         ea.rm = s->a_rm[l];
-        ea.ld_rm = kHid;
+        ea.ld_rm = H;
         ea.t = keep_t ? s->a_t[l] : nullptr;
         ea.ld_t = s->cap;
         ea.z = s->z[l];
         const CUtensorMap& A = l == 0 ? M.F_rm : M.a_rm[l - 1];
-        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, kHid, fan_in(l), 1, s->err, st);
+        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st);
     }
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, kOutPad);
         ea.bias = s->p + s->L.b[4];
         ea.f32 = s->Y;
         ea.ld_f32 = kOutPad;
-        e = launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, kHid, 1, s->err, st);
+        e = launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st);
     }
     return e;
 }
@@ -811,32 +823,33 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     loss_kernel<<<(n + 255) / 256, 256, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
                                                  s->loss, n, 1.0f / n, s->w);
     const int splits = split_for(n);
+    const int H = s->hid;
     // Head: dW5 = dY^T A4, then dA4 = dY W5 -> dZ4.
-    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, kHid, n, splits, s->g + s->L.w[4], st);
+    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, H, n, splits, s->g + s->L.w[4], st);
     if (e == cudaSuccess) {
-        EpiArgs ea = epi(n, kHid);
+        EpiArgs ea = epi(n, H);
         ea.rm = s->dz_rm[0];
-        ea.ld_rm = kHid;
+        ea.ld_rm = H;
         ea.t = s->dz_t[0];
         ea.ld_t = s->cap;
         ea.z = s->z[3];
         ea.colsum = s->g + s->L.b[3];
-        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, kHid, kOutPad, 1, s->err, st);
+        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st);
     }
     // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
         const CUtensorMap& Bop = l == 0 ? M.F_t : M.a_t[l - 1];
-        e = weight_grad(s, M.dz_t[cur], Bop, kHid, fan_in(l), n, splits, s->g + s->L.w[l], st);
+        e = weight_grad(s, M.dz_t[cur], Bop, H, fan_in(l, H), n, splits, s->g + s->L.w[l], st);
         if (e != cudaSuccess || l == 0) break;
-        EpiArgs ex = epi(n, kHid);
+        EpiArgs ex = epi(n, H);
         ex.rm = s->dz_rm[1 - cur];
-        ex.ld_rm = kHid;
+        ex.ld_rm = H;
         ex.t = s->dz_t[1 - cur];
         ex.ld_t = s->cap;
         ex.z = s->z[l - 1];
         ex.colsum = s->g + s->L.b[l - 1];
-        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, kHid, kHid, 1, s->err, st);
+        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st);
         cur = 1 - cur;
     }
     return e;
@@ -864,10 +877,25 @@ extern "C" {
 
 int64_t bhk_surrogate_num_params(void) { return static_cast<int64_t>(bhk::sur::ParamLayout().total); }
 
+int64_t bhk_surrogate_param_count(const bhk_surrogate* s) {
+    return s ? static_cast<int64_t>(s->L.total) : 0;
+}
+
+int32_t bhk_surrogate_width(const bhk_surrogate* s) { return s ? s->hid : 0; }
+
 bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bhk_surrogate** out) {
+    return bhk_surrogate_create_width(device, seed, max_batch, bhk::sur::kHidDefault, out);
+}
+
+bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_batch, int32_t width,
+                                      bhk_surrogate** out) {
     using namespace bhk::sur;
     if (!out || max_batch <= 0 || max_batch % kTileM) {
         set_last_error("bhk_surrogate_create: max_batch must be a positive multiple of 128");
+        return BHK_EINVAL;
+    }
+    if (!width_ok(width)) {
+        set_last_error("bhk_surrogate_create_width: the hidden width must be 64 or 256");
         return BHK_EINVAL;
     }
     *out = nullptr;
@@ -882,22 +910,25 @@ bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bh
     auto* s = new bhk_surrogate();
     s->device = device;
     s->cap = max_batch;
+    s->hid = width;
+    s->L = ParamLayout(width);
+    const int H = width;
     const size_t P = s->L.total, B = static_cast<size_t>(max_batch);
     bool ok = dalloc(s, &s->p, P) && dalloc(s, &s->g, P) && dalloc(s, &s->m, P) && dalloc(s, &s->v, P) &&
               dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) && dalloc(s, &s->F_t, B * kFeat) &&
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
               dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
-              dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * kHid) &&
-              dalloc(s, &s->ws, static_cast<size_t>(96) * kHid * kHid) &&
+              dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * H) &&
+              dalloc(s, &s->ws, static_cast<size_t>(96) * H * std::max(H, kFeat)) &&
               cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreate(&s->ev[i]) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
-        const size_t n = static_cast<size_t>(fan_out(l)) * fan_in(l);
+        const size_t n = static_cast<size_t>(fan_out(l, H)) * fan_in(l, H);
         ok = dalloc(s, &s->w_rm[l], n) && dalloc(s, &s->w_t[l], n);
     }
     for (int i = 0; i < 4 && ok; ++i)
-        ok = dalloc(s, &s->z[i], B * kHid) && dalloc(s, &s->a_rm[i], B * kHid) && dalloc(s, &s->a_t[i], B * kHid);
-    for (int i = 0; i < 2 && ok; ++i) ok = dalloc(s, &s->dz_rm[i], B * kHid) && dalloc(s, &s->dz_t[i], B * kHid);
+        ok = dalloc(s, &s->z[i], B * H) && dalloc(s, &s->a_rm[i], B * H) && dalloc(s, &s->a_t[i], B * H);
+    for (int i = 0; i < 2 && ok; ++i) ok = dalloc(s, &s->dz_rm[i], B * H) && dalloc(s, &s->dz_t[i], B * H);
     if (!ok) {
         bhk_surrogate_destroy(s);
         set_last_error("bhk_surrogate_create: device allocation failed");
@@ -915,10 +946,11 @@ bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bh
     };
     auto uni = [&]() { return (next() >> 11) * (1.0 / 9007199254740992.0); };
     for (int l = 0; l < kLayers; ++l) {
-        const double lim = std::sqrt(6.0 / fan_in(l)) * (l == kLayers - 1 ? 0.1 : 1.0);
-        for (int o = 0; o < fan_out(l); ++o)
-            for (int k = 0; k < fan_in(l); ++k)
-                hp[s->L.w[l] + static_cast<size_t>(o) * fan_in(l) + k] =
+        const int fi = fan_in(l, H), fo = fan_out(l, H);
+        const double lim = std::sqrt(6.0 / fi) * (l == kLayers - 1 ? 0.1 : 1.0);
+        for (int o = 0; o < fo; ++o)
+            for (int k = 0; k < fi; ++k)
+                hp[s->L.w[l] + static_cast<size_t>(o) * fi + k] =
                     (l == kLayers - 1 && o >= kOut) ? 0.0f : static_cast<float>((2.0 * uni() - 1.0) * lim);
     }
     // Fourier matrix: row j = f_j d_j with d_j a random unit direction and f_j growing geometrically
@@ -1245,19 +1277,25 @@ __global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc)
     }
 }
 
-constexpr int kInfStages = 3;               // weight ring: 3 x 32 KB in flight
+constexpr int kInfStages = 3;               // weight ring: 3 chunks in flight
 constexpr int kTileRays = 128;
 constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 of activations
-constexpr int kActBytes = 4 * kChunkBytes; // one tile's 256-wide activations
-constexpr int kWChunkBytes = 256 * 64 * 2; // 32 KB: all 256 output rows x 64 K of a hidden layer's weights
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
 constexpr int kEpiWarps = 16;              // per tile slot: 4 TMEM lane quadrants x 2 column halves
 constexpr int kInfThreads = 64 + 32 * kEpiWarps;
 constexpr int kInfMisc = 128 + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
-constexpr int kInfSmem = 2 * kActBytes + kInfStages * kWChunkBytes + 1024 + kInfMisc;
+// Per hidden width HID: one tile's activations (HID / 64 chunks of 64 columns), one weight chunk (all
+// HID output rows x 64 K of a hidden layer), the shared memory of the kernel.
+template <int HID>
+__host__ __device__ constexpr int act_bytes() { return (HID / 64) * kChunkBytes; }
+template <int HID>
+__host__ __device__ constexpr int wchunk_bytes() { return HID * 64 * 2; }
+template <int HID>
+__host__ __device__ constexpr int inf_smem() { return 2 * act_bytes<HID>() + kInfStages * wchunk_bytes<HID>() + 1024 + kInfMisc; }
 
-// Weight chunks per layer: 64-wide K slices of all output rows (N = 256 per MMA; the head N = 16).
-__host__ __device__ constexpr int layer_chunks(int l) { return l == 0 ? 1 : 4; }
+// Weight chunks per layer: 64-wide K slices of all output rows (N = HID per MMA; the head N = 16).
+template <int HID>
+__host__ __device__ constexpr int layer_chunks(int l) { return l == 0 ? 1 : HID / 64; }
 
 struct InferArgs {
     const SurFrame* frames;
@@ -1265,7 +1303,7 @@ struct InferArgs {
     long long n;
     const float* Bm;
     const float* bias[kLayers];
-    const float* half_bias;  // [4][256]: the hidden layers' biases halved
+    const float* half_bias;  // [4][HID]: the hidden layers' biases halved
     uint8_t* outcome;
     double *r_disk, *phi_disk, *g, *theta_inf, *phi_inf;
     int32_t *steps, *rejected;
@@ -1311,12 +1349,15 @@ __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb,
 // slot owns 256 TMEM columns and a 64 KB activation buffer; the weight ring is shared and filled
 // in the MMA's order (pair of tiles, layer, slot, chunk). Every MMA is 128 x 256 x 16, so each
 // activation slice is read from shared memory once per layer. CTA b takes tiles b, b + grid, ...
+template <int HID>
 __global__ void __launch_bounds__(kInfThreads, 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
              const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
              const __grid_constant__ CUtensorMap tW4, InferArgs ia) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr int kActBytes = act_bytes<HID>(), kWChunkBytes = wchunk_bytes<HID>();
+    constexpr uint32_t kTmemCols = 2 * HID;  // two tile slots of HID accumulator columns
     uint8_t* ring = base + 2 * kActBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kWChunkBytes);
     uint64_t* empty = full + kInfStages;
@@ -1351,7 +1392,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         tc::prefetch_tmap(&tW3);
         tc::prefetch_tmap(&tW4);
     }
-    if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
+    if (warp == 1) tc::tmem_alloc(tmem_slot, kTmemCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -1369,7 +1410,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                 for (int l = 0; l < kLayers && ok; ++l)
                     for (int sl = 0; sl < 2 && ok; ++sl) {
                         if (2 * p + sl >= n_my) continue;
-                        for (int c = 0; c < layer_chunks(l); ++c, ++q) {
+                        for (int c = 0; c < layer_chunks<HID>(l); ++c, ++q) {
                             if (*abort_flag) { ok = false; break; }
                             const int st = static_cast<int>(q % kInfStages);
                             const long long j = q / kInfStages;
@@ -1390,7 +1431,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---- MMA issuer
-            constexpr uint32_t kId256 = tc::idesc_bf16(128, 256), kId16 = tc::idesc_bf16(128, 16);
+            constexpr uint32_t kIdHid = tc::idesc_bf16(128, HID), kId16 = tc::idesc_bf16(128, 16);
             long long q = 0;
             uint32_t act_n[2] = {0u, 0u};
             bool ok = true;
@@ -1406,7 +1447,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                         ++act_n[sl];
                         tc::fence_after_sync();
                         uint8_t* act = base + sl * kActBytes;
-                        for (int c = 0; c < layer_chunks(l); ++c, ++q) {
+                        for (int c = 0; c < layer_chunks<HID>(l); ++c, ++q) {
                             const int st = static_cast<int>(q % kInfStages);
                             if (!tc::mbar_wait(&full[st], static_cast<uint32_t>((q / kInfStages) & 1))) {
                                 give_up();
@@ -1417,10 +1458,10 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                             const int kc = c;
                             const uint64_t ad = tc::smem_desc_sw128(act + kc * kChunkBytes);
                             const uint64_t bd = tc::smem_desc_sw128(ring + st * kWChunkBytes);
-                            const uint32_t d = tmem + static_cast<uint32_t>(256 * sl);
+                            const uint32_t d = tmem + static_cast<uint32_t>(HID * sl);
 #pragma unroll
                             for (int kk = 0; kk < 4; ++kk)
-                                tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kId256 : kId16, (kc | kk) ? 1u : 0u);
+                                tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kIdHid : kId16, (kc | kk) ? 1u : 0u);
                             tc::mma_commit(&empty[st]);
                         }
                         if (ok) tc::mma_commit(&acc_full[sl]);
@@ -1435,7 +1476,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         const int half = (ew >> 2) & 1;    // columns 128 half .. 128 half + 127 (and 16 of the 32 frequencies)
         const int q4 = warp & 3;           // TMEM lane quadrant this warp may access
         const int row = 32 * q4 + lane;
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16) + 256u * slot;
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16) + static_cast<uint32_t>(HID) * slot;
         uint8_t* act = base + slot * kActBytes;
         uint32_t acc_n = 0;
         // Every exit decision is taken by the whole warp (the TMEM loads and the list append are
@@ -1497,21 +1538,22 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                 }
                 ++acc_n;
                 tc::fence_after_sync();
-                const float* hb = ia.half_bias + l * kHid + 128 * half;
-                const uint32_t cb = trow + 128u * half;
+                constexpr int kHalf = HID / 2, kGroups = kHalf / 32;  // this warp's columns, in groups of 32
+                const float* hb = ia.half_bias + l * HID + kHalf * half;
+                const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
                 uint32_t ra[32], rb[32];
                 tc::tmem_ld32_issue(cb, ra);
                 tc::tmem_wait32(ra);
 #pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
+                for (int jj = 0; jj < kGroups; ++jj) {
                     uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
                     uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
-                    if (jj + 1 < 4) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
+                    if (jj + 1 < kGroups) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
                     uint32_t w[16];
                     silu32(cur, hb + 32 * jj, w);
-                    store_act16(act, row, 128 * half + 32 * jj, w);
-                    store_act16(act, row, 128 * half + 32 * jj + 16, w + 8);
-                    if (jj + 1 < 4) tc::tmem_wait32(nxt);
+                    store_act16(act, row, kHalf * half + 32 * jj, w);
+                    store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
+                    if (jj + 1 < kGroups) tc::tmem_wait32(nxt);
                 }
                 tc::fence_proxy_async();
                 tc::fence_before_sync();
@@ -1585,12 +1627,12 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 1) tc::tmem_dealloc(tmem, 512);
+    if (warp == 1) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 __global__ void halve_bias_kernel(const float* b0, const float* b1, const float* b2, const float* b3, float* out) {
     const float* b = blockIdx.x == 0 ? b0 : blockIdx.x == 1 ? b1 : blockIdx.x == 2 ? b2 : b3;
-    out[blockIdx.x * kHid + threadIdx.x] = 0.5f * b[threadIdx.x];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = 0.5f * b[threadIdx.x];  // blockDim.x = the hidden width
 }
 
 // Copies compact fallback results (entry i = pixel list[i]) into the full-image outputs.
@@ -1700,26 +1742,37 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
         e = cudaMemcpyAsync(ddesc, frames, sizeof(bhk_frame_desc) * nframes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail_cuda(e, "frame upload");
     curve_table_kernel<<<nframes, 256, 0, st>>>(dframes, ddesc);
+    const int H = s->hid;
+    auto* kern = H == 64 ? &infer_kernel<64> : &infer_kernel<256>;
+    const int smem = H == 64 ? inf_smem<64>() : inf_smem<256>();
     static std::once_flag attr;
-    std::call_once(attr, [] { cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInfSmem); });
-    int sms = 0;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(infer_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, inf_smem<64>());
+        cudaFuncSetAttribute(infer_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, inf_smem<256>());
+    });
+    int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
-    // One CTA per SM (it holds all 512 TMEM columns); the grid is the number of CTAs resident at once
-    // (the static tile schedule must not need a second wave).
-    const int resident = sms;
+    // The grid is the number of CTAs resident at once (the static tile schedule must not need a second
+    // wave): one per SM at width 256 (its shared memory and all 512 TMEM columns), as many as fit at 64
+    // (2 x 64 TMEM columns each).
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kInfThreads, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int resident = sms * std::min(per_sm, 4);
     Maps M;
     CUtensorMap w4;
-    const uint32_t slice = 256u;
-    if (!make_tmap(&M.W[0], s->w_rm[0], kHid, kFeat, slice) || !make_tmap(&M.W[1], s->w_rm[1], kHid, kHid, slice) ||
-        !make_tmap(&M.W[2], s->w_rm[2], kHid, kHid, slice) || !make_tmap(&M.W[3], s->w_rm[3], kHid, kHid, slice) ||
-        !make_tmap(&w4, s->w_rm[4], kOutPad, kHid, 16)) {
+    const uint32_t slice = static_cast<uint32_t>(H);
+    if (!make_tmap(&M.W[0], s->w_rm[0], H, kFeat, slice) || !make_tmap(&M.W[1], s->w_rm[1], H, H, slice) ||
+        !make_tmap(&M.W[2], s->w_rm[2], H, H, slice) || !make_tmap(&M.W[3], s->w_rm[3], H, H, slice) ||
+        !make_tmap(&w4, s->w_rm[4], kOutPad, H, 16)) {
         set_last_error("bhk_surrogate_render: tensor map creation failed");
         return BHK_ECUDA;
     }
     const long long ntiles = (total + kTileRays - 1) / kTileRays;
     const int grid = static_cast<int>(std::min<long long>(ntiles, resident));
-    halve_bias_kernel<<<4, 256, 0, st>>>(s->p + s->L.b[0], s->p + s->L.b[1], s->p + s->L.b[2], s->p + s->L.b[3],
-                                         s->half_bias);
+    halve_bias_kernel<<<4, H, 0, st>>>(s->p + s->L.b[0], s->p + s->L.b[1], s->p + s->L.b[2], s->p + s->L.b[3],
+                                       s->half_bias);
     InferArgs ia{};
     ia.accept = ro.accept;
     ia.half_bias = s->half_bias;
@@ -1745,7 +1798,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
     if (e != cudaSuccess) return fail_cuda(e, "launch set-up");
-    infer_kernel<<<grid, kInfThreads, kInfSmem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
+    kern<<<grid, kInfThreads, smem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->n_list_host, s->n_list, 8, cudaMemcpyDeviceToHost, st);

@@ -20,23 +20,31 @@ import numpy as np
 from . import bhk
 
 N_IN, N_OUT = 5, 8
-LAYERS = ((256, 64), (256, 256), (256, 256), (256, 256), (16, 256))  # (fan_out, fan_in), head padded to 16
+WIDTHS = (64, 256)  # hidden widths the kernels are built for (bhk_surrogate_create_width)
+
+
+def layers(width: int = 256):
+    """(fan_out, fan_in) of the five layers for a hidden width; the head is padded to 16 outputs."""
+    return ((width, 64), (width, width), (width, width), (width, width), (16, width))
+
+
+LAYERS = layers(256)
 R_DISK_SCALE = 30.0
 ACCEPT = {"all": 0, "captured": 1}  # bhk_render_opts.accept (BHK_ACCEPT_ALL, BHK_ACCEPT_CAPTURED)
 
 
-def layer_offsets():
+def layer_offsets(width: int = 256):
     """[(w_offset, b_offset, fan_out, fan_in)] into the flat FP32 parameter vector."""
     o, res = 0, []
-    for fo, fi in LAYERS:
+    for fo, fi in layers(width):
         res.append((o, o + fo * fi, fo, fi))
         o += fo * fi + fo
     return res
 
 
-def unpack(p: np.ndarray):
+def unpack(p: np.ndarray, width: int = 256):
     """Views (W, b) per layer of a flat parameter vector."""
-    return [(p[w:w + fo * fi].reshape(fo, fi), p[b:b + fo]) for w, b, fo, fi in layer_offsets()]
+    return [(p[w:w + fo * fi].reshape(fo, fi), p[b:b + fo]) for w, b, fo, fi in layer_offsets(width)]
 
 
 def targets_from_rays(out: dict):
@@ -62,11 +70,14 @@ def targets_from_rays(out: dict):
 class Surrogate:
     """A bhk_surrogate: FP32 master parameters, Adam state and BF16 weight copies on one device."""
 
-    def __init__(self, device: int = 0, seed: int = 1, max_batch: int = 65536):
+    def __init__(self, device: int = 0, seed: int = 1, max_batch: int = 65536, width: int = 256):
+        if width not in WIDTHS:
+            raise ValueError(f"hidden width must be one of {WIDTHS}")
         self._h = C.c_void_p()
-        bhk.check(bhk.lib().bhk_surrogate_create(device, seed, max_batch, C.byref(self._h)))
+        bhk.check(bhk.lib().bhk_surrogate_create_width(device, seed, max_batch, width, C.byref(self._h)))
         self.device = device
         self.max_batch = max_batch
+        self.width = width
 
     def close(self):
         if self._h:
@@ -85,9 +96,8 @@ class Surrogate:
         except Exception:
             pass
 
-    @staticmethod
-    def num_params() -> int:
-        return int(bhk.lib().bhk_surrogate_num_params())
+    def num_params(self) -> int:
+        return int(bhk.lib().bhk_surrogate_param_count(self._h))
 
     def params(self) -> np.ndarray:
         p = np.empty(self.num_params(), dtype=np.float32)

@@ -292,13 +292,20 @@ bhk_status bhk_tc_gemm(const void* A, const void* B, float* C, int32_t M, int32_
  * Adam state). Inputs are FP32 [n x 5] rows in device memory; class labels are 1/2/3 (the
  * bhk_ray_outcome values), targets FP32 [n x 8] rows in the output convention above. */
 typedef struct bhk_surrogate bhk_surrogate;
-int64_t bhk_surrogate_num_params(void);
-/* max_batch: rows of every activation buffer (a multiple of 128). Seeded initialisation. */
+int64_t bhk_surrogate_num_params(void);   /* of the default network (hidden width 256) */
+/* max_batch: rows of every activation buffer (a multiple of 128). Seeded initialisation. Hidden
+ * width 256. */
 bhk_status bhk_surrogate_create(int device, uint64_t seed, int32_t max_batch, bhk_surrogate** out);
+/* The same network with hidden width 64 or 256 (every other size and layer is unchanged): width 64
+ * costs 34,816 FLOPs per ray to evaluate against 434,176, for a coarser fit. */
+bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_batch, int32_t width,
+                                      bhk_surrogate** out);
+int32_t bhk_surrogate_width(const bhk_surrogate* s);
+int64_t bhk_surrogate_param_count(const bhk_surrogate* s);  /* the length of its parameter vector */
 bhk_status bhk_surrogate_destroy(bhk_surrogate* s);
 /* Copies the FP32 parameter vector out (set = 0) or in (set != 0); host memory. Layout: for each
- * layer W (fan_out x fan_in, row-major) then b; fan (64->256, 256->256 x 3, 256->16 with the head's
- * rows 8..15 padding that stays zero). */
+ * layer W (fan_out x fan_in, row-major) then b; fan (64->H, H->H x 3, H->16 with the head's rows 8..15
+ * padding that stays zero), H the hidden width. */
 bhk_status bhk_surrogate_params(bhk_surrogate* s, float* host, int32_t set);
 /* The Fourier matrix B (32 x 5, host) of the features [sin, cos](2 pi B u): read (set = 0) or
  * replaced (set != 0). It is not trained; the default is seeded (random directions, frequencies

@@ -3,7 +3,8 @@
 This is the oracle the tcgen05 training kernels' gradients are checked against (forward, loss and
 backward in float64 numpy). The reference has no learned model, so the network's definition is the
 library's own (black_simulation_gb300/csrc/bhk_surrogate.cu): inputs normalised to [-1, 1]^5,
-Fourier features [sin, cos](2 pi B u), 4 x (256, SiLU), a head of 8 outputs (padded to 16), loss =
+Fourier features [sin, cos](2 pi B u), 4 x (H, SiLU) with H = 256 or 64, a head of 8 outputs (padded
+to 16), loss =
 cross-entropy over 3 logits + squared errors of r_disk / 30 and ln g (disk rays) and of the escape
 unit vector (escaped rays), batch means.
 
@@ -17,13 +18,28 @@ from __future__ import annotations
 import numpy as np
 
 N_IN, N_FREQ, N_FEAT, N_HID, N_OUT, N_OUT_PAD = 5, 32, 64, 256, 8, 16
-LAYERS = ((256, 64), (256, 256), (256, 256), (256, 256), (16, 256))
 IMAGE_SCALE = 12.0
+
+
+def layers(width=N_HID):
+    """(fan_out, fan_in) per layer for hidden width `width`."""
+    return ((width, N_FEAT), (width, width), (width, width), (width, width), (N_OUT_PAD, width))
+
+
+LAYERS = layers()
+
+
+def width_of(p):
+    """The hidden width whose parameter count is the length of p."""
+    for w in (64, 256):
+        if sum(fo * fi + fo for fo, fi in layers(w)) == len(p):
+            return w
+    raise ValueError("parameter vector matches no hidden width")
 
 
 def unpack(p):
     res, o = [], 0
-    for fo, fi in LAYERS:
+    for fo, fi in layers(width_of(p)):
         W = p[o:o + fo * fi].reshape(fo, fi)
         o += fo * fi
         b = p[o:o + fo]
@@ -32,8 +48,8 @@ def unpack(p):
     return res
 
 
-def num_params():
-    return sum(fo * fi + fo for fo, fi in LAYERS)
+def num_params(width=N_HID):
+    return sum(fo * fi + fo for fo, fi in layers(width))
 
 
 def bf16(x):

@@ -74,6 +74,45 @@ def test_gradients_match_cpu_fp64_network(sur, n):
     assert _rel(g, g64) < 5e-2
 
 
+@pytest.fixture(scope="module")
+def sur64(cuda):
+    from black_simulation_gb300.surrogate import Surrogate
+    s = Surrogate(0, seed=11, max_batch=2048, width=64)
+    yield s
+    s.close()
+
+
+def test_width64_gradients_match_cpu_fp64_network(sur64):
+    """The hidden-width-64 network through the same tcgen05 chain (N = 64 tiles, one K chunk per
+    hidden layer) against the CPU FP64 network of that width, BF16 rounding emulated: <= 1e-2."""
+    import surrogate_mlp as sm
+    assert sur64.width == 64 and sur64.num_params() == sm.num_params(64)
+    x, cls, tgt, xd, cd, td = _batch(1024, 77)
+    w = (1.0, 3.0, 5.0, 7.0)
+    sur64.set_loss_weights(*w)
+    g, loss = sur64.gradients(xd, cd, td)
+    p, B = sur64.params(), sur64.fourier()
+    g_ref, terms = sm.gradients(p.astype(np.float64), B, x, cls, tgt, emulate_bf16=True, weights=w)
+    assert np.allclose(loss, terms, rtol=2e-3, atol=1e-6), (loss, terms)
+    offs = np.cumsum([0] + [fo * fi + fo for fo, fi in sm.layers(64)])
+    for l, (fo, fi) in enumerate(sm.layers(64)):
+        w0, b0, e = offs[l], offs[l] + fo * fi, offs[l + 1]
+        assert _rel(g[w0:b0], g_ref[w0:b0]) < 1e-2, (l, "W", _rel(g[w0:b0], g_ref[w0:b0]))
+        assert _rel(g[b0:e], g_ref[b0:e]) < 1e-2, (l, "b", _rel(g[b0:e], g_ref[b0:e]))
+    y = sur64.predict(xd).cpu().numpy()
+    Y, _ = sm.forward(p.astype(np.float64), B, x, emulate_bf16=True)
+    assert np.abs(y - Y[:, :8]).max() <= 1e-2 * max(1.0, np.abs(Y[:, :8]).max())
+
+
+def test_width_is_checked(cuda):
+    from black_simulation_gb300 import bhk
+    from black_simulation_gb300.surrogate import Surrogate
+    with pytest.raises(ValueError):
+        Surrogate(0, width=128)
+    h = bhk.C.c_void_p()
+    assert bhk.lib().bhk_surrogate_create_width(0, 1, 128, 128, bhk.C.byref(h)) == bhk.EINVAL
+
+
 def test_predict_matches_cpu_forward(sur):
     import surrogate_mlp as sm
     x, _, _, xd, _, _ = _batch(3000, 9)   # more rows than the batch capacity, not a multiple of 128
