@@ -1290,8 +1290,14 @@ template <int HID>
 __host__ __device__ constexpr int act_bytes() { return (HID / 64) * kChunkBytes; }
 template <int HID>
 __host__ __device__ constexpr int wchunk_bytes() { return HID * 64 * 2; }
+// Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 4 at width 64
+// (4 x 64 columns, 4 epilogue warps each -- one per TMEM lane quadrant).
 template <int HID>
-__host__ __device__ constexpr int inf_smem() { return 2 * act_bytes<HID>() + kInfStages * wchunk_bytes<HID>() + 1024 + kInfMisc; }
+__host__ __device__ constexpr int inf_slots() { return HID == 64 ? 4 : 2; }
+template <int HID>
+__host__ __device__ constexpr int inf_smem() {
+    return inf_slots<HID>() * act_bytes<HID>() + kInfStages * wchunk_bytes<HID>() + 1024 + kInfMisc;
+}
 
 // Weight chunks per layer: 64-wide K slices of all output rows (N = HID per MMA; the head N = 16).
 template <int HID>
@@ -1344,11 +1350,11 @@ __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb,
     }
 }
 
-// Two tiles in flight per CTA (one CTA per SM): while the tensor core runs one tile's layer, the
-// other tile's epilogue warps turn their accumulators into the next layer's operand. Each tile
-// slot owns 256 TMEM columns and a 64 KB activation buffer; the weight ring is shared and filled
-// in the MMA's order (pair of tiles, layer, slot, chunk). Every MMA is 128 x 256 x 16, so each
-// activation slice is read from shared memory once per layer. CTA b takes tiles b, b + grid, ...
+// NS = inf_slots<HID>() tiles in flight per CTA: while the tensor core runs one tile's layer, the other
+// tiles' epilogue warps turn their accumulators into the next layer's operand. Each tile slot owns HID
+// TMEM columns and an activation buffer of HID columns; the weight ring is shared and filled in the
+// MMA's order (group of NS tiles, layer, slot, chunk). Every MMA is 128 x HID x 16, so each activation
+// slice is read from shared memory once per layer. CTA b takes tiles b, b + grid, ...
 template <int HID>
 __global__ void __launch_bounds__(kInfThreads, 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
@@ -1356,14 +1362,17 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
              const __grid_constant__ CUtensorMap tW4, InferArgs ia) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr int NS = inf_slots<HID>();
     constexpr int kActBytes = act_bytes<HID>(), kWChunkBytes = wchunk_bytes<HID>();
-    constexpr uint32_t kTmemCols = 2 * HID;  // two tile slots of HID accumulator columns
-    uint8_t* ring = base + 2 * kActBytes;
+    constexpr uint32_t kTmemCols = NS * HID;  // NS tile slots of HID accumulator columns
+    constexpr int kWarpsPerSlot = kEpiWarps / NS, kHalves = kWarpsPerSlot / 4;
+    static_assert(3 + 3 + 2 * NS + 1 <= 16, "the mbarriers fit their 128 bytes");
+    uint8_t* ring = base + NS * kActBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kWChunkBytes);
     uint64_t* empty = full + kInfStages;
-    uint64_t* act_ready = empty + kInfStages;  // [2]
-    uint64_t* acc_full = act_ready + 2;        // [2]
-    uint64_t* drain = acc_full + 2;
+    uint64_t* act_ready = empty + kInfStages;  // [NS]
+    uint64_t* acc_full = act_ready + NS;       // [NS]
+    uint64_t* drain = acc_full + NS;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + 16);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* sB = reinterpret_cast<float*>(tmem_slot + 4);
@@ -1372,15 +1381,15 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
     const long long cid = blockIdx.x, ncl = gridDim.x;
     const long long n_my = cid < ntiles ? (ntiles - cid + ncl - 1) / ncl : 0;
-    const long long pairs = (n_my + 1) / 2;
+    const long long groups = (n_my + NS - 1) / NS;
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
     if (threadIdx.x == 0) {
         for (int st = 0; st < kInfStages; ++st) {
             tc::mbar_init(&full[st], 1);
             tc::mbar_init(&empty[st], 1);
         }
-        for (int sl = 0; sl < 2; ++sl) {
-            tc::mbar_init(&act_ready[sl], 32 * kEpiWarps / 2);
+        for (int sl = 0; sl < NS; ++sl) {
+            tc::mbar_init(&act_ready[sl], 32 * kWarpsPerSlot);
             tc::mbar_init(&acc_full[sl], 1);
         }
         tc::mbar_init(drain, 1);
@@ -1406,10 +1415,10 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         if (lane == 0) {  // ---- TMA producer, in the MMA's order
             long long q = 0;
             bool ok = true;
-            for (long long p = 0; p < pairs && ok; ++p)
+            for (long long p = 0; p < groups && ok; ++p)
                 for (int l = 0; l < kLayers && ok; ++l)
-                    for (int sl = 0; sl < 2 && ok; ++sl) {
-                        if (2 * p + sl >= n_my) continue;
+                    for (int sl = 0; sl < NS && ok; ++sl) {
+                        if (NS * p + sl >= n_my) continue;
                         for (int c = 0; c < layer_chunks<HID>(l); ++c, ++q) {
                             if (*abort_flag) { ok = false; break; }
                             const int st = static_cast<int>(q % kInfStages);
@@ -1433,12 +1442,12 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         if (lane == 0) {  // ---- MMA issuer
             constexpr uint32_t kIdHid = tc::idesc_bf16(128, HID), kId16 = tc::idesc_bf16(128, 16);
             long long q = 0;
-            uint32_t act_n[2] = {0u, 0u};
+            uint32_t act_n[NS] = {};
             bool ok = true;
-            for (long long p = 0; p < pairs && ok; ++p)
+            for (long long p = 0; p < groups && ok; ++p)
                 for (int l = 0; l < kLayers && ok; ++l)
-                    for (int sl = 0; sl < 2 && ok; ++sl) {
-                        if (2 * p + sl >= n_my) continue;
+                    for (int sl = 0; sl < NS && ok; ++sl) {
+                        if (NS * p + sl >= n_my) continue;
                         if (*abort_flag || !tc::mbar_wait(&act_ready[sl], act_n[sl] & 1)) {
                             if (!*abort_flag) give_up();
                             ok = false;
@@ -1472,45 +1481,50 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         }
     } else {  // ---- warps 2..17: features, epilogues, decode (thread = ray of its slot's tile)
         const int ew = warp - 2;
-        const int slot = ew >> 3;          // tile slot
-        const int half = (ew >> 2) & 1;    // columns 128 half .. 128 half + 127 (and 16 of the 32 frequencies)
-        const int q4 = warp & 3;           // TMEM lane quadrant this warp may access
+        const int slot = ew / kWarpsPerSlot;   // tile slot
+        const int half = (ew >> 2) % kHalves;  // its share of the columns (and of the 32 frequencies)
+        const int q4 = warp & 3;               // TMEM lane quadrant this warp may access
         const int row = 32 * q4 + lane;
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16) + static_cast<uint32_t>(HID) * slot;
         uint8_t* act = base + slot * kActBytes;
         uint32_t acc_n = 0;
         // Every exit decision is taken by the whole warp (the TMEM loads and the list append are
         // warp-collective).
-        for (long long k = slot; k < n_my; k += 2) {
+        for (long long k = slot; k < n_my; k += NS) {
             if (__any_sync(0xffffffffu, *abort_flag)) break;
             const long long tile = cid + k * ncl;
             const long long ray = tile * kTileRays + row;
             const bool live = ray < ia.n;
             int fi = 0;
             float alpha = 0.0f, beta = 0.0f;
-            {
-                uint32_t fs[8], fc[8];  // this half's 16 sines and 16 cosines, packed
+            constexpr int kFreqPer = kFreq / kHalves;  // frequencies of this thread, in blocks of 16
+            float u[kIn] = {};
+            if (live) {
+                int lo = 0, hi = ia.nframes - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
+                }
+                fi = lo;
+                const SurFrame& f = ia.frames[fi];
+                const int local = static_cast<int>(ray - f.offset);
+                const int pr = local / f.width, pc = local - pr * f.width;
+                alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
+                beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
+                const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
+                normalise(x, u);
+            }
+#pragma unroll
+            for (int fb = 0; fb < kFreqPer / 16; ++fb) {
+                const int j0 = kFreqPer * half + 16 * fb;  // first frequency of this block
+                uint32_t fs[8], fc[8];  // the block's 16 sines and 16 cosines, packed
                 if (live) {
-                    int lo = 0, hi = ia.nframes - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
-                    }
-                    fi = lo;
-                    const SurFrame& f = ia.frames[fi];
-                    const int local = static_cast<int>(ray - f.offset);
-                    const int pr = local / f.width, pc = local - pr * f.width;
-                    alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
-                    beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
-                    const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
-                    float u[kIn];
-                    normalise(x, u);
 #pragma unroll
                     for (int j = 0; j < 16; j += 2) {
                         float sv[2], cv[2];
 #pragma unroll
                         for (int e = 0; e < 2; ++e) {
-                            const int jj = 16 * half + j + e;
+                            const int jj = j0 + j + e;
                             float p = 0.0f;
 #pragma unroll
                             for (int i = 0; i < kIn; ++i) p += sB[jj * kIn + i] * u[i];
@@ -1523,8 +1537,8 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
 #pragma unroll
                     for (int j = 0; j < 8; ++j) fs[j] = fc[j] = 0u;
                 }
-                store_act16(act, row, 16 * half, fs);
-                store_act16(act, row, kFreq + 16 * half, fc);
+                store_act16(act, row, j0, fs);
+                store_act16(act, row, kFreq + j0, fc);
             }
             tc::fence_proxy_async();
             tc::fence_before_sync();
@@ -1538,7 +1552,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                 }
                 ++acc_n;
                 tc::fence_after_sync();
-                constexpr int kHalf = HID / 2, kGroups = kHalf / 32;  // this warp's columns, in groups of 32
+                constexpr int kHalf = HID / kHalves, kGroups = kHalf / 32;  // this warp's columns, in groups of 32
                 const float* hb = ia.half_bias + l * HID + kHalf * half;
                 const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
                 uint32_t ra[32], rb[32];
