@@ -48,7 +48,8 @@ class TraceOptsC(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_steps", C.c_int32), ("r_escape", C.c_double),
                 ("capture_eps", C.c_double), ("reproject_every", C.c_int32), ("block", C.c_int32),
                 ("chunk", C.c_int32), ("sort_buckets", C.c_int32), ("use_graph", C.c_int32),
-                ("reg_budget", C.c_int32), ("pole_step_frac", C.c_double)]
+                ("reg_budget", C.c_int32), ("pole_step_frac", C.c_double), ("fp64_turning", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class RaysOutC(C.Structure):
@@ -62,7 +63,7 @@ class StatsC(C.Structure):
     _fields_ = [("rays", C.c_int64), ("accepted_steps", C.c_int64), ("rejected_steps", C.c_int64),
                 ("rescued", C.c_int64), ("unfinished", C.c_int64), ("block", C.c_int32), ("chunk", C.c_int32),
                 ("sort_buckets", C.c_int32), ("grid", C.c_int32), ("reg_budget", C.c_int32), ("pad", C.c_int32),
-                ("kernel_ms", C.c_double)]
+                ("kernel_ms", C.c_double), ("fp64_turning_steps", C.c_int64)]
 
 
 class EhtViewC(C.Structure):
@@ -129,12 +130,13 @@ class TraceOpts:
     use_graph: bool = False
     reg_budget: int = 0
     pole_step_frac: float = 0.0
+    fp64_turning: bool = False
 
     def c(self) -> TraceOptsC:
         prec = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[self.precision]
         return TraceOptsC(prec, self.rtol, self.max_steps, self.r_escape, self.capture_eps, self.reproject_every,
                           self.block, self.chunk, self.sort_buckets, 1 if self.use_graph else 0, self.reg_budget,
-                          self.pole_step_frac)
+                          self.pole_step_frac, 1 if self.fp64_turning else 0, 0)
 
 
 _lib: Optional[C.CDLL] = None

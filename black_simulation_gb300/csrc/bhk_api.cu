@@ -166,6 +166,8 @@ Resolved resolve(bhk_context* ctx, const bhk_trace_opts* o) {
     r.graph = o->use_graph != 0;
     const int rb = o->reg_budget > 0 ? o->reg_budget : (ctx->tuned_regcap[pi] ? ctx->tuned_regcap[pi] : 1);
     r.regcap = (r.fp64 || rb >= 3) ? 0 : rb;
+    r.p.fp64_turning = (!r.fp64 && o->fp64_turning) ? 1 : 0;
+    if (r.p.fp64_turning) r.regcap = 1;  // the variant with FP64 turning-point attempts is built at <= 102
     if (r.regcap > 0 && r.block > 128) r.block = 128;
     r.block = std::min(r.block, 256);
     const int bps = trace_blocks_per_sm(r.fp64, r.regcap, r.block);
@@ -743,6 +745,7 @@ bhk_status bhk_get_stats(bhk_context* c, bhk_trace_stats* stats) {
     s.rejected_steps = static_cast<int64_t>(c->ctl_host->stats[1]);
     s.unfinished = static_cast<int64_t>(c->ctl_host->stats[2]);
     s.rescued = static_cast<int64_t>(c->ctl_host->stats[3]);
+    s.fp64_turning_steps = static_cast<int64_t>(c->ctl_host->stats[4]);
     s.kernel_ms = 0.0;
     if (c->timed_last) {
         float ms = 0.0f;

@@ -56,7 +56,8 @@ struct LaunchSoA {
 // Small control block reset at the start of every batch.
 struct Control {
     unsigned long long queue;     // next position in the ray queue
-    unsigned long long stats[4];  // accepted steps, rejected steps, unfinished rays, rescued rays
+    unsigned long long stats[5];  // accepted steps, rejected steps, unfinished rays, rescued rays,
+                                  // FP64 attempts near turning points
     long long n_rays;             // total rays of the batch (device-resident: graph friendly)
     unsigned int rescue_count;
     unsigned int pad;
@@ -86,6 +87,8 @@ struct TraceParams {
     double tol0;                  // photonStepSize tolerance of the first step
     float rtol_f, tol0_f;         // the same for the FP32 path (no conversions in the loop)
     float pole_frac;              // FP32: outgoing steps capped at pole_frac * r / |vr| (0 = no cap)
+    int32_t fp64_turning;         // FP32: attempts near turning points in FP64 (bhk_trace_opts.fp64_turning)
+    int32_t pad;
 };
 
 struct Outputs {

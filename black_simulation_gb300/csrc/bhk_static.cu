@@ -216,11 +216,12 @@ extern "C" bhk_status bhk_trace_frames_static(const bhk_frame_desc* frames, int3
     p.pole_frac = o.pole_step_frac > 0.0 ? static_cast<float>(o.pole_step_frac)
                   : (o.pole_step_frac < 0.0 ? 0.0f
                      : static_cast<float>(std::fmin(0.5, 0.1 * std::pow(p.rtol / 1e-6, 0.2))));
+    p.fp64_turning = (!fp64 && o.fp64_turning) ? 1 : 0;
     int block = o.block > 0 ? std::min(o.block, 256) : 128;
     p.chunk = ((o.chunk > 32 ? o.chunk : 32) + 31) / 32 * 32;  // whole batches of 32 (one per lane)
     p.buckets = std::min(o.sort_buckets > 0 ? o.sort_buckets : 1, kMaxBuckets);
     const int rb = o.reg_budget > 0 ? o.reg_budget : 1;
-    const int regcap = (fp64 || rb >= 3) ? 0 : rb;
+    const int regcap = p.fp64_turning ? 1 : ((fp64 || rb >= 3) ? 0 : rb);
     if (regcap > 0) block = std::min(block, 128);
     const int grid = std::max(1, trace_blocks_per_sm(fp64, regcap, block)) * sms;
 

@@ -738,17 +738,89 @@ __device__ __forceinline__ float error_norm2_f32(const float y[5], const float y
     return acc;
 }
 
+// A ray within ~0.05 M of a radial turning point (R ~ R'(r_t) (r - r_t), so |r - r_t| ~ vr^2 / |R'| with
+// R' = 2 k[3]) or within ~0.05 rad of a polar one (the same with Theta and k[4]).
+__device__ __forceinline__ bool near_turning_point(const Lane<float>& s) {
+    return s.y[3] * s.y[3] < 0.1f * fabsf(s.k[0][3]) || s.y[4] * s.y[4] < 0.1f * fabsf(s.k[0][4]);
+}
+
+// The Dormand-Prince attempt of an FP32 lane taken in FP64: the right-hand side at the step's start
+// (fresh, from the FP64 launch constants), the six stages, the 5th-order solution y5 and its
+// constraint potentials, and the error estimate -- the arithmetic of the FP64 tracer, on the lane's
+// hemisphere representation (the equations are symmetric under theta -> pi - theta). The stages and
+// y5 go back to the lane as FP32, so that the step's events, acceptance, re-projection and step control
+// stay the FP32 code's. Returns the squared error norm in the FP32 step's convention.
+__device__ __noinline__ float attempt_stages_f64(const float y[5], float k[7][5], float h, double rtol, double a,
+                                                 double E, double Lz, double Q, float y5[5], Proj<float>* pj) {
+    RayC<double> c;
+    c.set(a, E, Lz, Q);
+    double yd[5], kd[7][5], t[5], y5d[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) yd[i] = y[i];
+    const double hd = h;
+    rhs(c, yd, kd[0]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) t[i] = yd[i] + hd * (DP::a21 * kd[0][i]);
+    rhs(c, t, kd[1]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) t[i] = yd[i] + hd * (DP::a31 * kd[0][i] + DP::a32 * kd[1][i]);
+    rhs(c, t, kd[2]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) t[i] = yd[i] + hd * (DP::a41 * kd[0][i] + DP::a42 * kd[1][i] + DP::a43 * kd[2][i]);
+    rhs(c, t, kd[3]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        t[i] = yd[i] + hd * (DP::a51 * kd[0][i] + DP::a52 * kd[1][i] + DP::a53 * kd[2][i] + DP::a54 * kd[3][i]);
+    rhs(c, t, kd[4]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        t[i] = yd[i] + hd * (DP::a61 * kd[0][i] + DP::a62 * kd[1][i] + DP::a63 * kd[2][i] + DP::a64 * kd[3][i] +
+                             DP::a65 * kd[4][i]);
+    rhs(c, t, kd[5]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+        y5d[i] = yd[i] + hd * (DP::b1 * kd[0][i] + DP::b3 * kd[2][i] + DP::b4 * kd[3][i] + DP::b5 * kd[4][i] +
+                               DP::b6 * kd[5][i]);
+    Proj<double> pd;
+    rhs<double, true>(c, y5d, kd[6], &pd);
+    double acc = 0.0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const double e = DP::e1 * kd[0][i] + DP::e3 * kd[2][i] + DP::e4 * kd[3][i] + DP::e5 * kd[4][i] +
+                         DP::e6 * kd[5][i] + DP::e7 * kd[6][i];
+        const double q = e / (rtol + rtol * fmax(fabs(yd[i]), fabs(y5d[i])));
+        acc += q * q;
+    }
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+#pragma unroll
+        for (int i = 0; i < 5; ++i) k[j][i] = static_cast<float>(kd[j][i]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) y5[i] = static_cast<float>(y5d[i]);
+    pj->R = static_cast<float>(pd.R);
+    pj->Rz = static_cast<float>(pd.Rz);
+    pj->Th = static_cast<float>(pd.Th);
+    pj->Thz = static_cast<float>(pd.Thz);
+    return static_cast<float>(acc * 0.2 * hd * hd);
+}
+
 // One Dormand-Prince attempt on a lane's ray. Returns kContinue, kFinished (outputs written),
 // kRescue (FP32 only: hand the state to FP64) or kRestart (FP32 only: non-finite state).
-template <typename T>
+// kTP (FP32 only): attempts that start near a turning point are taken in FP64 (attempt_stages_f64);
+// n_tp counts them.
+template <typename T, bool kTP = false>
 __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long long ray, const Outputs& out,
                                        bool reproject, Control* ctl, const LaunchSoA& L,
-                                       const RayGeom* __restrict__ geom) {
+                                       const RayGeom* __restrict__ geom, unsigned* n_tp = nullptr) {
     constexpr bool F64 = sizeof(T) == 8;
     const T h = s.h;
     T t[5];
     T y5[5];
-    if constexpr (F64) {  // the oracle's operation order
+    bool tp_step = false;
+    if constexpr (!F64 && kTP) tp_step = near_turning_point(s);
+    if (tp_step) {
+        // (FP32 lanes only; the stages, y5, the FSAL stage's potentials and the error norm come below)
+    } else if constexpr (F64) {  // the oracle's operation order
 #pragma unroll
         for (int i = 0; i < 5; ++i) t[i] = s.y[i] + h * (T(DP::a21) * s.k[0][i]);
         rhs(s.c, t, s.k[1], static_cast<Proj<T>*>(nullptr), &s.kt[1]);
@@ -790,8 +862,20 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         stage_f32<15, 5>(s.y, s.k, hh, {0, 2, 3, 4, 5}, y5);
     }
     Proj<T> pj;
-    if constexpr (F64) rhs<T, false>(s.c, y5, s.k[6], &pj, &s.kt[6]);
-    else rhs<T, true>(s.c, y5, s.k[6], &pj);
+    float tp_e2 = 0.0f;
+    if constexpr (F64) {
+        rhs<T, false>(s.c, y5, s.k[6], &pj, &s.kt[6]);
+    } else {
+        if (tp_step) {
+            if constexpr (kTP) {
+                const RayGeom& G = geom[L.geom_id[ray]];
+                tp_e2 = attempt_stages_f64(s.y, s.k, h, p.rtol, G.a, L.E[ray], L.L[ray], L.Q[ray], y5, &pj);
+                ++*n_tp;
+            }
+        } else {
+            rhs<T, true>(s.c, y5, s.k[6], &pj);
+        }
+    }
     T rtol;
     if constexpr (F64) rtol = p.rtol;
     else rtol = p.rtol_f;
@@ -806,7 +890,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
             acc += q * q;
         }
     } else {
-        acc = error_norm2_f32(s.y, y5, s.k, rtol);  // without the factor h, applied once below
+        if (!tp_step) acc = error_norm2_f32(s.y, y5, s.k, rtol);  // without the factor h, applied once below
     }
     // err = sqrt(acc / 5); the FP32 path works with err^2.
     T err, e2;
@@ -816,7 +900,7 @@ __device__ __forceinline__ int attempt(Lane<T>& s, const TraceParams& p, long lo
         e2 = err;
         ok = err <= T(1);
     } else {
-        e2 = acc * (T(0.2) * h * h);
+        e2 = tp_step ? tp_e2 : acc * (T(0.2) * h * h);
         err = e2;
         ok = e2 <= T(1);
     }
@@ -1034,7 +1118,7 @@ __device__ __forceinline__ void push_rescue(Rescue* rescue, unsigned cap, Contro
 // kMinBlocks > 0 caps registers through __launch_bounds__(128, kMinBlocks) (blocks of <= 128 threads):
 // 5 -> <= 102 registers (20 warps/SM), 6 -> <= 85 (24 warps/SM); 0 leaves the compiler free (blocks
 // of <= 256 threads).
-template <typename T, int kMinBlocks>
+template <typename T, int kMinBlocks, bool kTP = false>
 __global__ void __launch_bounds__(kMinBlocks > 0 ? 128 : 256, kMinBlocks > 0 ? kMinBlocks : 1)
 trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __restrict__ order,
              Outputs out, Rescue* rescue, unsigned rescue_cap, TraceParams p, Control* ctl,
@@ -1047,7 +1131,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
     bool exhausted = false;
     int pool_pos = 0, pool_end = 0;  // this warp's chunk of the queue
     // Per-lane step counts, flushed to the 64-bit totals before they can wrap (a ray adds < 2^31).
-    unsigned n_acc = 0, n_rej = 0;
+    unsigned n_acc = 0, n_rej = 0, n_tp = 0;
     for (;;) {
         // A warp traces its rays in batches of 32 queue-adjacent rays -- neighbouring pixels, or rays
         // of one cost bucket -- and takes the next batch only when every lane's ray has ended. Rays
@@ -1121,7 +1205,7 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
         if (active) {
             // The optional FP64 re-projection on every reproject_every-th attempt of the ray.
             const bool reproject = p.reproject_every > 0 && (s.acc + s.rej + 1) % p.reproject_every == 0;
-            const int r = attempt<T>(s, p, ray, out, reproject, ctl, L, geom);
+            const int r = attempt<T, kTP>(s, p, ray, out, reproject, ctl, L, geom, &n_tp);
             if (r != kContinue) {
                 n_acc += static_cast<unsigned>(s.acc);
                 n_rej += static_cast<unsigned>(s.rej);
@@ -1163,6 +1247,9 @@ trace_kernel(LaunchSoA L, const RayGeom* __restrict__ geom, const int32_t* __res
     if (lane == 0) {
         atomicAdd(&ctl->stats[0], t_acc);
         atomicAdd(&ctl->stats[1], t_rej);
+    }
+    if constexpr (kTP) {
+        if (n_tp) atomicAdd(&ctl->stats[4], static_cast<unsigned long long>(n_tp));
     }
 }
 
@@ -1280,9 +1367,11 @@ namespace {
 using TraceFn = void (*)(LaunchSoA, const RayGeom*, const int32_t*, Outputs, Rescue*, unsigned, TraceParams, Control*,
                          const FrameDev*, int);
 
-// Variant by precision and register cap (see trace_kernel).
-TraceFn trace_variant(bool fp64, int regcap) {
+// Variant by precision and register cap (see trace_kernel); FP64 attempts near turning points have
+// their own variant at the <= 102-register cap.
+TraceFn trace_variant(bool fp64, int regcap, bool tp = false) {
     if (fp64) return trace_kernel<double, 0>;
+    if (tp) return trace_kernel<float, 5, true>;
     if (regcap == 1) return trace_kernel<float, 5>;
     if (regcap == 2) return trace_kernel<float, 6>;
     return trace_kernel<float, 0>;
@@ -1292,8 +1381,8 @@ TraceFn trace_variant(bool fp64, int regcap) {
 void launch_trace(bool fp64, int regcap, LaunchSoA L, const RayGeom* geom, const int32_t* order, Outputs out,
                   Rescue* rescue, unsigned rescue_cap, const TraceParams& p, Control* ctl, int block, int grid,
                   cudaStream_t s, const FrameDev* frames, int nframes) {
-    trace_variant(fp64, regcap)<<<grid, block, 0, s>>>(L, geom, order, out, rescue, rescue_cap, p, ctl, frames,
-                                                        nframes);
+    trace_variant(fp64, regcap, !fp64 && p.fp64_turning)<<<grid, block, 0, s>>>(L, geom, order, out, rescue,
+                                                                                  rescue_cap, p, ctl, frames, nframes);
 }
 
 void launch_constants_out(LaunchSoA L, Outputs out, const Control* ctl, int grid, cudaStream_t s) {

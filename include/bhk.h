@@ -132,6 +132,11 @@ typedef struct {
                                thread (20 warps/SM, blocks <= 128), 2: <= 85 (24 warps/SM), 3: uncapped */
     double pole_step_frac;  /* mixed: outgoing steps capped at this fraction of the Mino time left before
                                r runs off to infinity (~ r/|vr|); 0 -> 0.1 (rtol/1e-6)^(1/5), < 0 off */
+    int32_t fp64_turning;   /* mixed, 1: a step that starts within ~0.05 M of a radial turning point (vr^2 <
+                               0.1 |R'/2|) or ~0.05 rad of a polar one (vtheta^2 < 0.1 |Theta'/2|) is taken in
+                               FP64 (its stages, error estimate and constraint potentials), from the FP64 launch
+                               constants; its own compiled variant (<= 102 registers). 0: off (the default) */
+    int32_t pad;
 } bhk_trace_opts;
 
 /* Per-ray outputs, structure of arrays, n entries each (device memory unless stated). Any pointer
@@ -164,6 +169,7 @@ typedef struct {
     int32_t block, chunk, sort_buckets, grid, reg_budget, pad;
     double kernel_ms;    /* CUDA events on the launching stream: tracer + rescue kernels, or the
                             whole batch when it ran as a CUDA graph */
+    int64_t fp64_turning_steps;  /* step attempts taken in FP64 near turning points (fp64_turning) */
 } bhk_trace_stats;
 
 /* Traces every pixel of nframes frames (host descriptors) in one persistent launch. Ray i of frame f

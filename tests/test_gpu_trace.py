@@ -180,6 +180,29 @@ def test_batch_frames_against_oracle_dp5(ctx, oracle, a, r_obs, deg, w, h):
     assert quiet.mean() > 0.99 and em[quiet].max() < 1e-4
 
 
+def test_fp64_turning_point_attempts(ctx, oracle, golden):
+    """The option that takes attempts near radial and polar turning points in FP64: it does take them
+    (about a fifth of the attempts on this frame), and its results meet the mixed mode's bars against
+    the reference fixture (the same outcomes outside 1e-2 M of the critical curve, 1e-4; phi_disk 2e-4)."""
+    name, a, r_obs, deg, r_out = CASES[0]
+    g = golden(name)
+    f = frame_from_fixture(g, a, r_obs, deg, r_out)
+    out = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6, fp64_turning=True)))
+    st = ctx.stats()
+    frac = st["fp64_turning_steps"] / (st["accepted_steps"] + st["rejected_steps"])
+    outside = band_mask(oracle, g, a, r_obs, deg, 1e-2)
+    agree = np.mean(out["outcome"][outside] == g["outcome"][outside])
+    err = errors(out, g, outside)
+    print("fp64 turning-point attempts", frac, "outcome agreement", agree, err)
+    assert 0.02 < frac < 0.8 and st["unfinished"] == 0
+    assert agree == 1.0
+    for k, v in err.items():
+        assert v < (2e-4 if k == "phi_disk" else 1e-4), (k, v)
+    base = host(ctx.trace_frames([f], bhk.TraceOpts("mixed", rtol=1e-6)))
+    assert ctx.stats()["fp64_turning_steps"] == 0
+    assert np.mean(base["outcome"] == out["outcome"]) > 0.999
+
+
 def test_per_ray_api_equals_frame_api(ctx):
     f = bhk.frame_c1(20, 12)
     frame_out = host(ctx.trace_frames([f], bhk.TraceOpts("fp64")))
