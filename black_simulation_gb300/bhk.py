@@ -363,20 +363,54 @@ def pixel_alpha_beta(frame: "Frame", local):
     return alpha, beta
 
 
-def curve_distance(alpha, beta, curve_alpha, curve_beta, chunk: int = 2048):
-    """Image-plane distance (M) from each point (alpha, beta) to the closed polyline through
-    (curve_alpha, curve_beta) -- e.g. the analytic critical curve critical_curve() returns."""
-    alpha, beta = np.asarray(alpha, dtype=np.float64), np.asarray(beta, dtype=np.float64)
-    ax, ay = np.asarray(curve_alpha, dtype=np.float64), np.asarray(curve_beta, dtype=np.float64)
-    bx, by = np.roll(ax, -1), np.roll(ay, -1)
+def _segment_distance(px, py, ax, ay, bx, by):
     ex, ey = bx - ax, by - ay
     ll = np.maximum(ex * ex + ey * ey, 1e-300)
-    out = np.empty(alpha.size)
-    for i in range(0, alpha.size, chunk):
-        px, py = alpha[i:i + chunk, None], beta[i:i + chunk, None]
-        t = np.clip(((px - ax) * ex + (py - ay) * ey) / ll, 0.0, 1.0)
-        dx, dy = px - (ax + t * ex), py - (ay + t * ey)
-        out[i:i + chunk] = np.sqrt(dx * dx + dy * dy).min(axis=1)
+    t = np.clip(((px - ax) * ex + (py - ay) * ey) / ll, 0.0, 1.0)
+    dx, dy = px - (ax + t * ex), py - (ay + t * ey)
+    return np.sqrt(dx * dx + dy * dy)
+
+
+def curve_distance(alpha, beta, curve_alpha, curve_beta, spacing: float = 1e-3, near: float = 0.2):
+    """Image-plane distance (M) from each point (alpha, beta) to the closed polyline through
+    (curve_alpha, curve_beta): the analytic critical curve critical_curve() returns, symmetric about
+    beta = 0 and star-shaped about its centre. Every point gets the polar estimate |rho - rho_c(psi)|
+    rho_c / sqrt(rho_c^2 + rho_c'^2) about the centre; points it puts within `near` get the exact
+    distance (the polyline resampled to vertices at most `spacing` apart, the nearest vertex by k-d tree,
+    the distance taken to the two segments beside it)."""
+    alpha, beta = np.asarray(alpha, dtype=np.float64), np.asarray(beta, dtype=np.float64)
+    ax, ay = np.asarray(curve_alpha, dtype=np.float64), np.asarray(curve_beta, dtype=np.float64)
+    ac = 0.5 * (ax.min() + ax.max())
+    up = ay >= 0.0
+    psi_c = np.arctan2(ay[up], ax[up] - ac)
+    rho_c = np.hypot(ay[up], ax[up] - ac)
+    o = np.argsort(psi_c)
+    psi_c, rho_c = psi_c[o], rho_c[o]
+    drho = np.gradient(rho_c, psi_c) if psi_c.size > 2 else np.zeros_like(rho_c)
+    psi = np.arctan2(np.abs(beta), alpha - ac)
+    rho = np.hypot(beta, alpha - ac)
+    rc = np.interp(psi, psi_c, rho_c)
+    kn = rc / np.sqrt(rc * rc + np.interp(psi, psi_c, drho) ** 2)
+    out = np.abs(rho - rc) * kn
+    close = np.nonzero(out < near)[0]
+    if close.size == 0:
+        return out
+    bx, by = np.roll(ax, -1), np.roll(ay, -1)
+    seg = np.hypot(bx - ax, by - ay)
+    pieces = np.maximum(1, np.ceil(seg / spacing).astype(np.int64))
+    start = np.repeat(np.arange(ax.size), pieces)
+    frac = (np.arange(pieces.sum()) - np.repeat(np.cumsum(pieces) - pieces, pieces)) / np.repeat(pieces, pieces)
+    vx = ax[start] + frac * (bx - ax)[start]
+    vy = ay[start] + frac * (by - ay)[start]
+    from scipy.spatial import cKDTree
+    d, j = cKDTree(np.stack([vx, vy], 1)).query(np.stack([alpha[close], beta[close]], 1),
+                                               distance_upper_bound=2.0 * near)
+    ok = np.isfinite(d)
+    c, j = close[ok], j[ok]
+    nv = vx.size
+    prev, nxt = (j - 1) % nv, (j + 1) % nv
+    out[c] = np.minimum(_segment_distance(alpha[c], beta[c], vx[prev], vy[prev], vx[j], vy[j]),
+                        _segment_distance(alpha[c], beta[c], vx[j], vy[j], vx[nxt], vy[nxt]))
     return out
 
 

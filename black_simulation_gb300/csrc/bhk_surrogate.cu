@@ -1283,7 +1283,8 @@ constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 of activ
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
 constexpr int kEpiWarps = 16;              // per tile slot: 4 TMEM lane quadrants x 2 column halves
 constexpr int kInfThreads = 64 + 32 * kEpiWarps;
-constexpr int kInfMisc = 128 + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
+constexpr int kInfBars = 32;  // 64-bit mbarrier words reserved in shared memory
+constexpr int kInfMisc = 8 * kInfBars + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
 // Per hidden width HID: one tile's activations (HID / 64 chunks of 64 columns), one weight chunk (all
 // HID output rows x 64 K of a hidden layer), the shared memory of the kernel.
 template <int HID>
@@ -1291,12 +1292,23 @@ __host__ __device__ constexpr int act_bytes() { return (HID / 64) * kChunkBytes;
 template <int HID>
 __host__ __device__ constexpr int wchunk_bytes() { return HID * 64 * 2; }
 // Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 4 at width 64
-// (4 x 64 columns, 4 epilogue warps each -- one per TMEM lane quadrant).
+// (4 x 64 columns, 4 epilogue warps each -- one per TMEM lane quadrant). The epilogue can also serve
+// several tiles per warp group in turn; at width 64 eight tiles that way (all 512 columns) measured
+// slower than four (18.3 against 15.9 ms of inference on 124 M rays).
 template <int HID>
 __host__ __device__ constexpr int inf_slots() { return HID == 64 ? 4 : 2; }
+// At width 64 the whole network's weights (4 x 8 KB + the head's 2 KB) stay resident in shared memory,
+// loaded once per CTA, and the MMA issuer serves whichever tile is ready; at width 256 they stream
+// through a ring of kInfStages chunks in the MMA's order.
+template <int HID>
+__host__ __device__ constexpr bool inf_resident() { return HID == 64; }
+template <int HID>
+__host__ __device__ constexpr int inf_ring_bytes() {
+    return inf_resident<HID>() ? kLayers * wchunk_bytes<HID>() : kInfStages * wchunk_bytes<HID>();
+}
 template <int HID>
 __host__ __device__ constexpr int inf_smem() {
-    return inf_slots<HID>() * act_bytes<HID>() + kInfStages * wchunk_bytes<HID>() + 1024 + kInfMisc;
+    return inf_slots<HID>() * act_bytes<HID>() + inf_ring_bytes<HID>() + 1024 + kInfMisc;
 }
 
 // Weight chunks per layer: 64-wide K slices of all output rows (N = HID per MMA; the head N = 16).
@@ -1365,15 +1377,18 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     constexpr int NS = inf_slots<HID>();
     constexpr int kActBytes = act_bytes<HID>(), kWChunkBytes = wchunk_bytes<HID>();
     constexpr uint32_t kTmemCols = NS * HID;  // NS tile slots of HID accumulator columns
-    constexpr int kWarpsPerSlot = kEpiWarps / NS, kHalves = kWarpsPerSlot / 4;
-    static_assert(3 + 3 + 2 * NS + 1 <= 16, "the mbarriers fit their 128 bytes");
-    uint8_t* ring = base + NS * kActBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kInfStages * kWChunkBytes);
+    // A tile's epilogue: 4 warps (one per TMEM lane quadrant) at width 64, 8 (two column halves) at 256.
+    constexpr int kHalves = HID == 64 ? 1 : 2, kWarpsPerSlot = 4 * kHalves;
+    static_assert(kEpiWarps % kWarpsPerSlot == 0 && NS % (kEpiWarps / kWarpsPerSlot) == 0, "slot mapping");
+    static_assert(kInfStages + kInfStages + 2 * NS + 1 <= kInfBars, "the mbarriers fit their words");
+    constexpr bool kResident = inf_resident<HID>();
+    uint8_t* ring = base + NS * kActBytes;  // the weight ring, or (kResident) layer l's weights at l chunks
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + inf_ring_bytes<HID>());
     uint64_t* empty = full + kInfStages;
     uint64_t* act_ready = empty + kInfStages;  // [NS]
     uint64_t* acc_full = act_ready + NS;       // [NS]
     uint64_t* drain = acc_full + NS;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + 16);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + kInfBars);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* sB = reinterpret_cast<float*>(tmem_slot + 4);
 
@@ -1411,7 +1426,63 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         atomicExch(ia.err, 1);
     };
 
-    if (warp == 0) {
+    if (warp == 0 && kResident) {
+        if (lane == 0 && n_my > 0) {  // ---- the network's weights, once
+            tc::mbar_expect_tx(&full[0], 4 * kWChunkBytes + kHeadChunkBytes);
+            tc::tma_load_2d(ring + 0 * kWChunkBytes, &tW0, 0, 0, &full[0]);
+            tc::tma_load_2d(ring + 1 * kWChunkBytes, &tW1, 0, 0, &full[0]);
+            tc::tma_load_2d(ring + 2 * kWChunkBytes, &tW2, 0, 0, &full[0]);
+            tc::tma_load_2d(ring + 3 * kWChunkBytes, &tW3, 0, 0, &full[0]);
+            tc::tma_load_2d(ring + 4 * kWChunkBytes, &tW4, 0, 0, &full[0]);
+            tc::mbar_wait(&full[0], 0);  // landed before the CTA may exit (bounded)
+        }
+    } else if (warp == 1 && kResident) {
+        if (lane == 0) {  // ---- MMA issuer: whichever tile slot has its next layer's input ready
+            constexpr uint32_t kIdHid = tc::idesc_bf16(128, HID), kId16 = tc::idesc_bf16(128, 16);
+            uint32_t act_n[NS] = {};
+            int layer[NS] = {};
+            long long left[NS];
+            long long total = 0;
+            for (int sl = 0; sl < NS; ++sl) {
+                const long long tiles = sl < n_my ? (n_my - sl + NS - 1) / NS : 0;
+                left[sl] = tiles * kLayers;
+                total += left[sl];
+            }
+            bool ok = total == 0 || tc::mbar_wait(&full[0], 0);
+            if (!ok) give_up();
+            tc::fence_after_sync();
+            uint32_t idle = 0;  // sweeps without progress (bounded)
+            while (ok && total > 0) {
+                bool progress = false;
+                for (int sl = 0; sl < NS; ++sl) {
+                    if (left[sl] == 0 || !tc::mbar_test(&act_ready[sl], act_n[sl] & 1)) continue;
+                    ++act_n[sl];
+                    tc::fence_after_sync();
+                    const int l = layer[sl];
+                    const uint64_t ad = tc::smem_desc_sw128(base + sl * kActBytes);
+                    const uint64_t bd = tc::smem_desc_sw128(ring + l * kWChunkBytes);
+                    const uint32_t d = tmem + static_cast<uint32_t>(HID * sl);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk)
+                        tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kIdHid : kId16, kk ? 1u : 0u);
+                    tc::mma_commit(&acc_full[sl]);
+                    layer[sl] = l + 1 == kLayers ? 0 : l + 1;
+                    --left[sl];
+                    --total;
+                    progress = true;
+                }
+                if (progress) {
+                    idle = 0;
+                } else if (++idle > tc::kSpinLimit || *abort_flag) {
+                    if (!*abort_flag) give_up();
+                    ok = false;
+                }
+            }
+            // All MMAs issued have finished before TMEM is released (bounded).
+            tc::mma_commit(drain);
+            tc::mbar_wait(drain, 0);
+        }
+    } else if (warp == 0) {
         if (lane == 0) {  // ---- TMA producer, in the MMA's order
             long long q = 0;
             bool ok = true;
@@ -1480,162 +1551,193 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
             tc::mbar_wait(drain, 0);
         }
     } else {  // ---- warps 2..17: features, epilogues, decode (thread = ray of its slot's tile)
+        // kGroupsE warp groups of kWarpsPerSlot warps; group g serves the TPW slots g, g + kGroupsE, ...,
+        // one phase of each in turn (features, the four hidden epilogues, the head), so that one tile's
+        // MMA runs while the group works on its other tile.
+        constexpr int kGroupsE = kEpiWarps / kWarpsPerSlot, TPW = NS / kGroupsE;
         const int ew = warp - 2;
-        const int slot = ew / kWarpsPerSlot;   // tile slot
+        const int grp = ew / kWarpsPerSlot;
         const int half = (ew >> 2) % kHalves;  // its share of the columns (and of the 32 frequencies)
         const int q4 = warp & 3;               // TMEM lane quadrant this warp may access
         const int row = 32 * q4 + lane;
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * q4) << 16) + static_cast<uint32_t>(HID) * slot;
-        uint8_t* act = base + slot * kActBytes;
-        uint32_t acc_n = 0;
+        uint32_t acc_n[TPW] = {};
         // Every exit decision is taken by the whole warp (the TMEM loads and the list append are
         // warp-collective).
-        for (long long k = slot; k < n_my; k += NS) {
+        bool ok = true;
+        for (long long it = 0; ok; ++it) {
+            if (grp + NS * it >= n_my) break;  // (slot grp has the most tiles of this group's slots)
             if (__any_sync(0xffffffffu, *abort_flag)) break;
-            const long long tile = cid + k * ncl;
-            const long long ray = tile * kTileRays + row;
-            const bool live = ray < ia.n;
-            int fi = 0;
-            float alpha = 0.0f, beta = 0.0f;
-            constexpr int kFreqPer = kFreq / kHalves;  // frequencies of this thread, in blocks of 16
-            float u[kIn] = {};
-            if (live) {
-                int lo = 0, hi = ia.nframes - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (ia.frames[mid].offset <= ray) lo = mid; else hi = mid - 1;
-                }
-                fi = lo;
-                const SurFrame& f = ia.frames[fi];
-                const int local = static_cast<int>(ray - f.offset);
-                const int pr = local / f.width, pc = local - pr * f.width;
-                alpha = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
-                beta = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
-                const float x[kIn] = {f.a, f.th, f.log_r, alpha, beta};
-                normalise(x, u);
-            }
+            bool has[TPW], live[TPW];
+            long long ray[TPW];
+            int fi[TPW];
+            float alpha[TPW], beta[TPW];
 #pragma unroll
-            for (int fb = 0; fb < kFreqPer / 16; ++fb) {
-                const int j0 = kFreqPer * half + 16 * fb;  // first frequency of this block
-                uint32_t fs[8], fc[8];  // the block's 16 sines and 16 cosines, packed
-                if (live) {
-#pragma unroll
-                    for (int j = 0; j < 16; j += 2) {
-                        float sv[2], cv[2];
-#pragma unroll
-                        for (int e = 0; e < 2; ++e) {
-                            const int jj = j0 + j + e;
-                            float p = 0.0f;
-#pragma unroll
-                            for (int i = 0; i < kIn; ++i) p += sB[jj * kIn + i] * u[i];
-                            __sincosf(6.28318530717958648f * (p - rintf(p)), &sv[e], &cv[e]);
-                        }
-                        fs[j >> 1] = pack_bf16(sv[0], sv[1]);
-                        fc[j >> 1] = pack_bf16(cv[0], cv[1]);
+            for (int v = 0; v < TPW; ++v) {  // ---- features
+                const int slot = grp + kGroupsE * v;
+                has[v] = slot + NS * it < n_my;
+                ray[v] = (cid + (slot + NS * it) * ncl) * kTileRays + row;
+                live[v] = has[v] && ray[v] < ia.n;
+                fi[v] = 0;
+                alpha[v] = beta[v] = 0.0f;
+                if (!has[v]) continue;
+                uint8_t* act = base + slot * kActBytes;
+                constexpr int kFreqPer = kFreq / kHalves;  // frequencies of this thread, in blocks of 16
+                float u[kIn] = {};
+                if (live[v]) {
+                    int lo = 0, hi = ia.nframes - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (ia.frames[mid].offset <= ray[v]) lo = mid; else hi = mid - 1;
                     }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) fs[j] = fc[j] = 0u;
+                    fi[v] = lo;
+                    const SurFrame& f = ia.frames[lo];
+                    const int local = static_cast<int>(ray[v] - f.offset);
+                    const int pr = local / f.width, pc = local - pr * f.width;
+                    alpha[v] = static_cast<float>(f.alpha_lo + (pc + 0.5) * f.px);
+                    beta[v] = static_cast<float>(f.beta_hi - (pr + 0.5) * f.py);
+                    const float x[kIn] = {f.a, f.th, f.log_r, alpha[v], beta[v]};
+                    normalise(x, u);
                 }
-                store_act16(act, row, j0, fs);
-                store_act16(act, row, kFreq + j0, fc);
-            }
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            tc::mbar_arrive(&act_ready[slot]);
-            bool ok = true;
-            for (int l = 0; l < 4; ++l) {
-                if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n & 1))) {
-                    if (lane == 0) give_up();
-                    ok = false;
-                    break;
-                }
-                ++acc_n;
-                tc::fence_after_sync();
-                constexpr int kHalf = HID / kHalves, kGroups = kHalf / 32;  // this warp's columns, in groups of 32
-                const float* hb = ia.half_bias + l * HID + kHalf * half;
-                const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
-                uint32_t ra[32], rb[32];
-                tc::tmem_ld32_issue(cb, ra);
-                tc::tmem_wait32(ra);
 #pragma unroll
-                for (int jj = 0; jj < kGroups; ++jj) {
-                    uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
-                    uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
-                    if (jj + 1 < kGroups) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
-                    uint32_t w[16];
-                    silu32(cur, hb + 32 * jj, w);
-                    store_act16(act, row, kHalf * half + 32 * jj, w);
-                    store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
-                    if (jj + 1 < kGroups) tc::tmem_wait32(nxt);
+                for (int fb = 0; fb < kFreqPer / 16; ++fb) {
+                    const int j0 = kFreqPer * half + 16 * fb;  // first frequency of this block
+                    uint32_t fs[8], fc[8];  // the block's 16 sines and 16 cosines, packed
+                    if (live[v]) {
+#pragma unroll
+                        for (int j = 0; j < 16; j += 2) {
+                            float sv[2], cv[2];
+#pragma unroll
+                            for (int e = 0; e < 2; ++e) {
+                                const int jj = j0 + j + e;
+                                float pp = 0.0f;
+#pragma unroll
+                                for (int i = 0; i < kIn; ++i) pp += sB[jj * kIn + i] * u[i];
+                                __sincosf(6.28318530717958648f * (pp - rintf(pp)), &sv[e], &cv[e]);
+                            }
+                            fs[j >> 1] = pack_bf16(sv[0], sv[1]);
+                            fc[j >> 1] = pack_bf16(cv[0], cv[1]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) fs[j] = fc[j] = 0u;
+                    }
+                    store_act16(act, row, j0, fs);
+                    store_act16(act, row, kFreq + j0, fc);
                 }
                 tc::fence_proxy_async();
                 tc::fence_before_sync();
                 tc::mbar_arrive(&act_ready[slot]);
             }
-            if (!ok) break;
-            if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n & 1))) {
-                if (lane == 0) give_up();
-                break;
-            }
-            ++acc_n;
-            tc::fence_after_sync();
-            if (half == 1) {
-                tc::fence_before_sync();
-                continue;  // the head's 8 outputs are decoded by the first half
-            }
-            float y[16];
-            tc::tmem_ld16(trow, y);
-            tc::fence_before_sync();
-            bool fb = false;
-            if (live) {
-                const float* b4 = ia.bias[4];
+            for (int l = 0; l < 4 && ok; ++l) {  // ---- hidden layers
 #pragma unroll
-                for (int i = 0; i < kOut; ++i) y[i] += __ldg(b4 + i);
-                int cls = 0;
-                float mx = y[0];
-                if (y[1] > mx) { mx = y[1]; cls = 1; }
-                if (y[2] > mx) { mx = y[2]; cls = 2; }
-                const float zsum = __expf(y[0] - mx) + __expf(y[1] - mx) + __expf(y[2] - mx);
-                const float pmax = 1.0f / zsum;
-                const double nan = __longlong_as_double(0x7ff8000000000000ll);
-                double rd = nan, gg = nan, ti = nan, pi = nan;
-                if (cls == 1) {
-                    rd = 30.0 * y[3];
-                    gg = __expf(y[4]);
-                } else if (cls == 2) {
-                    const float nrm = sqrtf(y[5] * y[5] + y[6] * y[6] + y[7] * y[7]);
-                    const float dz = fminf(1.0f, fmaxf(-1.0f, y[7] / nrm));
-                    ti = acosf(dz);
-                    pi = atan2f(y[6], y[5]);
+                for (int v = 0; v < TPW; ++v) {
+                    if (!has[v] || !ok) continue;
+                    const int slot = grp + kGroupsE * v;
+                    if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n[v] & 1))) {
+                        if (lane == 0) give_up();
+                        ok = false;
+                        continue;
+                    }
+                    ++acc_n[v];
+                    tc::fence_after_sync();
+                    uint8_t* act = base + slot * kActBytes;
+                    const uint32_t trow =
+                        tmem + (static_cast<uint32_t>(32 * q4) << 16) + static_cast<uint32_t>(HID) * slot;
+                    constexpr int kHalf = HID / kHalves, kGroups = kHalf / 32;  // this warp's columns, in 32s
+                    const float* hb = ia.half_bias + l * HID + kHalf * half;
+                    const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
+                    uint32_t ra[32], rb[32];
+                    tc::tmem_ld32_issue(cb, ra);
+                    tc::tmem_wait32(ra);
+#pragma unroll
+                    for (int jj = 0; jj < kGroups; ++jj) {
+                        uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
+                        uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
+                        if (jj + 1 < kGroups) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
+                        uint32_t w[16];
+                        silu32(cur, hb + 32 * jj, w);
+                        store_act16(act, row, kHalf * half + 32 * jj, w);
+                        store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
+                        if (jj + 1 < kGroups) tc::tmem_wait32(nxt);
+                    }
+                    tc::fence_proxy_async();
+                    tc::fence_before_sync();
+                    tc::mbar_arrive(&act_ready[slot]);
                 }
-                const SurFrame& f = ia.frames[fi];
-                bool band = false;
-                if (f.curve_ok) {
-                    const float da = alpha - f.alpha_c, ab_ = fabsf(beta);
-                    const float psi = atan2f(ab_, da);
-                    const int jb = min(kCurveBins - 1, max(0, static_cast<int>(psi * (kCurveBins / 3.14159265f))));
-                    band = fabsf(sqrtf(da * da + ab_ * ab_) - f.rho[jb]) * f.kn[jb] < ia.band;
-                }
-                // Answers limited to captured rays carry no continuous output, so where the class is
-                // right they are exactly the tracer's (the network's r_disk, g and direction are not used).
-                fb = pmax < ia.p_min || band || fabsf(alpha) < f.snap || !(zsum == zsum) ||
-                     (ia.accept == BHK_ACCEPT_CAPTURED && cls != 0);
-                ia.outcome[ray] = static_cast<uint8_t>(cls + 1);
-                if (ia.r_disk) ia.r_disk[ray] = rd;
-                if (ia.phi_disk) ia.phi_disk[ray] = nan;
-                if (ia.g) ia.g[ray] = gg;
-                if (ia.theta_inf) ia.theta_inf[ray] = ti;
-                if (ia.phi_inf) ia.phi_inf[ray] = pi;
-                if (ia.steps) ia.steps[ray] = 0;
-                if (ia.rejected) ia.rejected[ray] = 0;
             }
-            const unsigned m = __ballot_sync(0xffffffffu, fb);
-            if (m) {
-                unsigned long long b0 = 0;
-                if (lane == 0) b0 = atomicAdd(ia.n_list, static_cast<unsigned long long>(__popc(m)));
-                b0 = __shfl_sync(0xffffffffu, b0, 0);
-                if (fb) ia.list[b0 + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(ray);
+            if (!ok) break;
+#pragma unroll
+            for (int v = 0; v < TPW; ++v) {  // ---- the head: decode and the fallback decision
+                if (!has[v] || !ok) continue;
+                const int slot = grp + kGroupsE * v;
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_full[slot], acc_n[v] & 1))) {
+                    if (lane == 0) give_up();
+                    ok = false;
+                    continue;
+                }
+                ++acc_n[v];
+                tc::fence_after_sync();
+                if (half == 1) {
+                    tc::fence_before_sync();
+                    continue;  // the head's 8 outputs are decoded by the first half
+                }
+                const uint32_t trow =
+                    tmem + (static_cast<uint32_t>(32 * q4) << 16) + static_cast<uint32_t>(HID) * slot;
+                float y[16];
+                tc::tmem_ld16(trow, y);
+                tc::fence_before_sync();
+                bool fb = false;
+                if (live[v]) {
+                    const float* b4 = ia.bias[4];
+#pragma unroll
+                    for (int i = 0; i < kOut; ++i) y[i] += __ldg(b4 + i);
+                    int cls = 0;
+                    float mx = y[0];
+                    if (y[1] > mx) { mx = y[1]; cls = 1; }
+                    if (y[2] > mx) { mx = y[2]; cls = 2; }
+                    const float zsum = __expf(y[0] - mx) + __expf(y[1] - mx) + __expf(y[2] - mx);
+                    const float pmax = 1.0f / zsum;
+                    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+                    double rd = nan, gg = nan, ti = nan, pi = nan;
+                    if (cls == 1) {
+                        rd = 30.0 * y[3];
+                        gg = __expf(y[4]);
+                    } else if (cls == 2) {
+                        const float nrm = sqrtf(y[5] * y[5] + y[6] * y[6] + y[7] * y[7]);
+                        const float dz = fminf(1.0f, fmaxf(-1.0f, y[7] / nrm));
+                        ti = acosf(dz);
+                        pi = atan2f(y[6], y[5]);
+                    }
+                    const SurFrame& f = ia.frames[fi[v]];
+                    bool band = false;
+                    if (f.curve_ok) {
+                        const float da = alpha[v] - f.alpha_c, ab_ = fabsf(beta[v]);
+                        const float psi = atan2f(ab_, da);
+                        const int jb = min(kCurveBins - 1, max(0, static_cast<int>(psi * (kCurveBins / 3.14159265f))));
+                        band = fabsf(sqrtf(da * da + ab_ * ab_) - f.rho[jb]) * f.kn[jb] < ia.band;
+                    }
+                    // Answers limited to captured rays carry no continuous output, so where the class
+                    // is right they are exactly the tracer's (the network's r_disk, g and direction
+                    // are not used).
+                    fb = pmax < ia.p_min || band || fabsf(alpha[v]) < f.snap || !(zsum == zsum) ||
+                         (ia.accept == BHK_ACCEPT_CAPTURED && cls != 0);
+                    const long long r = ray[v];
+                    ia.outcome[r] = static_cast<uint8_t>(cls + 1);
+                    if (ia.r_disk) ia.r_disk[r] = rd;
+                    if (ia.phi_disk) ia.phi_disk[r] = nan;
+                    if (ia.g) ia.g[r] = gg;
+                    if (ia.theta_inf) ia.theta_inf[r] = ti;
+                    if (ia.phi_inf) ia.phi_inf[r] = pi;
+                    if (ia.steps) ia.steps[r] = 0;
+                    if (ia.rejected) ia.rejected[r] = 0;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, fb);
+                if (m) {
+                    unsigned long long b0 = 0;
+                    if (lane == 0) b0 = atomicAdd(ia.n_list, static_cast<unsigned long long>(__popc(m)));
+                    b0 = __shfl_sync(0xffffffffu, b0, 0);
+                    if (fb) ia.list[b0 + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(ray[v]);
+                }
             }
         }
     }
