@@ -127,8 +127,12 @@ __device__ __forceinline__ float warp_colsum16(const float (&x)[16], int lane, i
     return v;
 }
 
+// Threads of a GEMM CTA: thread 0 loads and issues; in the epilogue, warps w and w + 4 read TMEM lane
+// quadrant w and split the tile's columns (BN >= 32; a 16-wide tile uses warps 0-3 alone).
+constexpr int kGemmThreads = 256;
+
 template <int BN, int EPI>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kGemmThreads, 2)
 gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
             int k_per_split, int* err) {
     constexpr int kStages = gemm_stages<BN>();
@@ -216,21 +220,28 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int acc_ready = __syncthreads_and(tc::mbar_wait(accbar, 0) ? 1 : 0);
     tc::fence_after_sync();
     if (!acc_ready && threadIdx.x == 0) atomicExch(err, 1);
+    constexpr int kJ = BN / 16;                      // 16-column groups of the tile
+    constexpr int kSplit = kJ >= 2 ? 2 : 1;          // warps sharing a lane quadrant
+    const int quad = warp & 3, part = warp >> 2;     // TMEM lane quadrant, share of the columns
+    const int j_lo = part * kJ / kSplit, j_hi = (part + 1) * kJ / kSplit;
+    // The decision to run the epilogue was taken by the whole CTA; warps without columns (a 16-wide
+    // tile's second four) only join the block barriers.
+    const bool has_cols = part < kSplit;
     if (acc_ready && !*fail && nchunks > 0) {
-        const int row = 32 * warp + lane;
+        const int row = 32 * quad + lane;
         const int m = m0 + row;
         const bool live = m < ea.M;
         // The pipeline's shared memory is idle now: 1 KB of transpose staging per warp, then the
         // CTA's column sums.
         bf16* stage = reinterpret_cast<bf16*>(sA + warp * 1024);
-        float* scol = reinterpret_cast<float*>(sA + 4096);
+        float* scol = reinterpret_cast<float*>(sA + 8192);
         if constexpr (EPI == kDsilu) {
             for (int i = threadIdx.x; i < BN; i += blockDim.x) scol[i] = 0.0f;
             __syncthreads();
         }
         // The accumulator is read 16 columns at a time, the next load in flight while the current
         // columns are processed (kDsilu: the pre-activations of both also loaded ahead).
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * warp) << 16);
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16);
         auto zload = [&](int j, uint4 (&zp)[2]) {
             if constexpr (EPI == kDsilu) {
                 const int nb = n0 + 16 * j;
@@ -293,7 +304,7 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 } else {
                     for (int i = 0; i < 16; ++i) ab[i] = __float2bfloat16_rn(0.0f);
                 }
-                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * warp, ea.M, ab, stage, lane);
+                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * quad, ea.M, ab, stage, lane);
             } else {  // kDsilu: d(pre-activation) = dA * silu'(z); bias gradient = column sums
                 float dz[16];
                 __align__(16) bf16 ob[16];
@@ -316,7 +327,7 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                         ob[i] = __float2bfloat16_rn(0.0f);
                     }
                 }
-                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * warp, ea.M, ob, stage, lane);
+                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * quad, ea.M, ob, stage, lane);
                 if (ea.colsum) {
                     int col;
                     const float tot = warp_colsum16(dz, lane, col);
@@ -324,27 +335,28 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 }
             }
                 };
-        constexpr int kJ = BN / 16;
-        uint32_t ra[16], rb[16];
-        uint4 za[2] = {}, zb2[2] = {};
-        tc::tmem_ld16_issue(trow, ra);
-        zload(0, za);
-        tc::tmem_wait16(ra);
+        if (has_cols) {
+            uint32_t ra[16], rb[16];
+            uint4 za[2] = {}, zb2[2] = {};
+            tc::tmem_ld16_issue(trow + 16 * j_lo, ra);
+            zload(j_lo, za);
+            tc::tmem_wait16(ra);
 #pragma unroll 1
-        for (int j = 0; j < kJ; j += 2) {
-            if (j + 1 < kJ) {
-                tc::tmem_ld16_issue(trow + 16 * (j + 1), rb);
-                zload(j + 1, zb2);
+            for (int j = j_lo; j < j_hi; j += 2) {
+                if (j + 1 < j_hi) {
+                    tc::tmem_ld16_issue(trow + 16 * (j + 1), rb);
+                    zload(j + 1, zb2);
+                }
+                process(j, ra, za);
+                if (j + 1 >= j_hi) break;
+                tc::tmem_wait16(rb);
+                if (j + 2 < j_hi) {
+                    tc::tmem_ld16_issue(trow + 16 * (j + 2), ra);
+                    zload(j + 2, za);
+                }
+                process(j + 1, rb, zb2);
+                if (j + 2 < j_hi) tc::tmem_wait16(ra);
             }
-            process(j, ra, za);
-            if (j + 1 >= kJ) break;
-            tc::tmem_wait16(rb);
-            if (j + 2 < kJ) {
-                tc::tmem_ld16_issue(trow + 16 * (j + 2), ra);
-                zload(j + 2, za);
-            }
-            process(j + 1, rb, zb2);
-            if (j + 2 < kJ) tc::tmem_wait16(ra);
         }
         if constexpr (EPI == kDsilu) {
             __syncthreads();
@@ -417,7 +429,7 @@ cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const Epi
     splits = splits < 1 ? 1 : splits;
     const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
     const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
-    gemm_kernel<BN, EPI><<<grid, 128, gemm_smem_bytes<BN>(), s>>>(a, b, ea, K, per, err);
+    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN>(), s>>>(a, b, ea, K, per, err);
     return cudaGetLastError();
 }
 
