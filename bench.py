@@ -55,6 +55,22 @@ SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.act
 T_START = time.perf_counter()
 
 
+def tracer_roofline(acc_steps: float, rej_steps: float, kernel_ms: float, peak: float) -> dict:
+    """FP32 roofline of the trace kernel: the FLOPs of every Dormand-Prince attempt it made (accepted steps
+    at bhk_flops_per_step, rejected attempts, which run the same stages and error norm, at
+    bhk_flops_per_rejected_step) over its CUDA-event time, against the measured FP32 FMA peak. The
+    accepted-only fraction is kept beside it."""
+    from black_simulation_gb300 import bhk
+    fa, fr = bhk.flops_per_step(), bhk.flops_per_rejected_step()
+    flops = acc_steps * fa + rej_steps * fr
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    acc_only = acc_steps * fa / (kernel_ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "frac_accepted_steps_only": acc_only / peak, "kernel_ms": kernel_ms, "flops_per_step": fa,
+            "flops_per_rejected_step": fr, "rejected_fraction": rej_steps / max(1.0, acc_steps + rej_steps),
+            "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run"}
+
+
 def log(msg: str):
     """Progress of the run on stderr (seconds since start), so a long default run shows where its time goes."""
     sys.stderr.write(f"[bench {time.perf_counter() - T_START:7.1f} s] {msg}\n")
@@ -256,7 +272,7 @@ def batch_measurement(args, ctx, dev, steps: int = 5, warmup: int = 3) -> dict:
     for _ in range(warmup):
         ctx.trace_frames(frames, opts, out=out)
     torch.cuda.synchronize()
-    ms, kms, acc = [], [], []
+    ms, kms, acc, rej = [], [], [], []
     with Clocks(dev.index or 0) as clk:
         for _ in range(steps):
             flush.zero_()
@@ -269,6 +285,7 @@ def batch_measurement(args, ctx, dev, steps: int = 5, warmup: int = 3) -> dict:
             ms.append(a.elapsed_time(b))
             kms.append(st["kernel_ms"])
             acc.append(st["accepted_steps"])
+            rej.append(st["rejected_steps"])
     errs = fp64_check(ctx, frames, out, dev, 1e-3, 65536, args.seed + 2)
     counts = {k: int(v) for k, v in zip(*np.unique(out["outcome"].cpu().numpy(), return_counts=True))}
     del out
@@ -282,18 +299,15 @@ def batch_measurement(args, ctx, dev, steps: int = 5, warmup: int = 3) -> dict:
     d2h = sum(v.numel() * v.element_size() for v in pinned.values())
     del pinned
     peak = bhk.fp32_fma_peak_tflops(dev.index or 0)
-    fps = bhk.flops_per_step()
     k_ms = float(np.mean(kms))
-    achieved = float(np.mean(acc)) * fps / (k_ms * 1e-3) / 1e12
+    roof = tracer_roofline(float(np.mean(acc)), float(np.mean(rej)), k_ms, peak)
     return {"workload": cfg["workload"], "rays": n, "steps": steps, "warmup": warmup, "precision": cfg["precision"],
             "rtol": opts.rtol, "launch": {**{k: tuned[k] for k in ("block", "chunk", "sort_buckets", "reg_budget")},
                                           "graph": True, "autotuned": True},
             "value": n / (float(np.mean(ms)) * 1e-3), "unit": "rays/s", "ms_per_step": float(np.mean(ms)),
             "e2e": {"value": n / float(np.mean(e2e)), "unit": "rays/s", "h2d_bytes_per_step":
                     len(frames) * bhk.C.sizeof(bhk.FrameDescC), "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None, "kernel_ms": k_ms, "flops_per_step": fps,
-                         "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run"},
+            "roofline": {**roof, "traffic": None},
             "mean_accepted_steps_per_ray": float(np.mean(acc)) / n,
             "outcomes": {"captured": counts.get(1, 0), "disk": counts.get(2, 0), "escaped": counts.get(3, 0),
                          "unfinished": counts.get(0, 0)},
@@ -358,9 +372,8 @@ def run_ours(args):
     d2h = sum(v.numel() * v.element_size() for v in pinned.values())
     h2d = len(frames) * bhk.C.sizeof(bhk.FrameDescC)
     peak = bhk.fp32_fma_peak_tflops(local)
-    fps = bhk.flops_per_step()
     k_ms = float(np.mean(kernel_ms))
-    achieved = float(np.mean(acc_steps)) * fps / (k_ms * 1e-3) / 1e12
+    roof = tracer_roofline(float(np.mean(acc_steps)), float(np.mean(rej_steps)), k_ms, peak)
     counts = {k: int(v) for k, v in zip(*np.unique(pinned["outcome"].numpy(), return_counts=True))}
     line = {
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -377,12 +390,8 @@ def run_ours(args):
                    "rescued_rays": int(np.mean(rescued)), "wall_s": wall},
         "e2e": {"value": world * n_rays / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC.get(args.workload) if args.scale == 1 else None,
-                     "algorithmic_bytes": BYTES_PER_RAY * n_rays,
-                     "peak_source": "measured FP32 FMA throughput (bhk_fp32_fma_peak) in this run",
-                     "kernel_ms": k_ms, "flops_per_step": fps},
+        "roofline": {**roof, "traffic": NCU_TRAFFIC.get(args.workload) if args.scale == 1 else None,
+                     "algorithmic_bytes": BYTES_PER_RAY * n_rays},
         "gpu_launches": 2 * args.steps,  # per step: trace (with the launch and the tile order), rescue
         "clocks": clk.summary(),
     }

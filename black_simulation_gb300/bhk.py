@@ -157,6 +157,7 @@ def lib() -> C.CDLL:
         "bhk_last_error": (C.c_char_p, []),
         "bhk_version": (C.c_char_p, []),
         "bhk_flops_per_step": (d, []),
+        "bhk_flops_per_rejected_step": (d, []),
         "bhk_derivatives": (C.c_int, [d, vp, vp, vp, i64, vp]),
         "bhk_step_mino": (C.c_int, [d, vp, vp, vp, i64, vp]),
         "bhk_photon_step_size": (C.c_int, [d, vp, vp, d, vp, i64, vp]),
@@ -442,6 +443,10 @@ def predict(a: float, c, s, max_time: float, min_spacing: float = 0.5, max_point
 
 def flops_per_step() -> float:
     return float(lib().bhk_flops_per_step())
+
+
+def flops_per_rejected_step() -> float:
+    return float(lib().bhk_flops_per_rejected_step())
 
 
 def tc_gemm(A, B, splits: int = 1, stream=None):

@@ -66,7 +66,9 @@ struct GraphKey {
 //   stage sums y + h sum_j a_ij k_j over 5 components (bhk_trace.cu stage_f32): per stage of M terms
 //     and component a product, M - 1 FMA and the FMA by h, 2M + 1 -> 5 x (2 x 20 + 6) = 230;
 //   error estimate and weighted norm: 5 x 16 + 2 = 82;  step control and pole cap: 8.
+// A rejected attempt does the same stages, sums and norm, then only shrinks the step (3 products).
 constexpr double kFlopsPerStep = 617.0;
+constexpr double kFlopsPerRejected = 282.0 + 15.0 + 230.0 + 82.0 + 3.0;
 
 }  // namespace
 
@@ -456,6 +458,7 @@ bhk_status bhk_trace_pixels(bhk_context* c, const bhk_frame_desc* frames, int32_
 const char* bhk_last_error(void) { return g_last_error.c_str(); }
 const char* bhk_version(void) { return "bhk 0.1 (sm_103a)"; }
 double bhk_flops_per_step(void) { return kFlopsPerStep; }
+double bhk_flops_per_rejected_step(void) { return kFlopsPerRejected; }
 
 bhk_status bhk_create(int device, bhk_context** out) {
     if (!out) return fail(BHK_EINVAL, "out is null");

@@ -283,6 +283,8 @@ bhk_status bhk_eht_calibrate(const bhk_eht_view* view, const bhk_eht_flow* flow,
 
 /* FLOPs one accepted FP32 Dormand-Prince step costs in the mixed tracer, counted from its source. */
 double bhk_flops_per_step(void);
+/* FLOPs of a rejected FP32 attempt: the same stages, sums and error norm, only the step shrink after. */
+double bhk_flops_per_rejected_step(void);
 
 /* Diagnostic: C (M x N, FP32, row-major) = A (M x K) * B (N x K)^T, A and B BF16 row-major in device
  * memory, on the surrogate's tcgen05 GEMM kernel (TMA, TMEM accumulator). N <= 256, K % 8 == 0.

@@ -26,6 +26,8 @@ def test_every_declared_symbol_is_exported(libbhk):
 def test_version_and_flop_count(libbhk):
     assert b"sm_103a" in libbhk.bhk_version()
     assert bhk.flops_per_step() > 100
+    # a rejected attempt runs the stages and the error norm, not the accepted step's tail
+    assert 0.9 * bhk.flops_per_step() < bhk.flops_per_rejected_step() < bhk.flops_per_step()
 
 
 def test_struct_layouts_match_header():
