@@ -54,17 +54,18 @@ struct EpiArgs {
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
 };
 
-// Pipeline depth by tile width: two CTAs (each 256 TMEM columns at most) fit on an SM, so one
-// CTA's epilogue overlaps the other's main loop; the network's K is at most 256 (4 chunks), except
-// for split-K weight gradients.
-template <int BN>
+// Pipeline depth: the network's GEMMs have K <= 256 (4 chunks) and run two CTAs (each 256 TMEM
+// columns at most) per SM, so that one CTA's epilogue overlaps the other's main loop. The split-K
+// weight gradients stream long K ranges (~14 chunks a CTA) with a light epilogue: one CTA per SM with
+// a deep ring, so that the TMA latency of the next chunks hides behind the current MMAs.
+template <int BN, int EPI>
 __host__ __device__ constexpr int gemm_stages() {
-    return BN >= 256 ? 2 : 4;
+    return EPI == kPartialF32 ? (BN >= 256 ? 4 : 8) : (BN >= 256 ? 2 : 4);
 }
 
-template <int BN>
+template <int BN, int EPI>
 __host__ __device__ constexpr int gemm_smem_bytes() {
-    return gemm_stages<BN>() * (kABytes + BN * kChunkK * 2) + 1024 + 256;
+    return gemm_stages<BN, EPI>() * (kABytes + BN * kChunkK * 2) + 1024 + 256;
 }
 
 // Logistic sigmoid as 1/2 + tanh(z/2)/2 on the hardware tanh (one MUFU operation; relative error of
@@ -135,7 +136,7 @@ template <int BN, int EPI>
 __global__ void __launch_bounds__(kGemmThreads, 2)
 gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
             int k_per_split, int* err) {
-    constexpr int kStages = gemm_stages<BN>();
+    constexpr int kStages = gemm_stages<BN, EPI>();
     constexpr int kBBytes = BN * kChunkK * 2;
     constexpr uint32_t kCols = BN < 32 ? 32 : BN;
     constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, BN);
@@ -370,19 +371,42 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 }
 
 // dst[i] += sum over the splits of ws[split * count + i] (count a multiple of 4, 16-byte aligned).
-__global__ void reduce_splits_kernel(const float* __restrict__ ws, int splits, long long count, float* dst) {
+// A block of 256 threads takes 32 float4 of dst at a time: warp g sums splits g, g + 8, g + 16, ...
+// of them (each warp load is 512 contiguous bytes), and warp 0 adds the eight partial sums to dst in
+// warp order, so the result does not depend on timing.
+constexpr int kReduceGroups = 8;
+__global__ void __launch_bounds__(32 * kReduceGroups)
+reduce_splits_kernel(const float* __restrict__ ws, int splits, long long count, float* dst) {
+    __shared__ float4 part[kReduceGroups][32];
     const long long n4 = count / 4;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n4;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        float4 acc = reinterpret_cast<float4*>(dst)[i];
-        for (int sp = 0; sp < splits; ++sp) {
-            const float4 w = reinterpret_cast<const float4*>(ws + sp * count)[i];
-            acc.x += w.x;
-            acc.y += w.y;
-            acc.z += w.z;
-            acc.w += w.w;
+    const int c = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const float4* w4 = reinterpret_cast<const float4*>(ws);
+    for (long long base = blockIdx.x * 32LL; base < n4; base += static_cast<long long>(gridDim.x) * 32) {
+        const long long i = base + c;
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (i < n4) {
+            for (int sp = g; sp < splits; sp += kReduceGroups) {
+                const float4 w = w4[sp * n4 + i];
+                acc.x += w.x;
+                acc.y += w.y;
+                acc.z += w.z;
+                acc.w += w.w;
+            }
         }
-        reinterpret_cast<float4*>(dst)[i] = acc;
+        part[g][c] = acc;
+        __syncthreads();
+        if (g == 0 && i < n4) {
+            float4 d = reinterpret_cast<float4*>(dst)[i];
+#pragma unroll
+            for (int q = 0; q < kReduceGroups; ++q) {
+                d.x += part[q][c].x;
+                d.y += part[q][c].y;
+                d.z += part[q][c].z;
+                d.w += part[q][c].w;
+            }
+            reinterpret_cast<float4*>(dst)[i] = d;
+        }
+        __syncthreads();
     }
 }
 
@@ -424,12 +448,13 @@ cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const Epi
                            int splits, int* err, cudaStream_t s) {
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem_bytes<BN>());
+        cudaFuncSetAttribute(gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             gemm_smem_bytes<BN, EPI>());
     });
     splits = splits < 1 ? 1 : splits;
     const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
     const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
-    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN>(), s>>>(a, b, ea, K, per, err);
+    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, ea, K, per, err);
     return cudaGetLastError();
 }
 
@@ -700,6 +725,7 @@ struct bhk_surrogate {
     int device = 0;
     int cap = 0;  // batch capacity (rows of every activation buffer)
     int hid = bhk::sur::kHidDefault;  // hidden width
+    int sms = 1;  // the device's SM count (grid sizes)
     bhk::sur::ParamLayout L;
     float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     bhk::sur::bf16* w_rm[bhk::sur::kLayers] = {};
@@ -810,21 +836,30 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, bool keep_t, cudaStr
     return e;
 }
 
-int split_for(int n) {
-    const int s = n / 1024;
-    return s < 1 ? 1 : (s > 96 ? 96 : s);
+// K splits of a weight gradient (M x N, K = n rows): one CTA per SM over the M tiles, each split at
+// least 512 rows, and at most what the workspace (96 x H x max(H, 64) floats) holds.
+int split_for(const bhk_surrogate* s, int n, int M, int N) {
+    const int mtiles = (M + kTileM - 1) / kTileM;
+    const long long ws_floats = 96LL * s->hid * std::max(s->hid, kFeat);
+    long long sp = s->sms / mtiles;
+    sp = std::min<long long>(sp, n / 512);
+    sp = std::min<long long>(sp, ws_floats / (static_cast<long long>(M) * N));
+    return sp < 1 ? 1 : static_cast<int>(sp);
 }
 
 // dst (M x N FP32, dense) += A^T-style weight gradient: the split-K partial products go to the
 // workspace with plain stores, then one pass sums them into dst.
-cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, int splits,
-                        float* dst, cudaStream_t st) {
+cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, float* dst,
+                        cudaStream_t st) {
+    const int splits = split_for(s, K, M, N);
     EpiArgs ea = epi(M, N);
     ea.f32 = s->ws;
     ea.ld_f32 = N;
     cudaError_t e = launch_gemm<kPartialF32>(A, B, ea, M, N, K, splits, s->err, st);
     if (e != cudaSuccess) return e;
-    reduce_splits_kernel<<<256, 256, 0, st>>>(s->ws, grid_splits(K, splits), static_cast<long long>(M) * N, dst);
+    const long long count = static_cast<long long>(M) * N;
+    const int blocks = static_cast<int>(std::min<long long>((count / 4 + 31) / 32, 8LL * s->sms));
+    reduce_splits_kernel<<<blocks, 32 * kReduceGroups, 0, st>>>(s->ws, grid_splits(K, splits), count, dst);
     return cudaGetLastError();
 }
 
@@ -834,10 +869,9 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     if (e != cudaSuccess) return e;
     loss_kernel<<<(n + 255) / 256, 256, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
                                                  s->loss, n, 1.0f / n, s->w);
-    const int splits = split_for(n);
     const int H = s->hid;
     // Head: dW5 = dY^T A4, then dA4 = dY W5 -> dZ4.
-    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, H, n, splits, s->g + s->L.w[4], st);
+    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, H, n, s->g + s->L.w[4], st);
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, H);
         ea.rm = s->dz_rm[0];
@@ -852,7 +886,7 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
         const CUtensorMap& Bop = l == 0 ? M.F_t : M.a_t[l - 1];
-        e = weight_grad(s, M.dz_t[cur], Bop, H, fan_in(l, H), n, splits, s->g + s->L.w[l], st);
+        e = weight_grad(s, M.dz_t[cur], Bop, H, fan_in(l, H), n, s->g + s->L.w[l], st);
         if (e != cudaSuccess || l == 0) break;
         EpiArgs ex = epi(n, H);
         ex.rm = s->dz_rm[1 - cur];
@@ -922,6 +956,7 @@ bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_bat
     auto* s = new bhk_surrogate();
     s->device = device;
     s->cap = max_batch;
+    if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || s->sms < 1) s->sms = 1;
     s->hid = width;
     s->L = ParamLayout(width);
     const int H = width;
