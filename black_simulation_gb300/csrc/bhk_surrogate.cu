@@ -46,11 +46,8 @@ struct EpiArgs {
     float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32; kPartialF32: split z
                            // writes its partial product at f32 + z * M * ld_f32
     int ld_f32;
-    bf16* rm;              // row-major BF16 output [M x ld_rm]
-    int ld_rm;
-    bf16* t;               // transposed BF16 output [N x ld_t]
-    int ld_t;
-    bf16* z;               // kBiasSilu: pre-activation written here; kDsilu: pre-activation read here
+    int store_t;           // kBiasSilu / kDsilu: also write the transposed BF16 output (the BF16
+                           // outputs and the pre-activations go through the kernel's tensor maps)
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
 };
 
@@ -65,7 +62,7 @@ __host__ __device__ constexpr int gemm_stages() {
 
 template <int BN, int EPI>
 __host__ __device__ constexpr int gemm_smem_bytes() {
-    return gemm_stages<BN, EPI>() * (kABytes + BN * kChunkK * 2) + 1024 + 256;
+    return gemm_stages<BN, EPI>() * (kABytes + BN * kChunkK * 2) + 1024 + 256 + BN * 4;
 }
 
 // Logistic sigmoid as 1/2 + tanh(z/2)/2 on the hardware tanh (one MUFU operation; relative error of
@@ -86,29 +83,6 @@ __device__ __forceinline__ uint32_t silu2_half(float h0, float h1) {
     asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(hb));
     asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(a) : "r"(hb), "r"(t));
     return a;
-}
-
-// Writes this warp's 32 rows x 16 columns (lane = row, vals = its 16 values) transposed into
-// t[(nb + i) * ld + m0w + lane], through a 1 KB per-warp staging area in shared memory, as 16-byte
-// vectors (rows at or past M are not written).
-__device__ __forceinline__ void store_transposed16(bf16* t, int ld, int nb, int m0w, int M, const bf16* vals,
-                                                   bf16* stage, int lane) {
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < 16; ++i) stage[i * 32 + lane] = vals[i];
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const int v = lane + 32 * k, i = v >> 2, part = v & 3;
-        const int r0 = m0w + part * 8;
-        bf16* dst = t + static_cast<size_t>(nb + i) * ld + r0;
-        const bf16* src = stage + i * 32 + part * 8;
-        if (r0 + 8 <= M) {
-            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
-        } else {
-            for (int q = 0; q < 8 && r0 + q < M; ++q) dst[q] = src[q];
-        }
-    }
 }
 
 // Sums each of 16 per-lane values over the warp's 32 lanes by recursive halving (16 shuffles). The
@@ -132,10 +106,147 @@ __device__ __forceinline__ float warp_colsum16(const float (&x)[16], int lane, i
 // quadrant w and split the tile's columns (BN >= 32; a 16-wide tile uses warps 0-3 alone).
 constexpr int kGemmThreads = 256;
 
+// Shared memory a warp of the staged epilogue uses (three 4 KB TMA boxes), carved from the idle ring.
+constexpr int kWarpStage = 12288;
+
+// Staged epilogue of the hidden layers (kBiasSilu: Z = acc + b and A = silu(Z); kDsilu: dZ = acc *
+// silu'(Z) and the bias gradient). Warp (quad, part) owns the 32 rows of TMEM lane quadrant `quad` and
+// kBoxes 64-column boxes of the tile. Each box's outputs are written into shared memory in the layout of
+// a TMA box -- row-major [32 rows][64 columns] under the 128-byte swizzle (the 16-byte chunk c of row r at
+// chunk c ^ (r & 7)) and transposed [64 columns][32 rows] -- and leave with one TMA tensor store per
+// output, so a warp issues a few bulk stores per box instead of 32-row scattered vector stores. kDsilu
+// reads Z the same way: TMA loads of the warp's boxes, dZ written over them in place. sx holds the
+// tile's bias (kBiasSilu) or its column sums (kDsilu). Returns false if a wait for the Z loads timed out.
+template <int BN, int EPI>
+__device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CUtensorMap* tmR, const CUtensorMap* tmT,
+                                                const EpiArgs& ea, uint32_t tmem, uint8_t* stage_base, float* sx,
+                                                uint64_t* zbar, int m0, int n0) {
+    static_assert(BN % 64 == 0, "the staged epilogue works on 64-column boxes");
+    constexpr int kSplitS = BN >= 128 ? 2 : 1;   // warps sharing a lane quadrant
+    constexpr int kBoxes = BN / (64 * kSplitS);  // boxes per warp
+    constexpr int kG = 4 * kBoxes;               // 16-column groups per warp
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quad = warp & 3, part = warp >> 2;
+    if constexpr (EPI == kBiasSilu) {
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) sx[i] = n0 + i < ea.N ? ea.bias[n0 + i] : 0.0f;
+    } else {
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) sx[i] = 0.0f;
+    }
+    __syncthreads();
+    bool ok = true;
+    if (part < kSplitS) {
+        uint8_t* wb = stage_base + warp * kWarpStage;
+        const int y0 = m0 + 32 * quad;
+        const bool live = y0 + lane < ea.M;
+        const int c_lo = part * kBoxes * 64;  // the warp's first tile column
+        if constexpr (EPI == kDsilu) {
+            if (lane == 0) {
+                tc::mbar_expect_tx(&zbar[warp], kBoxes * 4096);
+                for (int b = 0; b < kBoxes; ++b) tc::tma_load_2d(wb + b * 4096, tmZ, n0 + c_lo + 64 * b, y0, &zbar[warp]);
+            }
+        }
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16);
+        const int sw = lane & 7;
+        bf16* T = reinterpret_cast<bf16*>(wb + 8192);
+        auto process = [&](int gi, const uint32_t (&r)[16]) {
+            const int b = gi >> 2, g = gi & 3, cb = c_lo + 16 * gi;
+            if (g == 0 && b > 0) {  // the previous box's stores must have read the staging it reuses
+                if (lane == 0) tc::bulk_wait_read_all();
+                __syncwarp();
+            }
+            __align__(16) bf16 ob[16];
+            if constexpr (EPI == kBiasSilu) {
+                __align__(16) bf16 zb[16];
+#pragma unroll
+                for (int i = 0; i < 16; i += 2) {
+                    const float z0 = __uint_as_float(r[i]) + sx[cb + i], z1 = __uint_as_float(r[i + 1]) + sx[cb + i + 1];
+                    zb[i] = __float2bfloat16_rn(z0);
+                    zb[i + 1] = __float2bfloat16_rn(z1);
+                    *reinterpret_cast<uint32_t*>(&ob[i]) = silu2_half(0.5f * z0, 0.5f * z1);
+                }
+                uint4* zrow = reinterpret_cast<uint4*>(wb + lane * 128);
+                uint4* arow = reinterpret_cast<uint4*>(wb + 4096 + lane * 128);
+                zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(zb)[0];
+                zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(zb)[1];
+                arow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
+                arow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
+            } else {
+                uint4* zrow = reinterpret_cast<uint4*>(wb + b * 4096 + lane * 128);
+                __align__(16) bf16 zin[16];
+                reinterpret_cast<uint4*>(zin)[0] = zrow[(2 * g) ^ sw];
+                reinterpret_cast<uint4*>(zin)[1] = zrow[(2 * g + 1) ^ sw];
+                float dz[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const float z = __bfloat162float(zin[i]);
+                    const float sg = sigmoidf(z);
+                    dz[i] = live ? __uint_as_float(r[i]) * sg * (1.0f + z * (1.0f - sg)) : 0.0f;
+                    ob[i] = __float2bfloat16_rn(dz[i]);
+                }
+                zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
+                zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
+                if (ea.colsum) {
+                    int col;
+                    const float tot = warp_colsum16(dz, lane, col);
+                    if (!(lane & 1)) atomicAdd(&sx[cb + col], tot);
+                }
+            }
+            if (ea.store_t) {
+                const bf16 zero = __float2bfloat16_rn(0.0f);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) T[(16 * g + i) * 32 + lane] = live ? ob[i] : zero;
+            }
+            if (g == 3) {  // the box is complete: hand it to the TMA unit
+                tc::fence_proxy_async();
+                __syncwarp();
+                if (lane == 0) {
+                    const int x = n0 + c_lo + 64 * b;
+                    if constexpr (EPI == kBiasSilu) {
+                        tc::tma_store_2d(tmZ, wb, x, y0);
+                        tc::tma_store_2d(tmR, wb + 4096, x, y0);
+                    } else {
+                        tc::tma_store_2d(tmR, wb + b * 4096, x, y0);
+                    }
+                    if (ea.store_t) tc::tma_store_2d(tmT, T, y0, x);
+                    tc::bulk_commit();
+                }
+            }
+        };
+        uint32_t ra[16], rb[16];
+        tc::tmem_ld16_issue(trow + c_lo, ra);
+        if constexpr (EPI == kDsilu) {
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&zbar[warp], 0) ? 1 : 0) != 0;
+            // A timed-out wait: give the loads in flight a second bounded wait before the CTA exits.
+            if (!ok) tc::mbar_wait(&zbar[warp], 0);
+        }
+        tc::tmem_wait16(ra);
+        if (ok) {
+#pragma unroll 1
+            for (int gi = 0; gi < kG; gi += 2) {
+                tc::tmem_ld16_issue(trow + c_lo + 16 * (gi + 1), rb);
+                process(gi, ra);
+                tc::tmem_wait16(rb);
+                if (gi + 2 < kG) tc::tmem_ld16_issue(trow + c_lo + 16 * (gi + 2), ra);
+                process(gi + 1, rb);
+                if (gi + 2 < kG) tc::tmem_wait16(ra);
+            }
+        }
+        if (lane == 0) tc::bulk_wait_all();
+        __syncwarp();
+    }
+    if constexpr (EPI == kDsilu) {
+        __syncthreads();
+        if (ea.colsum)
+            for (int i = threadIdx.x; i < BN && n0 + i < ea.N; i += blockDim.x) atomicAdd(&ea.colsum[n0 + i], sx[i]);
+    }
+    return ok;
+}
+
 template <int BN, int EPI>
 __global__ void __launch_bounds__(kGemmThreads, 2)
-gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, EpiArgs ea, int K,
-            int k_per_split, int* err) {
+gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+            const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR,
+            const __grid_constant__ CUtensorMap tmT, EpiArgs ea, int K, int k_per_split, int* err) {
     constexpr int kStages = gemm_stages<BN, EPI>();
     constexpr int kBBytes = BN * kChunkK * 2;
     constexpr uint32_t kCols = BN < 32 ? 32 : BN;
@@ -147,8 +258,10 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * kBBytes);
     uint64_t* empty = full + kStages;
     uint64_t* accbar = empty + kStages;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accbar + 1);
+    uint64_t* zbar = accbar + 1;  // one per warp: the staged epilogue's Z loads (kDsilu)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(zbar + kGemmThreads / 32);
     int* fail = reinterpret_cast<int*>(tmem_slot + 1);
+    float* sx = reinterpret_cast<float*>(full) + 64;  // past the barriers (<= 256 bytes): BN floats
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * BN;
@@ -162,6 +275,7 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             tc::mbar_init(&empty[s], 1);
         }
         tc::mbar_init(accbar, 1);
+        for (int w = 0; w < kGemmThreads / 32; ++w) tc::mbar_init(&zbar[w], 1);
         *fail = 0;
         tc::fence_mbar_init();
         tc::prefetch_tmap(&tmA);
@@ -221,54 +335,35 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int acc_ready = __syncthreads_and(tc::mbar_wait(accbar, 0) ? 1 : 0);
     tc::fence_after_sync();
     if (!acc_ready && threadIdx.x == 0) atomicExch(err, 1);
-    constexpr int kJ = BN / 16;                      // 16-column groups of the tile
-    constexpr int kSplit = kJ >= 2 ? 2 : 1;          // warps sharing a lane quadrant
-    const int quad = warp & 3, part = warp >> 2;     // TMEM lane quadrant, share of the columns
-    const int j_lo = part * kJ / kSplit, j_hi = (part + 1) * kJ / kSplit;
-    // The decision to run the epilogue was taken by the whole CTA; warps without columns (a 16-wide
-    // tile's second four) only join the block barriers.
-    const bool has_cols = part < kSplit;
     if (acc_ready && !*fail && nchunks > 0) {
-        const int row = 32 * quad + lane;
-        const int m = m0 + row;
-        const bool live = m < ea.M;
-        // The pipeline's shared memory is idle now: 1 KB of transpose staging per warp, then the
-        // CTA's column sums.
-        bf16* stage = reinterpret_cast<bf16*>(sA + warp * 1024);
-        float* scol = reinterpret_cast<float*>(sA + 8192);
-        if constexpr (EPI == kDsilu) {
-            for (int i = threadIdx.x; i < BN; i += blockDim.x) scol[i] = 0.0f;
-            __syncthreads();
-        }
-        // The accumulator is read 16 columns at a time, the next load in flight while the current
-        // columns are processed (kDsilu: the pre-activations of both also loaded ahead).
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16);
-        auto zload = [&](int j, uint4 (&zp)[2]) {
-            if constexpr (EPI == kDsilu) {
-                const int nb = n0 + 16 * j;
-                if (live && nb < ea.N) {
-                    const uint4* zs = reinterpret_cast<const uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
-                    zp[0] = zs[0];
-                    zp[1] = zs[1];
-                }
-            }
-        };
-        auto process = [&](int j, const uint32_t (&r)[16], const uint4 (&zpre)[2]) {
-            float v[16];
+        if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
+            // The pipeline's shared memory is idle now: it holds the warps' output boxes.
+            if (!epilogue_staged<BN, EPI>(&tmZ, &tmR, &tmT, ea, tmem, sA, sx, zbar, m0, n0)) atomicExch(err, 1);
+        } else {
+            constexpr int kJ = BN / 16;                  // 16-column groups of the tile
+            constexpr int kSplit = kJ >= 2 ? 2 : 1;      // warps sharing a lane quadrant
+            const int quad = warp & 3, part = warp >> 2; // TMEM lane quadrant, share of the columns
+            const int j_lo = part * kJ / kSplit, j_hi = (part + 1) * kJ / kSplit;
+            const int row = 32 * quad + lane;
+            const int m = m0 + row;
+            const bool live = m < ea.M;
+            // The accumulator is read 16 columns at a time, the next load in flight while the current
+            // columns are processed.
+            const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16);
+            auto process = [&](int j, const uint32_t (&r)[16]) {
+                float v[16];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-            const int nb = n0 + 16 * j;
-            if (nb >= ea.N) return;
-            if constexpr (EPI == kStoreF32) {
-                if (live)
+                for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+                const int nb = n0 + 16 * j;
+                if (nb >= ea.N || !live) return;
+                if constexpr (EPI == kStoreF32) {
                     for (int i = 0; i < 16; ++i)
-                        if (nb + i < ea.N) ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i] = v[i] + (ea.bias ? ea.bias[nb + i] : 0.0f);
-            } else if constexpr (EPI == kAtomicF32) {
-                if (live)
+                        if (nb + i < ea.N)
+                            ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i] = v[i] + (ea.bias ? ea.bias[nb + i] : 0.0f);
+                } else if constexpr (EPI == kAtomicF32) {
                     for (int i = 0; i < 16; ++i)
                         if (nb + i < ea.N) atomicAdd(&ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i], v[i]);
-            } else if constexpr (EPI == kPartialF32) {
-                if (live) {
+                } else {  // kPartialF32: split z writes its partial product at f32 + z * M * ld_f32
                     float* dst = ea.f32 + static_cast<size_t>(blockIdx.z) * ea.M * ea.ld_f32 +
                                  static_cast<size_t>(m) * ea.ld_f32 + nb;
                     if (nb + 16 <= ea.N) {
@@ -279,90 +374,23 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                         for (int i = 0; i < 16 && nb + i < ea.N; ++i) dst[i] = v[i];
                     }
                 }
-            } else if constexpr (EPI == kBiasSilu) {
-                __align__(16) bf16 zb[16], ab[16];
-                if (live) {
-                    float bb[16];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const float4 b = __ldg(reinterpret_cast<const float4*>(ea.bias + nb) + q);
-                        bb[4 * q] = b.x; bb[4 * q + 1] = b.y; bb[4 * q + 2] = b.z; bb[4 * q + 3] = b.w;
-                    }
-#pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        const float z0 = v[i] + bb[i], z1 = v[i + 1] + bb[i + 1];
-                        zb[i] = __float2bfloat16_rn(z0);
-                        zb[i + 1] = __float2bfloat16_rn(z1);
-                        const uint32_t a2 = silu2_half(0.5f * z0, 0.5f * z1);
-                        *reinterpret_cast<uint32_t*>(&ab[i]) = a2;
-                    }
-                    uint4* zd = reinterpret_cast<uint4*>(ea.z + static_cast<size_t>(m) * ea.ld_rm + nb);
-                    uint4* ad = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
-                    zd[0] = reinterpret_cast<const uint4*>(zb)[0];
-                    zd[1] = reinterpret_cast<const uint4*>(zb)[1];
-                    ad[0] = reinterpret_cast<const uint4*>(ab)[0];
-                    ad[1] = reinterpret_cast<const uint4*>(ab)[1];
-                } else {
-                    for (int i = 0; i < 16; ++i) ab[i] = __float2bfloat16_rn(0.0f);
-                }
-                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * quad, ea.M, ab, stage, lane);
-            } else {  // kDsilu: d(pre-activation) = dA * silu'(z); bias gradient = column sums
-                float dz[16];
-                __align__(16) bf16 ob[16];
-                if (live) {
-                    __align__(16) bf16 zin[16];
-                    reinterpret_cast<uint4*>(zin)[0] = zpre[0];
-                    reinterpret_cast<uint4*>(zin)[1] = zpre[1];
-                    for (int i = 0; i < 16; ++i) {
-                        const float z = __bfloat162float(zin[i]);
-                        const float sg = sigmoidf(z);
-                        dz[i] = v[i] * sg * (1.0f + z * (1.0f - sg));
-                        ob[i] = __float2bfloat16_rn(dz[i]);
-                    }
-                    uint4* od = reinterpret_cast<uint4*>(ea.rm + static_cast<size_t>(m) * ea.ld_rm + nb);
-                    od[0] = reinterpret_cast<const uint4*>(ob)[0];
-                    od[1] = reinterpret_cast<const uint4*>(ob)[1];
-                } else {
-                    for (int i = 0; i < 16; ++i) {
-                        dz[i] = 0.0f;
-                        ob[i] = __float2bfloat16_rn(0.0f);
-                    }
-                }
-                if (ea.t) store_transposed16(ea.t, ea.ld_t, nb, m0 + 32 * quad, ea.M, ob, stage, lane);
-                if (ea.colsum) {
-                    int col;
-                    const float tot = warp_colsum16(dz, lane, col);
-                    if (!(lane & 1)) atomicAdd(&scol[16 * j + col], tot);
-                }
-            }
-                };
-        if (has_cols) {
-            uint32_t ra[16], rb[16];
-            uint4 za[2] = {}, zb2[2] = {};
-            tc::tmem_ld16_issue(trow + 16 * j_lo, ra);
-            zload(j_lo, za);
-            tc::tmem_wait16(ra);
+            };
+            // Warps without columns (a 16-wide tile's second four) have nothing to do.
+            if (part < kSplit) {
+                uint32_t ra[16], rb[16];
+                tc::tmem_ld16_issue(trow + 16 * j_lo, ra);
+                tc::tmem_wait16(ra);
 #pragma unroll 1
-            for (int j = j_lo; j < j_hi; j += 2) {
-                if (j + 1 < j_hi) {
-                    tc::tmem_ld16_issue(trow + 16 * (j + 1), rb);
-                    zload(j + 1, zb2);
+                for (int j = j_lo; j < j_hi; j += 2) {
+                    if (j + 1 < j_hi) tc::tmem_ld16_issue(trow + 16 * (j + 1), rb);
+                    process(j, ra);
+                    if (j + 1 >= j_hi) break;
+                    tc::tmem_wait16(rb);
+                    if (j + 2 < j_hi) tc::tmem_ld16_issue(trow + 16 * (j + 2), ra);
+                    process(j + 1, rb);
+                    if (j + 2 < j_hi) tc::tmem_wait16(ra);
                 }
-                process(j, ra, za);
-                if (j + 1 >= j_hi) break;
-                tc::tmem_wait16(rb);
-                if (j + 2 < j_hi) {
-                    tc::tmem_ld16_issue(trow + 16 * (j + 2), ra);
-                    zload(j + 2, za);
-                }
-                process(j + 1, rb, zb2);
-                if (j + 2 < j_hi) tc::tmem_wait16(ra);
             }
-        }
-        if constexpr (EPI == kDsilu) {
-            __syncthreads();
-            if (ea.colsum)
-                for (int i = threadIdx.x; i < BN && n0 + i < ea.N; i += blockDim.x) atomicAdd(&ea.colsum[n0 + i], scol[i]);
         }
     }
     tc::fence_before_sync();
@@ -430,22 +458,41 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // Tensor map of a row-major BF16 matrix [rows x cols] read in boxes of box_rows x 64 (128-byte
 // swizzle; reads past the matrix are zero).
-bool make_tmap(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+bool make_tmap_box(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_cols,
+                   uint32_t box_rows, bool swizzle128) {
     auto fn = encode_fn();
     if (!fn) return false;
     if ((reinterpret_cast<uintptr_t>(base) & 15) || ((cols * 2) & 15)) return false;
     const cuuint64_t dims[2] = {cols, rows};
     const cuuint64_t strides[1] = {cols * 2};
-    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kChunkK), box_rows};
+    const cuuint32_t box[2] = {box_cols, box_rows};
     const cuuint32_t estr[2] = {1, 1};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+              CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+bool make_tmap(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    return make_tmap_box(map, base, rows, cols, kChunkK, box_rows, true);
+}
+
+// Staged-epilogue boxes: a row-major [rows x cols] output in [32 rows][64 columns] boxes (128-byte
+// swizzle), and a transposed one in [64 rows][32 columns] boxes (no swizzle).
+bool make_tmap_rows32(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols) {
+    return make_tmap_box(map, base, rows, cols, 64, 32, true);
+}
+bool make_tmap_cols32(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols) {
+    return make_tmap_box(map, base, rows, cols, 32, 64, false);
+}
+
+// Output tensor maps of the staged epilogue (kBiasSilu: Z, A, A^T; kDsilu: Z read, dZ, dZ^T).
+struct OutMaps {
+    CUtensorMap z, r, t;
+};
 
 template <int BN, int EPI>
 cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K,
-                           int splits, int* err, cudaStream_t s) {
+                           int splits, int* err, cudaStream_t s, const OutMaps* om) {
     static std::once_flag attr;
     std::call_once(attr, [] {
         cudaFuncSetAttribute(gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -454,17 +501,26 @@ cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const Epi
     splits = splits < 1 ? 1 : splits;
     const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
     const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
-    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, ea, K, per, err);
+    static const OutMaps none{};
+    const OutMaps& o = om ? *om : none;
+    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, o.z, o.r, o.t, ea, K, per, err);
     return cudaGetLastError();
 }
 
 // C = A * B^T tile-width choice by N.
+// (The hidden layers' epilogues, kBiasSilu and kDsilu, have N = the hidden width, 64 or 256, and the
+// output maps; their tiles are at least 64 wide.)
 template <int EPI>
 cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K, int splits,
-                        int* err, cudaStream_t s) {
-    if (N <= 16) return launch_gemm_bn<16, EPI>(a, b, ea, M, N, K, splits, err, s);
-    if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s);
-    return launch_gemm_bn<256, EPI>(a, b, ea, M, N, K, splits, err, s);
+                        int* err, cudaStream_t s, const OutMaps* om = nullptr) {
+    if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
+        if (!om) return cudaErrorInvalidValue;
+        if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s, om);
+    } else {
+        if (N <= 16) return launch_gemm_bn<16, EPI>(a, b, ea, M, N, K, splits, err, s, om);
+        if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s, om);
+    }
+    return launch_gemm_bn<256, EPI>(a, b, ea, M, N, K, splits, err, s, om);
 }
 
 int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
@@ -782,6 +838,8 @@ AdamArgs adam_args(bhk_surrogate* s) {
 
 struct Maps {
     CUtensorMap F_rm, F_t, dy_rm, dy_t, W[kLayers], Wt[kLayers], a_rm[4], a_t[4], dz_rm[2], dz_t[2];
+    // the staged epilogue's boxes: Z, A and dZ row-major, A^T and dZ^T transposed
+    CUtensorMap zs[4], as[4], ats[4], dzs[2], dzts[2];
 };
 
 // Tensor maps of the row-major operands for batches of n rows (weights, features, activations,
@@ -795,12 +853,17 @@ bool build_maps(bhk_surrogate* s, int n, bool transposed, Maps* M) {
              make_tmap(&M->Wt[l], s->w_t[l], fi, fo, box_rows_for(fi));
     }
     const int H = s->hid;
-    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_rm[i], s->a_rm[i], n, H, kTileM);
-    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, H, kTileM);
+    for (int i = 0; i < 4 && ok; ++i)
+        ok = make_tmap(&M->a_rm[i], s->a_rm[i], n, H, kTileM) && make_tmap_rows32(&M->zs[i], s->z[i], n, H) &&
+             make_tmap_rows32(&M->as[i], s->a_rm[i], n, H);
+    for (int i = 0; i < 2 && ok; ++i)
+        ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, H, kTileM) && make_tmap_rows32(&M->dzs[i], s->dz_rm[i], n, H);
     if (!transposed) return ok;
     ok = ok && make_tmap(&M->F_t, s->F_t, kFeat, s->cap, 64) && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM);
-    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->a_t[i], s->a_t[i], H, s->cap, box_rows_for(H));
-    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dz_t[i], s->dz_t[i], H, s->cap, kTileM);
+    for (int i = 0; i < 4 && ok; ++i)
+        ok = make_tmap(&M->a_t[i], s->a_t[i], H, s->cap, box_rows_for(H)) && make_tmap_cols32(&M->ats[i], s->a_t[i], H, s->cap);
+    for (int i = 0; i < 2 && ok; ++i)
+        ok = make_tmap(&M->dz_t[i], s->dz_t[i], H, s->cap, kTileM) && make_tmap_cols32(&M->dzts[i], s->dz_t[i], H, s->cap);
     return ok;
 }
 
@@ -818,13 +881,13 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, bool keep_t, cudaStr
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
         EpiArgs ea = epi(n, H);
         ea.bias = s->p + s->L.b[l];
-        ea.rm = s->a_rm[l];
-        ea.ld_rm = H;
-        ea.t = keep_t ? s->a_t[l] : nullptr;
-        ea.ld_t = s->cap;
-        ea.z = s->z[l];
+        ea.store_t = keep_t ? 1 : 0;
+        OutMaps om;
+        om.z = M.zs[l];
+        om.r = M.as[l];
+        if (keep_t) om.t = M.ats[l];
         const CUtensorMap& A = l == 0 ? M.F_rm : M.a_rm[l - 1];
-        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st);
+        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st, &om);
     }
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, kOutPad);
@@ -874,13 +937,13 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, H, n, s->g + s->L.w[4], st);
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, H);
-        ea.rm = s->dz_rm[0];
-        ea.ld_rm = H;
-        ea.t = s->dz_t[0];
-        ea.ld_t = s->cap;
-        ea.z = s->z[3];
+        ea.store_t = 1;
         ea.colsum = s->g + s->L.b[3];
-        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st);
+        OutMaps om;
+        om.z = M.zs[3];
+        om.r = M.dzs[0];
+        om.t = M.dzts[0];
+        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
     }
     // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
     int cur = 0;
@@ -889,13 +952,13 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
         e = weight_grad(s, M.dz_t[cur], Bop, H, fan_in(l, H), n, s->g + s->L.w[l], st);
         if (e != cudaSuccess || l == 0) break;
         EpiArgs ex = epi(n, H);
-        ex.rm = s->dz_rm[1 - cur];
-        ex.ld_rm = H;
-        ex.t = s->dz_t[1 - cur];
-        ex.ld_t = s->cap;
-        ex.z = s->z[l - 1];
+        ex.store_t = 1;
         ex.colsum = s->g + s->L.b[l - 1];
-        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st);
+        OutMaps om;
+        om.z = M.zs[l - 1];
+        om.r = M.dzs[1 - cur];
+        om.t = M.dzts[1 - cur];
+        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
         cur = 1 - cur;
     }
     return e;
