@@ -5,17 +5,19 @@
 // 64 Fourier features [sin, cos](2 pi B u) with a fixed seeded B (32 x 5) -> 4 x (256, SiLU) ->
 // head of 8 (3 outcome logits, r_disk / 30, log g, unit escape vector), padded to 16 for the MMA.
 //
-// Every GEMM is C = A * B^T with A (M x K) and B (N x K) both K-major BF16 in global memory:
-//   forward   Y   = X * W^T         A = activations [rows x K],  B = W [N x K]
-//   backward  dX  = dY * W          A = dY [rows x N],           B = W^T stored [K x N]
-//             dW  = dY^T * X        A = dY^T [N x rows],         B = X^T [K x rows] (split over rows)
-// so activations and gradients are kept in both layouts (the epilogues write both).
+// Every GEMM is C = A * B^T with BF16 operands in global memory, row-major:
+//   forward   Y   = X * W^T         A = activations [rows x K] (K-major),  B = W [N x K] (K-major)
+//   backward  dX  = dY * W          A = dY [rows x N] (K-major),           B = W^T stored [K x N] (K-major)
+//             dW  = dY^T * X        A = dY [rows x N] read MN-major,       B = X [rows x K] read MN-major
+//                                   (split over rows; the head's dY^T, 16 rows, is stored K-major)
+// so the activations and gradients exist in one layout only.
 //
 // GEMM kernel: one CTA computes a 128 x BN tile; TMA brings 64-wide K chunks of A and B into a ring
-// of 4 shared-memory stages (128-byte swizzle); one thread issues tcgen05.mma (M = 128, N = BN,
-// K = 16 per instruction) into a TMEM accumulator and commits each stage back to the producer; after
-// the last chunk four warps read the accumulator with tcgen05.ld (warp w owns rows 32w..32w+31) and
-// run the epilogue. Every wait is bounded; a timeout sets an error flag the host checks.
+// of shared-memory stages (128-byte swizzle); one thread issues tcgen05.mma (M = 128, N = BN, K = 16
+// per instruction) into a TMEM accumulator and commits each stage back to the producer; after the
+// last chunk eight warps read the accumulator with tcgen05.ld (warps w and w + 4 own rows 32w..32w+31)
+// and run the epilogue: the hidden layers' through shared-memory boxes and TMA tensor stores. Every
+// wait is bounded; a timeout sets an error flag the host checks.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
@@ -46,8 +48,6 @@ struct EpiArgs {
     float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32; kPartialF32: split z
                            // writes its partial product at f32 + z * M * ld_f32
     int ld_f32;
-    int store_t;           // kBiasSilu / kDsilu: also write the transposed BF16 output (the BF16
-                           // outputs and the pre-activations go through the kernel's tensor maps)
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
 };
 
@@ -106,21 +106,21 @@ __device__ __forceinline__ float warp_colsum16(const float (&x)[16], int lane, i
 // quadrant w and split the tile's columns (BN >= 32; a 16-wide tile uses warps 0-3 alone).
 constexpr int kGemmThreads = 256;
 
-// Shared memory a warp of the staged epilogue uses (three 4 KB TMA boxes), carved from the idle ring.
-constexpr int kWarpStage = 12288;
+// Shared memory a warp of the staged epilogue uses (two 4 KB TMA boxes), carved from the idle ring.
+constexpr int kWarpStage = 8192;
 
 // Staged epilogue of the hidden layers (kBiasSilu: Z = acc + b and A = silu(Z); kDsilu: dZ = acc *
 // silu'(Z) and the bias gradient). Warp (quad, part) owns the 32 rows of TMEM lane quadrant `quad` and
 // kBoxes 64-column boxes of the tile. Each box's outputs are written into shared memory in the layout of
 // a TMA box -- row-major [32 rows][64 columns] under the 128-byte swizzle (the 16-byte chunk c of row r at
-// chunk c ^ (r & 7)) and transposed [64 columns][32 rows] -- and leave with one TMA tensor store per
-// output, so a warp issues a few bulk stores per box instead of 32-row scattered vector stores. kDsilu
-// reads Z the same way: TMA loads of the warp's boxes, dZ written over them in place. sx holds the
-// tile's bias (kBiasSilu) or its column sums (kDsilu). Returns false if a wait for the Z loads timed out.
+// chunk c ^ (r & 7)) -- and leave with one TMA tensor store per output, so a warp issues a few bulk
+// stores per box instead of 32-row scattered vector stores. kDsilu reads Z the same way: TMA loads of
+// the warp's boxes, dZ written over them in place. sx holds the tile's bias (kBiasSilu) or its column
+// sums (kDsilu). Returns false if a wait for the Z loads timed out.
 template <int BN, int EPI>
-__device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CUtensorMap* tmR, const CUtensorMap* tmT,
-                                                const EpiArgs& ea, uint32_t tmem, uint8_t* stage_base, float* sx,
-                                                uint64_t* zbar, int m0, int n0) {
+__device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CUtensorMap* tmR, const EpiArgs& ea,
+                                                uint32_t tmem, uint8_t* stage_base, float* sx, uint64_t* zbar, int m0,
+                                                int n0) {
     static_assert(BN % 64 == 0, "the staged epilogue works on 64-column boxes");
     constexpr int kSplitS = BN >= 128 ? 2 : 1;   // warps sharing a lane quadrant
     constexpr int kBoxes = BN / (64 * kSplitS);  // boxes per warp
@@ -147,12 +147,13 @@ __device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CU
         }
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16);
         const int sw = lane & 7;
-        bf16* T = reinterpret_cast<bf16*>(wb + 8192);
         auto process = [&](int gi, const uint32_t (&r)[16]) {
             const int b = gi >> 2, g = gi & 3, cb = c_lo + 16 * gi;
-            if (g == 0 && b > 0) {  // the previous box's stores must have read the staging it reuses
-                if (lane == 0) tc::bulk_wait_read_all();
-                __syncwarp();
+            if constexpr (EPI == kBiasSilu) {
+                if (g == 0 && b > 0) {  // the previous box's stores must have read the staging it reuses
+                    if (lane == 0) tc::bulk_wait_read_all();
+                    __syncwarp();
+                }
             }
             __align__(16) bf16 ob[16];
             if constexpr (EPI == kBiasSilu) {
@@ -191,11 +192,6 @@ __device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CU
                     if (!(lane & 1)) atomicAdd(&sx[cb + col], tot);
                 }
             }
-            if (ea.store_t) {
-                const bf16 zero = __float2bfloat16_rn(0.0f);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) T[(16 * g + i) * 32 + lane] = live ? ob[i] : zero;
-            }
             if (g == 3) {  // the box is complete: hand it to the TMA unit
                 tc::fence_proxy_async();
                 __syncwarp();
@@ -207,7 +203,6 @@ __device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CU
                     } else {
                         tc::tma_store_2d(tmR, wb + b * 4096, x, y0);
                     }
-                    if (ea.store_t) tc::tma_store_2d(tmT, T, y0, x);
                     tc::bulk_commit();
                 }
             }
@@ -242,15 +237,19 @@ __device__ __forceinline__ bool epilogue_staged(const CUtensorMap* tmZ, const CU
     return ok;
 }
 
-template <int BN, int EPI>
+// MAJ bit 0: A is MN-major (a row-major [K x M] matrix, loaded as 64 x 64 boxes, two per 128-row tile);
+// bit 1: B is MN-major ([K x N], BN / 64 boxes). Otherwise the operand is K-major ([M x K], [N x K]).
+template <int BN, int EPI, int MAJ = 0>
 __global__ void __launch_bounds__(kGemmThreads, 2)
 gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-            const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR,
-            const __grid_constant__ CUtensorMap tmT, EpiArgs ea, int K, int k_per_split, int* err) {
+            const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR, EpiArgs ea, int K,
+            int k_per_split, int* err) {
     constexpr int kStages = gemm_stages<BN, EPI>();
     constexpr int kBBytes = BN * kChunkK * 2;
     constexpr uint32_t kCols = BN < 32 ? 32 : BN;
-    constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, BN);
+    constexpr bool kAmn = (MAJ & 1) != 0, kBmn = (MAJ & 2) != 0;
+    static_assert(!kBmn || BN % 64 == 0, "an MN-major B tile is made of 64-wide boxes");
+    constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, BN, kAmn, kBmn);
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* sA = smem;
@@ -291,8 +290,19 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         auto load = [&](int stage, int chunk) {
             tc::mbar_expect_tx(&full[stage], kABytes + kBBytes);
             const int kx = k_begin + chunk * kChunkK;
-            tc::tma_load_2d(sA + stage * kABytes, &tmA, kx, m0, &full[stage]);
-            tc::tma_load_2d(sB + stage * kBBytes, &tmB, kx, n0, &full[stage]);
+            if constexpr (kAmn) {
+                tc::tma_load_2d(sA + stage * kABytes, &tmA, m0, kx, &full[stage]);
+                tc::tma_load_2d(sA + stage * kABytes + kABytes / 2, &tmA, m0 + 64, kx, &full[stage]);
+            } else {
+                tc::tma_load_2d(sA + stage * kABytes, &tmA, kx, m0, &full[stage]);
+            }
+            if constexpr (kBmn) {
+#pragma unroll
+                for (int j = 0; j < BN / 64; ++j)
+                    tc::tma_load_2d(sB + stage * kBBytes + j * 8192, &tmB, n0 + 64 * j, kx, &full[stage]);
+            } else {
+                tc::tma_load_2d(sB + stage * kBBytes, &tmB, kx, n0, &full[stage]);
+            }
         };
         bool ok = true;
         int loaded = 0;
@@ -305,11 +315,14 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                 break;
             }
             tc::fence_after_sync();
-            const uint64_t ad = tc::smem_desc_sw128(sA + s * kABytes);
-            const uint64_t bd = tc::smem_desc_sw128(sB + s * kBBytes);
+            // A K = 16 slice: +32 bytes inside the atom (K-major), +2048 bytes (MN-major: two 8-row atoms).
+            const uint64_t ad = kAmn ? tc::smem_desc_sw128_mn(sA + s * kABytes, kABytes / 2)
+                                     : tc::smem_desc_sw128(sA + s * kABytes);
+            const uint64_t bd = kBmn ? tc::smem_desc_sw128_mn(sB + s * kBBytes, 8192) : tc::smem_desc_sw128(sB + s * kBBytes);
+            constexpr uint64_t kStepA = kAmn ? 2048 >> 4 : 2, kStepB = kBmn ? 2048 >> 4 : 2;
 #pragma unroll
-            for (int kk = 0; kk < kChunkK / 16; ++kk)  // +32 bytes per K = 16 slice inside the atom
-                tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < kChunkK / 16; ++kk)
+                tc::mma_bf16(tmem, ad + kStepA * kk, bd + kStepB * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
             tc::mma_commit(&empty[s]);
             // Refill the stage of the previous chunk once its MMAs are done (they run in order).
             if (c >= 1 && loaded < nchunks) {
@@ -338,7 +351,7 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     if (acc_ready && !*fail && nchunks > 0) {
         if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
             // The pipeline's shared memory is idle now: it holds the warps' output boxes.
-            if (!epilogue_staged<BN, EPI>(&tmZ, &tmR, &tmT, ea, tmem, sA, sx, zbar, m0, n0)) atomicExch(err, 1);
+            if (!epilogue_staged<BN, EPI>(&tmZ, &tmR, ea, tmem, sA, sx, zbar, m0, n0)) atomicExch(err, 1);
         } else {
             constexpr int kJ = BN / 16;                  // 16-column groups of the tile
             constexpr int kSplit = kJ >= 2 ? 2 : 1;      // warps sharing a lane quadrant
@@ -485,17 +498,17 @@ bool make_tmap_cols32(CUtensorMap* map, const void* base, uint64_t rows, uint64_
     return make_tmap_box(map, base, rows, cols, 32, 64, false);
 }
 
-// Output tensor maps of the staged epilogue (kBiasSilu: Z, A, A^T; kDsilu: Z read, dZ, dZ^T).
+// Tensor maps of the staged epilogue (kBiasSilu: Z and A written; kDsilu: Z read, dZ written).
 struct OutMaps {
-    CUtensorMap z, r, t;
+    CUtensorMap z, r;
 };
 
-template <int BN, int EPI>
+template <int BN, int EPI, int MAJ>
 cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K,
                            int splits, int* err, cudaStream_t s, const OutMaps* om) {
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(gemm_kernel<BN, EPI, MAJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              gemm_smem_bytes<BN, EPI>());
     });
     splits = splits < 1 ? 1 : splits;
@@ -503,24 +516,26 @@ cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const Epi
     const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
     static const OutMaps none{};
     const OutMaps& o = om ? *om : none;
-    gemm_kernel<BN, EPI><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, o.z, o.r, o.t, ea, K, per, err);
+    gemm_kernel<BN, EPI, MAJ><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, o.z, o.r, ea, K, per, err);
     return cudaGetLastError();
 }
 
 // C = A * B^T tile-width choice by N.
 // (The hidden layers' epilogues, kBiasSilu and kDsilu, have N = the hidden width, 64 or 256, and the
-// output maps; their tiles are at least 64 wide.)
-template <int EPI>
+// output maps; their tiles are at least 64 wide, as are those of an MN-major B.)
+template <int EPI, int MAJ = 0>
 cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K, int splits,
                         int* err, cudaStream_t s, const OutMaps* om = nullptr) {
     if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
         if (!om) return cudaErrorInvalidValue;
-        if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s, om);
-    } else {
-        if (N <= 16) return launch_gemm_bn<16, EPI>(a, b, ea, M, N, K, splits, err, s, om);
-        if (N <= 64) return launch_gemm_bn<64, EPI>(a, b, ea, M, N, K, splits, err, s, om);
     }
-    return launch_gemm_bn<256, EPI>(a, b, ea, M, N, K, splits, err, s, om);
+    if constexpr (EPI == kBiasSilu || EPI == kDsilu || (MAJ & 2) != 0) {
+        if (N <= 64) return launch_gemm_bn<64, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
+    } else {
+        if (N <= 16) return launch_gemm_bn<16, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
+        if (N <= 64) return launch_gemm_bn<64, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
+    }
+    return launch_gemm_bn<256, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
 }
 
 int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
@@ -637,8 +652,7 @@ __device__ __forceinline__ void fourier_features(const float* x, const float* sb
 }
 
 // Fourier features of n rays: row-major [n x 64] and, when t is given, transposed [64 x ld_t].
-__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm,
-                               bf16* __restrict__ t, int ld_t, int n) {
+__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm, int n) {
     __shared__ float sb[kFreq * kIn];
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
     __syncthreads();
@@ -649,8 +663,6 @@ __global__ void feature_kernel(const float* __restrict__ x, const float* __restr
     uint4* dst = reinterpret_cast<uint4*>(rm + static_cast<size_t>(r) * kFeat);
 #pragma unroll
     for (int q = 0; q < kFeat / 8; ++q) dst[q] = reinterpret_cast<const uint4*>(f)[q];
-    if (t)
-        for (int j = 0; j < kFeat; ++j) t[static_cast<size_t>(j) * ld_t + r] = f[j];
 }
 
 // Loss of a batch and its gradient with respect to the head outputs Y (n x 16, FP32):
@@ -787,8 +799,8 @@ struct bhk_surrogate {
     bhk::sur::bf16* w_rm[bhk::sur::kLayers] = {};
     bhk::sur::bf16* w_t[bhk::sur::kLayers] = {};
     float* Bm = nullptr;
-    bhk::sur::bf16 *F_rm = nullptr, *F_t = nullptr, *dy_rm = nullptr, *dy_t = nullptr;
-    bhk::sur::bf16 *z[4] = {}, *a_rm[4] = {}, *a_t[4] = {}, *dz_rm[2] = {}, *dz_t[2] = {};
+    bhk::sur::bf16 *F_rm = nullptr, *dy_rm = nullptr, *dy_t = nullptr;
+    bhk::sur::bf16 *z[4] = {}, *a_rm[4] = {}, *dz_rm[2] = {};
     float* Y = nullptr;
     float* loss = nullptr;
     int* err = nullptr;
@@ -837,15 +849,15 @@ AdamArgs adam_args(bhk_surrogate* s) {
 }
 
 struct Maps {
-    CUtensorMap F_rm, F_t, dy_rm, dy_t, W[kLayers], Wt[kLayers], a_rm[4], a_t[4], dz_rm[2], dz_t[2];
-    // the staged epilogue's boxes: Z, A and dZ row-major, A^T and dZ^T transposed
-    CUtensorMap zs[4], as[4], ats[4], dzs[2], dzts[2];
+    CUtensorMap F_rm, dy_rm, dy_t, W[kLayers], Wt[kLayers], a_rm[4], dz_rm[2];
+    CUtensorMap zs[4], as[4], dzs[2];  // the staged epilogue's [32 x 64] boxes of Z, A and dZ
+    CUtensorMap Fm, am[4], dzm[2];     // F, A and dZ as MN-major operands ([64 rows x 64] boxes)
 };
 
-// Tensor maps of the row-major operands for batches of n rows (weights, features, activations,
-// gradients), and with `transposed` also of the transposed copies, whose rows are `cap` long (the
-// K extent of each gradient GEMM, n, bounds what is read of them).
-bool build_maps(bhk_surrogate* s, int n, bool transposed, Maps* M) {
+// Tensor maps of the operands for batches of n rows (weights, features, activations, gradients), and
+// with `training` also of the weight gradients' MN-major operands and of dY^T, whose rows are `cap` long
+// (the K extent of the head's weight gradient, n, bounds what is read of it).
+bool build_maps(bhk_surrogate* s, int n, bool training, Maps* M) {
     bool ok = make_tmap(&M->F_rm, s->F_rm, n, kFeat, kTileM) && make_tmap(&M->dy_rm, s->dy_rm, n, kOutPad, kTileM);
     for (int l = 0; l < kLayers && ok; ++l) {
         const int fi = fan_in(l, s->hid), fo = fan_out(l, s->hid);
@@ -858,12 +870,10 @@ bool build_maps(bhk_surrogate* s, int n, bool transposed, Maps* M) {
              make_tmap_rows32(&M->as[i], s->a_rm[i], n, H);
     for (int i = 0; i < 2 && ok; ++i)
         ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, H, kTileM) && make_tmap_rows32(&M->dzs[i], s->dz_rm[i], n, H);
-    if (!transposed) return ok;
-    ok = ok && make_tmap(&M->F_t, s->F_t, kFeat, s->cap, 64) && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM);
-    for (int i = 0; i < 4 && ok; ++i)
-        ok = make_tmap(&M->a_t[i], s->a_t[i], H, s->cap, box_rows_for(H)) && make_tmap_cols32(&M->ats[i], s->a_t[i], H, s->cap);
-    for (int i = 0; i < 2 && ok; ++i)
-        ok = make_tmap(&M->dz_t[i], s->dz_t[i], H, s->cap, kTileM) && make_tmap_cols32(&M->dzts[i], s->dz_t[i], H, s->cap);
+    if (!training) return ok;
+    ok = ok && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM) && make_tmap(&M->Fm, s->F_rm, n, kFeat, 64);
+    for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->am[i], s->a_rm[i], n, H, 64);
+    for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dzm[i], s->dz_rm[i], n, H, 64);
     return ok;
 }
 
@@ -874,18 +884,16 @@ EpiArgs epi(int M, int N) {
     return e;
 }
 
-// Forward pass of n rows (features already in F): z, activations in both layouts, head into Y.
-cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, bool keep_t, cudaStream_t st) {
+// Forward pass of n rows (features already in F): z, activations, head into Y.
+cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
         EpiArgs ea = epi(n, H);
         ea.bias = s->p + s->L.b[l];
-        ea.store_t = keep_t ? 1 : 0;
         OutMaps om;
         om.z = M.zs[l];
         om.r = M.as[l];
-        if (keep_t) om.t = M.ats[l];
         const CUtensorMap& A = l == 0 ? M.F_rm : M.a_rm[l - 1];
         e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st, &om);
     }
@@ -910,15 +918,17 @@ int split_for(const bhk_surrogate* s, int n, int M, int N) {
     return sp < 1 ? 1 : static_cast<int>(sp);
 }
 
-// dst (M x N FP32, dense) += A^T-style weight gradient: the split-K partial products go to the
-// workspace with plain stores, then one pass sums them into dst.
+// dst (M x N FP32, dense) += the weight gradient sum over K of A_k B_k^T: the split-K partial products go
+// to the workspace with plain stores, then one pass sums them into dst. MAJ as for gemm_kernel: the
+// hidden layers' operands are the row-major activations and gradients themselves, read MN-major.
+template <int MAJ>
 cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, float* dst,
                         cudaStream_t st) {
     const int splits = split_for(s, K, M, N);
     EpiArgs ea = epi(M, N);
     ea.f32 = s->ws;
     ea.ld_f32 = N;
-    cudaError_t e = launch_gemm<kPartialF32>(A, B, ea, M, N, K, splits, s->err, st);
+    cudaError_t e = launch_gemm<kPartialF32, MAJ>(A, B, ea, M, N, K, splits, s->err, st);
     if (e != cudaSuccess) return e;
     const long long count = static_cast<long long>(M) * N;
     const int blocks = static_cast<int>(std::min<long long>((count / 4 + 31) / 32, 8LL * s->sms));
@@ -933,31 +943,27 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     loss_kernel<<<(n + 255) / 256, 256, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
                                                  s->loss, n, 1.0f / n, s->w);
     const int H = s->hid;
-    // Head: dW5 = dY^T A4, then dA4 = dY W5 -> dZ4.
-    e = weight_grad(s, M.dy_t, M.a_t[3], kOutPad, H, n, s->g + s->L.w[4], st);
+    // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
+    e = weight_grad<2>(s, M.dy_t, M.am[3], kOutPad, H, n, s->g + s->L.w[4], st);
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, H);
-        ea.store_t = 1;
         ea.colsum = s->g + s->L.b[3];
         OutMaps om;
         om.z = M.zs[3];
         om.r = M.dzs[0];
-        om.t = M.dzts[0];
         e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
     }
     // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
-        const CUtensorMap& Bop = l == 0 ? M.F_t : M.a_t[l - 1];
-        e = weight_grad(s, M.dz_t[cur], Bop, H, fan_in(l, H), n, s->g + s->L.w[l], st);
+        const CUtensorMap& Bop = l == 0 ? M.Fm : M.am[l - 1];
+        e = weight_grad<3>(s, M.dzm[cur], Bop, H, fan_in(l, H), n, s->g + s->L.w[l], st);
         if (e != cudaSuccess || l == 0) break;
         EpiArgs ex = epi(n, H);
-        ex.store_t = 1;
         ex.colsum = s->g + s->L.b[l - 1];
         OutMaps om;
         om.z = M.zs[l - 1];
         om.r = M.dzs[1 - cur];
-        om.t = M.dzts[1 - cur];
         e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
         cur = 1 - cur;
     }
@@ -1025,7 +1031,7 @@ bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_bat
     const int H = width;
     const size_t P = s->L.total, B = static_cast<size_t>(max_batch);
     bool ok = dalloc(s, &s->p, P) && dalloc(s, &s->g, P) && dalloc(s, &s->m, P) && dalloc(s, &s->v, P) &&
-              dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) && dalloc(s, &s->F_t, B * kFeat) &&
+              dalloc(s, &s->Bm, kFreq * kIn) && dalloc(s, &s->F_rm, B * kFeat) &&
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
               dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
               dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * H) &&
@@ -1037,8 +1043,8 @@ bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_bat
         ok = dalloc(s, &s->w_rm[l], n) && dalloc(s, &s->w_t[l], n);
     }
     for (int i = 0; i < 4 && ok; ++i)
-        ok = dalloc(s, &s->z[i], B * H) && dalloc(s, &s->a_rm[i], B * H) && dalloc(s, &s->a_t[i], B * H);
-    for (int i = 0; i < 2 && ok; ++i) ok = dalloc(s, &s->dz_rm[i], B * H) && dalloc(s, &s->dz_t[i], B * H);
+        ok = dalloc(s, &s->z[i], B * H) && dalloc(s, &s->a_rm[i], B * H);
+    for (int i = 0; i < 2 && ok; ++i) ok = dalloc(s, &s->dz_rm[i], B * H);
     if (!ok) {
         bhk_surrogate_destroy(s);
         set_last_error("bhk_surrogate_create: device allocation failed");
@@ -1190,8 +1196,8 @@ bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8
     cudaStream_t st = nullptr;
     cudaMemsetAsync(s->err, 0, sizeof(int), st);
     cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
-    feature_kernel<<<(n + 127) / 128, 128, 0, st>>>(x, s->Bm, s->F_rm, s->F_t, s->cap, n);
-    cudaError_t e = forward(s, M, n, true, st);
+    feature_kernel<<<(n + 127) / 128, 128, 0, st>>>(x, s->Bm, s->F_rm, n);
+    cudaError_t e = forward(s, M, n, st);
     if (e == cudaSuccess) e = backward(s, M, cls, tgt, n, st);
     if (e != cudaSuccess) {
         set_last_error(std::string("bhk_surrogate_gradients: ") + cudaGetErrorString(e));
@@ -1233,8 +1239,8 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
     for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
         const int64_t off = (t % nb) * batch;
         cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
-        feature_kernel<<<(batch + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, s->F_t, s->cap, batch);
-        e = forward(s, M, batch, true, st);
+        feature_kernel<<<(batch + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, batch);
+        e = forward(s, M, batch, st);
         if (e == cudaSuccess) e = backward(s, M, cls + off, tgt + off * kOut, batch, st);
         ++s->step;
         aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
@@ -1273,8 +1279,8 @@ bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, fl
             set_last_error("bhk_surrogate_predict: tensor map creation failed");
             return BHK_ECUDA;
         }
-        feature_kernel<<<(rows + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, nullptr, 0, rows);
-        cudaError_t e = forward(s, M, rows, false, st);
+        feature_kernel<<<(rows + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, rows);
+        cudaError_t e = forward(s, M, rows, st);
         if (e == cudaSuccess)
             e = cudaMemcpy2DAsync(out + off * kOut, kOut * sizeof(float), s->Y, kOutPad * sizeof(float),
                                   kOut * sizeof(float), rows, cudaMemcpyDeviceToDevice, st);

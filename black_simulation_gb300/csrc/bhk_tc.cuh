@@ -5,7 +5,9 @@
 // Operand layout: K-major tiles of 64 BF16 (128 bytes) per row, 128-byte swizzled, as TMA writes them
 // with CU_TENSOR_MAP_SWIZZLE_128B into 1024-byte aligned shared memory: 8-row atoms of 1024 bytes,
 // stacked along M (or N). The shared-memory descriptor therefore has SBO = 1024 bytes, layout
-// "128-byte swizzle", and advances by 32 bytes per K = 16 slice inside the atom.
+// "128-byte swizzle", and advances by 32 bytes per K = 16 slice inside the atom. MN-major tiles (a
+// row-major matrix read with K along its rows) are the same boxes turned: rows of 64 elements along M
+// (or N) stepping along K, each 64-wide block of M (N) a box of its own (smem_desc_sw128_mn).
 #pragma once
 
 #include <cstdint>
@@ -127,10 +129,26 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(const void* tile) {
     return d;
 }
 
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, shape M x N.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
-           (static_cast<uint32_t>(M >> 4) << 24);
+// Shared-memory matrix descriptor: MN-major, 128-byte swizzle. The tile is stored as K rows of 64
+// elements along M (or N), 128 bytes each, in 1024-byte swizzle atoms of 8 K rows (stride byte offset
+// 1024); successive 64-element blocks along M (N) lie mn_stride bytes apart (leading byte offset). A
+// K = 16 slice starts 2048 bytes (two atoms) further on.
+__device__ __forceinline__ uint64_t smem_desc_sw128_mn(const void* tile, uint32_t mn_stride) {
+    const uint64_t addr = smem_u32(tile);
+    uint64_t d = 0;
+    d |= (addr >> 4) & 0x3FFFull;                              // start address
+    d |= static_cast<uint64_t>((mn_stride >> 4) & 0x3FFF) << 16; // leading byte offset: next 64 along M/N
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;               // stride byte offset: next 8 K rows
+    d |= static_cast<uint64_t>(1) << 46;                       // descriptor version
+    d |= static_cast<uint64_t>(2) << 61;                       // layout: 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, shape M x N; A and B K-major unless a_mn /
+// b_mn (bits 15 and 16: the operand is MN-major).
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool a_mn = false, bool b_mn = false) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u) |
+           (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T for one K = 16 slice; issued by a single thread.
