@@ -411,6 +411,262 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
+// ---- persistent hidden-layer GEMM (width 256) ----
+// Y[rows x 256] = A[rows x K] W^T with the hidden layers' epilogues (kBiasSilu, kDsilu), one CTA per SM
+// for the whole batch. CTA pairs split the 256 output columns into two 128-wide halves, and each CTA
+// keeps its half's weights [128 x K] resident in shared memory for all of its row tiles. Warp roles:
+// warp 8 lane 0 streams the 128 x 64 chunks of A through a 4-stage TMA ring; warp 9 lane 0 issues the
+// MMAs (128 x 128 x 16) into one of two TMEM accumulators, so that a tile's MMAs overlap the previous
+// tile's epilogue; warps 0-7 run the staged epilogue (warp w: TMEM lane quadrant w & 3, columns
+// 64 (w >> 2) .. + 63 of the half) and hand the accumulator back. Every wait is bounded; after a
+// timeout the roles stop, the loads in flight are waited for (bounded) and the error flag is set.
+constexpr int kLayerN = 128;                  // output columns per CTA
+constexpr int kLayerRing = 4;                 // A-chunk stages
+constexpr int kLayerEpiWarps = 8;
+constexpr int kLayerThreads = 32 * (kLayerEpiWarps + 2);
+constexpr int kLayerWBytes = 4 * kLayerN * kChunkK * 2;  // K <= 256: four 16 KB chunks of W
+constexpr int kLayerStage = 8192;                        // per epilogue warp: two 4 KB boxes
+
+__host__ __device__ constexpr int layer_smem_bytes() {
+    return kLayerWBytes + kLayerRing * kABytes + kLayerEpiWarps * kLayerStage + 1024 /* alignment */ +
+           512 /* barriers */ + kLayerN * 4 /* bias or column sums */;
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kLayerThreads, 1)
+layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW,
+             const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR, EpiArgs ea, int K,
+             int* err) {
+    static_assert(EPI == kBiasSilu || EPI == kDsilu, "hidden-layer epilogues only");
+    constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, kLayerN);
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* sW = smem;
+    uint8_t* sRing = sW + kLayerWBytes;
+    uint8_t* sStage = sRing + kLayerRing * kABytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sStage + kLayerEpiWarps * kLayerStage);
+    uint64_t* empty = full + kLayerRing;
+    uint64_t* tfull = empty + kLayerRing;       // accumulator b holds a finished tile
+    uint64_t* tempty = tfull + 2;               // accumulator b has been read by the epilogue
+    uint64_t* wbar = tempty + 2;                // the weights have landed
+    uint64_t* zbar = wbar + 1;                  // [warp][buffer]: kDsilu pre-activation boxes
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(zbar + 2 * kLayerEpiWarps);
+    volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* consumed = fail + 1;  // A chunks the MMA thread has taken (for the drain)
+    float* sx = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(full) + 512);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nh = ea.N / kLayerN;                       // column halves (2)
+    const int n0 = (blockIdx.x % nh) * kLayerN;
+    const int pairs = gridDim.x / nh;
+    const int pair = blockIdx.x / nh;
+    const int mtiles = (ea.M + kTileM - 1) / kTileM;
+    const int my_tiles = pair < mtiles ? (mtiles - pair + pairs - 1) / pairs : 0;  // tiles pair, pair + pairs, ...
+    const int kc = (K + kChunkK - 1) / kChunkK;          // K chunks (<= 4)
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kLayerRing; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], kLayerEpiWarps);
+        }
+        tc::mbar_init(wbar, 1);
+        for (int i = 0; i < 2 * kLayerEpiWarps; ++i) tc::mbar_init(&zbar[i], 1);
+        *fail = 0;
+        *consumed = 0;
+        tc::fence_mbar_init();
+    }
+    if constexpr (EPI == kBiasSilu) {
+        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
+    } else {
+        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
+    }
+    if (warp == kLayerEpiWarps + 1) tc::tmem_alloc(tmem_slot, 2 * kLayerN);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == kLayerEpiWarps) {
+        // ---- producer: the weights once, then the A chunks of every tile through the ring ----
+        if (lane == 0) {
+            tc::mbar_expect_tx(wbar, kc * kABytes);
+            for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
+            int issued = 0;
+            for (int t = 0; t < my_tiles && !*fail; ++t) {
+                const int m0 = (pair + t * pairs) * kTileM;
+                for (int c = 0; c < kc; ++c, ++issued) {
+                    const int s = issued % kLayerRing, ph = (issued / kLayerRing) & 1;
+                    if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
+                        *fail = 1;
+                        break;
+                    }
+                    tc::mbar_expect_tx(&full[s], kABytes);
+                    tc::tma_load_2d(sRing + s * kABytes, &tmA, c * kChunkK, m0, &full[s]);
+                }
+            }
+            // Drain (bounded): every chunk issued has landed before the CTA may exit.
+            if (!tc::mbar_wait(wbar, 0)) *fail = 1;
+            for (int q = *consumed; q < issued; ++q) tc::mbar_wait(&full[q % kLayerRing], (q / kLayerRing) & 1);
+        }
+    } else if (warp == kLayerEpiWarps + 1) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            bool ok = tc::mbar_wait(wbar, 0);
+            int taken = 0;
+            for (int t = 0; t < my_tiles && ok; ++t) {
+                const int b = t & 1, u = t >> 1;
+                ok = tc::mbar_wait(&tempty[b], (u & 1) ^ 1) && !*fail;
+                tc::fence_after_sync();
+                const uint32_t d = tmem + b * kLayerN;
+                for (int c = 0; c < kc && ok; ++c, ++taken) {
+                    const int s = taken % kLayerRing, ph = (taken / kLayerRing) & 1;
+                    if (!tc::mbar_wait(&full[s], ph) || *fail) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const uint64_t ad = tc::smem_desc_sw128(sRing + s * kABytes);
+                    const uint64_t bd = tc::smem_desc_sw128(sW + c * kABytes);
+#pragma unroll
+                    for (int kk = 0; kk < kChunkK / 16; ++kk)
+                        tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
+                    tc::mma_commit(&empty[s]);
+                    *consumed = taken + 1;
+                }
+                if (ok) tc::mma_commit(&tfull[b]);
+            }
+            if (!ok) {
+                *fail = 1;
+                // the MMAs already issued complete in order: wait (bounded) for the last one's commit
+                if (taken > 0) tc::mbar_wait(&empty[(taken - 1) % kLayerRing], ((taken - 1) / kLayerRing) & 1);
+            }
+        }
+    } else {
+        // ---- epilogue warps ----
+        const int quad = warp & 3, part = warp >> 2;
+        uint8_t* wb = sStage + warp * kLayerStage;
+        const int sw = lane & 7;
+        const uint32_t tq = tmem + (static_cast<uint32_t>(32 * quad) << 16) + 64 * part;
+        const int x = n0 + 64 * part;  // the warp's first output column
+        bool ok = true;
+        int z_issued = 0, z_waited = 0;  // kDsilu: pre-activation box loads (lane 0 issues)
+        auto load_z = [&](int t) {      // the box of tile t into buffer t & 1 (lane 0)
+            uint64_t* bar = &zbar[2 * warp + (t & 1)];
+            tc::mbar_expect_tx(bar, 4096);
+            tc::tma_load_2d(wb + (t & 1) * 4096, &tmZ, x, (pair + t * pairs) * kTileM + 32 * quad, bar);
+            ++z_issued;
+        };
+        if constexpr (EPI == kDsilu) {
+            if (lane == 0 && my_tiles > 0) load_z(0);
+        }
+        for (int t = 0; t < my_tiles; ++t) {
+            const int b = t & 1, u = t >> 1;
+            const int y0 = (pair + t * pairs) * kTileM + 32 * quad;
+            const bool live = y0 + lane < ea.M;
+            if (lane == 0) tc::bulk_wait_read_all();  // the stores of tile t - 1 have read the staging
+            if constexpr (EPI == kDsilu) {
+                if (lane == 0 && t + 1 < my_tiles) load_z(t + 1);  // one tile ahead, into the other buffer
+            }
+            __syncwarp();
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&tfull[b], u & 1) ? 1 : 0) != 0 && !*fail;
+            if constexpr (EPI == kDsilu) {
+                if (ok) {
+                    ok = __all_sync(0xffffffffu, tc::mbar_wait(&zbar[2 * warp + (t & 1)], (t >> 1) & 1) ? 1 : 0) != 0;
+                    if (ok) ++z_waited;
+                }
+            }
+            if (!ok) break;
+            tc::fence_after_sync();
+            // The tile's 64 columns at once; the accumulator goes back to the MMA thread right away.
+            uint32_t ra[32], rb[32];
+            tc::tmem_ld32_issue(tq + b * kLayerN, ra);
+            tc::tmem_ld32_issue(tq + b * kLayerN + 32, rb);
+            tc::tmem_wait32(ra);
+            tc::tmem_wait32(rb);
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&tempty[b]);
+            uint8_t* zin = wb + (t & 1) * 4096;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                const uint32_t* r = g < 2 ? ra + 16 * g : rb + 16 * (g - 2);
+                const int cb = 64 * part + 16 * g;  // column within the CTA's half
+                __align__(16) bf16 ob[16];
+                if constexpr (EPI == kBiasSilu) {
+                    __align__(16) bf16 zb[16];
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2) {
+                        const float z0 = __uint_as_float(r[i]) + sx[cb + i];
+                        const float z1 = __uint_as_float(r[i + 1]) + sx[cb + i + 1];
+                        zb[i] = __float2bfloat16_rn(z0);
+                        zb[i + 1] = __float2bfloat16_rn(z1);
+                        *reinterpret_cast<uint32_t*>(&ob[i]) = silu2_half(0.5f * z0, 0.5f * z1);
+                    }
+                    uint4* zrow = reinterpret_cast<uint4*>(wb + lane * 128);
+                    uint4* arow = reinterpret_cast<uint4*>(wb + 4096 + lane * 128);
+                    zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(zb)[0];
+                    zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(zb)[1];
+                    arow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
+                    arow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
+                } else {
+                    uint4* zrow = reinterpret_cast<uint4*>(zin + lane * 128);
+                    __align__(16) bf16 zv[16];
+                    reinterpret_cast<uint4*>(zv)[0] = zrow[(2 * g) ^ sw];
+                    reinterpret_cast<uint4*>(zv)[1] = zrow[(2 * g + 1) ^ sw];
+                    float dz[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const float z = __bfloat162float(zv[i]);
+                        const float sg = sigmoidf(z);
+                        dz[i] = live ? __uint_as_float(r[i]) * sg * (1.0f + z * (1.0f - sg)) : 0.0f;
+                        ob[i] = __float2bfloat16_rn(dz[i]);
+                    }
+                    zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
+                    zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
+                    if (ea.colsum) {
+                        int col;
+                        const float tot = warp_colsum16(dz, lane, col);
+                        if (!(lane & 1)) atomicAdd(&sx[cb + col], tot);
+                    }
+                }
+            }
+            tc::fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                if constexpr (EPI == kBiasSilu) {
+                    tc::tma_store_2d(&tmZ, wb, x, y0);
+                    tc::tma_store_2d(&tmR, wb + 4096, x, y0);
+                } else {
+                    tc::tma_store_2d(&tmR, zin, x, y0);
+                }
+                tc::bulk_commit();
+            }
+        }
+        if (lane == 0) {
+            tc::bulk_wait_all();
+            if (!ok) {
+                *fail = 1;
+                // pre-activation loads still in flight land before the CTA may exit (bounded)
+                for (int j = z_waited; j < z_issued; ++j) tc::mbar_wait(&zbar[2 * warp + (j & 1)], (j >> 1) & 1);
+            }
+        }
+    }
+    __syncwarp();
+    if constexpr (EPI == kDsilu) {
+        __syncthreads();
+        if (ea.colsum && !*fail)
+            for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) atomicAdd(&ea.colsum[n0 + i], sx[i]);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0 && *fail) atomicExch(err, 1);
+    if (warp == kLayerEpiWarps + 1) tc::tmem_dealloc(tmem, 2 * kLayerN);
+}
+
 // dst[i] += sum over the splits of ws[split * count + i] (count a multiple of 4, 16-byte aligned).
 // A block of 256 threads takes 32 float4 of dst at a time: warp g sums splits g, g + 8, g + 16, ...
 // of them (each warp load is 512 contiguous bytes), and warp 0 adds the eight partial sums to dst in
@@ -426,7 +682,21 @@ reduce_splits_kernel(const float* __restrict__ ws, int splits, long long count, 
         const long long i = base + c;
         float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (i < n4) {
-            for (int sp = g; sp < splits; sp += kReduceGroups) {
+            // four splits' loads in flight at a time
+            int sp = g;
+            for (; sp + 3 * kReduceGroups < splits; sp += 4 * kReduceGroups) {
+                float4 w[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) w[u] = w4[(sp + u * kReduceGroups) * n4 + i];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    acc.x += w[u].x;
+                    acc.y += w[u].y;
+                    acc.z += w[u].z;
+                    acc.w += w[u].w;
+                }
+            }
+            for (; sp < splits; sp += kReduceGroups) {
                 const float4 w = w4[sp * n4 + i];
                 acc.x += w.x;
                 acc.y += w.y;
@@ -489,13 +759,10 @@ bool make_tmap(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols,
     return make_tmap_box(map, base, rows, cols, kChunkK, box_rows, true);
 }
 
-// Staged-epilogue boxes: a row-major [rows x cols] output in [32 rows][64 columns] boxes (128-byte
-// swizzle), and a transposed one in [64 rows][32 columns] boxes (no swizzle).
+// Staged-epilogue boxes: a row-major [rows x cols] matrix in [32 rows][64 columns] boxes (128-byte
+// swizzle).
 bool make_tmap_rows32(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols) {
     return make_tmap_box(map, base, rows, cols, 64, 32, true);
-}
-bool make_tmap_cols32(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols) {
-    return make_tmap_box(map, base, rows, cols, 32, 64, false);
 }
 
 // Tensor maps of the staged epilogue (kBiasSilu: Z and A written; kDsilu: Z read, dZ written).
@@ -539,6 +806,24 @@ cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArg
 }
 
 int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
+
+// The persistent hidden-layer GEMM of a width-256 network: A (rows x K, K <= 256) row-major with a
+// [128 rows x 64] box map, W [256 x K] with a [128 x 64] box map, the staged epilogue's maps; one CTA per
+// SM (CTA pairs over the two column halves) or fewer for small batches.
+template <int EPI>
+cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMaps& om, const EpiArgs& ea, int K,
+                         int sms, int* err, cudaStream_t s) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(layer_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, layer_smem_bytes());
+    });
+    if (ea.N % kLayerN != 0 || K > 4 * kChunkK) return cudaErrorInvalidValue;
+    const int nh = ea.N / kLayerN;
+    const int mtiles = (ea.M + kTileM - 1) / kTileM;
+    const int pairs = std::max(1, std::min(mtiles, sms / nh));
+    layer_kernel<EPI><<<pairs * nh, kLayerThreads, layer_smem_bytes(), s>>>(a, w, om.z, om.r, ea, K, err);
+    return cudaGetLastError();
+}
 
 // K splits launch_gemm makes for `splits` requested (grid z).
 int grid_splits(int K, int splits) {
@@ -651,7 +936,7 @@ __device__ __forceinline__ void fourier_features(const float* x, const float* sb
     }
 }
 
-// Fourier features of n rays: row-major [n x 64] and, when t is given, transposed [64 x ld_t].
+// Fourier features of n rays, row-major [n x 64].
 __global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm, int n) {
     __shared__ float sb[kFreq * kIn];
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
@@ -671,7 +956,8 @@ __global__ void feature_kernel(const float* __restrict__ x, const float* __restr
 //   3-vector escape direction. Mean over the batch. The gradient is that of the weighted sum
 //   w.x CE + w.y MSE(r) + w.z MSE(ln g) + w.w MSE(dir); the loss terms are reported unweighted. dY goes
 //   out as BF16 in both layouts, the head's bias gradient and the loss terms are summed atomically.
-__global__ void loss_kernel(const float* __restrict__ Y, const uint8_t* __restrict__ cls,
+constexpr int kLossThreads = 256;
+__global__ void __launch_bounds__(kLossThreads) loss_kernel(const float* __restrict__ Y, const uint8_t* __restrict__ cls,
                             const float* __restrict__ tgt, bf16* __restrict__ dy_rm, bf16* __restrict__ dy_t, int ld_t,
                             float* __restrict__ db, float* __restrict__ loss, int n, float inv_n, float4 w) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -714,17 +1000,26 @@ __global__ void loss_kernel(const float* __restrict__ Y, const uint8_t* __restri
 #pragma unroll
         for (int i = 0; i < kOutPad; ++i) dy_t[static_cast<size_t>(i) * ld_t + r] = ob[i];
     }
+    // Bias gradient and loss terms: sums over the warp (shuffles), then over the block's warps in
+    // shared memory, then one atomic per block and value.
+    __shared__ float part[kLossThreads / 32][kOutPad + 4];
+    const int warp = threadIdx.x >> 5;
+    const float terms[4] = {ce, lr_, lg, le};
 #pragma unroll
-    for (int i = 0; i < kOutPad; ++i) {
-        float v = d[i];
+    for (int i = 0; i < kOutPad + 4; ++i) {
+        float v = i < kOutPad ? d[i] : terms[i - kOutPad] * inv_n;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0 && v != 0.0f) atomicAdd(&db[i], v);
+        if (lane == 0) part[warp][i] = v;
     }
-    float terms[4] = {ce, lr_, lg, le};
-    for (int k = 0; k < 4; ++k) {
-        float v = terms[k] * inv_n;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) atomicAdd(&loss[k], v);
+    __syncthreads();
+    if (threadIdx.x < kOutPad + 4) {
+        float v = 0.0f;
+        for (int q = 0; q < kLossThreads / 32; ++q) v += part[q][threadIdx.x];
+        if (threadIdx.x < kOutPad) {
+            if (v != 0.0f) atomicAdd(&db[threadIdx.x], v);
+        } else {
+            atomicAdd(&loss[threadIdx.x - kOutPad], v);
+        }
     }
 }
 
@@ -852,6 +1147,7 @@ struct Maps {
     CUtensorMap F_rm, dy_rm, dy_t, W[kLayers], Wt[kLayers], a_rm[4], dz_rm[2];
     CUtensorMap zs[4], as[4], dzs[2];  // the staged epilogue's [32 x 64] boxes of Z, A and dZ
     CUtensorMap Fm, am[4], dzm[2];     // F, A and dZ as MN-major operands ([64 rows x 64] boxes)
+    CUtensorMap Wl[kLayers], Wtl[kLayers];  // W and W^T in [128 x 64] boxes (the persistent layer GEMM)
 };
 
 // Tensor maps of the operands for batches of n rows (weights, features, activations, gradients), and
@@ -862,7 +1158,8 @@ bool build_maps(bhk_surrogate* s, int n, bool training, Maps* M) {
     for (int l = 0; l < kLayers && ok; ++l) {
         const int fi = fan_in(l, s->hid), fo = fan_out(l, s->hid);
         ok = make_tmap(&M->W[l], s->w_rm[l], fo, fi, box_rows_for(fo)) &&
-             make_tmap(&M->Wt[l], s->w_t[l], fi, fo, box_rows_for(fi));
+             make_tmap(&M->Wt[l], s->w_t[l], fi, fo, box_rows_for(fi)) &&
+             make_tmap(&M->Wl[l], s->w_rm[l], fo, fi, kLayerN) && make_tmap(&M->Wtl[l], s->w_t[l], fi, fo, kLayerN);
     }
     const int H = s->hid;
     for (int i = 0; i < 4 && ok; ++i)
@@ -895,7 +1192,8 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
         om.z = M.zs[l];
         om.r = M.as[l];
         const CUtensorMap& A = l == 0 ? M.F_rm : M.a_rm[l - 1];
-        e = launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st, &om);
+        e = H == kLayerN * 2 ? launch_layer<kBiasSilu>(A, M.Wl[l], om, ea, fan_in(l, H), s->sms, s->err, st)
+                             : launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st, &om);
     }
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, kOutPad);
@@ -940,7 +1238,7 @@ cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMa
 cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const float* tgt, int n, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(s->g, 0, sizeof(float) * s->L.total, st);
     if (e != cudaSuccess) return e;
-    loss_kernel<<<(n + 255) / 256, 256, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
+    loss_kernel<<<(n + kLossThreads - 1) / kLossThreads, kLossThreads, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
                                                  s->loss, n, 1.0f / n, s->w);
     const int H = s->hid;
     // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
@@ -951,7 +1249,8 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
         OutMaps om;
         om.z = M.zs[3];
         om.r = M.dzs[0];
-        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
+        e = H == kLayerN * 2 ? launch_layer<kDsilu>(M.dy_rm, M.Wtl[4], om, ea, kOutPad, s->sms, s->err, st)
+                             : launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
     }
     // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
     int cur = 0;
@@ -964,7 +1263,8 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
         OutMaps om;
         om.z = M.zs[l - 1];
         om.r = M.dzs[1 - cur];
-        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
+        e = H == kLayerN * 2 ? launch_layer<kDsilu>(M.dz_rm[cur], M.Wtl[l], om, ex, H, s->sms, s->err, st)
+                             : launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
         cur = 1 - cur;
     }
     return e;
