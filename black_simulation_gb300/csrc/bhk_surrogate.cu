@@ -40,13 +40,12 @@ constexpr int kTileM = 128;
 constexpr int kChunkK = 64;
 constexpr int kABytes = kTileM * kChunkK * 2;  // 16 KB
 
-enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3, kPartialF32 = 4 };
+enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3, kReduceF32 = 5 };
 
 struct EpiArgs {
     int M, N;              // logical output extent (rows, columns)
     const float* bias;     // [N] or null
-    float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32; kPartialF32: split z
-                           // writes its partial product at f32 + z * M * ld_f32
+    float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32
     int ld_f32;
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
 };
@@ -57,7 +56,7 @@ struct EpiArgs {
 // a deep ring, so that the TMA latency of the next chunks hides behind the current MMAs.
 template <int BN, int EPI>
 __host__ __device__ constexpr int gemm_stages() {
-    return EPI == kPartialF32 ? (BN >= 256 ? 4 : 8) : (BN >= 256 ? 2 : 4);
+    return EPI == kReduceF32 ? (BN >= 256 ? 4 : 8) : (BN >= 256 ? 2 : 4);
 }
 
 template <int BN, int EPI>
@@ -108,6 +107,48 @@ constexpr int kGemmThreads = 256;
 
 // Shared memory a warp of the staged epilogue uses (two 4 KB TMA boxes), carved from the idle ring.
 constexpr int kWarpStage = 8192;
+
+// Split-K weight-gradient epilogue (kReduceF32): the tile's FP32 partial product goes straight into the
+// FP32 gradient through TMA reductions (element-wise adds performed in L2) -- no workspace and no
+// reduction pass; the order in which the splits' adds land is not fixed. Warp (quad, part) owns the 32
+// rows of TMEM lane quadrant `quad` and BN / 2 columns: per 32 columns one tcgen05.ld, one [32 x 32] FP32
+// box written into shared memory under the 128-byte swizzle (double-buffered per warp) and one TMA
+// reduction. Rows at or past M are skipped a whole box at a time (TMA clips partial boxes).
+template <int BN>
+__device__ __forceinline__ void epilogue_reduce(const CUtensorMap* tmG, const EpiArgs& ea, uint32_t tmem,
+                                                uint8_t* stage_base, int m0, int n0) {
+    static_assert(BN % 64 == 0, "two warps of 32-column boxes per lane quadrant");
+    constexpr int kColsW = BN / 2;  // columns per warp
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quad = warp & 3, part = warp >> 2;
+    const int y0 = m0 + 32 * quad;
+    if (y0 >= ea.M) return;
+    uint8_t* wb = stage_base + warp * kWarpStage;
+    const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16) + part * kColsW;
+    const int sw = lane & 7;
+#pragma unroll 1
+    for (int j = 0; j < kColsW / 32; ++j) {
+        uint32_t r[32];
+        tc::tmem_ld32_issue(trow + 32 * j, r);
+        tc::tmem_wait32(r);
+        uint8_t* box = wb + (j & 1) * 4096;
+        if (j >= 2) {  // the reduction of box j - 2 has read this buffer
+            if (lane == 0) tc::bulk_wait_read_but_one();
+            __syncwarp();
+        }
+        uint4* row = reinterpret_cast<uint4*>(box + lane * 128);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) row[c ^ sw] = make_uint4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+        tc::fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) {
+            tc::tma_reduce_add_2d(tmG, box, n0 + part * kColsW + 32 * j, y0);
+            tc::bulk_commit();
+        }
+    }
+    if (lane == 0) tc::bulk_wait_all();
+    __syncwarp();
+}
 
 // Staged epilogue of the hidden layers (kBiasSilu: Z = acc + b and A = silu(Z); kDsilu: dZ = acc *
 // silu'(Z) and the bias gradient). Warp (quad, part) owns the 32 rows of TMEM lane quadrant `quad` and
@@ -352,6 +393,8 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
             // The pipeline's shared memory is idle now: it holds the warps' output boxes.
             if (!epilogue_staged<BN, EPI>(&tmZ, &tmR, ea, tmem, sA, sx, zbar, m0, n0)) atomicExch(err, 1);
+        } else if constexpr (EPI == kReduceF32) {
+            epilogue_reduce<BN>(&tmZ, ea, tmem, sA, m0, n0);
         } else {
             constexpr int kJ = BN / 16;                  // 16-column groups of the tile
             constexpr int kSplit = kJ >= 2 ? 2 : 1;      // warps sharing a lane quadrant
@@ -373,19 +416,9 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                     for (int i = 0; i < 16; ++i)
                         if (nb + i < ea.N)
                             ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i] = v[i] + (ea.bias ? ea.bias[nb + i] : 0.0f);
-                } else if constexpr (EPI == kAtomicF32) {
+                } else {  // kAtomicF32
                     for (int i = 0; i < 16; ++i)
                         if (nb + i < ea.N) atomicAdd(&ea.f32[static_cast<size_t>(m) * ea.ld_f32 + nb + i], v[i]);
-                } else {  // kPartialF32: split z writes its partial product at f32 + z * M * ld_f32
-                    float* dst = ea.f32 + static_cast<size_t>(blockIdx.z) * ea.M * ea.ld_f32 +
-                                 static_cast<size_t>(m) * ea.ld_f32 + nb;
-                    if (nb + 16 <= ea.N) {
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-                    } else {
-                        for (int i = 0; i < 16 && nb + i < ea.N; ++i) dst[i] = v[i];
-                    }
                 }
             };
             // Warps without columns (a 16-wide tile's second four) have nothing to do.
@@ -667,60 +700,6 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     if (warp == kLayerEpiWarps + 1) tc::tmem_dealloc(tmem, 2 * kLayerN);
 }
 
-// dst[i] += sum over the splits of ws[split * count + i] (count a multiple of 4, 16-byte aligned).
-// A block of 256 threads takes 32 float4 of dst at a time: warp g sums splits g, g + 8, g + 16, ...
-// of them (each warp load is 512 contiguous bytes), and warp 0 adds the eight partial sums to dst in
-// warp order, so the result does not depend on timing.
-constexpr int kReduceGroups = 8;
-__global__ void __launch_bounds__(32 * kReduceGroups)
-reduce_splits_kernel(const float* __restrict__ ws, int splits, long long count, float* dst) {
-    __shared__ float4 part[kReduceGroups][32];
-    const long long n4 = count / 4;
-    const int c = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const float4* w4 = reinterpret_cast<const float4*>(ws);
-    for (long long base = blockIdx.x * 32LL; base < n4; base += static_cast<long long>(gridDim.x) * 32) {
-        const long long i = base + c;
-        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (i < n4) {
-            // four splits' loads in flight at a time
-            int sp = g;
-            for (; sp + 3 * kReduceGroups < splits; sp += 4 * kReduceGroups) {
-                float4 w[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) w[u] = w4[(sp + u * kReduceGroups) * n4 + i];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    acc.x += w[u].x;
-                    acc.y += w[u].y;
-                    acc.z += w[u].z;
-                    acc.w += w[u].w;
-                }
-            }
-            for (; sp < splits; sp += kReduceGroups) {
-                const float4 w = w4[sp * n4 + i];
-                acc.x += w.x;
-                acc.y += w.y;
-                acc.z += w.z;
-                acc.w += w.w;
-            }
-        }
-        part[g][c] = acc;
-        __syncthreads();
-        if (g == 0 && i < n4) {
-            float4 d = reinterpret_cast<float4*>(dst)[i];
-#pragma unroll
-            for (int q = 0; q < kReduceGroups; ++q) {
-                d.x += part[q][c].x;
-                d.y += part[q][c].y;
-                d.z += part[q][c].z;
-                d.w += part[q][c].w;
-            }
-            reinterpret_cast<float4*>(dst)[i] = d;
-        }
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------------------------------------------ host side ----
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -765,10 +744,26 @@ bool make_tmap_rows32(CUtensorMap* map, const void* base, uint64_t rows, uint64_
     return make_tmap_box(map, base, rows, cols, 64, 32, true);
 }
 
-// Tensor maps of the staged epilogue (kBiasSilu: Z and A written; kDsilu: Z read, dZ written).
+// Tensor maps of the epilogue (kBiasSilu: Z and A written; kDsilu: Z read, dZ written; kReduceF32: the
+// FP32 gradient, in z).
 struct OutMaps {
     CUtensorMap z, r;
 };
+
+// An FP32 row-major [rows x cols] matrix in [32 rows][32 columns] boxes (128-byte swizzle), the target of
+// the weight gradients' TMA reductions.
+bool make_tmap_f32_32(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((cols * 4) & 15)) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 4};
+    const cuuint32_t box[2] = {32, 32};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 template <int BN, int EPI, int MAJ>
 cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const EpiArgs& ea, int M, int N, int K,
@@ -796,7 +791,7 @@ cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const EpiArg
     if constexpr (EPI == kBiasSilu || EPI == kDsilu) {
         if (!om) return cudaErrorInvalidValue;
     }
-    if constexpr (EPI == kBiasSilu || EPI == kDsilu || (MAJ & 2) != 0) {
+    if constexpr (EPI == kBiasSilu || EPI == kDsilu || EPI == kReduceF32 || (MAJ & 2) != 0) {
         if (N <= 64) return launch_gemm_bn<64, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
     } else {
         if (N <= 16) return launch_gemm_bn<16, EPI, MAJ>(a, b, ea, M, N, K, splits, err, s, om);
@@ -823,13 +818,6 @@ cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMa
     const int pairs = std::max(1, std::min(mtiles, sms / nh));
     layer_kernel<EPI><<<pairs * nh, kLayerThreads, layer_smem_bytes(), s>>>(a, w, om.z, om.r, ea, K, err);
     return cudaGetLastError();
-}
-
-// K splits launch_gemm makes for `splits` requested (grid z).
-int grid_splits(int K, int splits) {
-    splits = splits < 1 ? 1 : splits;
-    const int per = ((K + splits - 1) / splits + kChunkK - 1) / kChunkK * kChunkK;
-    return (K + per - 1) / per;
 }
 
 }  // namespace sur
@@ -1107,7 +1095,6 @@ struct bhk_surrogate {
     size_t cap_list = 0;
     unsigned long long* n_list = nullptr;
     float* half_bias = nullptr;
-    float* ws = nullptr;  // split-K partial products of the weight gradients (96 x 256 x 256)
     unsigned long long* n_list_host = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
@@ -1148,6 +1135,7 @@ struct Maps {
     CUtensorMap zs[4], as[4], dzs[2];  // the staged epilogue's [32 x 64] boxes of Z, A and dZ
     CUtensorMap Fm, am[4], dzm[2];     // F, A and dZ as MN-major operands ([64 rows x 64] boxes)
     CUtensorMap Wl[kLayers], Wtl[kLayers];  // W and W^T in [128 x 64] boxes (the persistent layer GEMM)
+    CUtensorMap gm[kLayers];                // the FP32 weight gradients, targets of TMA reductions
 };
 
 // Tensor maps of the operands for batches of n rows (weights, features, activations, gradients), and
@@ -1169,6 +1157,8 @@ bool build_maps(bhk_surrogate* s, int n, bool training, Maps* M) {
         ok = make_tmap(&M->dz_rm[i], s->dz_rm[i], n, H, kTileM) && make_tmap_rows32(&M->dzs[i], s->dz_rm[i], n, H);
     if (!training) return ok;
     ok = ok && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM) && make_tmap(&M->Fm, s->F_rm, n, kFeat, 64);
+    for (int l = 0; l < kLayers && ok; ++l)
+        ok = make_tmap_f32_32(&M->gm[l], s->g + s->L.w[l], fan_out(l, H), fan_in(l, H));
     for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->am[i], s->a_rm[i], n, H, 64);
     for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dzm[i], s->dz_rm[i], n, H, 64);
     return ok;
@@ -1206,32 +1196,25 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
 }
 
 // K splits of a weight gradient (M x N, K = n rows): one CTA per SM over the M tiles, each split at
-// least 512 rows, and at most what the workspace (96 x H x max(H, 64) floats) holds.
-int split_for(const bhk_surrogate* s, int n, int M, int N) {
+// least 512 rows.
+int split_for(const bhk_surrogate* s, int n, int M) {
     const int mtiles = (M + kTileM - 1) / kTileM;
-    const long long ws_floats = 96LL * s->hid * std::max(s->hid, kFeat);
     long long sp = s->sms / mtiles;
     sp = std::min<long long>(sp, n / 512);
-    sp = std::min<long long>(sp, ws_floats / (static_cast<long long>(M) * N));
     return sp < 1 ? 1 : static_cast<int>(sp);
 }
 
-// dst (M x N FP32, dense) += the weight gradient sum over K of A_k B_k^T: the split-K partial products go
-// to the workspace with plain stores, then one pass sums them into dst. MAJ as for gemm_kernel: the
-// hidden layers' operands are the row-major activations and gradients themselves, read MN-major.
+// The gradient of layer l's weights (M x N FP32 in s->g, zeroed before the backward pass) += the sum
+// over K of A_k B_k^T: each K split adds its partial product with TMA reductions. MAJ as for
+// gemm_kernel: the hidden layers' operands are the row-major activations and gradients themselves,
+// read MN-major.
 template <int MAJ>
-cudaError_t weight_grad(bhk_surrogate* s, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, float* dst,
-                        cudaStream_t st) {
-    const int splits = split_for(s, K, M, N);
+cudaError_t weight_grad(bhk_surrogate* s, const Maps& maps, int l, const CUtensorMap& A, const CUtensorMap& B, int M,
+                        int N, int K, cudaStream_t st) {
     EpiArgs ea = epi(M, N);
-    ea.f32 = s->ws;
-    ea.ld_f32 = N;
-    cudaError_t e = launch_gemm<kPartialF32, MAJ>(A, B, ea, M, N, K, splits, s->err, st);
-    if (e != cudaSuccess) return e;
-    const long long count = static_cast<long long>(M) * N;
-    const int blocks = static_cast<int>(std::min<long long>((count / 4 + 31) / 32, 8LL * s->sms));
-    reduce_splits_kernel<<<blocks, 32 * kReduceGroups, 0, st>>>(s->ws, grid_splits(K, splits), count, dst);
-    return cudaGetLastError();
+    OutMaps om;
+    om.z = maps.gm[l];
+    return launch_gemm<kReduceF32, MAJ>(A, B, ea, M, N, K, split_for(s, K, M), s->err, st, &om);
 }
 
 // Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss.
@@ -1242,7 +1225,7 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
                                                  s->loss, n, 1.0f / n, s->w);
     const int H = s->hid;
     // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
-    e = weight_grad<2>(s, M.dy_t, M.am[3], kOutPad, H, n, s->g + s->L.w[4], st);
+    e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, H);
         ea.colsum = s->g + s->L.b[3];
@@ -1256,7 +1239,7 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
         const CUtensorMap& Bop = l == 0 ? M.Fm : M.am[l - 1];
-        e = weight_grad<3>(s, M.dzm[cur], Bop, H, fan_in(l, H), n, s->g + s->L.w[l], st);
+        e = weight_grad<3>(s, M, l, M.dzm[cur], Bop, H, fan_in(l, H), n, st);
         if (e != cudaSuccess || l == 0) break;
         EpiArgs ex = epi(n, H);
         ex.colsum = s->g + s->L.b[l - 1];
@@ -1335,7 +1318,6 @@ bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_bat
               dalloc(s, &s->dy_rm, B * kOutPad) && dalloc(s, &s->dy_t, B * kOutPad) &&
               dalloc(s, &s->Y, B * kOutPad) && dalloc(s, &s->loss, 4) && dalloc(s, &s->err, 1) &&
               dalloc(s, &s->n_list, 1) && dalloc(s, &s->half_bias, 4 * H) &&
-              dalloc(s, &s->ws, static_cast<size_t>(96) * H * std::max(H, kFeat)) &&
               cudaMallocHost(reinterpret_cast<void**>(&s->n_list_host), 8) == cudaSuccess;
     for (int i = 0; i < 3 && ok; ++i) ok = cudaEventCreate(&s->ev[i]) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
