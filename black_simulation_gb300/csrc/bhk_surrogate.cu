@@ -587,6 +587,12 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int x = n0 + 64 * part;  // the warp's first output column
         bool ok = true;
         int z_issued = 0, z_waited = 0;  // kDsilu: pre-activation box loads (lane 0 issues)
+        // kDsilu: this lane's share of the bias gradient of the warp's 64 columns, summed over the rows it
+        // meets in all of the CTA's tiles (the CTA's columns are the same for every tile); the sums over
+        // the warp's lanes are taken once, after the last tile.
+        float csum[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) csum[i] = 0.0f;
         auto load_z = [&](int t) {      // the box of tile t into buffer t & 1 (lane 0)
             uint64_t* bar = &zbar[2 * warp + (t & 1)];
             tc::mbar_expect_tx(bar, 4096);
@@ -660,11 +666,8 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
                     zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
                     zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
-                    if (ea.colsum) {
-                        int col;
-                        const float tot = warp_colsum16(dz, lane, col);
-                        if (!(lane & 1)) atomicAdd(&sx[cb + col], tot);
-                    }
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) csum[16 * g + i] += dz[i];
                 }
             }
             tc::fence_proxy_async();
@@ -677,6 +680,19 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     tc::tma_store_2d(&tmR, zin, x, y0);
                 }
                 tc::bulk_commit();
+            }
+        }
+        if constexpr (EPI == kDsilu) {
+            if (ea.colsum) {
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    float v[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = csum[16 * g + i];
+                    int col;
+                    const float tot = warp_colsum16(v, lane, col);
+                    if (!(lane & 1)) atomicAdd(&sx[64 * part + 16 * g + col], tot);
+                }
             }
         }
         if (lane == 0) {
