@@ -326,6 +326,9 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
+    // Launched programmatically: the previous grid of the stream has finished before any global access.
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
 
     if (threadIdx.x == 0) {
         auto load = [&](int stage, int chunk) {
@@ -512,16 +515,20 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         *consumed = 0;
         tc::fence_mbar_init();
     }
-    if constexpr (EPI == kBiasSilu) {
-        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
-    } else {
-        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
-    }
     if (warp == kLayerEpiWarps + 1) tc::tmem_alloc(tmem_slot, 2 * kLayerN);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
+    // Launched programmatically: the previous grid of the stream has finished before any global access.
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
+    if constexpr (EPI == kBiasSilu) {
+        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
+    } else {
+        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
+    }
+    __syncthreads();
 
     if (warp == kLayerEpiWarps) {
         // ---- producer: the weights once, then the A chunks of every tile through the ring ----
@@ -718,6 +725,24 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
 
 // ------------------------------------------------------------------------------ host side ----
 
+// Launch with programmatic stream serialization: the grid may be scheduled while the previous grid of
+// the stream is finishing; every kernel launched this way waits for it (grid_dep_wait) before it
+// touches global memory, so only its set-up (barriers, TMEM) overlaps.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at{};
+    at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -794,8 +819,8 @@ cudaError_t launch_gemm_bn(const CUtensorMap& a, const CUtensorMap& b, const Epi
     const dim3 grid((M + kTileM - 1) / kTileM, (N + BN - 1) / BN, (K + per - 1) / per);
     static const OutMaps none{};
     const OutMaps& o = om ? *om : none;
-    gemm_kernel<BN, EPI, MAJ><<<grid, kGemmThreads, gemm_smem_bytes<BN, EPI>(), s>>>(a, b, o.z, o.r, ea, K, per, err);
-    return cudaGetLastError();
+    return launch_pdl(gemm_kernel<BN, EPI, MAJ>, grid, dim3(kGemmThreads), gemm_smem_bytes<BN, EPI>(), s, a, b, o.z, o.r,
+                      ea, K, per, err);
 }
 
 // C = A * B^T tile-width choice by N.
@@ -832,8 +857,8 @@ cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMa
     const int nh = ea.N / kLayerN;
     const int mtiles = (ea.M + kTileM - 1) / kTileM;
     const int pairs = std::max(1, std::min(mtiles, sms / nh));
-    layer_kernel<EPI><<<pairs * nh, kLayerThreads, layer_smem_bytes(), s>>>(a, w, om.z, om.r, ea, K, err);
-    return cudaGetLastError();
+    return launch_pdl(layer_kernel<EPI>, dim3(pairs * nh), dim3(kLayerThreads), layer_smem_bytes(), s, a, w, om.z, om.r,
+                      ea, K, err);
 }
 
 }  // namespace sur
@@ -940,9 +965,17 @@ __device__ __forceinline__ void fourier_features(const float* x, const float* sb
     }
 }
 
-// Fourier features of n rays, row-major [n x 64].
-__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm, int n) {
+// Fourier features of n rays, row-major [n x 64]. The first kernel of a training step also zeroes what
+// the step accumulates into (the gradient, n_a floats at zero_a, and the loss terms, n_b at zero_b).
+__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm, int n,
+                               float* zero_a, long long n_a, float* zero_b, int n_b) {
     __shared__ float sb[kFreq * kIn];
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n_a;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        zero_a[i] = 0.0f;
+    if (blockIdx.x == 0 && threadIdx.x < n_b) zero_b[threadIdx.x] = 0.0f;
     for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
     __syncthreads();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -964,6 +997,8 @@ constexpr int kLossThreads = 256;
 __global__ void __launch_bounds__(kLossThreads) loss_kernel(const float* __restrict__ Y, const uint8_t* __restrict__ cls,
                             const float* __restrict__ tgt, bf16* __restrict__ dy_rm, bf16* __restrict__ dy_t, int ld_t,
                             float* __restrict__ db, float* __restrict__ loss, int n, float inv_n, float4 w) {
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     float d[kOutPad];
@@ -1039,9 +1074,14 @@ struct AdamArgs {
     size_t total;
     int hid;                        // hidden width of the network
     float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
+    const float* loss;              // with hist: the step's four loss terms, copied to hist
+    float* hist;
 };
 
 __global__ void adam_kernel(AdamArgs a) {
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
+    if (a.hist && blockIdx.x == 0 && threadIdx.x < 4) a.hist[threadIdx.x] = a.loss[threadIdx.x];
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
          i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const float g = a.g[i];
@@ -1233,12 +1273,13 @@ cudaError_t weight_grad(bhk_surrogate* s, const Maps& maps, int l, const CUtenso
     return launch_gemm<kReduceF32, MAJ>(A, B, ea, M, N, K, split_for(s, K, M), s->err, st, &om);
 }
 
-// Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss.
+// Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss, which the caller has
+// zeroed (the training step's feature_kernel does).
 cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const float* tgt, int n, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(s->g, 0, sizeof(float) * s->L.total, st);
+    cudaError_t e = launch_pdl(loss_kernel, dim3((n + kLossThreads - 1) / kLossThreads), dim3(kLossThreads), 0, st,
+                               static_cast<const float*>(s->Y), cls, tgt, s->dy_rm, s->dy_t, s->cap,
+                               s->g + s->L.b[4], s->loss, n, 1.0f / n, s->w);
     if (e != cudaSuccess) return e;
-    loss_kernel<<<(n + kLossThreads - 1) / kLossThreads, kLossThreads, 0, st>>>(s->Y, cls, tgt, s->dy_rm, s->dy_t, s->cap, s->g + s->L.b[4],
-                                                 s->loss, n, 1.0f / n, s->w);
     const int H = s->hid;
     // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
     e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
@@ -1493,9 +1534,10 @@ bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8
     }
     cudaStream_t st = nullptr;
     cudaMemsetAsync(s->err, 0, sizeof(int), st);
-    cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
-    feature_kernel<<<(n + 127) / 128, 128, 0, st>>>(x, s->Bm, s->F_rm, n);
-    cudaError_t e = forward(s, M, n, st);
+    cudaError_t e = launch_pdl(feature_kernel, dim3((n + 127) / 128), dim3(128), 0, st, x,
+                               static_cast<const float*>(s->Bm), s->F_rm, n, s->g,
+                               static_cast<long long>(s->L.total), s->loss, 4);
+    if (e == cudaSuccess) e = forward(s, M, n, st);
     if (e == cudaSuccess) e = backward(s, M, cls, tgt, n, st);
     if (e != cudaSuccess) {
         set_last_error(std::string("bhk_surrogate_gradients: ") + cudaGetErrorString(e));
@@ -1534,22 +1576,22 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
     aa.b1 = 0.9f;
     aa.b2 = 0.999f;
     aa.eps = 1e-8f;
+    // One step: features (zeroing the gradient and the loss terms), forward, loss and backward, Adam
+    // (copying the loss terms to the history) -- kernels launched programmatically back to back.
+    aa.loss = s->loss;
     for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
         const int64_t off = (t % nb) * batch;
-        cudaMemsetAsync(s->loss, 0, 4 * sizeof(float), st);
-        feature_kernel<<<(batch + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, batch);
-        e = forward(s, M, batch, st);
+        e = launch_pdl(feature_kernel, dim3((batch + 127) / 128), dim3(128), 0, st, x + off * kIn,
+                       static_cast<const float*>(s->Bm), s->F_rm, batch, s->g, static_cast<long long>(s->L.total),
+                       s->loss, 4);
+        if (e == cudaSuccess) e = forward(s, M, batch, st);
         if (e == cudaSuccess) e = backward(s, M, cls + off, tgt + off * kOut, batch, st);
         ++s->step;
         aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
         aa.c1 = static_cast<float>(1.0 / (1.0 - std::pow(0.9, static_cast<double>(s->step))));
         aa.c2 = static_cast<float>(1.0 / (1.0 - std::pow(0.999, static_cast<double>(s->step))));
-        if (e == cudaSuccess) {
-            adam_kernel<<<256, 256, 0, st>>>(aa);
-            e = cudaGetLastError();
-        }
-        if (hist && e == cudaSuccess)
-            e = cudaMemcpyAsync(hist + 4 * t, s->loss, 4 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        aa.hist = hist ? hist + 4 * t : nullptr;
+        if (e == cudaSuccess) e = launch_pdl(adam_kernel, dim3(256), dim3(256), 0, st, aa);
     }
     bhk_status rs = e == cudaSuccess ? check_err(s, st) : BHK_ECUDA;
     if (e != cudaSuccess) set_last_error(std::string("bhk_surrogate_train: ") + cudaGetErrorString(e));
@@ -1577,8 +1619,10 @@ bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, fl
             set_last_error("bhk_surrogate_predict: tensor map creation failed");
             return BHK_ECUDA;
         }
-        feature_kernel<<<(rows + 127) / 128, 128, 0, st>>>(x + off * kIn, s->Bm, s->F_rm, rows);
-        cudaError_t e = forward(s, M, rows, st);
+        cudaError_t e = launch_pdl(feature_kernel, dim3((rows + 127) / 128), dim3(128), 0, st, x + off * kIn,
+                                   static_cast<const float*>(s->Bm), s->F_rm, rows, static_cast<float*>(nullptr),
+                                   0LL, static_cast<float*>(nullptr), 0);
+        if (e == cudaSuccess) e = forward(s, M, rows, st);
         if (e == cudaSuccess)
             e = cudaMemcpy2DAsync(out + off * kOut, kOut * sizeof(float), s->Y, kOutPad * sizeof(float),
                                   kOut * sizeof(float), rows, cudaMemcpyDeviceToDevice, st);

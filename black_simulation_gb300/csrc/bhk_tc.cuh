@@ -106,6 +106,15 @@ __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bu
 // Waits until every committed bulk store of this thread has completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// Programmatic dependent launch. grid_dep_wait: returns once the grid before this one in the stream
+// has completed and its memory is visible (at once for a grid launched without the programmatic
+// attribute); every global access that may depend on that grid comes after it. grid_dep_launch: lets
+// the next grid of the stream be scheduled (its threads then wait in their own grid_dep_wait); the
+// kernels here call it after their own wait and after taking their TMEM, so that a grid waiting for
+// this one never holds TMEM this one still needs.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
