@@ -48,6 +48,7 @@ struct EpiArgs {
     float* f32;            // kStoreF32 / kAtomicF32 output, row-major with ld_f32
     int ld_f32;
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
+    int no_store;          // kDsilu in layer_kernel: dZ is not written (only the fused gradients are used)
 };
 
 // Pipeline depth: the network's GEMMs have K <= 256 (4 chunks) and run two CTAs (each 256 TMEM
@@ -457,24 +458,41 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 // 64 (w >> 2) .. + 63 of the half) and hand the accumulator back. Every wait is bounded; after a
 // timeout the roles stop, the loads in flight are waited for (bounded) and the error flag is set.
 constexpr int kLayerN = 128;                  // output columns per CTA
-constexpr int kLayerRing = 4;                 // A-chunk stages
 constexpr int kLayerEpiWarps = 8;
 constexpr int kLayerThreads = 32 * (kLayerEpiWarps + 2);
 constexpr int kLayerWBytes = 4 * kLayerN * kChunkK * 2;  // K <= 256: four 16 KB chunks of W
 constexpr int kLayerStage = 8192;                        // per epilogue warp: two 4 KB boxes
 
-__host__ __device__ constexpr int layer_smem_bytes() {
-    return kLayerWBytes + kLayerRing * kABytes + kLayerEpiWarps * kLayerStage + 1024 /* alignment */ +
+// Ring stages (16 KB each): the fused weight gradient streams its second operand through the ring too.
+__host__ __device__ constexpr int layer_ring(int wg) { return wg ? 6 : 4; }
+
+__host__ __device__ constexpr int layer_smem_bytes(int wg) {
+    return kLayerWBytes + layer_ring(wg) * kABytes + kLayerEpiWarps * kLayerStage + 1024 /* alignment */ +
            512 /* barriers */ + kLayerN * 4 /* bias or column sums */;
 }
 
-template <int EPI>
+// WG > 0 (kDsilu only): the kernel also computes the weight gradient of the layer whose dZ it produces,
+// dW[n0 + i][j] += sum over the tile's rows r of dZ[r][n0 + i] Ain[r][j] (j < WG, Ain = the layer's input
+// activations, row-major [rows x WG], map tmB2 in [32 rows x 64] boxes): per tile one more set of MMAs
+// (M = 128 dZ columns, N = WG, K = the tile's 128 rows), both operands MN-major -- dZ straight from the
+// epilogue's staging boxes, which are laid out as the 128-byte-swizzled MN-major operand, Ain through
+// the ring -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
+// FP32 gradient (map tmG) with TMA reductions at the end. The ring carries the tiles' chunks in the
+// order D(0), D(1), G(0), D(2), G(1), ... (D = the layer GEMM's A, G = Ain), so that the weight
+// gradient of tile t, which waits for tile t's epilogue, never holds up the MMAs of tile t + 1.
+template <int EPI, int WG = 0>
 __global__ void __launch_bounds__(kLayerThreads, 1)
 layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW,
-             const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR, EpiArgs ea, int K,
+             const __grid_constant__ CUtensorMap tmZ, const __grid_constant__ CUtensorMap tmR,
+             const __grid_constant__ CUtensorMap tmB2, const __grid_constant__ CUtensorMap tmG, EpiArgs ea, int K,
              int* err) {
     static_assert(EPI == kBiasSilu || EPI == kDsilu, "hidden-layer epilogues only");
+    static_assert(WG == 0 || (EPI == kDsilu && (WG == 64 || WG == 256)), "a fused weight gradient of width 64 or 256");
+    constexpr int kLayerRing = layer_ring(WG);
     constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, kLayerN);
+    constexpr uint32_t kIdescG = tc::idesc_bf16(kTileM, WG ? WG : 64, true, true);
+    constexpr uint32_t kTmemCols = WG ? 512 : 2 * kLayerN;
+    constexpr int kGBytes = WG * 32 * 2;  // one 32-row chunk of Ain
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* sW = smem;
@@ -486,7 +504,10 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     uint64_t* tempty = tfull + 2;               // accumulator b has been read by the epilogue
     uint64_t* wbar = tempty + 2;                // the weights have landed
     uint64_t* zbar = wbar + 1;                  // [warp][buffer]: kDsilu pre-activation boxes
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(zbar + 2 * kLayerEpiWarps);
+    uint64_t* dzready = zbar + 2 * kLayerEpiWarps;  // (WG) staging buffer b holds a tile's dZ
+    uint64_t* dzfree = dzready + 2;                 // (WG) the weight-gradient MMAs have read buffer b
+    uint64_t* wdone = dzfree + 2;                   // (WG) every weight-gradient MMA has completed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wdone + 1);
     volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
     volatile int* consumed = fail + 1;  // A chunks the MMA thread has taken (for the drain)
     float* sx = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(full) + 512);
@@ -511,11 +532,16 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
         tc::mbar_init(wbar, 1);
         for (int i = 0; i < 2 * kLayerEpiWarps; ++i) tc::mbar_init(&zbar[i], 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&dzready[b], kLayerEpiWarps);
+            tc::mbar_init(&dzfree[b], 1);
+        }
+        tc::mbar_init(wdone, 1);
         *fail = 0;
         *consumed = 0;
         tc::fence_mbar_init();
     }
-    if (warp == kLayerEpiWarps + 1) tc::tmem_alloc(tmem_slot, 2 * kLayerN);
+    if (warp == kLayerEpiWarps + 1) tc::tmem_alloc(tmem_slot, kTmemCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -536,16 +562,39 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             tc::mbar_expect_tx(wbar, kc * kABytes);
             for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
             int issued = 0;
-            for (int t = 0; t < my_tiles && !*fail; ++t) {
-                const int m0 = (pair + t * pairs) * kTileM;
-                for (int c = 0; c < kc; ++c, ++issued) {
-                    const int s = issued % kLayerRing, ph = (issued / kLayerRing) & 1;
-                    if (!tc::mbar_wait(&empty[s], ph ^ 1)) {
-                        *fail = 1;
-                        break;
+            // Takes the next ring stage (false: a wait timed out).
+            auto next_stage = [&](int& s) {
+                s = issued % kLayerRing;
+                if (!tc::mbar_wait(&empty[s], ((issued / kLayerRing) & 1) ^ 1)) {
+                    *fail = 1;
+                    return false;
+                }
+                return true;
+            };
+            bool ok = true;
+            for (int t = 0; t <= my_tiles && ok && !*fail; ++t) {
+                if (t < my_tiles) {  // D(t): the layer GEMM's A chunks
+                    const int m0 = (pair + t * pairs) * kTileM;
+                    for (int c = 0; c < kc && ok; ++c) {
+                        int s;
+                        if (!(ok = next_stage(s))) break;
+                        tc::mbar_expect_tx(&full[s], kABytes);
+                        tc::tma_load_2d(sRing + s * kABytes, &tmA, c * kChunkK, m0, &full[s]);
+                        ++issued;
                     }
-                    tc::mbar_expect_tx(&full[s], kABytes);
-                    tc::tma_load_2d(sRing + s * kABytes, &tmA, c * kChunkK, m0, &full[s]);
+                }
+                if constexpr (WG > 0) {
+                    if (t >= 1 && ok) {  // G(t - 1): the weight gradient's Ain rows, 32 at a time
+                        const int m0 = (pair + (t - 1) * pairs) * kTileM;
+                        for (int c = 0; c < kTileM / 32 && ok; ++c) {
+                            int s;
+                            if (!(ok = next_stage(s))) break;
+                            tc::mbar_expect_tx(&full[s], kGBytes);
+                            for (int j = 0; j < WG / 64; ++j)
+                                tc::tma_load_2d(sRing + s * kABytes + j * 4096, &tmB2, 64 * j, m0 + 32 * c, &full[s]);
+                            ++issued;
+                        }
+                    }
                 }
             }
             // Drain (bounded): every chunk issued has landed before the CTA may exit.
@@ -557,27 +606,57 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         if (lane == 0) {
             bool ok = tc::mbar_wait(wbar, 0);
             int taken = 0;
-            for (int t = 0; t < my_tiles && ok; ++t) {
-                const int b = t & 1, u = t >> 1;
-                ok = tc::mbar_wait(&tempty[b], (u & 1) ^ 1) && !*fail;
+            // The next ring stage, once its chunk has landed (false: a wait timed out or a role failed).
+            auto take = [&](int& s) {
+                s = taken % kLayerRing;
+                if (!tc::mbar_wait(&full[s], (taken / kLayerRing) & 1) || *fail) return false;
                 tc::fence_after_sync();
-                const uint32_t d = tmem + b * kLayerN;
-                for (int c = 0; c < kc && ok; ++c, ++taken) {
-                    const int s = taken % kLayerRing, ph = (taken / kLayerRing) & 1;
-                    if (!tc::mbar_wait(&full[s], ph) || *fail) {
-                        ok = false;
-                        break;
-                    }
+                return true;
+            };
+            for (int t = 0; t <= my_tiles && ok; ++t) {
+                if (t < my_tiles) {  // D(t) into accumulator t & 1
+                    const int b = t & 1, u = t >> 1;
+                    ok = tc::mbar_wait(&tempty[b], (u & 1) ^ 1) && !*fail;
                     tc::fence_after_sync();
-                    const uint64_t ad = tc::smem_desc_sw128(sRing + s * kABytes);
-                    const uint64_t bd = tc::smem_desc_sw128(sW + c * kABytes);
+                    const uint32_t d = tmem + b * kLayerN;
+                    for (int c = 0; c < kc && ok; ++c) {
+                        int s;
+                        if (!(ok = take(s))) break;
+                        const uint64_t ad = tc::smem_desc_sw128(sRing + s * kABytes);
+                        const uint64_t bd = tc::smem_desc_sw128(sW + c * kABytes);
 #pragma unroll
-                    for (int kk = 0; kk < kChunkK / 16; ++kk)
-                        tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
-                    tc::mma_commit(&empty[s]);
-                    *consumed = taken + 1;
+                        for (int kk = 0; kk < kChunkK / 16; ++kk)
+                            tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
+                        tc::mma_commit(&empty[s]);
+                        *consumed = ++taken;
+                    }
+                    if (ok) tc::mma_commit(&tfull[b]);
                 }
-                if (ok) tc::mma_commit(&tfull[b]);
+                if constexpr (WG > 0) {
+                    if (t >= 1 && ok) {  // G(t - 1): dW += dZ(t - 1)^T Ain(t - 1), K = 16 rows per MMA
+                        const int tg = t - 1, b = tg & 1;
+                        ok = tc::mbar_wait(&dzready[b], (tg >> 1) & 1) && !*fail;
+                        tc::fence_after_sync();
+                        for (int c = 0; c < kTileM / 32 && ok; ++c) {  // rows 32 c .. 32 c + 31: quad c's boxes
+                            int s;
+                            if (!(ok = take(s))) break;
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                // dZ: M = the CTA's 128 columns (part 0 and part 1 boxes, 4 warps apart)
+                                const uint64_t ad =
+                                    tc::smem_desc_sw128_mn(sStage + c * kLayerStage + b * 4096 + h * 2048, 4 * kLayerStage);
+                                const uint64_t bd = tc::smem_desc_sw128_mn(sRing + s * kABytes + h * 2048, 4096);
+                                tc::mma_bf16(tmem + 2 * kLayerN, ad, bd, kIdescG, (tg > 0 || c > 0 || h > 0) ? 1u : 0u);
+                            }
+                            tc::mma_commit(&empty[s]);
+                            *consumed = ++taken;
+                        }
+                        if (ok) tc::mma_commit(&dzfree[b]);
+                    }
+                }
+            }
+            if constexpr (WG > 0) {
+                if (ok) tc::mma_commit(wdone);
             }
             if (!ok) {
                 *fail = 1;
@@ -614,7 +693,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             const int y0 = (pair + t * pairs) * kTileM + 32 * quad;
             const bool live = y0 + lane < ea.M;
             if (lane == 0) tc::bulk_wait_read_all();  // the stores of tile t - 1 have read the staging
-            if constexpr (EPI == kDsilu) {
+            if constexpr (EPI == kDsilu && WG == 0) {
                 if (lane == 0 && t + 1 < my_tiles) load_z(t + 1);  // one tile ahead, into the other buffer
             }
             __syncwarp();
@@ -684,9 +763,25 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     tc::tma_store_2d(&tmZ, wb, x, y0);
                     tc::tma_store_2d(&tmR, wb + 4096, x, y0);
                 } else {
-                    tc::tma_store_2d(&tmR, zin, x, y0);
+                    if (!ea.no_store) tc::tma_store_2d(&tmR, zin, x, y0);
                 }
                 tc::bulk_commit();
+                if constexpr (WG > 0) tc::mbar_arrive(&dzready[t & 1]);  // dZ(t) for the weight-gradient MMAs
+            }
+            if constexpr (WG > 0) {
+                // The next tile's Z box goes into the buffer of tile t - 1 once the weight-gradient MMAs have
+                // read it (its dZ store has: the wait at the top of this iteration).
+                if (t + 1 < my_tiles) {
+                    int zok = 1;
+                    if (lane == 0) {
+                        if (t >= 1) zok = tc::mbar_wait(&dzfree[(t - 1) & 1], ((t - 1) >> 1) & 1) ? 1 : 0;
+                        if (zok) load_z(t + 1);
+                    }
+                    if (!__shfl_sync(0xffffffffu, zok, 0)) {
+                        ok = false;
+                        break;
+                    }
+                }
             }
         }
         if constexpr (EPI == kDsilu) {
@@ -699,6 +794,41 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     int col;
                     const float tot = warp_colsum16(v, lane, col);
                     if (!(lane & 1)) atomicAdd(&sx[64 * part + 16 * g + col], tot);
+                }
+            }
+        }
+        if constexpr (WG > 0) {
+            // The CTA's weight-gradient rows n0 .. n0 + 127 (the lanes of TMEM columns 256 ..): warp (quad,
+            // part) adds rows n0 + 32 quad .. and columns part WG / 2 .. into the FP32 gradient, a [32 x 32]
+            // box at a time through its (now idle) staging, double-buffered.
+            if (ok) {
+                if (lane == 0) tc::bulk_wait_all();
+                __syncwarp();
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(wdone, 0) ? 1 : 0) != 0;
+            }
+            if (ok) {
+                tc::fence_after_sync();
+                constexpr int kColsW = WG / 2;
+                const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16) + 2 * kLayerN + part * kColsW;
+#pragma unroll 1
+                for (int j = 0; j < kColsW / 32; ++j) {
+                    uint32_t r[32];
+                    tc::tmem_ld32_issue(trow + 32 * j, r);
+                    tc::tmem_wait32(r);
+                    uint8_t* box = wb + (j & 1) * 4096;
+                    if (j >= 2) {
+                        if (lane == 0) tc::bulk_wait_read_but_one();
+                        __syncwarp();
+                    }
+                    uint4* row = reinterpret_cast<uint4*>(box + lane * 128);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) row[c ^ sw] = make_uint4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+                    tc::fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) {
+                        tc::tma_reduce_add_2d(&tmG, box, part * kColsW + 32 * j, n0 + 32 * quad);
+                        tc::bulk_commit();
+                    }
                 }
             }
         }
@@ -720,7 +850,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && *fail) atomicExch(err, 1);
-    if (warp == kLayerEpiWarps + 1) tc::tmem_dealloc(tmem, 2 * kLayerN);
+    if (warp == kLayerEpiWarps + 1) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 // ------------------------------------------------------------------------------ host side ----
@@ -845,20 +975,24 @@ int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
 
 // The persistent hidden-layer GEMM of a width-256 network: A (rows x K, K <= 256) row-major with a
 // [128 rows x 64] box map, W [256 x K] with a [128 x 64] box map, the staged epilogue's maps; one CTA per
-// SM (CTA pairs over the two column halves) or fewer for small batches.
-template <int EPI>
+// SM (CTA pairs over the two column halves) or fewer for small batches. WG > 0 (kDsilu): with the fused
+// weight gradient of width WG, from the input activations' [32 x 64]-box map `ain` into the FP32
+// gradient's [32 x 32]-box map `grad`.
+template <int EPI, int WG = 0>
 cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMaps& om, const EpiArgs& ea, int K,
-                         int sms, int* err, cudaStream_t s) {
+                         int sms, int* err, cudaStream_t s, const CUtensorMap* ain = nullptr,
+                         const CUtensorMap* grad = nullptr) {
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(layer_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, layer_smem_bytes());
+        cudaFuncSetAttribute(layer_kernel<EPI, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, layer_smem_bytes(WG));
     });
-    if (ea.N % kLayerN != 0 || K > 4 * kChunkK) return cudaErrorInvalidValue;
+    if (ea.N % kLayerN != 0 || K > 4 * kChunkK || (WG > 0 && (!ain || !grad))) return cudaErrorInvalidValue;
+    static const CUtensorMap none{};
     const int nh = ea.N / kLayerN;
     const int mtiles = (ea.M + kTileM - 1) / kTileM;
     const int pairs = std::max(1, std::min(mtiles, sms / nh));
-    return launch_pdl(layer_kernel<EPI>, dim3(pairs * nh), dim3(kLayerThreads), layer_smem_bytes(), s, a, w, om.z, om.r,
-                      ea, K, err);
+    return launch_pdl(layer_kernel<EPI, WG>, dim3(pairs * nh), dim3(kLayerThreads), layer_smem_bytes(WG), s, a, w, om.z,
+                      om.r, ain ? *ain : none, grad ? *grad : none, ea, K, err);
 }
 
 }  // namespace sur
@@ -1192,6 +1326,7 @@ struct Maps {
     CUtensorMap Fm, am[4], dzm[2];     // F, A and dZ as MN-major operands ([64 rows x 64] boxes)
     CUtensorMap Wl[kLayers], Wtl[kLayers];  // W and W^T in [128 x 64] boxes (the persistent layer GEMM)
     CUtensorMap gm[kLayers];                // the FP32 weight gradients, targets of TMA reductions
+    CUtensorMap Fs;                         // F in [32 x 64] boxes (the fused first-layer weight gradient)
 };
 
 // Tensor maps of the operands for batches of n rows (weights, features, activations, gradients), and
@@ -1215,6 +1350,7 @@ bool build_maps(bhk_surrogate* s, int n, bool training, Maps* M) {
     ok = ok && make_tmap(&M->dy_t, s->dy_t, kOutPad, s->cap, kTileM) && make_tmap(&M->Fm, s->F_rm, n, kFeat, 64);
     for (int l = 0; l < kLayers && ok; ++l)
         ok = make_tmap_f32_32(&M->gm[l], s->g + s->L.w[l], fan_out(l, H), fan_in(l, H));
+    ok = ok && make_tmap_rows32(&M->Fs, s->F_rm, n, kFeat);
     for (int i = 0; i < 4 && ok; ++i) ok = make_tmap(&M->am[i], s->a_rm[i], n, H, 64);
     for (int i = 0; i < 2 && ok; ++i) ok = make_tmap(&M->dzm[i], s->dz_rm[i], n, H, 64);
     return ok;
@@ -1283,16 +1419,35 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
     const int H = s->hid;
     // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
     e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
+    if (e == cudaSuccess && H == kLayerN * 2) {
+        // Width 256: dZ_l = (dZ_{l+1} W_{l+1}) silu'(z_l) for l = 3 .. 0 (dY W5 for l = 3), each kernel with
+        // the weight gradient dW_l = dZ_l^T A_{l-1} (F for l = 0) and the bias gradient fused in; dZ_l goes
+        // to buffer (3 - l) & 1, and dZ_0, which nothing reads, is not written.
+        for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
+            EpiArgs ex = epi(n, H);
+            ex.colsum = s->g + s->L.b[l];
+            ex.no_store = l == 0 ? 1 : 0;
+            OutMaps om;
+            om.z = M.zs[l];
+            om.r = M.dzs[(3 - l) & 1];
+            const CUtensorMap& A = l == 3 ? M.dy_rm : M.dz_rm[(2 - l) & 1];
+            const CUtensorMap& W = M.Wtl[l + 1];
+            const int K = l == 3 ? kOutPad : H;
+            e = l == 0 ? launch_layer<kDsilu, kFeat>(A, W, om, ex, K, s->sms, s->err, st, &M.Fs, &M.gm[0])
+                       : launch_layer<kDsilu, kLayerN * 2>(A, W, om, ex, K, s->sms, s->err, st, &M.as[l - 1], &M.gm[l]);
+        }
+        return e;
+    }
     if (e == cudaSuccess) {
         EpiArgs ea = epi(n, H);
         ea.colsum = s->g + s->L.b[3];
         OutMaps om;
         om.z = M.zs[3];
         om.r = M.dzs[0];
-        e = H == kLayerN * 2 ? launch_layer<kDsilu>(M.dy_rm, M.Wtl[4], om, ea, kOutPad, s->sms, s->err, st)
-                             : launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
+        e = launch_gemm<kDsilu>(M.dy_rm, M.Wt[4], ea, n, H, kOutPad, 1, s->err, st, &om);
     }
-    // Hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l) silu'(z_{l-1}).
+    // Width 64, hidden layers l = 3 .. 0: dW_l = dZ_l^T A_{l-1} (F for l = 0), dZ_{l-1} = (dZ_l W_l)
+    // silu'(z_{l-1}).
     int cur = 0;
     for (int l = 3; l >= 0 && e == cudaSuccess; --l) {
         const CUtensorMap& Bop = l == 0 ? M.Fm : M.am[l - 1];
@@ -1303,8 +1458,7 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const 
         OutMaps om;
         om.z = M.zs[l - 1];
         om.r = M.dzs[1 - cur];
-        e = H == kLayerN * 2 ? launch_layer<kDsilu>(M.dz_rm[cur], M.Wtl[l], om, ex, H, s->sms, s->err, st)
-                             : launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
+        e = launch_gemm<kDsilu>(M.dz_rm[cur], M.Wt[l], ex, n, H, H, 1, s->err, st, &om);
         cur = 1 - cur;
     }
     return e;
