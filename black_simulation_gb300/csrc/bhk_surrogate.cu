@@ -461,13 +461,15 @@ constexpr int kLayerN = 128;                  // output columns per CTA
 constexpr int kLayerEpiWarps = 8;
 constexpr int kLayerThreads = 32 * (kLayerEpiWarps + 2);
 constexpr int kLayerWBytes = 4 * kLayerN * kChunkK * 2;  // K <= 256: four 16 KB chunks of W
-constexpr int kLayerStage = 8192;                        // per epilogue warp: two 4 KB boxes
+// Ring stages (16 KB each) and staging per epilogue warp: the forward kernel writes its Z and A boxes
+// one after the other through one 4 KB box and keeps eight chunks (two tiles of A) in flight; the
+// input-gradient kernel double-buffers its Z / dZ boxes (8 KB) and streams the fused weight gradient's
+// operand through its six stages too.
+__host__ __device__ constexpr int layer_ring(int epi) { return epi == 1 /* kBiasSilu */ ? 8 : 6; }
+__host__ __device__ constexpr int layer_stage(int epi) { return epi == 1 /* kBiasSilu */ ? 4096 : 8192; }
 
-// Ring stages (16 KB each): the fused weight gradient streams its second operand through the ring too.
-__host__ __device__ constexpr int layer_ring(int wg) { return wg ? 6 : 4; }
-
-__host__ __device__ constexpr int layer_smem_bytes(int wg) {
-    return kLayerWBytes + layer_ring(wg) * kABytes + kLayerEpiWarps * kLayerStage + 1024 /* alignment */ +
+__host__ __device__ constexpr int layer_smem_bytes(int epi) {
+    return kLayerWBytes + layer_ring(epi) * kABytes + kLayerEpiWarps * layer_stage(epi) + 1024 /* alignment */ +
            512 /* barriers */ + kLayerN * 4 /* bias or column sums */;
 }
 
@@ -488,7 +490,9 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
              int* err) {
     static_assert(EPI == kBiasSilu || EPI == kDsilu, "hidden-layer epilogues only");
     static_assert(WG == 0 || (EPI == kDsilu && (WG == 64 || WG == 256)), "a fused weight gradient of width 64 or 256");
-    constexpr int kLayerRing = layer_ring(WG);
+    static_assert(kBiasSilu == 1, "layer_ring and layer_stage name the forward epilogue by its value");
+    constexpr int kLayerRing = layer_ring(EPI);
+    constexpr int kLayerStage = layer_stage(EPI);
     constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, kLayerN);
     constexpr uint32_t kIdescG = tc::idesc_bf16(kTileM, WG ? WG : 64, true, true);
     constexpr uint32_t kTmemCols = WG ? 512 : 2 * kLayerN;
@@ -716,6 +720,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&tempty[b]);
             uint8_t* zin = wb + (t & 1) * 4096;
+            uint4 av[8];  // kBiasSilu: the tile's A values (BF16) wait here while the Z box is stored
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 const uint32_t* r = g < 2 ? ra + 16 * g : rb + 16 * (g - 2);
@@ -732,11 +737,10 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         *reinterpret_cast<uint32_t*>(&ob[i]) = silu2_half(0.5f * z0, 0.5f * z1);
                     }
                     uint4* zrow = reinterpret_cast<uint4*>(wb + lane * 128);
-                    uint4* arow = reinterpret_cast<uint4*>(wb + 4096 + lane * 128);
                     zrow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(zb)[0];
                     zrow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(zb)[1];
-                    arow[(2 * g) ^ sw] = reinterpret_cast<const uint4*>(ob)[0];
-                    arow[(2 * g + 1) ^ sw] = reinterpret_cast<const uint4*>(ob)[1];
+                    av[2 * g] = reinterpret_cast<const uint4*>(ob)[0];
+                    av[2 * g + 1] = reinterpret_cast<const uint4*>(ob)[1];
                 } else {
                     uint4* zrow = reinterpret_cast<uint4*>(zin + lane * 128);
                     __align__(16) bf16 zv[16];
@@ -758,10 +762,23 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             }
             tc::fence_proxy_async();
             __syncwarp();
+            if constexpr (EPI == kBiasSilu) {
+                // Z leaves first; once the TMA unit has read the box, A goes through the same box.
+                if (lane == 0) {
+                    tc::tma_store_2d(&tmZ, wb, x, y0);
+                    tc::bulk_commit();
+                    tc::bulk_wait_read_all();
+                }
+                __syncwarp();
+                uint4* arow = reinterpret_cast<uint4*>(wb + lane * 128);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) arow[c ^ sw] = av[c];
+                tc::fence_proxy_async();
+                __syncwarp();
+            }
             if (lane == 0) {
                 if constexpr (EPI == kBiasSilu) {
-                    tc::tma_store_2d(&tmZ, wb, x, y0);
-                    tc::tma_store_2d(&tmR, wb + 4096, x, y0);
+                    tc::tma_store_2d(&tmR, wb, x, y0);
                 } else {
                     if (!ea.no_store) tc::tma_store_2d(&tmR, zin, x, y0);
                 }
@@ -984,14 +1001,14 @@ cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMa
                          const CUtensorMap* grad = nullptr) {
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(layer_kernel<EPI, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, layer_smem_bytes(WG));
+        cudaFuncSetAttribute(layer_kernel<EPI, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, layer_smem_bytes(EPI));
     });
     if (ea.N % kLayerN != 0 || K > 4 * kChunkK || (WG > 0 && (!ain || !grad))) return cudaErrorInvalidValue;
     static const CUtensorMap none{};
     const int nh = ea.N / kLayerN;
     const int mtiles = (ea.M + kTileM - 1) / kTileM;
     const int pairs = std::max(1, std::min(mtiles, sms / nh));
-    return launch_pdl(layer_kernel<EPI, WG>, dim3(pairs * nh), dim3(kLayerThreads), layer_smem_bytes(WG), s, a, w, om.z,
+    return launch_pdl(layer_kernel<EPI, WG>, dim3(pairs * nh), dim3(kLayerThreads), layer_smem_bytes(EPI), s, a, w, om.z,
                       om.r, ain ? *ain : none, grad ? *grad : none, ea, K, err);
 }
 
