@@ -1098,44 +1098,32 @@ __device__ __forceinline__ void normalise(const float* x, float u[kIn]) {
     u[4] = x[4] * (1.0f / kImageScale);
 }
 
-// Fourier features f = [sin(2 pi B u), cos(2 pi B u)] of one ray (x: a, theta, log10 r, alpha, beta).
-__device__ __forceinline__ void fourier_features(const float* x, const float* sb, bf16 f[kFeat]) {
-    float u[kIn];
-    normalise(x, u);
-#pragma unroll
-    for (int j = 0; j < kFreq; ++j) {
-        float p = 0.0f;
-#pragma unroll
-        for (int i = 0; i < kIn; ++i) p += sb[j * kIn + i] * u[i];
-        // sin and cos of 2 pi p: exact reduction to r = p - rint(p) in [-1/2, 1/2], then the hardware
-        // sine and cosine (absolute error ~2^-21 on [-pi, pi], far below the BF16 rounding that follows).
-        float s, c;
-        __sincosf(6.28318530717958648f * (p - rintf(p)), &s, &c);
-        f[j] = __float2bfloat16_rn(s);
-        f[kFreq + j] = __float2bfloat16_rn(c);
-    }
-}
-
-// Fourier features of n rays, row-major [n x 64]. The first kernel of a training step also zeroes what
-// the step accumulates into (the gradient, n_a floats at zero_a, and the loss terms, n_b at zero_b).
-__global__ void feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm, bf16* __restrict__ rm, int n,
-                               float* zero_a, long long n_a, float* zero_b, int n_b) {
-    __shared__ float sb[kFreq * kIn];
+// Fourier features of n rays, row-major [n x 64]: one thread per ray and frequency (a warp takes one
+// ray's 32 frequencies, so that its sines and its cosines are written as two contiguous 64-byte runs).
+// The first kernel of a training step also zeroes what the step accumulates into (the gradient, n_a
+// floats at zero_a, and the loss terms, n_b at zero_b).
+__global__ void __launch_bounds__(256) feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm,
+                                                      bf16* __restrict__ rm, int n, float* zero_a, long long n_a,
+                                                      float* zero_b, int n_b) {
     tc::grid_dep_wait();
     tc::grid_dep_launch();
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n_a;
-         i += static_cast<long long>(gridDim.x) * blockDim.x)
-        zero_a[i] = 0.0f;
-    if (blockIdx.x == 0 && threadIdx.x < n_b) zero_b[threadIdx.x] = 0.0f;
-    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sb[i] = Bm[i];
-    __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    for (long long i = t; i < n_a; i += static_cast<long long>(gridDim.x) * blockDim.x) zero_a[i] = 0.0f;
+    if (t < n_b) zero_b[t] = 0.0f;
+    const long long r = t >> 5;
+    const int j = static_cast<int>(t & 31);
     if (r >= n) return;
-    __align__(16) bf16 f[kFeat];
-    fourier_features(x + static_cast<size_t>(r) * kIn, sb, f);
-    uint4* dst = reinterpret_cast<uint4*>(rm + static_cast<size_t>(r) * kFeat);
+    float u[kIn];
+    normalise(x + r * kIn, u);
+    float p = 0.0f;
 #pragma unroll
-    for (int q = 0; q < kFeat / 8; ++q) dst[q] = reinterpret_cast<const uint4*>(f)[q];
+    for (int i = 0; i < kIn; ++i) p += __ldg(&Bm[j * kIn + i]) * u[i];
+    // sin and cos of 2 pi p: exact reduction to r = p - rint(p) in [-1/2, 1/2], then the hardware sine
+    // and cosine (absolute error ~2^-21 on [-pi, pi], far below the BF16 rounding that follows).
+    float sn, cs;
+    __sincosf(6.28318530717958648f * (p - rintf(p)), &sn, &cs);
+    rm[r * kFeat + j] = __float2bfloat16_rn(sn);
+    rm[r * kFeat + kFreq + j] = __float2bfloat16_rn(cs);
 }
 
 // Loss of a batch and its gradient with respect to the head outputs Y (n x 16, FP32):
@@ -1229,48 +1217,70 @@ struct AdamArgs {
     float* hist;
 };
 
-__global__ void adam_kernel(AdamArgs a) {
-    tc::grid_dep_wait();
-    tc::grid_dep_launch();
-    if (a.hist && blockIdx.x == 0 && threadIdx.x < 4) a.hist[threadIdx.x] = a.loss[threadIdx.x];
-    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const float g = a.g[i];
-        const float m = a.b1 * a.m[i] + (1.0f - a.b1) * g;
-        const float v = a.b2 * a.v[i] + (1.0f - a.b2) * g * g;
-        a.m[i] = m;
-        a.v[i] = v;
-        const float w = a.p[i] - a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
-        a.p[i] = w;
-        for (int l = 0; l < kLayers; ++l) {
-            const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
-            const size_t n = static_cast<size_t>(fo) * fi;
-            if (i >= a.wofs[l] && i < a.wofs[l] + n) {
-                const size_t j = i - a.wofs[l];
-                const int o = static_cast<int>(j / fi), k = static_cast<int>(j % fi);
-                const bf16 wb = __float2bfloat16_rn(w);
-                a.w_rm[l][j] = wb;
-                a.w_t[l][static_cast<size_t>(k) * fo + o] = wb;
-            }
-        }
-    }
+// Weight tiles of 32 x 32 per block (the head's 16 rows in one tile row), then one block for the biases.
+__host__ __device__ inline int weight_tiles(int l, int hid) {
+    return ((fan_out(l, hid) + 31) / 32) * ((fan_in(l, hid) + 31) / 32);
+}
+__host__ __device__ inline int weights_blocks(int hid) {
+    int n = 1;
+    for (int l = 0; l < kLayers; ++l) n += weight_tiles(l, hid);
+    return n;
 }
 
-// Writes the BF16 copies of the weights from the FP32 parameters (after initialisation or a set).
-__global__ void refresh_bf16_kernel(AdamArgs a) {
-    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < a.total;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        for (int l = 0; l < kLayers; ++l) {
-            const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
-            const size_t n = static_cast<size_t>(fo) * fi;
-            if (i >= a.wofs[l] && i < a.wofs[l] + n) {
-                const size_t j = i - a.wofs[l];
-                const int o = static_cast<int>(j / fi), k = static_cast<int>(j % fi);
-                const bf16 wb = __float2bfloat16_rn(a.p[i]);
-                a.w_rm[l][j] = wb;
-                a.w_t[l][static_cast<size_t>(k) * fo + o] = wb;
-            }
+// kAdam: one Adam step on the FP32 parameters (m, v, p), else the parameters as they are; either way
+// the BF16 copies W (fan_out x fan_in) and W^T follow. A block takes a 32 x 32 tile of one layer's
+// weights: 256 threads read and write the FP32 state and W along the rows (coalesced), and write W^T
+// along its rows through a shared-memory transpose; the last block takes the biases.
+template <bool kAdam>
+__global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
+    __shared__ bf16 tile[32][34];
+    if constexpr (kAdam) {
+        tc::grid_dep_wait();
+        tc::grid_dep_launch();
+        if (a.hist && blockIdx.x == 0 && threadIdx.x < 4) a.hist[threadIdx.x] = a.loss[threadIdx.x];
+    }
+    auto update = [&](size_t i) {
+        float w = a.p[i];
+        if constexpr (kAdam) {
+            const float g = a.g[i];
+            const float m = a.b1 * a.m[i] + (1.0f - a.b1) * g;
+            const float v = a.b2 * a.v[i] + (1.0f - a.b2) * g * g;
+            a.m[i] = m;
+            a.v[i] = v;
+            w -= a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
+            a.p[i] = w;
         }
+        return w;
+    };
+    int b = blockIdx.x;
+    int l = 0;
+    for (; l < kLayers && b >= weight_tiles(l, a.hid); ++l) b -= weight_tiles(l, a.hid);
+    if (l == kLayers) {  // the biases, each right after its layer's weights
+        for (int q = 0; q < kLayers; ++q) {
+            const size_t bo = a.wofs[q] + static_cast<size_t>(fan_out(q, a.hid)) * fan_in(q, a.hid);
+            for (int j = threadIdx.x; j < fan_out(q, a.hid); j += blockDim.x) update(bo + j);
+        }
+        return;
+    }
+    const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
+    const int kt = (fi + 31) / 32;
+    const int o0 = (b / kt) * 32, k0 = (b % kt) * 32;
+    const int c = threadIdx.x & 31, r = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int o = o0 + r + 8 * q, k = k0 + c;
+        if (o < fo && k < fi) {
+            const size_t j = static_cast<size_t>(o) * fi + k;
+            const bf16 wb = __float2bfloat16_rn(update(a.wofs[l] + j));
+            a.w_rm[l][j] = wb;
+            tile[r + 8 * q][c] = wb;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int k = k0 + r + 8 * q, o = o0 + c;
+        if (o < fo && k < fi) a.w_t[l][static_cast<size_t>(k) * fo + o] = tile[c][r + 8 * q];
     }
 }
 
@@ -1599,7 +1609,7 @@ bhk_status bhk_surrogate_create_width(int device, uint64_t seed, int32_t max_bat
     if (e == cudaSuccess) e = cudaMemset(s->v, 0, P * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(s->err, 0, sizeof(int));
     if (e == cudaSuccess) {
-        refresh_bf16_kernel<<<256, 256>>>(adam_args(s));
+        weights_kernel<false><<<weights_blocks(s->hid), 256>>>(adam_args(s));
         e = cudaDeviceSynchronize();
     }
     if (e != cudaSuccess) {
@@ -1633,7 +1643,7 @@ bhk_status bhk_surrogate_params(bhk_surrogate* s, float* host, int32_t set) {
     cudaError_t e = set ? cudaMemcpy(s->p, host, bytes, cudaMemcpyHostToDevice)
                         : cudaMemcpy(host, s->p, bytes, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && set) {
-        bhk::sur::refresh_bf16_kernel<<<256, 256>>>(bhk::sur::adam_args(s));
+        bhk::sur::weights_kernel<false><<<bhk::sur::weights_blocks(s->hid), 256>>>(bhk::sur::adam_args(s));
         e = cudaDeviceSynchronize();
     }
     if (e != cudaSuccess) {
@@ -1705,7 +1715,7 @@ bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8
     }
     cudaStream_t st = nullptr;
     cudaMemsetAsync(s->err, 0, sizeof(int), st);
-    cudaError_t e = launch_pdl(feature_kernel, dim3((n + 127) / 128), dim3(128), 0, st, x,
+    cudaError_t e = launch_pdl(feature_kernel, dim3((n + 7) / 8), dim3(256), 0, st, x,
                                static_cast<const float*>(s->Bm), s->F_rm, n, s->g,
                                static_cast<long long>(s->L.total), s->loss, 4);
     if (e == cudaSuccess) e = forward(s, M, n, st);
@@ -1752,7 +1762,7 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
     aa.loss = s->loss;
     for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
         const int64_t off = (t % nb) * batch;
-        e = launch_pdl(feature_kernel, dim3((batch + 127) / 128), dim3(128), 0, st, x + off * kIn,
+        e = launch_pdl(feature_kernel, dim3((batch + 7) / 8), dim3(256), 0, st, x + off * kIn,
                        static_cast<const float*>(s->Bm), s->F_rm, batch, s->g, static_cast<long long>(s->L.total),
                        s->loss, 4);
         if (e == cudaSuccess) e = forward(s, M, batch, st);
@@ -1762,7 +1772,7 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
         aa.c1 = static_cast<float>(1.0 / (1.0 - std::pow(0.9, static_cast<double>(s->step))));
         aa.c2 = static_cast<float>(1.0 / (1.0 - std::pow(0.999, static_cast<double>(s->step))));
         aa.hist = hist ? hist + 4 * t : nullptr;
-        if (e == cudaSuccess) e = launch_pdl(adam_kernel, dim3(256), dim3(256), 0, st, aa);
+        if (e == cudaSuccess) e = launch_pdl(weights_kernel<true>, dim3(weights_blocks(s->hid)), dim3(256), 0, st, aa);
     }
     bhk_status rs = e == cudaSuccess ? check_err(s, st) : BHK_ECUDA;
     if (e != cudaSuccess) set_last_error(std::string("bhk_surrogate_train: ") + cudaGetErrorString(e));
@@ -1790,7 +1800,7 @@ bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, fl
             set_last_error("bhk_surrogate_predict: tensor map creation failed");
             return BHK_ECUDA;
         }
-        cudaError_t e = launch_pdl(feature_kernel, dim3((rows + 127) / 128), dim3(128), 0, st, x + off * kIn,
+        cudaError_t e = launch_pdl(feature_kernel, dim3((rows + 7) / 8), dim3(256), 0, st, x + off * kIn,
                                    static_cast<const float*>(s->Bm), s->F_rm, rows, static_cast<float*>(nullptr),
                                    0LL, static_cast<float*>(nullptr), 0);
         if (e == cudaSuccess) e = forward(s, M, rows, st);
