@@ -36,11 +36,14 @@ namespace sur {
 
 using bf16 = __nv_bfloat16;
 
+// The network's shape: 5 inputs, 32 Fourier frequencies (64 features), 8 outputs padded to 16 for the
+// MMA, 5 layers.
+constexpr int kIn = 5, kFreq = 32, kFeat = 64, kOut = 8, kOutPad = 16, kLayers = 5;
 constexpr int kTileM = 128;
 constexpr int kChunkK = 64;
 constexpr int kABytes = kTileM * kChunkK * 2;  // 16 KB
 
-enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3, kReduceF32 = 5 };
+enum Epi : int { kStoreF32 = 0, kBiasSilu = 1, kDsilu = 2, kAtomicF32 = 3, kReduceF32 = 5, kHeadLoss = 6 };
 
 struct EpiArgs {
     int M, N;              // logical output extent (rows, columns)
@@ -49,7 +52,49 @@ struct EpiArgs {
     int ld_f32;
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
     int no_store;          // kDsilu in layer_kernel: dZ is not written (only the fused gradients are used)
+    // kHeadLoss (the head's forward with the loss fused in; colsum takes the head's bias gradient):
+    const uint8_t* cls;    // per row: target class 1 captured, 2 disk, 3 escaped
+    const float* tgt;      // per row: 8 targets
+    bf16* dy_rm;           // dLoss/dY, row-major [M x 16], and transposed [16 x ld_t]
+    bf16* dy_t;
+    int ld_t;
+    float* loss;           // the four loss terms, atomically
+    float inv_n;
+    float4 lw;             // loss weights (CE, r_disk, ln g, direction)
 };
+
+// Loss of one row (y: the head's 16 outputs, c: target class - 1, tg: its 8 targets) and its gradient d
+// with respect to y, scaled by inv_n; terms = (cross-entropy, r_disk, ln g, direction) unweighted:
+//   cross-entropy over the 3 outcome logits; disk rays: squared error of r_disk / 30 and of log g;
+//   escaped rays: squared error of the 3-vector escape direction. The gradient is that of the weighted
+//   sum w.x CE + w.y MSE(r) + w.z MSE(ln g) + w.w MSE(dir).
+__device__ __forceinline__ void row_loss(const float (&y)[kOutPad], int c, const float* __restrict__ tg, float inv_n,
+                                         float4 w, float (&d)[kOutPad], float (&terms)[4]) {
+#pragma unroll
+    for (int i = 0; i < kOutPad; ++i) d[i] = 0.0f;
+    terms[0] = terms[1] = terms[2] = terms[3] = 0.0f;
+    const float mx = fmaxf(y[0], fmaxf(y[1], y[2]));
+    const float e0 = __expf(y[0] - mx), e1 = __expf(y[1] - mx), e2 = __expf(y[2] - mx);
+    const float z = e0 + e1 + e2;
+    const float p[3] = {e0 / z, e1 / z, e2 / z};
+    if (c >= 0 && c < 3) {
+        terms[0] = -__logf(fmaxf(p[c], 1e-30f));
+        for (int k = 0; k < 3; ++k) d[k] = w.x * (p[k] - (k == c ? 1.0f : 0.0f)) * inv_n;
+    }
+    if (c == 1) {  // disk
+        const float er = y[3] - tg[3], eg = y[4] - tg[4];
+        terms[1] = er * er;
+        terms[2] = eg * eg;
+        d[3] = w.y * 2.0f * er * inv_n;
+        d[4] = w.z * 2.0f * eg * inv_n;
+    } else if (c == 2) {  // escaped
+        for (int k = 5; k < 8; ++k) {
+            const float ev = y[k] - tg[k];
+            terms[3] += ev * ev;
+            d[k] = w.w * 2.0f * ev * inv_n;
+        }
+    }
+}
 
 // Pipeline depth: the network's GEMMs have K <= 256 (4 chunks) and run two CTAs (each 256 TMEM
 // columns at most) per SM, so that one CTA's epilogue overlaps the other's main loop. The split-K
@@ -399,6 +444,54 @@ gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (!epilogue_staged<BN, EPI>(&tmZ, &tmR, ea, tmem, sA, sx, zbar, m0, n0)) atomicExch(err, 1);
         } else if constexpr (EPI == kReduceF32) {
             epilogue_reduce<BN>(&tmZ, ea, tmem, sA, m0, n0);
+        } else if constexpr (EPI == kHeadLoss) {
+            // The head (BN = 16: warps 0-3, lane = row) with the loss: Y = acc + b, then the row's loss
+            // terms and dLoss/dY (BF16, both layouts); the bias gradient and the loss terms summed over the
+            // CTA's rows (shuffles, then the four warps through the idle ring) and added atomically.
+            static_assert(BN == 16, "the head is 16 wide");
+            float d[kOutPad], terms[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int i = 0; i < kOutPad; ++i) d[i] = 0.0f;
+            if (warp < 4) {
+                const int m = m0 + 32 * warp + lane;
+                uint32_t r[16];
+                tc::tmem_ld16_issue(tmem + (static_cast<uint32_t>(32 * warp) << 16), r);
+                tc::tmem_wait16(r);
+                if (m < ea.M) {
+                    float y[kOutPad];
+#pragma unroll
+                    for (int i = 0; i < kOutPad; ++i) y[i] = __uint_as_float(r[i]) + ea.bias[i];
+                    row_loss(y, static_cast<int>(ea.cls[m]) - 1, ea.tgt + static_cast<size_t>(m) * kOut, ea.inv_n,
+                             ea.lw, d, terms);
+                    __align__(16) bf16 ob[kOutPad];
+#pragma unroll
+                    for (int i = 0; i < kOutPad; ++i) ob[i] = __float2bfloat16_rn(d[i]);
+                    uint4* dst = reinterpret_cast<uint4*>(ea.dy_rm + static_cast<size_t>(m) * kOutPad);
+                    dst[0] = reinterpret_cast<const uint4*>(ob)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(ob)[1];
+#pragma unroll
+                    for (int i = 0; i < kOutPad; ++i) ea.dy_t[static_cast<size_t>(i) * ea.ld_t + m] = ob[i];
+                }
+            }
+            float* red = reinterpret_cast<float*>(sA);
+            if (warp < 4) {
+#pragma unroll
+                for (int i = 0; i < kOutPad + 4; ++i) {
+                    float v = i < kOutPad ? d[i] : terms[i - kOutPad] * ea.inv_n;
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                    if (lane == 0) red[warp * (kOutPad + 4) + i] = v;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < kOutPad + 4) {
+                float v = 0.0f;
+                for (int q = 0; q < 4; ++q) v += red[q * (kOutPad + 4) + threadIdx.x];
+                if (threadIdx.x < kOutPad) {
+                    if (v != 0.0f) atomicAdd(&ea.colsum[threadIdx.x], v);
+                } else {
+                    atomicAdd(&ea.loss[threadIdx.x - kOutPad], v);
+                }
+            }
         } else {
             constexpr int kJ = BN / 16;                  // 16-column groups of the tile
             constexpr int kSplit = kJ >= 2 ? 2 : 1;      // warps sharing a lane quadrant
@@ -1065,7 +1158,6 @@ namespace sur {
 
 // The hidden width (kHidden, the four SiLU layers) is a property of each network: 256 (the default) or
 // 64 (a network 12.5 x cheaper to evaluate, for the speed/accuracy trade of the learned path).
-constexpr int kIn = 5, kFreq = 32, kFeat = 64, kOut = 8, kOutPad = 16, kLayers = 5;
 constexpr int kHidDefault = 256;
 __host__ __device__ constexpr bool width_ok(int hid) { return hid == 64 || hid == 256; }
 __host__ __device__ constexpr int fan_in(int l, int hid) { return l == 0 ? kFeat : hid; }
@@ -1124,81 +1216,6 @@ __global__ void __launch_bounds__(256) feature_kernel(const float* __restrict__ 
     __sincosf(6.28318530717958648f * (p - rintf(p)), &sn, &cs);
     rm[r * kFeat + j] = __float2bfloat16_rn(sn);
     rm[r * kFeat + kFreq + j] = __float2bfloat16_rn(cs);
-}
-
-// Loss of a batch and its gradient with respect to the head outputs Y (n x 16, FP32):
-//   cross-entropy over the 3 outcome logits (targets cls in {1 captured, 2 disk, 3 escaped});
-//   disk rays: squared error of r_disk / 30 and of log g;  escaped rays: squared error of the
-//   3-vector escape direction. Mean over the batch. The gradient is that of the weighted sum
-//   w.x CE + w.y MSE(r) + w.z MSE(ln g) + w.w MSE(dir); the loss terms are reported unweighted. dY goes
-//   out as BF16 in both layouts, the head's bias gradient and the loss terms are summed atomically.
-constexpr int kLossThreads = 256;
-__global__ void __launch_bounds__(kLossThreads) loss_kernel(const float* __restrict__ Y, const uint8_t* __restrict__ cls,
-                            const float* __restrict__ tgt, bf16* __restrict__ dy_rm, bf16* __restrict__ dy_t, int ld_t,
-                            float* __restrict__ db, float* __restrict__ loss, int n, float inv_n, float4 w) {
-    tc::grid_dep_wait();
-    tc::grid_dep_launch();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    float d[kOutPad];
-#pragma unroll
-    for (int i = 0; i < kOutPad; ++i) d[i] = 0.0f;
-    float ce = 0.0f, lr_ = 0.0f, lg = 0.0f, le = 0.0f;
-    if (r < n) {
-        const float* y = Y + static_cast<size_t>(r) * kOutPad;
-        const float* tg = tgt + static_cast<size_t>(r) * kOut;
-        const int c = static_cast<int>(cls[r]) - 1;
-        const float mx = fmaxf(y[0], fmaxf(y[1], y[2]));
-        const float e0 = __expf(y[0] - mx), e1 = __expf(y[1] - mx), e2 = __expf(y[2] - mx);
-        const float z = e0 + e1 + e2;
-        const float p[3] = {e0 / z, e1 / z, e2 / z};
-        if (c >= 0 && c < 3) {
-            ce = -__logf(fmaxf(p[c], 1e-30f));
-            for (int k = 0; k < 3; ++k) d[k] = w.x * (p[k] - (k == c ? 1.0f : 0.0f)) * inv_n;
-        }
-        if (c == 1) {  // disk
-            const float er = y[3] - tg[3], eg = y[4] - tg[4];
-            lr_ = er * er;
-            lg = eg * eg;
-            d[3] = w.y * 2.0f * er * inv_n;
-            d[4] = w.z * 2.0f * eg * inv_n;
-        } else if (c == 2) {  // escaped
-            for (int k = 5; k < 8; ++k) {
-                const float ev = y[k] - tg[k];
-                le += ev * ev;
-                d[k] = w.w * 2.0f * ev * inv_n;
-            }
-        }
-        __align__(16) bf16 ob[kOutPad];
-#pragma unroll
-        for (int i = 0; i < kOutPad; ++i) ob[i] = __float2bfloat16_rn(d[i]);
-        uint4* dst = reinterpret_cast<uint4*>(dy_rm + static_cast<size_t>(r) * kOutPad);
-        dst[0] = reinterpret_cast<const uint4*>(ob)[0];
-        dst[1] = reinterpret_cast<const uint4*>(ob)[1];
-#pragma unroll
-        for (int i = 0; i < kOutPad; ++i) dy_t[static_cast<size_t>(i) * ld_t + r] = ob[i];
-    }
-    // Bias gradient and loss terms: sums over the warp (shuffles), then over the block's warps in
-    // shared memory, then one atomic per block and value.
-    __shared__ float part[kLossThreads / 32][kOutPad + 4];
-    const int warp = threadIdx.x >> 5;
-    const float terms[4] = {ce, lr_, lg, le};
-#pragma unroll
-    for (int i = 0; i < kOutPad + 4; ++i) {
-        float v = i < kOutPad ? d[i] : terms[i - kOutPad] * inv_n;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) part[warp][i] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kOutPad + 4) {
-        float v = 0.0f;
-        for (int q = 0; q < kLossThreads / 32; ++q) v += part[q][threadIdx.x];
-        if (threadIdx.x < kOutPad) {
-            if (v != 0.0f) atomicAdd(&db[threadIdx.x], v);
-        } else {
-            atomicAdd(&loss[threadIdx.x - kOutPad], v);
-        }
-    }
 }
 
 // Adam on the flat FP32 parameters; refreshes the BF16 copies W (fan_out x fan_in) and W^T.
@@ -1390,8 +1407,9 @@ EpiArgs epi(int M, int N) {
     return e;
 }
 
-// Forward pass of n rows (features already in F): z, activations, head into Y.
-cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
+// Forward pass of n rows (features already in F): z, activations, and the head -- into Y, or with `loss`
+// (training: the loss's targets and outputs) the loss and dLoss/dY straight from the head's epilogue.
+cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, const EpiArgs* loss = nullptr) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
@@ -1405,13 +1423,31 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
                              : launch_gemm<kBiasSilu>(A, M.W[l], ea, n, H, fan_in(l, H), 1, s->err, st, &om);
     }
     if (e == cudaSuccess) {
-        EpiArgs ea = epi(n, kOutPad);
+        EpiArgs ea = loss ? *loss : epi(n, kOutPad);
+        ea.M = n;
+        ea.N = kOutPad;
         ea.bias = s->p + s->L.b[4];
         ea.f32 = s->Y;
         ea.ld_f32 = kOutPad;
-        e = launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st);
+        e = loss ? launch_gemm_bn<16, kHeadLoss, 0>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st, nullptr)
+                 : launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st);
     }
     return e;
+}
+
+// The loss of a training batch of n rows, fused into the head's forward (targets cls and tgt).
+EpiArgs loss_args(bhk_surrogate* s, const uint8_t* cls, const float* tgt, int n) {
+    EpiArgs ea = epi(n, kOutPad);
+    ea.cls = cls;
+    ea.tgt = tgt;
+    ea.dy_rm = s->dy_rm;
+    ea.dy_t = s->dy_t;
+    ea.ld_t = s->cap;
+    ea.loss = s->loss;
+    ea.inv_n = 1.0f / n;
+    ea.lw = s->w;
+    ea.colsum = s->g + s->L.b[4];
+    return ea;
 }
 
 // K splits of a weight gradient (M x N, K = n rows): one CTA per SM over the M tiles, each split at
@@ -1436,13 +1472,11 @@ cudaError_t weight_grad(bhk_surrogate* s, const Maps& maps, int l, const CUtenso
     return launch_gemm<kReduceF32, MAJ>(A, B, ea, M, N, K, split_for(s, K, M), s->err, st, &om);
 }
 
-// Loss and gradients of a batch of n rows (n % 128 == 0) into s->g and s->loss, which the caller has
-// zeroed (the training step's feature_kernel does).
-cudaError_t backward(bhk_surrogate* s, const Maps& M, const uint8_t* cls, const float* tgt, int n, cudaStream_t st) {
-    cudaError_t e = launch_pdl(loss_kernel, dim3((n + kLossThreads - 1) / kLossThreads), dim3(kLossThreads), 0, st,
-                               static_cast<const float*>(s->Y), cls, tgt, s->dy_rm, s->dy_t, s->cap,
-                               s->g + s->L.b[4], s->loss, n, 1.0f / n, s->w);
-    if (e != cudaSuccess) return e;
+// Gradients of a batch of n rows (n % 128 == 0) into s->g, after forward() with the loss (which wrote
+// dLoss/dY, the head's bias gradient and the loss terms). The caller has zeroed s->g and s->loss (the
+// training step's feature_kernel does).
+cudaError_t backward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
     const int H = s->hid;
     // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
     e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
@@ -1718,8 +1752,9 @@ bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8
     cudaError_t e = launch_pdl(feature_kernel, dim3((n + 7) / 8), dim3(256), 0, st, x,
                                static_cast<const float*>(s->Bm), s->F_rm, n, s->g,
                                static_cast<long long>(s->L.total), s->loss, 4);
-    if (e == cudaSuccess) e = forward(s, M, n, st);
-    if (e == cudaSuccess) e = backward(s, M, cls, tgt, n, st);
+    const EpiArgs la = loss_args(s, cls, tgt, n);
+    if (e == cudaSuccess) e = forward(s, M, n, st, &la);
+    if (e == cudaSuccess) e = backward(s, M, n, st);
     if (e != cudaSuccess) {
         set_last_error(std::string("bhk_surrogate_gradients: ") + cudaGetErrorString(e));
         return BHK_ECUDA;
@@ -1765,8 +1800,9 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
         e = launch_pdl(feature_kernel, dim3((batch + 7) / 8), dim3(256), 0, st, x + off * kIn,
                        static_cast<const float*>(s->Bm), s->F_rm, batch, s->g, static_cast<long long>(s->L.total),
                        s->loss, 4);
-        if (e == cudaSuccess) e = forward(s, M, batch, st);
-        if (e == cudaSuccess) e = backward(s, M, cls + off, tgt + off * kOut, batch, st);
+        const EpiArgs la = loss_args(s, cls + off, tgt + off * kOut, batch);
+        if (e == cudaSuccess) e = forward(s, M, batch, st, &la);
+        if (e == cudaSuccess) e = backward(s, M, batch, st);
         ++s->step;
         aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
         aa.c1 = static_cast<float>(1.0 / (1.0 - std::pow(0.9, static_cast<double>(s->step))));
