@@ -97,12 +97,14 @@ __device__ __forceinline__ void row_loss(const float (&y)[kOutPad], int c, const
 }
 
 // Pipeline depth: the network's GEMMs have K <= 256 (4 chunks) and run two CTAs (each 256 TMEM
-// columns at most) per SM, so that one CTA's epilogue overlaps the other's main loop. The split-K
+// columns at most) per SM, so that one CTA's epilogue overlaps the other's main loop. The training
+// head (kHeadLoss, 16 wide, one 128-row tile per CTA) keeps two stages, so that four CTAs fit an SM and
+// the whole batch runs in one wave. The split-K
 // weight gradients stream long K ranges (~14 chunks a CTA) with a light epilogue: one CTA per SM with
 // a deep ring, so that the TMA latency of the next chunks hides behind the current MMAs.
 template <int BN, int EPI>
 __host__ __device__ constexpr int gemm_stages() {
-    return EPI == kReduceF32 ? (BN >= 256 ? 4 : 8) : (BN >= 256 ? 2 : 4);
+    return EPI == kReduceF32 ? (BN >= 256 ? 4 : 8) : EPI == kHeadLoss ? 2 : (BN >= 256 ? 2 : 4);
 }
 
 template <int BN, int EPI>
