@@ -2081,7 +2081,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
             tc::mbar_init(&empty[st], 1);
         }
         for (int sl = 0; sl < NS; ++sl) {
-            tc::mbar_init(&act_ready[sl], 32 * kWarpsPerSlot);
+            tc::mbar_init(&act_ready[sl], kWarpsPerSlot);  // one arrival per warp
             tc::mbar_init(&acc_full[sl], 1);
         }
         tc::mbar_init(drain, 1);
@@ -2301,9 +2301,11 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                     store_act16(act, row, j0, fs);
                     store_act16(act, row, kFreq + j0, fc);
                 }
+                // Every lane's activations are visible to the tensor core before its warp's one arrival.
                 tc::fence_proxy_async();
                 tc::fence_before_sync();
-                tc::mbar_arrive(&act_ready[slot]);
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&act_ready[slot]);
             }
             for (int l = 0; l < 4 && ok; ++l) {  // ---- hidden layers
 #pragma unroll
@@ -2339,7 +2341,8 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                     }
                     tc::fence_proxy_async();
                     tc::fence_before_sync();
-                    tc::mbar_arrive(&act_ready[slot]);
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&act_ready[slot]);
                 }
             }
             if (!ok) break;
