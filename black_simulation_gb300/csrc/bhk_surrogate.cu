@@ -1958,8 +1958,12 @@ constexpr int kInfStages = 3;               // weight ring: 3 chunks in flight
 constexpr int kTileRays = 128;
 constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 of activations
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
-constexpr int kEpiWarps = 16;              // per tile slot: 4 TMEM lane quadrants x 2 column halves
-constexpr int kInfThreads = 64 + 32 * kEpiWarps;
+// Epilogue warps per CTA (after the TMA and MMA warps): 16 at width 256 (two tile slots of 8: 4 TMEM lane
+// quadrants x 2 column halves), 24 at width 64 (six slots of 4 warps, one per lane quadrant).
+template <int HID>
+__host__ __device__ constexpr int inf_epi_warps() { return HID == 64 ? 24 : 16; }
+template <int HID>
+__host__ __device__ constexpr int inf_threads() { return 64 + 32 * inf_epi_warps<HID>(); }
 constexpr int kInfBars = 32;  // 64-bit mbarrier words reserved in shared memory
 constexpr int kInfMisc = 8 * kInfBars + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
 // Per hidden width HID: one tile's activations (HID / 64 chunks of 64 columns), one weight chunk (all
@@ -1968,12 +1972,12 @@ template <int HID>
 __host__ __device__ constexpr int act_bytes() { return (HID / 64) * kChunkBytes; }
 template <int HID>
 __host__ __device__ constexpr int wchunk_bytes() { return HID * 64 * 2; }
-// Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 4 at width 64
-// (4 x 64 columns, 4 epilogue warps each -- one per TMEM lane quadrant). The epilogue can also serve
-// several tiles per warp group in turn; at width 64 eight tiles that way (all 512 columns) measured
-// slower than four (18.3 against 15.9 ms of inference on 124 M rays).
+// Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 6 at width 64
+// (6 x 64 of the 512 columns, 4 epilogue warps each -- one per TMEM lane quadrant -- at 72 registers a
+// thread; four tiles at 96 registers ran 11 % slower, eight spill at 56). The epilogue can also serve
+// several tiles per warp group in turn; at width 64 eight tiles that way measured slower than four.
 template <int HID>
-__host__ __device__ constexpr int inf_slots() { return HID == 64 ? 4 : 2; }
+__host__ __device__ constexpr int inf_slots() { return HID == 64 ? 6 : 2; }
 // At width 64 the whole network's weights (4 x 8 KB + the head's 2 KB) stay resident in shared memory,
 // loaded once per CTA, and the MMA issuer serves whichever tile is ready; at width 256 they stream
 // through a ring of kInfStages chunks in the MMA's order.
@@ -2045,7 +2049,7 @@ __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb,
 // MMA's order (group of NS tiles, layer, slot, chunk). Every MMA is 128 x HID x 16, so each activation
 // slice is read from shared memory once per layer. CTA b takes tiles b, b + grid, ...
 template <int HID>
-__global__ void __launch_bounds__(kInfThreads, 1)
+__global__ void __launch_bounds__(inf_threads<HID>(), 1)
 infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
              const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3,
              const __grid_constant__ CUtensorMap tW4, InferArgs ia) {
@@ -2053,9 +2057,10 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     constexpr int NS = inf_slots<HID>();
     constexpr int kActBytes = act_bytes<HID>(), kWChunkBytes = wchunk_bytes<HID>();
-    constexpr uint32_t kTmemCols = NS * HID;  // NS tile slots of HID accumulator columns
+    constexpr uint32_t kTmemCols = NS * HID <= 256 ? 256 : 512;  // NS tile slots of HID columns (a power of 2)
     // A tile's epilogue: 4 warps (one per TMEM lane quadrant) at width 64, 8 (two column halves) at 256.
     constexpr int kHalves = HID == 64 ? 1 : 2, kWarpsPerSlot = 4 * kHalves;
+    constexpr int kEpiWarps = inf_epi_warps<HID>();
     static_assert(kEpiWarps % kWarpsPerSlot == 0 && NS % (kEpiWarps / kWarpsPerSlot) == 0, "slot mapping");
     static_assert(kInfStages + kInfStages + 2 * NS + 1 <= kInfBars, "the mbarriers fit their words");
     constexpr bool kResident = inf_resident<HID>();
@@ -2325,19 +2330,32 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                     constexpr int kHalf = HID / kHalves, kGroups = kHalf / 32;  // this warp's columns, in 32s
                     const float* hb = ia.half_bias + l * HID + kHalf * half;
                     const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
-                    uint32_t ra[32], rb[32];
-                    tc::tmem_ld32_issue(cb, ra);
-                    tc::tmem_wait32(ra);
+                    if constexpr (HID == 64) {  // 32 columns at a time (the register budget of 24 warps)
+                        uint32_t ra[32];
+#pragma unroll 1
+                        for (int jj = 0; jj < kGroups; ++jj) {
+                            tc::tmem_ld32_issue(cb + 32u * jj, ra);
+                            tc::tmem_wait32(ra);
+                            uint32_t w[16];
+                            silu32(ra, hb + 32 * jj, w);
+                            store_act16(act, row, kHalf * half + 32 * jj, w);
+                            store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
+                        }
+                    } else {  // the next 32 columns' load in flight while the current ones are processed
+                        uint32_t ra[32], rb[32];
+                        tc::tmem_ld32_issue(cb, ra);
+                        tc::tmem_wait32(ra);
 #pragma unroll
-                    for (int jj = 0; jj < kGroups; ++jj) {
-                        uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
-                        uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
-                        if (jj + 1 < kGroups) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
-                        uint32_t w[16];
-                        silu32(cur, hb + 32 * jj, w);
-                        store_act16(act, row, kHalf * half + 32 * jj, w);
-                        store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
-                        if (jj + 1 < kGroups) tc::tmem_wait32(nxt);
+                        for (int jj = 0; jj < kGroups; ++jj) {
+                            uint32_t(&cur)[32] = (jj & 1) ? rb : ra;
+                            uint32_t(&nxt)[32] = (jj & 1) ? ra : rb;
+                            if (jj + 1 < kGroups) tc::tmem_ld32_issue(cb + 32u * (jj + 1), nxt);
+                            uint32_t w[16];
+                            silu32(cur, hb + 32 * jj, w);
+                            store_act16(act, row, kHalf * half + 32 * jj, w);
+                            store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
+                            if (jj + 1 < kGroups) tc::tmem_wait32(nxt);
+                        }
                     }
                     tc::fence_proxy_async();
                     tc::fence_before_sync();
@@ -2541,6 +2559,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     const int H = s->hid;
     auto* kern = H == 64 ? &infer_kernel<64> : &infer_kernel<256>;
     const int smem = H == 64 ? inf_smem<64>() : inf_smem<256>();
+    const int threads = H == 64 ? inf_threads<64>() : inf_threads<256>();
     static std::once_flag attr;
     std::call_once(attr, [] {
         cudaFuncSetAttribute(infer_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, inf_smem<64>());
@@ -2551,7 +2570,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     // The grid is the number of CTAs resident at once (the static tile schedule must not need a second
     // wave): one per SM at width 256 (its shared memory and all 512 TMEM columns), as many as fit at 64
     // (2 x 64 TMEM columns each).
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kInfThreads, smem) != cudaSuccess || per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
@@ -2594,7 +2613,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     if (e == cudaSuccess) e = cudaMemsetAsync(s->err, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], st);
     if (e != cudaSuccess) return fail_cuda(e, "launch set-up");
-    kern<<<grid, kInfThreads, smem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
+    kern<<<grid, threads, smem, st>>>(M.W[0], M.W[1], M.W[2], M.W[3], w4, ia);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->n_list_host, s->n_list, 8, cudaMemcpyDeviceToHost, st);
