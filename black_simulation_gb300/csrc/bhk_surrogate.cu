@@ -1959,9 +1959,10 @@ constexpr int kTileRays = 128;
 constexpr int kChunkBytes = 128 * 64 * 2;  // 16 KB: 128 rows x 64 BF16 of activations
 constexpr int kHeadChunkBytes = 16 * 64 * 2;
 // Epilogue warps per CTA (after the TMA and MMA warps): 16 at width 256 (two tile slots of 8: 4 TMEM lane
-// quadrants x 2 column halves), 24 at width 64 (six slots of 4 warps, one per lane quadrant).
+// quadrants x 2 column halves), 28 at width 64 (seven slots of 4 warps, one per lane quadrant; 960
+// threads -- eight slots would pass the 1,024-thread limit of a block).
 template <int HID>
-__host__ __device__ constexpr int inf_epi_warps() { return HID == 64 ? 24 : 16; }
+__host__ __device__ constexpr int inf_epi_warps() { return HID == 64 ? 28 : 16; }
 template <int HID>
 __host__ __device__ constexpr int inf_threads() { return 64 + 32 * inf_epi_warps<HID>(); }
 constexpr int kInfBars = 32;  // 64-bit mbarrier words reserved in shared memory
@@ -1972,12 +1973,12 @@ template <int HID>
 __host__ __device__ constexpr int act_bytes() { return (HID / 64) * kChunkBytes; }
 template <int HID>
 __host__ __device__ constexpr int wchunk_bytes() { return HID * 64 * 2; }
-// Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 6 at width 64
-// (6 x 64 of the 512 columns, 4 epilogue warps each -- one per TMEM lane quadrant -- at 72 registers a
-// thread; four tiles at 96 registers ran 11 % slower, eight spill at 56). The epilogue can also serve
-// several tiles per warp group in turn; at width 64 eight tiles that way measured slower than four.
+// Tiles in flight per CTA: 2 at width 256 (2 x 256 TMEM columns, 8 epilogue warps each), 7 at width 64
+// (7 x 64 of the 512 columns, 4 epilogue warps each -- one per TMEM lane quadrant -- at 64 registers a
+// thread; six tiles at 72 registers ran 1.2 % slower, four at 96 registers 12 % slower). The epilogue can
+// also serve several tiles per warp group in turn; at width 64 eight tiles that way measured slower.
 template <int HID>
-__host__ __device__ constexpr int inf_slots() { return HID == 64 ? 6 : 2; }
+__host__ __device__ constexpr int inf_slots() { return HID == 64 ? 7 : 2; }
 // At width 64 the whole network's weights (4 x 8 KB + the head's 2 KB) stay resident in shared memory,
 // loaded once per CTA, and the MMA issuer serves whichever tile is ready; at width 256 they stream
 // through a ring of kInfStages chunks in the MMA's order.
