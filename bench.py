@@ -11,8 +11,9 @@ frame descriptors (the pixel index is the ray), so every launch recomputes all 2
           around each step (set-up, FP64 launch, sort, trace, rescue), L2 flushed between steps.
 `e2e`     the same through bhk_trace_frames_host: host descriptors in, host SoA outputs back
           (pinned), wall clock per call.
-`roofline` the tracer kernel against the measured FP32 FMA peak: accepted steps x FLOPs per step
-          (counted from the kernel source) / kernel time (CUDA events inside the library).
+`roofline` the tracer kernel against the measured FP32 FMA peak: the FLOPs of its Dormand-Prince
+          attempts (accepted and rejected, each at its count from the kernel source) / kernel time
+          (CUDA events inside the library).
 `cpu_baseline` the reference integrator (its RK4 loop shape at its product tolerance 1e-2, which
           meets the 1e-4 accuracy bar) on all host cores, a bounded sample of the same frame.
 
@@ -439,6 +440,18 @@ def mac_fwd(width: int) -> int:
 MAC_TRAIN = 2 * MAC_FWD + 256 * 16 + 3 * 256 * 256
 
 
+def train_bytes_per_row(width: int = 256) -> int:
+    """Algorithmic HBM bytes per batch row of one training step (BF16 activations of `width`, 64 features,
+    16 padded outputs), as the step's kernels move them: features written; per hidden layer its input
+    read and Z and A written; the head's input read, dY written in two layouts with the targets read;
+    the head's weight gradient reading dY^T and A3; per hidden layer of the backward dZ of the layer
+    above, Z and the layer's input read and dZ written (not dZ_0)."""
+    a, f, o = 2 * width, 2 * 64, 2 * 16
+    forward = f + (f + 2 * a) + 3 * (a + 2 * a) + a + 2 * o + 33
+    backward = (o + a) + (o + a + a + a) + 2 * (a + a + a + a) + (a + a + f)
+    return f + forward + backward
+
+
 def measured_peak(key: str, fallback: float):
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -811,6 +824,12 @@ def run_train(args):
                    "dataset_s": t_data, "final_loss": [float(v) for v in hist[-50:].mean(axis=0)]},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": src, "flops_per_ray": 2 * MAC_TRAIN},
+        # The same step against the HBM copy bandwidth: its algorithmic activation and gradient traffic
+        # (the parameters' few MB aside) over its time.
+        "roofline_hbm": {"bound": "hbm", "algorithmic_bytes_per_step": train_bytes_per_row() * 65536,
+                         "achieved": train_bytes_per_row() * rays_s / 1e9, "unit": "GB/s",
+                         "peak": measured_peak("hbm_gbs", 6800.0)[0],
+                         "frac": train_bytes_per_row() * rays_s / 1e9 / measured_peak("hbm_gbs", 6800.0)[0]},
         "clocks": clk.summary(),
     }
     s.close()
