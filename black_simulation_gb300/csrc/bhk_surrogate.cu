@@ -573,7 +573,7 @@ __host__ __device__ constexpr int layer_smem_bytes(int epi) {
 // activations, row-major [rows x WG], map tmB2 in [32 rows x 64] boxes): per tile one more set of MMAs
 // (M = 128 dZ columns, N = WG, K = the tile's 128 rows), both operands MN-major -- dZ straight from the
 // epilogue's staging boxes, which are laid out as the 128-byte-swizzled MN-major operand, Ain through
-// the ring -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
+// the ring (as many 32-row chunks per stage as fit: one for WG 256, four for WG 64) -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
 // FP32 gradient (map tmG) with TMA reductions at the end. The ring carries the tiles' chunks in the
 // order D(0), D(1), G(0), D(2), G(1), ... (D = the layer GEMM's A, G = Ain), so that the weight
 // gradient of tile t, which waits for tile t's epilogue, never holds up the MMAs of tile t + 1.
@@ -592,6 +592,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     constexpr uint32_t kIdescG = tc::idesc_bf16(kTileM, WG ? WG : 64, true, true);
     constexpr uint32_t kTmemCols = WG ? 512 : 2 * kLayerN;
     constexpr int kGBytes = WG * 32 * 2;  // one 32-row chunk of Ain
+    constexpr int kGRows = WG ? 32 * (kABytes / kGBytes) : 32;  // Ain rows per ring stage (128 for WG 64)
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* sW = smem;
@@ -608,7 +609,6 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     uint64_t* wdone = dzfree + 2;                   // (WG) every weight-gradient MMA has completed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wdone + 1);
     volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    volatile int* consumed = fail + 1;  // A chunks the MMA thread has taken (for the drain)
     float* sx = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(full) + 512);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -637,7 +637,6 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
         tc::mbar_init(wdone, 1);
         *fail = 0;
-        *consumed = 0;
         tc::fence_mbar_init();
     }
     if (warp == kLayerEpiWarps + 1) tc::tmem_alloc(tmem_slot, kTmemCols);
@@ -683,34 +682,39 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
                 }
                 if constexpr (WG > 0) {
-                    if (t >= 1 && ok) {  // G(t - 1): the weight gradient's Ain rows, 32 at a time
+                    if (t >= 1 && ok) {  // G(t - 1): the weight gradient's Ain rows, kGRows per stage
                         const int m0 = (pair + (t - 1) * pairs) * kTileM;
-                        for (int c = 0; c < kTileM / 32 && ok; ++c) {
+                        for (int c = 0; c < kTileM / kGRows && ok; ++c) {
                             int s;
                             if (!(ok = next_stage(s))) break;
-                            tc::mbar_expect_tx(&full[s], kGBytes);
-                            for (int j = 0; j < WG / 64; ++j)
-                                tc::tma_load_2d(sRing + s * kABytes + j * 4096, &tmB2, 64 * j, m0 + 32 * c, &full[s]);
+                            tc::mbar_expect_tx(&full[s], (kGRows / 32) * kGBytes);
+                            for (int q = 0; q < kGRows / 32; ++q)
+                                for (int j = 0; j < WG / 64; ++j)
+                                    tc::tma_load_2d(sRing + s * kABytes + q * kGBytes + j * 4096, &tmB2, 64 * j,
+                                                    m0 + kGRows * c + 32 * q, &full[s]);
                             ++issued;
                         }
                     }
                 }
             }
-            // Drain (bounded): every chunk issued has landed before the CTA may exit.
+            // Drain (bounded): every chunk issued has landed before the CTA may exit. A stage is refilled
+            // only after its previous chunk was consumed, so only the last kLayerRing chunks can still be
+            // in flight, each the latest phase of its stage.
             if (!tc::mbar_wait(wbar, 0)) *fail = 1;
-            for (int q = *consumed; q < issued; ++q) tc::mbar_wait(&full[q % kLayerRing], (q / kLayerRing) & 1);
+            for (int q = issued > kLayerRing ? issued - kLayerRing : 0; q < issued; ++q)
+                tc::mbar_wait(&full[q % kLayerRing], (q / kLayerRing) & 1);
         }
     } else if (warp == kLayerEpiWarps + 1) {
         // ---- MMA issuer ----
         if (lane == 0) {
             bool ok = tc::mbar_wait(wbar, 0);
             int taken = 0;
-            // The next ring stage, once its chunk has landed (false: a wait timed out or a role failed).
+            // The next ring stage, once its chunk has landed (false: the wait timed out). The chunk came
+            // by TMA, whose completion on the barrier orders it before the MMAs; the other roles' failures
+            // are checked once per tile.
             auto take = [&](int& s) {
                 s = taken % kLayerRing;
-                if (!tc::mbar_wait(&full[s], (taken / kLayerRing) & 1) || *fail) return false;
-                tc::fence_after_sync();
-                return true;
+                return tc::mbar_wait(&full[s], (taken / kLayerRing) & 1);
             };
             for (int t = 0; t <= my_tiles && ok; ++t) {
                 if (t < my_tiles) {  // D(t) into accumulator t & 1
@@ -727,7 +731,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         for (int kk = 0; kk < kChunkK / 16; ++kk)
                             tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
                         tc::mma_commit(&empty[s]);
-                        *consumed = ++taken;
+                        ++taken;
                     }
                     if (ok) tc::mma_commit(&tfull[b]);
                 }
@@ -736,19 +740,25 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         const int tg = t - 1, b = tg & 1;
                         ok = tc::mbar_wait(&dzready[b], (tg >> 1) & 1) && !*fail;
                         tc::fence_after_sync();
-                        for (int c = 0; c < kTileM / 32 && ok; ++c) {  // rows 32 c .. 32 c + 31: quad c's boxes
+                        for (int c = 0; c < kTileM / kGRows && ok; ++c) {
                             int s;
                             if (!(ok = take(s))) break;
 #pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                // dZ: M = the CTA's 128 columns (part 0 and part 1 boxes, 4 warps apart)
-                                const uint64_t ad =
-                                    tc::smem_desc_sw128_mn(sStage + c * kLayerStage + b * 4096 + h * 2048, 4 * kLayerStage);
-                                const uint64_t bd = tc::smem_desc_sw128_mn(sRing + s * kABytes + h * 2048, 4096);
-                                tc::mma_bf16(tmem + 2 * kLayerN, ad, bd, kIdescG, (tg > 0 || c > 0 || h > 0) ? 1u : 0u);
+                            for (int q = 0; q < kGRows / 32; ++q) {
+                                const int r32 = c * (kGRows / 32) + q;  // rows 32 r32 .. + 31: quad r32's boxes
+#pragma unroll
+                                for (int h = 0; h < 2; ++h) {
+                                    // dZ: M = the CTA's 128 columns (part 0 and part 1 boxes, 4 warps apart)
+                                    const uint64_t ad = tc::smem_desc_sw128_mn(
+                                        sStage + r32 * kLayerStage + b * 4096 + h * 2048, 4 * kLayerStage);
+                                    const uint64_t bd =
+                                        tc::smem_desc_sw128_mn(sRing + s * kABytes + q * kGBytes + h * 2048, 4096);
+                                    tc::mma_bf16(tmem + 2 * kLayerN, ad, bd, kIdescG,
+                                                 (tg > 0 || r32 > 0 || h > 0) ? 1u : 0u);
+                                }
                             }
                             tc::mma_commit(&empty[s]);
-                            *consumed = ++taken;
+                            ++taken;
                         }
                         if (ok) tc::mma_commit(&dzfree[b]);
                     }
