@@ -1998,9 +1998,16 @@ template <int HID>
 __host__ __device__ constexpr int inf_ring_bytes() {
     return inf_resident<HID>() ? kLayers * wchunk_bytes<HID>() : kInfStages * wchunk_bytes<HID>();
 }
+// (Resident weights) the biases as one more K slice of every layer's MMAs: a [128 x 64] tile whose first
+// three columns are ones, and per layer a weight-layout tile whose first three columns hold the bias split
+// into three BF16 parts (hi + mid + lo = the FP32 bias), the head's 16 rows last.
+template <int HID>
+__host__ __device__ constexpr int inf_bias_bytes() {
+    return inf_resident<HID>() ? kChunkBytes + 4 * wchunk_bytes<HID>() + kHeadChunkBytes : 0;
+}
 template <int HID>
 __host__ __device__ constexpr int inf_smem() {
-    return inf_slots<HID>() * act_bytes<HID>() + inf_ring_bytes<HID>() + 1024 + kInfMisc;
+    return inf_slots<HID>() * act_bytes<HID>() + inf_ring_bytes<HID>() + inf_bias_bytes<HID>() + 1024 + kInfMisc;
 }
 
 // Weight chunks per layer: 64-wide K slices of all output rows (N = HID per MMA; the head N = 16).
@@ -2043,6 +2050,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return r;
 }
 
+// SiLU of 32 accumulator columns that already hold z / 2 (raw FP32 bits) -> 16 packed BF16x2 words.
+__device__ __forceinline__ void silu32_half(const uint32_t (&v)[32], uint32_t (&w)[16]) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) w[q] = silu2_half(__uint_as_float(v[2 * q]), __uint_as_float(v[2 * q + 1]));
+}
+
 // SiLU of 32 accumulator columns (raw FP32 bits) with halved biases hb -> 16 packed BF16x2 words.
 __device__ __forceinline__ void silu32(const uint32_t (&v)[32], const float* hb, uint32_t (&w)[16]) {
 #pragma unroll
@@ -2076,7 +2089,9 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     static_assert(kInfStages + kInfStages + 2 * NS + 1 <= kInfBars, "the mbarriers fit their words");
     constexpr bool kResident = inf_resident<HID>();
     uint8_t* ring = base + NS * kActBytes;  // the weight ring, or (kResident) layer l's weights at l chunks
-    uint64_t* full = reinterpret_cast<uint64_t*>(ring + inf_ring_bytes<HID>());
+    uint8_t* sOnes = ring + inf_ring_bytes<HID>();  // (kResident) the ones tile, then the bias tiles
+    uint8_t* sBiasT = sOnes + kChunkBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sOnes + inf_bias_bytes<HID>());
     uint64_t* empty = full + kInfStages;
     uint64_t* act_ready = empty + kInfStages;  // [NS]
     uint64_t* acc_full = act_ready + NS;       // [NS]
@@ -2119,16 +2134,55 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
         atomicExch(ia.err, 1);
     };
 
-    if (warp == 0 && kResident) {
-        if (lane == 0 && n_my > 0) {  // ---- the network's weights, once
-            tc::mbar_expect_tx(&full[0], 4 * kWChunkBytes + kHeadChunkBytes);
-            tc::tma_load_2d(ring + 0 * kWChunkBytes, &tW0, 0, 0, &full[0]);
-            tc::tma_load_2d(ring + 1 * kWChunkBytes, &tW1, 0, 0, &full[0]);
-            tc::tma_load_2d(ring + 2 * kWChunkBytes, &tW2, 0, 0, &full[0]);
-            tc::tma_load_2d(ring + 3 * kWChunkBytes, &tW3, 0, 0, &full[0]);
-            tc::tma_load_2d(ring + 4 * kWChunkBytes, &tW4, 0, 0, &full[0]);
-            tc::mbar_wait(&full[0], 0);  // landed before the CTA may exit (bounded)
+    if constexpr (kResident) {
+        // ---- the network's weights, once, prepared by all threads: the hidden layers' halved (exact), so
+        // that the accumulators hold z / 2, the SiLU's argument; the biases (halved for the hidden layers)
+        // as the MMA chain's last K slice against the ones tile.
+        if (n_my > 0) {
+            if (threadIdx.x == 0) {
+                tc::mbar_expect_tx(&full[0], 4 * kWChunkBytes + kHeadChunkBytes);
+                tc::tma_load_2d(ring + 0 * kWChunkBytes, &tW0, 0, 0, &full[0]);
+                tc::tma_load_2d(ring + 1 * kWChunkBytes, &tW1, 0, 0, &full[0]);
+                tc::tma_load_2d(ring + 2 * kWChunkBytes, &tW2, 0, 0, &full[0]);
+                tc::tma_load_2d(ring + 3 * kWChunkBytes, &tW3, 0, 0, &full[0]);
+                tc::tma_load_2d(ring + 4 * kWChunkBytes, &tW4, 0, 0, &full[0]);
+            }
+            for (int i = threadIdx.x; i < kTileRays * 2; i += blockDim.x) {  // columns 0-7 and 8-15 of each row
+                const int r = i >> 1, h = i & 1;
+                *reinterpret_cast<uint4*>(sOnes + sw128(r, 8 * h)) =
+                    h == 0 ? make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+            }
+            for (int i = threadIdx.x; i < 4 * HID + 16; i += blockDim.x) {
+                const int l = i < 4 * HID ? i / HID : 4, n = i < 4 * HID ? i % HID : i - 4 * HID;
+                const float b = l < 4 ? 0.5f * ia.bias[l][n] : (n < kOut ? ia.bias[4][n] : 0.0f);
+                const bf16 hi = __float2bfloat16_rn(b);
+                const float r1 = b - __bfloat162float(hi);
+                const bf16 mid = __float2bfloat16_rn(r1);
+                const bf16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+                uint8_t* t = sBiasT + l * kWChunkBytes;
+                *reinterpret_cast<uint4*>(t + sw128(n, 0)) =
+                    make_uint4(static_cast<uint32_t>(__bfloat16_as_ushort(hi)) |
+                                   (static_cast<uint32_t>(__bfloat16_as_ushort(mid)) << 16),
+                               static_cast<uint32_t>(__bfloat16_as_ushort(lo)), 0u, 0u);
+                *reinterpret_cast<uint4*>(t + sw128(n, 8)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            if (!tc::mbar_wait(&full[0], 0)) {  // landed (bounded)
+                if (threadIdx.x == 0) give_up();
+            } else {
+                uint32_t* w = reinterpret_cast<uint32_t*>(ring);
+                for (int i = threadIdx.x; i < 4 * kWChunkBytes / 4; i += blockDim.x) {
+                    uint32_t h;
+                    asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(w[i]), "r"(0x3F003F00u));
+                    w[i] = h;
+                }
+            }
+            tc::fence_proxy_async();  // the generic-proxy writes, before the tensor core reads them
         }
+        __syncthreads();
+    }
+
+    if (warp == 0 && kResident) {
+        // (the weights were loaded above)
     } else if (warp == 1 && kResident) {
         if (lane == 0) {  // ---- MMA issuer: whichever tile slot has its next layer's input ready
             constexpr uint32_t kIdHid = tc::idesc_bf16(128, HID), kId16 = tc::idesc_bf16(128, 16);
@@ -2144,6 +2198,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
             bool ok = total == 0 || tc::mbar_wait(&full[0], 0);
             if (!ok) give_up();
             tc::fence_after_sync();
+            const uint64_t ones_d = tc::smem_desc_sw128(sOnes);
             uint32_t idle = 0;  // sweeps without progress (bounded)
             while (ok && total > 0) {
                 bool progress = false;
@@ -2158,6 +2213,7 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
                         tc::mma_bf16(d, ad + 2 * kk, bd + 2 * kk, l < 4 ? kIdHid : kId16, kk ? 1u : 0u);
+                    tc::mma_bf16(d, ones_d, tc::smem_desc_sw128(sBiasT + l * kWChunkBytes), l < 4 ? kIdHid : kId16, 1u);
                     tc::mma_commit(&acc_full[sl]);
                     layer[sl] = l + 1 == kLayers ? 0 : l + 1;
                     --left[sl];
@@ -2341,14 +2397,15 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                     constexpr int kHalf = HID / kHalves, kGroups = kHalf / 32;  // this warp's columns, in 32s
                     const float* hb = ia.half_bias + l * HID + kHalf * half;
                     const uint32_t cb = trow + static_cast<uint32_t>(kHalf) * half;
-                    if constexpr (HID == 64) {  // 32 columns at a time (the register budget of 24 warps)
+                    if constexpr (kResident) {  // 32 columns at a time (the register budget of 28 warps)
+                        static_assert(HID == 64, "resident weights at width 64");
                         uint32_t ra[32];
 #pragma unroll 1
                         for (int jj = 0; jj < kGroups; ++jj) {
                             tc::tmem_ld32_issue(cb + 32u * jj, ra);
                             tc::tmem_wait32(ra);
                             uint32_t w[16];
-                            silu32(ra, hb + 32 * jj, w);
+                            silu32_half(ra, w);  // the accumulator holds z / 2, bias included
                             store_act16(act, row, kHalf * half + 32 * jj, w);
                             store_act16(act, row, kHalf * half + 32 * jj + 16, w + 8);
                         }
@@ -2397,9 +2454,11 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                 tc::fence_before_sync();
                 bool fb = false;
                 if (live[v]) {
-                    const float* b4 = ia.bias[4];
+                    if constexpr (!kResident) {  // (resident weights: the MMAs added the bias)
+                        const float* b4 = ia.bias[4];
 #pragma unroll
-                    for (int i = 0; i < kOut; ++i) y[i] += __ldg(b4 + i);
+                        for (int i = 0; i < kOut; ++i) y[i] += __ldg(b4 + i);
+                    }
                     int cls = 0;
                     float mx = y[0];
                     if (y[1] > mx) { mx = y[1]; cls = 1; }
