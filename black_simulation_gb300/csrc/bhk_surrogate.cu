@@ -1202,10 +1202,12 @@ __device__ __forceinline__ void normalise(const float* x, float u[kIn]) {
     u[4] = x[4] * (1.0f / kImageScale);
 }
 
-// Fourier features of n rays, row-major [n x 64]: one thread per ray and frequency (a warp takes one
-// ray's 32 frequencies, so that its sines and its cosines are written as two contiguous 64-byte runs).
-// The first kernel of a training step also zeroes what the step accumulates into (the gradient, n_a
-// floats at zero_a, and the loss terms, n_b at zero_b).
+// Fourier features of n rays, row-major [n x 64]: lane j of a warp takes frequency j of eight
+// consecutive rays (so that each ray's sines and cosines are written as two contiguous 64-byte runs),
+// with the eight rays' inputs loaded up front and the lane's Fourier coefficients held in registers;
+// the batch is one wave of blocks. The first kernel of a training step also zeroes what the step
+// accumulates into (the gradient, n_a floats at zero_a, and the loss terms, n_b at zero_b).
+constexpr int kFeatRaysPerWarp = 8;
 __global__ void __launch_bounds__(256) feature_kernel(const float* __restrict__ x, const float* __restrict__ Bm,
                                                       bf16* __restrict__ rm, int n, float* zero_a, long long n_a,
                                                       float* zero_b, int n_b) {
@@ -1214,20 +1216,40 @@ __global__ void __launch_bounds__(256) feature_kernel(const float* __restrict__ 
     const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     for (long long i = t; i < n_a; i += static_cast<long long>(gridDim.x) * blockDim.x) zero_a[i] = 0.0f;
     if (t < n_b) zero_b[t] = 0.0f;
-    const long long r = t >> 5;
+    const long long r0 = (t >> 5) * kFeatRaysPerWarp;
     const int j = static_cast<int>(t & 31);
-    if (r >= n) return;
-    float u[kIn];
-    normalise(x + r * kIn, u);
-    float p = 0.0f;
+    if (r0 >= n) return;
+    float bj[kIn];
 #pragma unroll
-    for (int i = 0; i < kIn; ++i) p += __ldg(&Bm[j * kIn + i]) * u[i];
-    // sin and cos of 2 pi p: exact reduction to r = p - rint(p) in [-1/2, 1/2], then the hardware sine
-    // and cosine (absolute error ~2^-21 on [-pi, pi], far below the BF16 rounding that follows).
-    float sn, cs;
-    __sincosf(6.28318530717958648f * (p - rintf(p)), &sn, &cs);
-    rm[r * kFeat + j] = __float2bfloat16_rn(sn);
-    rm[r * kFeat + kFreq + j] = __float2bfloat16_rn(cs);
+    for (int i = 0; i < kIn; ++i) bj[i] = __ldg(&Bm[j * kIn + i]);
+    float xs[kFeatRaysPerWarp][kIn];
+#pragma unroll
+    for (int k = 0; k < kFeatRaysPerWarp; ++k)
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) xs[k][i] = r0 + k < n ? __ldg(x + (r0 + k) * kIn + i) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kFeatRaysPerWarp; ++k) {
+        const long long r = r0 + k;
+        if (r >= n) break;
+        float u[kIn];
+        normalise(xs[k], u);
+        float p = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) p += bj[i] * u[i];
+        // sin and cos of 2 pi p: exact reduction to r = p - rint(p) in [-1/2, 1/2], then the hardware sine
+        // and cosine (absolute error ~2^-21 on [-pi, pi], far below the BF16 rounding that follows).
+        float sn, cs;
+        __sincosf(6.28318530717958648f * (p - rintf(p)), &sn, &cs);
+        rm[r * kFeat + j] = __float2bfloat16_rn(sn);
+        rm[r * kFeat + kFreq + j] = __float2bfloat16_rn(cs);
+    }
+}
+
+// Blocks of feature_kernel for n rays that also zero n_a floats (at most 16 per thread).
+inline unsigned feature_blocks(long long n, long long n_a) {
+    const long long rays = (n + 8 * kFeatRaysPerWarp - 1) / (8 * kFeatRaysPerWarp);
+    const long long zero = (n_a + 16 * 256 - 1) / (16 * 256);
+    return static_cast<unsigned>(std::max<long long>(1, std::max(rays, zero)));
 }
 
 // Adam on the flat FP32 parameters; refreshes the BF16 copies W (fan_out x fan_in) and W^T.
@@ -1761,7 +1783,7 @@ bhk_status bhk_surrogate_gradients(bhk_surrogate* s, const float* x, const uint8
     }
     cudaStream_t st = nullptr;
     cudaMemsetAsync(s->err, 0, sizeof(int), st);
-    cudaError_t e = launch_pdl(feature_kernel, dim3((n + 7) / 8), dim3(256), 0, st, x,
+    cudaError_t e = launch_pdl(feature_kernel, dim3(feature_blocks(n, s->L.total)), dim3(256), 0, st, x,
                                static_cast<const float*>(s->Bm), s->F_rm, n, s->g,
                                static_cast<long long>(s->L.total), s->loss, 4);
     const EpiArgs la = loss_args(s, cls, tgt, n);
@@ -1809,7 +1831,7 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
     aa.loss = s->loss;
     for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
         const int64_t off = (t % nb) * batch;
-        e = launch_pdl(feature_kernel, dim3((batch + 7) / 8), dim3(256), 0, st, x + off * kIn,
+        e = launch_pdl(feature_kernel, dim3(feature_blocks(batch, s->L.total)), dim3(256), 0, st, x + off * kIn,
                        static_cast<const float*>(s->Bm), s->F_rm, batch, s->g, static_cast<long long>(s->L.total),
                        s->loss, 4);
         const EpiArgs la = loss_args(s, cls + off, tgt + off * kOut, batch);
@@ -1848,7 +1870,7 @@ bhk_status bhk_surrogate_predict(bhk_surrogate* s, const float* x, int64_t n, fl
             set_last_error("bhk_surrogate_predict: tensor map creation failed");
             return BHK_ECUDA;
         }
-        cudaError_t e = launch_pdl(feature_kernel, dim3((rows + 7) / 8), dim3(256), 0, st, x + off * kIn,
+        cudaError_t e = launch_pdl(feature_kernel, dim3(feature_blocks(rows, 0)), dim3(256), 0, st, x + off * kIn,
                                    static_cast<const float*>(s->Bm), s->F_rm, rows, static_cast<float*>(nullptr),
                                    0LL, static_cast<float*>(nullptr), 0);
         if (e == cudaSuccess) e = forward(s, M, rows, st);
