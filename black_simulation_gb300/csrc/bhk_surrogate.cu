@@ -1281,7 +1281,9 @@ __host__ __device__ inline int weights_blocks(int hid) {
 // kAdam: one Adam step on the FP32 parameters (m, v, p), else the parameters as they are; either way
 // the BF16 copies W (fan_out x fan_in) and W^T follow. A block takes a 32 x 32 tile of one layer's
 // weights: 256 threads read and write the FP32 state and W along the rows (coalesced), and write W^T
-// along its rows through a shared-memory transpose; the last block takes the biases.
+// along its rows through a shared-memory transpose; the last block takes the biases. Each thread
+// loads all its elements' state before it updates any (the stores may not be assumed apart from the
+// next element's loads, so interleaving them would expose one load latency per element).
 template <bool kAdam>
 __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
     __shared__ bf16 tile[32][34];
@@ -1290,27 +1292,50 @@ __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
         tc::grid_dep_launch();
         if (a.hist && blockIdx.x == 0 && threadIdx.x < 4) a.hist[threadIdx.x] = a.loss[threadIdx.x];
     }
-    auto update = [&](size_t i) {
-        float w = a.p[i];
-        if constexpr (kAdam) {
-            const float g = a.g[i];
-            const float m = a.b1 * a.m[i] + (1.0f - a.b1) * g;
-            const float v = a.b2 * a.v[i] + (1.0f - a.b2) * g * g;
-            a.m[i] = m;
-            a.v[i] = v;
-            w -= a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
-            a.p[i] = w;
+    constexpr int kPer = 5;  // elements per thread (4 in a weight tile; up to 5 of the biases)
+    size_t idx[kPer];
+    bool in[kPer];
+    float pw[kPer], gw[kPer], mw[kPer], vw[kPer];
+    // Loads the state of the elements marked in[], then updates them (Adam) and stores it back.
+    auto update_all = [&]() {
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            if (!in[q]) continue;
+            pw[q] = a.p[idx[q]];
+            if constexpr (kAdam) {
+                gw[q] = a.g[idx[q]];
+                mw[q] = a.m[idx[q]];
+                vw[q] = a.v[idx[q]];
+            }
         }
-        return w;
+        if constexpr (kAdam) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                if (!in[q]) continue;
+                const float g = gw[q];
+                const float m = a.b1 * mw[q] + (1.0f - a.b1) * g;
+                const float v = a.b2 * vw[q] + (1.0f - a.b2) * g * g;
+                a.m[idx[q]] = m;
+                a.v[idx[q]] = v;
+                pw[q] -= a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
+                a.p[idx[q]] = pw[q];
+            }
+        }
     };
     int b = blockIdx.x;
     int l = 0;
     for (; l < kLayers && b >= weight_tiles(l, a.hid); ++l) b -= weight_tiles(l, a.hid);
-    if (l == kLayers) {  // the biases, each right after its layer's weights
-        for (int q = 0; q < kLayers; ++q) {
-            const size_t bo = a.wofs[q] + static_cast<size_t>(fan_out(q, a.hid)) * fan_in(q, a.hid);
-            for (int j = threadIdx.x; j < fan_out(q, a.hid); j += blockDim.x) update(bo + j);
+    if (l == kLayers) {  // the biases (each stored right after its layer's weights), all layers at once
+        const int nb = 4 * a.hid + kOutPad;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int j = threadIdx.x + q * blockDim.x;
+            in[q] = j < nb;
+            const int ql = j < 4 * a.hid ? j / a.hid : kLayers - 1;
+            const int jj = j < 4 * a.hid ? j - ql * a.hid : j - 4 * a.hid;
+            idx[q] = in[q] ? a.wofs[ql] + static_cast<size_t>(fan_out(ql, a.hid)) * fan_in(ql, a.hid) + jj : 0;
         }
+        update_all();
         return;
     }
     const int fi = fan_in(l, a.hid), fo = fan_out(l, a.hid);
@@ -1318,11 +1343,18 @@ __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
     const int o0 = (b / kt) * 32, k0 = (b % kt) * 32;
     const int c = threadIdx.x & 31, r = threadIdx.x >> 5;
 #pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        const int o = o0 + r + 8 * q, k = k0 + c;
+        in[q] = q < 4 && o < fo && k < fi;
+        idx[q] = in[q] ? a.wofs[l] + static_cast<size_t>(o) * fi + k : 0;
+    }
+    update_all();
+#pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int o = o0 + r + 8 * q, k = k0 + c;
-        if (o < fo && k < fi) {
+        if (in[q]) {
             const size_t j = static_cast<size_t>(o) * fi + k;
-            const bf16 wb = __float2bfloat16_rn(update(a.wofs[l] + j));
+            const bf16 wb = __float2bfloat16_rn(pw[q]);
             a.w_rm[l][j] = wb;
             tile[r + 8 * q][c] = wb;
         }
