@@ -975,6 +975,236 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     if (warp == kLayerEpiWarps + 1) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+// The training head of the width-256 network, forward and weight gradient in one pass over A3 (the last
+// hidden layer's activations, [rows x 256] row-major): per 128-row tile, Y = A3 W5^T + b5 (MMAs against
+// the resident W5, TMEM columns 16 b), the rows' loss terms and dLoss/dY (to dy_rm, which the input
+// gradient reads), and dW5^T += A3^T dY from the same tile in shared memory -- A3 as an MN-major operand
+// straight from its K-major chunks, dY^T staged by the epilogue as a K-major [16 x 128] operand --
+// accumulated in TMEM columns 32-63 over the CTA's tiles and added into the FP32 gradient with TMA
+// reductions at the end. The MMA thread runs Y(t) before the weight gradient of tile t - 1, so that tile
+// t's epilogue overlaps it. Persistent: CTA c takes tiles c, c + grid, ...; warp 0 loads, warp 1 issues,
+// warps 2-5 (one per TMEM lane quadrant) are the epilogue.
+constexpr int kHeadThreads = 32 * 6;
+constexpr int kHeadTileBytes = 4 * kABytes;  // 128 rows x 256 BF16, four [128 x 64] chunks
+constexpr int kHeadW5Bytes = 16 * 64 * 2;    // one [16 x 64] chunk of W5 (or of dY^T)
+constexpr int kHeadSmem = 2 * kHeadTileBytes + 4 * kHeadW5Bytes + 2 * 2 * kHeadW5Bytes + 1024 /* alignment */ + 256 +
+                          4 * 20 * 4 + 256;
+
+__global__ void __launch_bounds__(kHeadThreads, 1)
+head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW,
+            const __grid_constant__ CUtensorMap tmG, EpiArgs ea, int* err) {
+    constexpr uint32_t kIdY = tc::idesc_bf16(kTileM, 16);              // Y: A3 (K-major) x W5^T
+    constexpr uint32_t kIdG = tc::idesc_bf16(kTileM, 16, true, false);  // dW5^T: A3^T (MN-major) x dY
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* sA = smem;                          // two A3 tiles
+    uint8_t* sW = sA + 2 * kHeadTileBytes;       // W5, four K chunks
+    uint8_t* sD = sW + 4 * kHeadW5Bytes;         // dY^T, two buffers of two K chunks
+    uint64_t* full = reinterpret_cast<uint64_t*>(sD + 4 * kHeadW5Bytes);
+    uint64_t* empty = full + 2;    // the tile's MMAs (Y and weight gradient) have read buffer b
+    uint64_t* yfull = empty + 2;   // Y of buffer b's tile is in TMEM
+    uint64_t* yempty = yfull + 2;  // the epilogue has read it
+    uint64_t* dyready = yempty + 2;
+    uint64_t* dyfree = dyready + 2;
+    uint64_t* wbar = dyfree + 2;
+    uint64_t* wdone = wbar + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(wdone + 1);
+    volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    float* red = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(full) + 256);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (ea.M + kTileM - 1) / kTileM;
+    const int my = static_cast<int>(blockIdx.x) < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&full[b], 1);
+            tc::mbar_init(&empty[b], 1);
+            tc::mbar_init(&yfull[b], 1);
+            tc::mbar_init(&yempty[b], 4);
+            tc::mbar_init(&dyready[b], 4);
+            tc::mbar_init(&dyfree[b], 1);
+        }
+        tc::mbar_init(wbar, 1);
+        tc::mbar_init(wdone, 1);
+        *fail = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) tc::tmem_alloc(tmem_slot, 64);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
+
+    if (warp == 0) {
+        if (lane == 0 && my > 0) {  // ---- producer: W5 once, then the A3 tiles, double-buffered
+            tc::mbar_expect_tx(wbar, 4 * kHeadW5Bytes);
+            for (int c = 0; c < 4; ++c) tc::tma_load_2d(sW + c * kHeadW5Bytes, &tmW, 64 * c, 0, wbar);
+            int t = 0;
+            for (; t < my && !*fail; ++t) {
+                const int b = t & 1;
+                if (!tc::mbar_wait(&empty[b], ((t >> 1) & 1) ^ 1)) {
+                    *fail = 1;
+                    break;
+                }
+                const int m0 = (blockIdx.x + t * gridDim.x) * kTileM;
+                tc::mbar_expect_tx(&full[b], kHeadTileBytes);
+                for (int c = 0; c < 4; ++c) tc::tma_load_2d(sA + b * kHeadTileBytes + c * kABytes, &tmA, 64 * c, m0, &full[b]);
+            }
+            // Drain (bounded): the loads issued have landed before the CTA may exit.
+            tc::mbar_wait(wbar, 0);
+            for (int q = t > 2 ? t - 2 : 0; q < t; ++q) tc::mbar_wait(&full[q & 1], (q >> 1) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && my > 0) {  // ---- MMA issuer: Y(t), then the weight gradient of tile t - 1
+            bool ok = tc::mbar_wait(wbar, 0);
+            for (int t = 0; t <= my && ok; ++t) {
+                if (t < my) {
+                    const int b = t & 1;
+                    ok = tc::mbar_wait(&full[b], (t >> 1) & 1) && tc::mbar_wait(&yempty[b], ((t >> 1) & 1) ^ 1) && !*fail;
+                    if (!ok) break;
+                    tc::fence_after_sync();
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint64_t ad = tc::smem_desc_sw128(sA + b * kHeadTileBytes + c * kABytes);
+                        const uint64_t bd = tc::smem_desc_sw128(sW + c * kHeadW5Bytes);
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                            tc::mma_bf16(tmem + 16 * b, ad + 2 * kk, bd + 2 * kk, kIdY, (c | kk) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&yfull[b]);
+                }
+                if (t >= 1) {
+                    const int tg = t - 1, b = tg & 1;
+                    ok = tc::mbar_wait(&dyready[b], (tg >> 1) & 1) && !*fail;
+                    if (!ok) break;
+                    tc::fence_after_sync();
+#pragma unroll
+                    for (int p = 0; p < 2; ++p)      // A3 columns 128 p .. 128 p + 127 (chunks 2 p, 2 p + 1)
+#pragma unroll
+                        for (int kk = 0; kk < 8; ++kk) {  // rows 16 kk .. 16 kk + 15
+                            const uint64_t ad = tc::smem_desc_sw128_mn(
+                                sA + b * kHeadTileBytes + 2 * p * kABytes + kk * 2048, kABytes);
+                            const uint64_t bd = tc::smem_desc_sw128(sD + b * 2 * kHeadW5Bytes + (kk >> 2) * kHeadW5Bytes) +
+                                                2 * (kk & 3);
+                            tc::mma_bf16(tmem + 32 + 16 * p, ad, bd, kIdG, (tg > 0 || kk > 0) ? 1u : 0u);
+                        }
+                    tc::mma_commit(&empty[b]);
+                    tc::mma_commit(&dyfree[b]);
+                }
+            }
+            if (!ok) *fail = 1;
+            tc::mma_commit(wdone);  // every MMA issued has completed when this arrives
+        }
+    } else {
+        // ---- epilogue: lane = row of the tile (warp w reads TMEM lanes 32 (w % 4) ..)
+        const int quad = warp & 3;
+        const int row = 32 * quad + lane;
+        float csum[kOutPad], tsum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int i = 0; i < kOutPad; ++i) csum[i] = 0.0f;
+        bool ok = true;
+        for (int t = 0; t < my && ok; ++t) {
+            const int b = t & 1;
+            const int m = (blockIdx.x + t * gridDim.x) * kTileM + row;
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&yfull[b], (t >> 1) & 1) ? 1 : 0) != 0 && !*fail;
+            if (!ok) break;
+            tc::fence_after_sync();
+            uint32_t r[16];
+            tc::tmem_ld16_issue(tmem + (static_cast<uint32_t>(32 * quad) << 16) + 16 * b, r);
+            tc::tmem_wait16(r);
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&yempty[b]);
+            float d[kOutPad], terms[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int i = 0; i < kOutPad; ++i) d[i] = 0.0f;
+            if (m < ea.M) {
+                float y[kOutPad];
+#pragma unroll
+                for (int i = 0; i < kOutPad; ++i) y[i] = __uint_as_float(r[i]) + ea.bias[i];
+                row_loss(y, static_cast<int>(ea.cls[m]) - 1, ea.tgt + static_cast<size_t>(m) * kOut, ea.inv_n, ea.lw, d,
+                         terms);
+            }
+            __align__(16) bf16 ob[kOutPad];
+#pragma unroll
+            for (int i = 0; i < kOutPad; ++i) {
+                ob[i] = __float2bfloat16_rn(d[i]);
+                csum[i] += d[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) tsum[i] += terms[i];
+            if (m < ea.M) {
+                uint4* dst = reinterpret_cast<uint4*>(ea.dy_rm + static_cast<size_t>(m) * kOutPad);
+                dst[0] = reinterpret_cast<const uint4*>(ob)[0];
+                dst[1] = reinterpret_cast<const uint4*>(ob)[1];
+            }
+            // dY^T of the tile (zeros past the last row) into buffer b once the weight gradient of tile
+            // t - 2 has read it: element (output i, row) at row i, column row of the K-major operand.
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&dyfree[b], ((t >> 1) & 1) ^ 1) ? 1 : 0) != 0;
+            if (!ok) break;
+            uint8_t* dt = sD + b * 2 * kHeadW5Bytes + (row >> 6) * kHeadW5Bytes;
+#pragma unroll
+            for (int i = 0; i < kOutPad; ++i)
+                *reinterpret_cast<bf16*>(dt + i * 128 + ((((row & 63) >> 3) ^ (i & 7)) << 4) + ((row & 7) << 1)) = ob[i];
+            tc::fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&dyready[b]);
+        }
+        if (!ok && lane == 0) *fail = 1;
+        // The bias gradient and the loss terms of the CTA's rows: warp sums, then the four warps.
+#pragma unroll
+        for (int i = 0; i < kOutPad + 4; ++i) {
+            float v = i < kOutPad ? csum[i] : tsum[i - kOutPad] * ea.inv_n;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[quad * (kOutPad + 4) + i] = v;
+        }
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (warp == 2 && lane < kOutPad + 4 && ok && my > 0) {
+            float v = 0.0f;
+            for (int q = 0; q < 4; ++q) v += red[q * (kOutPad + 4) + lane];
+            if (lane < kOutPad) {
+                if (v != 0.0f) atomicAdd(&ea.colsum[lane], v);
+            } else {
+                atomicAdd(&ea.loss[lane - kOutPad], v);
+            }
+        }
+        // dW5 += the CTA's partial: TMEM lane c of columns 32 + 16 p holds dW5[.][128 p + c] (c = 32 quad +
+        // lane); each warp stages its [16 x 32] block per p as a [32 x 32] FP32 box (rows 16-31 lie past
+        // the 16 rows of W5 and are not written) in the idle A3 buffers and adds it with a TMA reduction.
+        if (my > 0) {
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(wdone, 0) ? 1 : 0) != 0 && !*fail;
+            if (ok) {
+                tc::fence_after_sync();
+#pragma unroll
+                for (int p = 0; p < 2; ++p) {
+                    uint32_t v[16];
+                    tc::tmem_ld16_issue(tmem + (static_cast<uint32_t>(32 * quad) << 16) + 32 + 16 * p, v);
+                    tc::tmem_wait16(v);
+                    uint8_t* box = sA + (2 * quad + p) * 4096;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        *reinterpret_cast<uint32_t*>(box + i * 128 + (((lane >> 2) ^ (i & 7)) << 4) + ((lane & 3) << 2)) = v[i];
+                    tc::fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) {
+                        tc::tma_reduce_add_2d(&tmG, box, 128 * p + 32 * quad, 0);
+                        tc::bulk_commit();
+                    }
+                }
+                if (lane == 0) tc::bulk_wait_all();
+            } else if (lane == 0) {
+                *fail = 1;
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0 && *fail) atomicExch(err, 1);
+    if (warp == 1) tc::tmem_dealloc(tmem, 64);
+}
+
 // ------------------------------------------------------------------------------ host side ----
 
 // Launch with programmatic stream serialization: the grid may be scheduled while the previous grid of
@@ -1473,8 +1703,20 @@ EpiArgs epi(int M, int N) {
     return e;
 }
 
+// The width-256 training head (head_kernel): persistent, one CTA per SM or fewer.
+cudaError_t launch_head(const Maps& M, const EpiArgs& ea, int sms, int* err, cudaStream_t s) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(head_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kHeadSmem);
+    });
+    const int ntiles = (ea.M + kTileM - 1) / kTileM;
+    const int grid = std::max(1, std::min(ntiles, sms));
+    return launch_pdl(head_kernel, dim3(grid), dim3(kHeadThreads), kHeadSmem, s, M.a_rm[3], M.W[4], M.gm[4], ea, err);
+}
+
 // Forward pass of n rows (features already in F): z, activations, and the head -- into Y, or with `loss`
-// (training: the loss's targets and outputs) the loss and dLoss/dY straight from the head's epilogue.
+// (training: the loss's targets and outputs) the loss and dLoss/dY straight from the head's epilogue;
+// at width 256 the head's weight gradient too (head_kernel).
 cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, const EpiArgs* loss = nullptr) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
@@ -1495,8 +1737,12 @@ cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, con
         ea.bias = s->p + s->L.b[4];
         ea.f32 = s->Y;
         ea.ld_f32 = kOutPad;
-        e = loss ? launch_gemm_bn<16, kHeadLoss, 0>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st, nullptr)
-                 : launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st);
+        if (!loss)
+            e = launch_gemm<kStoreF32>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st);
+        else if (H == kLayerN * 2)
+            e = launch_head(M, ea, s->sms, s->err, st);
+        else
+            e = launch_gemm_bn<16, kHeadLoss, 0>(M.a_rm[3], M.W[4], ea, n, kOutPad, H, 1, s->err, st, nullptr);
     }
     return e;
 }
@@ -1544,8 +1790,9 @@ cudaError_t weight_grad(bhk_surrogate* s, const Maps& maps, int l, const CUtenso
 cudaError_t backward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
-    // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major), then dA4 = dY W5 -> dZ4.
-    e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
+    // Head: dW5 = dY^T A4 (A = dY^T K-major, 16 rows; B = A4 MN-major; at width 256 head_kernel computed
+    // it with the forward), then dA4 = dY W5 -> dZ4.
+    if (H != kLayerN * 2) e = weight_grad<2>(s, M, 4, M.dy_t, M.am[3], kOutPad, H, n, st);
     if (e == cudaSuccess && H == kLayerN * 2) {
         // Width 256: dZ_l = (dZ_{l+1} W_{l+1}) silu'(z_l) for l = 3 .. 0 (dY W5 for l = 3), each kernel with
         // the weight gradient dW_l = dZ_l^T A_{l-1} (F for l = 0) and the bias gradient fused in; dZ_l goes
