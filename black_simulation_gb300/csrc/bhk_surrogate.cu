@@ -982,12 +982,13 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
 // straight from its K-major chunks, dY^T staged by the epilogue as a K-major [16 x 128] operand --
 // accumulated in TMEM columns 32-63 over the CTA's tiles and added into the FP32 gradient with TMA
 // reductions at the end. The MMA thread runs Y(t) before the weight gradient of tile t - 1, so that tile
-// t's epilogue overlaps it. Persistent: CTA c takes tiles c, c + grid, ...; warp 0 loads, warp 1 issues,
-// warps 2-5 (one per TMEM lane quadrant) are the epilogue.
+// t's epilogue overlaps it. Persistent: CTA c takes tiles c, c + grid, ..., three A3 tiles in flight;
+// warp 0 loads, warp 1 issues, warps 2-5 (one per TMEM lane quadrant) are the epilogue.
 constexpr int kHeadThreads = 32 * 6;
 constexpr int kHeadTileBytes = 4 * kABytes;  // 128 rows x 256 BF16, four [128 x 64] chunks
+constexpr int kHeadBufs = 3;                 // A3 tiles in flight per CTA
 constexpr int kHeadW5Bytes = 16 * 64 * 2;    // one [16 x 64] chunk of W5 (or of dY^T)
-constexpr int kHeadSmem = 2 * kHeadTileBytes + 4 * kHeadW5Bytes + 2 * 2 * kHeadW5Bytes + 1024 /* alignment */ + 256 +
+constexpr int kHeadSmem = kHeadBufs * kHeadTileBytes + 4 * kHeadW5Bytes + 2 * 2 * kHeadW5Bytes + 1024 /* alignment */ + 256 +
                           4 * 20 * 4 + 256;
 
 __global__ void __launch_bounds__(kHeadThreads, 1)
@@ -997,12 +998,12 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     constexpr uint32_t kIdG = tc::idesc_bf16(kTileM, 16, true, false);  // dW5^T: A3^T (MN-major) x dY
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t* sA = smem;                          // two A3 tiles
-    uint8_t* sW = sA + 2 * kHeadTileBytes;       // W5, four K chunks
+    uint8_t* sA = smem;                          // kHeadBufs A3 tiles
+    uint8_t* sW = sA + kHeadBufs * kHeadTileBytes;  // W5, four K chunks
     uint8_t* sD = sW + 4 * kHeadW5Bytes;         // dY^T, two buffers of two K chunks
     uint64_t* full = reinterpret_cast<uint64_t*>(sD + 4 * kHeadW5Bytes);
-    uint64_t* empty = full + 2;    // the tile's MMAs (Y and weight gradient) have read buffer b
-    uint64_t* yfull = empty + 2;   // Y of buffer b's tile is in TMEM
+    uint64_t* empty = full + kHeadBufs;  // the tile's MMAs (Y and weight gradient) have read A3 buffer a
+    uint64_t* yfull = empty + kHeadBufs;  // Y of tile t is in TMEM columns 16 (t & 1)
     uint64_t* yempty = yfull + 2;  // the epilogue has read it
     uint64_t* dyready = yempty + 2;
     uint64_t* dyfree = dyready + 2;
@@ -1016,9 +1017,11 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int ntiles = (ea.M + kTileM - 1) / kTileM;
     const int my = static_cast<int>(blockIdx.x) < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
     if (threadIdx.x == 0) {
+        for (int a = 0; a < kHeadBufs; ++a) {
+            tc::mbar_init(&full[a], 1);
+            tc::mbar_init(&empty[a], 1);
+        }
         for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&full[b], 1);
-            tc::mbar_init(&empty[b], 1);
             tc::mbar_init(&yfull[b], 1);
             tc::mbar_init(&yempty[b], 4);
             tc::mbar_init(&dyready[b], 4);
@@ -1038,36 +1041,39 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     tc::grid_dep_launch();
 
     if (warp == 0) {
-        if (lane == 0 && my > 0) {  // ---- producer: W5 once, then the A3 tiles, double-buffered
+        if (lane == 0 && my > 0) {  // ---- producer: W5 once, then the A3 tiles through kHeadBufs buffers
             tc::mbar_expect_tx(wbar, 4 * kHeadW5Bytes);
             for (int c = 0; c < 4; ++c) tc::tma_load_2d(sW + c * kHeadW5Bytes, &tmW, 64 * c, 0, wbar);
             int t = 0;
             for (; t < my && !*fail; ++t) {
-                const int b = t & 1;
-                if (!tc::mbar_wait(&empty[b], ((t >> 1) & 1) ^ 1)) {
+                const int a = t % kHeadBufs;
+                if (!tc::mbar_wait(&empty[a], ((t / kHeadBufs) & 1) ^ 1)) {
                     *fail = 1;
                     break;
                 }
                 const int m0 = (blockIdx.x + t * gridDim.x) * kTileM;
-                tc::mbar_expect_tx(&full[b], kHeadTileBytes);
-                for (int c = 0; c < 4; ++c) tc::tma_load_2d(sA + b * kHeadTileBytes + c * kABytes, &tmA, 64 * c, m0, &full[b]);
+                tc::mbar_expect_tx(&full[a], kHeadTileBytes);
+                for (int c = 0; c < 4; ++c) tc::tma_load_2d(sA + a * kHeadTileBytes + c * kABytes, &tmA, 64 * c, m0, &full[a]);
             }
-            // Drain (bounded): the loads issued have landed before the CTA may exit.
+            // Drain (bounded): the loads issued have landed before the CTA may exit (the last kHeadBufs,
+            // each the latest phase of its buffer).
             tc::mbar_wait(wbar, 0);
-            for (int q = t > 2 ? t - 2 : 0; q < t; ++q) tc::mbar_wait(&full[q & 1], (q >> 1) & 1);
+            for (int q = t > kHeadBufs ? t - kHeadBufs : 0; q < t; ++q)
+                tc::mbar_wait(&full[q % kHeadBufs], (q / kHeadBufs) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0 && my > 0) {  // ---- MMA issuer: Y(t), then the weight gradient of tile t - 1
             bool ok = tc::mbar_wait(wbar, 0);
             for (int t = 0; t <= my && ok; ++t) {
                 if (t < my) {
-                    const int b = t & 1;
-                    ok = tc::mbar_wait(&full[b], (t >> 1) & 1) && tc::mbar_wait(&yempty[b], ((t >> 1) & 1) ^ 1) && !*fail;
+                    const int a = t % kHeadBufs, b = t & 1;
+                    ok = tc::mbar_wait(&full[a], (t / kHeadBufs) & 1) && tc::mbar_wait(&yempty[b], ((t >> 1) & 1) ^ 1) &&
+                         !*fail;
                     if (!ok) break;
                     tc::fence_after_sync();
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        const uint64_t ad = tc::smem_desc_sw128(sA + b * kHeadTileBytes + c * kABytes);
+                        const uint64_t ad = tc::smem_desc_sw128(sA + a * kHeadTileBytes + c * kABytes);
                         const uint64_t bd = tc::smem_desc_sw128(sW + c * kHeadW5Bytes);
 #pragma unroll
                         for (int kk = 0; kk < 4; ++kk)
@@ -1076,7 +1082,7 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
                     tc::mma_commit(&yfull[b]);
                 }
                 if (t >= 1) {
-                    const int tg = t - 1, b = tg & 1;
+                    const int tg = t - 1, a = tg % kHeadBufs, b = tg & 1;
                     ok = tc::mbar_wait(&dyready[b], (tg >> 1) & 1) && !*fail;
                     if (!ok) break;
                     tc::fence_after_sync();
@@ -1085,12 +1091,12 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
                         for (int kk = 0; kk < 8; ++kk) {  // rows 16 kk .. 16 kk + 15
                             const uint64_t ad = tc::smem_desc_sw128_mn(
-                                sA + b * kHeadTileBytes + 2 * p * kABytes + kk * 2048, kABytes);
+                                sA + a * kHeadTileBytes + 2 * p * kABytes + kk * 2048, kABytes);
                             const uint64_t bd = tc::smem_desc_sw128(sD + b * 2 * kHeadW5Bytes + (kk >> 2) * kHeadW5Bytes) +
                                                 2 * (kk & 3);
                             tc::mma_bf16(tmem + 32 + 16 * p, ad, bd, kIdG, (tg > 0 || kk > 0) ? 1u : 0u);
                         }
-                    tc::mma_commit(&empty[b]);
+                    tc::mma_commit(&empty[a]);
                     tc::mma_commit(&dyfree[b]);
                 }
             }
