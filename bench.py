@@ -443,12 +443,15 @@ MAC_TRAIN = 2 * MAC_FWD + 256 * 16 + 3 * 256 * 256
 def train_bytes_per_row(width: int = 256) -> int:
     """Algorithmic HBM bytes per batch row of one training step (BF16 activations of `width`, 64 features,
     16 padded outputs), as the step's kernels move them: features written; per hidden layer its input
-    read and Z and A written; the head's input read, dY written in two layouts with the targets read;
-    the head's weight gradient reading dY^T and A3; per hidden layer of the backward dZ of the layer
-    above, Z and the layer's input read and dZ written (not dZ_0)."""
+    read and Z and A written; the head's input read with the targets, and dY written -- at width 256 the
+    head's weight gradient comes from the same read of A3, at width 64 a second kernel reads dY^T and A3
+    (dY written in both layouts); per hidden layer of the backward dZ of the layer above, Z and the
+    layer's input read and dZ written (not dZ_0)."""
     a, f, o = 2 * width, 2 * 64, 2 * 16
-    forward = f + (f + 2 * a) + 3 * (a + 2 * a) + a + 2 * o + 33
-    backward = (o + a) + (o + a + a + a) + 2 * (a + a + a + a) + (a + a + f)
+    fused_head = width == 256
+    forward = (f + 2 * a) + 3 * (a + 2 * a) + a + 33 + (o if fused_head else 2 * o)
+    head_weight_gradient = 0 if fused_head else o + a
+    backward = head_weight_gradient + (o + a + a + a) + 2 * (a + a + a + a) + (a + a + f)
     return f + forward + backward
 
 
