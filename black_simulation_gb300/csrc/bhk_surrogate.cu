@@ -644,7 +644,15 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    // Launched programmatically: the previous grid of the stream has finished before any global access.
+    // The weights are loaded before the wait on the previous grid, overlapping its tail: they were
+    // written by the optimiser step (or a weight upload) at least two launches upstream, and no kernel
+    // in between writes them.
+    if (warp == kLayerEpiWarps && lane == 0) {
+        tc::mbar_expect_tx(wbar, kc * kABytes);
+        for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
+    }
+    // Launched programmatically: the previous grid of the stream has finished before any other global
+    // access.
     tc::grid_dep_wait();
     tc::grid_dep_launch();
     if constexpr (EPI == kBiasSilu) {
@@ -655,10 +663,8 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     __syncthreads();
 
     if (warp == kLayerEpiWarps) {
-        // ---- producer: the weights once, then the A chunks of every tile through the ring ----
+        // ---- producer: the A chunks of every tile through the ring (the weights are on their way) ----
         if (lane == 0) {
-            tc::mbar_expect_tx(wbar, kc * kABytes);
-            for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
             int issued = 0;
             // Takes the next ring stage (false: a wait timed out).
             auto next_stage = [&](int& s) {
@@ -1037,13 +1043,16 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
+    // W5 before the wait on the previous grid (written by the optimiser step, launches upstream).
+    if (warp == 0 && lane == 0 && my > 0) {
+        tc::mbar_expect_tx(wbar, 4 * kHeadW5Bytes);
+        for (int c = 0; c < 4; ++c) tc::tma_load_2d(sW + c * kHeadW5Bytes, &tmW, 64 * c, 0, wbar);
+    }
     tc::grid_dep_wait();
     tc::grid_dep_launch();
 
     if (warp == 0) {
-        if (lane == 0 && my > 0) {  // ---- producer: W5 once, then the A3 tiles through kHeadBufs buffers
-            tc::mbar_expect_tx(wbar, 4 * kHeadW5Bytes);
-            for (int c = 0; c < 4; ++c) tc::tma_load_2d(sW + c * kHeadW5Bytes, &tmW, 64 * c, 0, wbar);
+        if (lane == 0 && my > 0) {  // ---- producer: the A3 tiles through kHeadBufs buffers
             int t = 0;
             for (; t < my && !*fail; ++t) {
                 const int a = t % kHeadBufs;
