@@ -651,15 +651,24 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         tc::mbar_expect_tx(wbar, kc * kABytes);
         for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
     }
-    // Launched programmatically: the previous grid of the stream has finished before any other global
-    // access.
-    tc::grid_dep_wait();
-    tc::grid_dep_launch();
+    // So is each epilogue warp's first pre-activation box (kDsilu): Z was written by the forward pass.
+    if constexpr (EPI == kDsilu) {
+        if (warp < kLayerEpiWarps && lane == 0 && my_tiles > 0) {
+            tc::mbar_expect_tx(&zbar[2 * warp], 4096);
+            tc::tma_load_2d(sStage + warp * kLayerStage, &tmZ, n0 + 64 * (warp >> 2), pair * kTileM + 32 * (warp & 3),
+                            &zbar[2 * warp]);
+        }
+    }
+    // And the biases (the optimiser's too), or the zeroed bias-gradient sums.
     if constexpr (EPI == kBiasSilu) {
         for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
     } else {
         for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
     }
+    // Launched programmatically: the previous grid of the stream has finished before any other global
+    // access.
+    tc::grid_dep_wait();
+    tc::grid_dep_launch();
     __syncthreads();
 
     if (warp == kLayerEpiWarps) {
@@ -787,7 +796,8 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const uint32_t tq = tmem + (static_cast<uint32_t>(32 * quad) << 16) + 64 * part;
         const int x = n0 + 64 * part;  // the warp's first output column
         bool ok = true;
-        int z_issued = 0, z_waited = 0;  // kDsilu: pre-activation box loads (lane 0 issues)
+        // kDsilu: pre-activation box loads (lane 0 issues; tile 0's before the launch wait)
+        int z_issued = EPI == kDsilu && my_tiles > 0 ? 1 : 0, z_waited = 0;
         // kDsilu: this lane's share of the bias gradient of the warp's 64 columns, summed over the rows it
         // meets in all of the CTA's tiles (the CTA's columns are the same for every tile); the sums over
         // the warp's lanes are taken once, after the last tile.
@@ -800,9 +810,6 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             tc::tma_load_2d(wb + (t & 1) * 4096, &tmZ, x, (pair + t * pairs) * kTileM + 32 * quad, bar);
             ++z_issued;
         };
-        if constexpr (EPI == kDsilu) {
-            if (lane == 0 && my_tiles > 0) load_z(0);
-        }
         for (int t = 0; t < my_tiles; ++t) {
             const int b = t & 1, u = t >> 1;
             const int y0 = (pair + t * pairs) * kTileM + 32 * quad;
