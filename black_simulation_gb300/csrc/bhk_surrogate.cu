@@ -52,6 +52,8 @@ struct EpiArgs {
     int ld_f32;
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
     int no_store;          // kDsilu in layer_kernel: dZ is not written (only the fused gradients are used)
+    int late_weights;      // layer_kernel: the weights and biases were written by the kernel launched just
+                           // before (the optimiser step): load them after the programmatic-launch wait
     // kHeadLoss (the head's forward with the loss fused in; colsum takes the head's bias gradient):
     const uint8_t* cls;    // per row: target class 1 captured, 2 disk, 3 escaped
     const float* tgt;      // per row: 8 targets
@@ -644,13 +646,21 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    // The weights are loaded before the wait on the previous grid, overlapping its tail: they were
-    // written by the optimiser step (or a weight upload) at least two launches upstream, and no kernel
-    // in between writes them.
-    if (warp == kLayerEpiWarps && lane == 0) {
-        tc::mbar_expect_tx(wbar, kc * kABytes);
-        for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
-    }
+    // The weights are loaded before the wait on the previous grid, overlapping its tail, unless the
+    // previous kernel wrote them (late_weights): otherwise they were written by the optimiser step (or a
+    // weight upload) at least two launches upstream, and no kernel in between writes them.
+    auto load_weights = [&]() {
+        if (warp == kLayerEpiWarps && lane == 0) {
+            tc::mbar_expect_tx(wbar, kc * kABytes);
+            for (int c = 0; c < kc; ++c) tc::tma_load_2d(sW + c * kABytes, &tmW, c * kChunkK, n0, wbar);
+        }
+        if constexpr (EPI == kBiasSilu) {  // the biases too, or the zeroed bias-gradient sums
+            for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
+        } else {
+            for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
+        }
+    };
+    if (!ea.late_weights) load_weights();
     // So is each epilogue warp's first pre-activation box (kDsilu): Z was written by the forward pass.
     if constexpr (EPI == kDsilu) {
         if (warp < kLayerEpiWarps && lane == 0 && my_tiles > 0) {
@@ -659,16 +669,11 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             &zbar[2 * warp]);
         }
     }
-    // And the biases (the optimiser's too), or the zeroed bias-gradient sums.
-    if constexpr (EPI == kBiasSilu) {
-        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = ea.bias[n0 + i];
-    } else {
-        for (int i = threadIdx.x; i < kLayerN; i += blockDim.x) sx[i] = 0.0f;
-    }
     // Launched programmatically: the previous grid of the stream has finished before any other global
     // access.
     tc::grid_dep_wait();
     tc::grid_dep_launch();
+    if (ea.late_weights) load_weights();
     __syncthreads();
 
     if (warp == kLayerEpiWarps) {
@@ -1507,7 +1512,7 @@ inline unsigned feature_blocks(long long n, long long n_a) {
 // Adam on the flat FP32 parameters; refreshes the BF16 copies W (fan_out x fan_in) and W^T.
 struct AdamArgs {
     float* p;
-    const float* g;
+    float* g;  // (kAdam) read, then zeroed for the next step
     float* m;
     float* v;
     bf16* w_rm[kLayers];
@@ -1516,7 +1521,7 @@ struct AdamArgs {
     size_t total;
     int hid;                        // hidden width of the network
     float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
-    const float* loss;              // with hist: the step's four loss terms, copied to hist
+    float* loss;                    // the step's four loss terms: copied to hist (if any), then zeroed
     float* hist;
 };
 
@@ -1542,7 +1547,10 @@ __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
     if constexpr (kAdam) {
         tc::grid_dep_wait();
         tc::grid_dep_launch();
-        if (a.hist && blockIdx.x == 0 && threadIdx.x < 4) a.hist[threadIdx.x] = a.loss[threadIdx.x];
+        if (blockIdx.x == 0 && threadIdx.x < 4 && a.loss) {
+            if (a.hist) a.hist[threadIdx.x] = a.loss[threadIdx.x];
+            a.loss[threadIdx.x] = 0.0f;  // for the next step, as the gradient below
+        }
     }
     constexpr int kPer = 5;  // elements per thread (4 in a weight tile; up to 5 of the biases)
     size_t idx[kPer];
@@ -1559,6 +1567,11 @@ __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
                 mw[q] = a.m[idx[q]];
                 vw[q] = a.v[idx[q]];
             }
+        }
+        if constexpr (kAdam) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q)
+                if (in[q]) a.g[idx[q]] = 0.0f;  // the next step accumulates from zero
         }
         if constexpr (kAdam) {
 #pragma unroll
@@ -1648,6 +1661,8 @@ struct bhk_surrogate {
     unsigned long long* n_list = nullptr;
     float* half_bias = nullptr;
     unsigned long long* n_list_host = nullptr;
+    bhk::sur::bf16* F_all = nullptr;  // training: the features of all the batches' rows (grow-only)
+    size_t cap_F_all = 0;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     float4 w = make_float4(1.0f, 10.0f, 10.0f, 10.0f);  // loss weights (CE, r_disk, ln g, direction)
     std::vector<void*> allocs;
@@ -1718,6 +1733,13 @@ bool build_maps(bhk_surrogate* s, int n, bool training, Maps* M) {
     return ok;
 }
 
+// The features' tensor maps for n rows starting at F: the first layer's [128 x 64] boxes, the fused
+// first-layer weight gradient's [32 x 64] boxes and the MN-major [64 x 64] boxes.
+bool feature_maps(const bf16* F, int n, Maps* M) {
+    return make_tmap(&M->F_rm, F, n, kFeat, kTileM) && make_tmap_rows32(&M->Fs, F, n, kFeat) &&
+           make_tmap(&M->Fm, F, n, kFeat, 64);
+}
+
 EpiArgs epi(int M, int N) {
     EpiArgs e{};
     e.M = M;
@@ -1738,13 +1760,16 @@ cudaError_t launch_head(const Maps& M, const EpiArgs& ea, int sms, int* err, cud
 
 // Forward pass of n rows (features already in F): z, activations, and the head -- into Y, or with `loss`
 // (training: the loss's targets and outputs) the loss and dLoss/dY straight from the head's epilogue;
-// at width 256 the head's weight gradient too (head_kernel).
-cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, const EpiArgs* loss = nullptr) {
+// at width 256 the head's weight gradient too (head_kernel). late_weights: the kernel launched just
+// before wrote the weights (the first layer may not load them ahead of its launch wait).
+cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, const EpiArgs* loss = nullptr,
+                    bool late_weights = false) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
         EpiArgs ea = epi(n, H);
         ea.bias = s->p + s->L.b[l];
+        ea.late_weights = l == 0 && late_weights ? 1 : 0;
         OutMaps om;
         om.z = M.zs[l];
         om.r = M.as[l];
@@ -1996,6 +2021,7 @@ bhk_status bhk_surrogate_destroy(bhk_surrogate* s) {
     cudaDeviceSynchronize();
     for (void* q : s->allocs) cudaFree(q);
     if (s->frames_dev) cudaFree(s->frames_dev);
+    if (s->F_all) cudaFree(s->F_all);
     if (s->list) cudaFree(s->list);
     if (s->n_list_host) cudaFreeHost(s->n_list_host);
     for (cudaEvent_t e : s->ev)
@@ -2117,26 +2143,49 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
         set_last_error("bhk_surrogate_train: tensor map creation failed");
         return BHK_ECUDA;
     }
+    const int64_t nb = n / batch;
+    // The features of all the batches' rows, once per call (the Fourier matrix does not change during
+    // training); each step reads its batch's rows at their offset.
+    const int64_t rows = nb * batch;
+    if (rows > INT32_MAX) {
+        set_last_error("bhk_surrogate_train: at most 2^31 - 1 training rows per call");
+        return BHK_EINVAL;
+    }
+    if (static_cast<size_t>(rows) > s->cap_F_all) {
+        if (s->F_all) cudaFree(s->F_all);
+        s->F_all = nullptr;
+        s->cap_F_all = 0;
+        if (cudaMalloc(&s->F_all, static_cast<size_t>(rows) * kFeat * sizeof(bf16)) != cudaSuccess) {
+            set_last_error("bhk_surrogate_train: out of device memory for the training features");
+            return BHK_ENOMEM;
+        }
+        s->cap_F_all = static_cast<size_t>(rows);
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     float* hist = nullptr;
     if (loss_history && cudaMalloc(&hist, sizeof(float) * 4 * steps) != cudaSuccess) return BHK_ENOMEM;
     cudaMemsetAsync(s->err, 0, sizeof(int), st);
-    const int64_t nb = n / batch;
     cudaError_t e = cudaSuccess;
     AdamArgs aa = adam_args(s);
     aa.b1 = 0.9f;
     aa.b2 = 0.999f;
     aa.eps = 1e-8f;
-    // One step: features (zeroing the gradient and the loss terms), forward, loss and backward, Adam
-    // (copying the loss terms to the history) -- kernels launched programmatically back to back.
+    // The features' launch also zeroes the gradient and the loss terms; from then on each step's Adam
+    // zeroes them after use (and copies the loss terms to the history). One step: forward, loss and
+    // backward, Adam -- kernels launched programmatically back to back.
     aa.loss = s->loss;
+    e = launch_pdl(feature_kernel, dim3(feature_blocks(rows, s->L.total)), dim3(256), 0, st, x,
+                   static_cast<const float*>(s->Bm), s->F_all, static_cast<int>(rows), s->g,
+                   static_cast<long long>(s->L.total), s->loss, 4);
     for (int64_t t = 0; t < steps && e == cudaSuccess; ++t) {
         const int64_t off = (t % nb) * batch;
-        e = launch_pdl(feature_kernel, dim3(feature_blocks(batch, s->L.total)), dim3(256), 0, st, x + off * kIn,
-                       static_cast<const float*>(s->Bm), s->F_rm, batch, s->g, static_cast<long long>(s->L.total),
-                       s->loss, 4);
+        if (!feature_maps(s->F_all + off * kFeat, batch, &M)) {
+            e = cudaErrorInvalidValue;
+            break;
+        }
         const EpiArgs la = loss_args(s, cls + off, tgt + off * kOut, batch);
-        if (e == cudaSuccess) e = forward(s, M, batch, st, &la);
+        // (the first layer follows the previous step's Adam, which wrote its weights)
+        if (e == cudaSuccess) e = forward(s, M, batch, st, &la, true);
         if (e == cudaSuccess) e = backward(s, M, batch, st);
         ++s->step;
         aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
