@@ -842,6 +842,13 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&tempty[b]);
+            if constexpr (WG > 0) {
+                // The next tile's Z box as early as its buffer (tile t - 1's) is free: if the weight-gradient
+                // MMAs have read it by now, issue the load here; else at the end of this iteration.
+                if (lane == 0 && t + 1 < my_tiles && z_issued == t + 1 &&
+                    (t == 0 || tc::mbar_test(&dzfree[(t - 1) & 1], ((t - 1) >> 1) & 1)))
+                    load_z(t + 1);
+            }
             uint8_t* zin = wb + (t & 1) * 4096;
             uint4 av[8];  // kBiasSilu: the tile's A values (BF16) wait here while the Z box is stored
 #pragma unroll
@@ -913,7 +920,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 // read it (its dZ store has: the wait at the top of this iteration).
                 if (t + 1 < my_tiles) {
                     int zok = 1;
-                    if (lane == 0) {
+                    if (lane == 0 && z_issued == t + 1) {
                         if (t >= 1) zok = tc::mbar_wait(&dzfree[(t - 1) & 1], ((t - 1) >> 1) & 1) ? 1 : 0;
                         if (zok) load_z(t + 1);
                     }
