@@ -1139,9 +1139,29 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
         for (int i = 0; i < kOutPad; ++i) csum[i] = 0.0f;
         bool ok = true;
+        float bias[kOutPad];  // the head's bias, once
+#pragma unroll
+        for (int i = 0; i < kOutPad; ++i) bias[i] = ea.bias[i];
         for (int t = 0; t < my && ok; ++t) {
             const int b = t & 1;
             const int m = (blockIdx.x + t * gridDim.x) * kTileM + row;
+            // The row's class and targets, loaded while the tile's MMAs run.
+            int cl = 0;
+            float tgv[kOut];
+#pragma unroll
+            for (int i = 0; i < kOut; ++i) tgv[i] = 0.0f;
+            if (m < ea.M) {
+                cl = static_cast<int>(ea.cls[m]) - 1;
+                const float* tr = ea.tgt + static_cast<size_t>(m) * kOut;
+                if ((reinterpret_cast<uintptr_t>(ea.tgt) & 15) == 0) {  // rows of 32 bytes from an aligned base
+                    const float4 t0 = reinterpret_cast<const float4*>(tr)[0], t1 = reinterpret_cast<const float4*>(tr)[1];
+                    tgv[0] = t0.x; tgv[1] = t0.y; tgv[2] = t0.z; tgv[3] = t0.w;
+                    tgv[4] = t1.x; tgv[5] = t1.y; tgv[6] = t1.z; tgv[7] = t1.w;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < kOut; ++i) tgv[i] = tr[i];
+                }
+            }
             ok = __all_sync(0xffffffffu, tc::mbar_wait(&yfull[b], (t >> 1) & 1) ? 1 : 0) != 0 && !*fail;
             if (!ok) break;
             tc::fence_after_sync();
@@ -1157,9 +1177,8 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (m < ea.M) {
                 float y[kOutPad];
 #pragma unroll
-                for (int i = 0; i < kOutPad; ++i) y[i] = __uint_as_float(r[i]) + ea.bias[i];
-                row_loss(y, static_cast<int>(ea.cls[m]) - 1, ea.tgt + static_cast<size_t>(m) * kOut, ea.inv_n, ea.lw, d,
-                         terms);
+                for (int i = 0; i < kOutPad; ++i) y[i] = __uint_as_float(r[i]) + bias[i];
+                row_loss(y, cl, tgv, ea.inv_n, ea.lw, d, terms);
             }
             __align__(16) bf16 ob[kOutPad];
 #pragma unroll
