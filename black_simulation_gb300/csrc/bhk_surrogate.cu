@@ -54,6 +54,8 @@ struct EpiArgs {
     int no_store;          // kDsilu in layer_kernel: dZ is not written (only the fused gradients are used)
     int late_weights;      // layer_kernel: the weights and biases were written by the kernel launched just
                            // before (the optimiser step): load them after the programmatic-launch wait
+    int early_a;           // layer_kernel (forward): A was written at least two launches upstream, so the
+                           // first ring's worth of its chunks may be loaded before that wait
     // kHeadLoss (the head's forward with the loss fused in; colsum takes the head's bias gradient):
     const uint8_t* cls;    // per row: target class 1 captured, 2 disk, 3 escaped
     const float* tgt;      // per row: 8 targets
@@ -661,6 +663,17 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
     };
     if (!ea.late_weights) load_weights();
+    int pre_issued = 0;  // (producer) A chunks issued before the launch wait, into the fresh ring stages
+    if constexpr (EPI == kBiasSilu) {
+        if (ea.early_a && warp == kLayerEpiWarps && lane == 0) {
+            for (; pre_issued < kLayerRing && pre_issued < my_tiles * kc; ++pre_issued) {
+                const int t = pre_issued / kc, c = pre_issued % kc;
+                tc::mbar_expect_tx(&full[pre_issued], kABytes);
+                tc::tma_load_2d(sRing + pre_issued * kABytes, &tmA, c * kChunkK, (pair + t * pairs) * kTileM,
+                                &full[pre_issued]);
+            }
+        }
+    }
     // So is each epilogue warp's first pre-activation box (kDsilu): Z was written by the forward pass.
     if constexpr (EPI == kDsilu) {
         if (warp < kLayerEpiWarps && lane == 0 && my_tiles > 0) {
@@ -679,7 +692,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     if (warp == kLayerEpiWarps) {
         // ---- producer: the A chunks of every tile through the ring (the weights are on their way) ----
         if (lane == 0) {
-            int issued = 0;
+            int issued = pre_issued;
             // Takes the next ring stage (false: a wait timed out).
             auto next_stage = [&](int& s) {
                 s = issued % kLayerRing;
@@ -694,6 +707,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 if (t < my_tiles) {  // D(t): the layer GEMM's A chunks
                     const int m0 = (pair + t * pairs) * kTileM;
                     for (int c = 0; c < kc && ok; ++c) {
+                        if (t * kc + c < pre_issued) continue;  // loaded before the launch wait
                         int s;
                         if (!(ok = next_stage(s))) break;
                         tc::mbar_expect_tx(&full[s], kABytes);
@@ -1570,31 +1584,33 @@ __host__ __device__ inline int weights_blocks(int hid) {
 template <bool kAdam>
 __global__ void __launch_bounds__(256) weights_kernel(AdamArgs a) {
     __shared__ bf16 tile[32][34];
-    if constexpr (kAdam) {
-        tc::grid_dep_wait();
-        tc::grid_dep_launch();
-        if (blockIdx.x == 0 && threadIdx.x < 4 && a.loss) {
-            if (a.hist) a.hist[threadIdx.x] = a.loss[threadIdx.x];
-            a.loss[threadIdx.x] = 0.0f;  // for the next step, as the gradient below
-        }
-    }
     constexpr int kPer = 5;  // elements per thread (4 in a weight tile; up to 5 of the biases)
     size_t idx[kPer];
     bool in[kPer];
     float pw[kPer], gw[kPer], mw[kPer], vw[kPer];
-    // Loads the state of the elements marked in[], then updates them (Adam) and stores it back.
+    // Loads the state of the elements marked in[], then updates them (Adam) and stores it back. The
+    // parameters and moments are loaded before the wait on the previous grid (only the optimiser step
+    // writes them, a step earlier); the gradient and the loss terms after it.
     auto update_all = [&]() {
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             if (!in[q]) continue;
             pw[q] = a.p[idx[q]];
             if constexpr (kAdam) {
-                gw[q] = a.g[idx[q]];
                 mw[q] = a.m[idx[q]];
                 vw[q] = a.v[idx[q]];
             }
         }
         if constexpr (kAdam) {
+            tc::grid_dep_wait();
+            tc::grid_dep_launch();
+            if (blockIdx.x == 0 && threadIdx.x < 4 && a.loss) {
+                if (a.hist) a.hist[threadIdx.x] = a.loss[threadIdx.x];
+                a.loss[threadIdx.x] = 0.0f;  // for the next step, as the gradient below
+            }
+#pragma unroll
+            for (int q = 0; q < kPer; ++q)
+                if (in[q]) gw[q] = a.g[idx[q]];
 #pragma unroll
             for (int q = 0; q < kPer; ++q)
                 if (in[q]) a.g[idx[q]] = 0.0f;  // the next step accumulates from zero
@@ -1787,15 +1803,17 @@ cudaError_t launch_head(const Maps& M, const EpiArgs& ea, int sms, int* err, cud
 // Forward pass of n rows (features already in F): z, activations, and the head -- into Y, or with `loss`
 // (training: the loss's targets and outputs) the loss and dLoss/dY straight from the head's epilogue;
 // at width 256 the head's weight gradient too (head_kernel). late_weights: the kernel launched just
-// before wrote the weights (the first layer may not load them ahead of its launch wait).
+// before wrote the weights (the first layer may not load them ahead of its launch wait);
+// early_features: the features were written at least two launches upstream (it may load them ahead).
 cudaError_t forward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st, const EpiArgs* loss = nullptr,
-                    bool late_weights = false) {
+                    bool late_weights = false, bool early_features = false) {
     cudaError_t e = cudaSuccess;
     const int H = s->hid;
     for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
         EpiArgs ea = epi(n, H);
         ea.bias = s->p + s->L.b[l];
         ea.late_weights = l == 0 && late_weights ? 1 : 0;
+        ea.early_a = l == 0 && early_features ? 1 : 0;
         OutMaps om;
         om.z = M.zs[l];
         om.r = M.as[l];
@@ -2210,8 +2228,9 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
             break;
         }
         const EpiArgs la = loss_args(s, cls + off, tgt + off * kOut, batch);
-        // (the first layer follows the previous step's Adam, which wrote its weights)
-        if (e == cudaSuccess) e = forward(s, M, batch, st, &la, true);
+        // The first layer follows the previous step's Adam, which wrote its weights; its features were
+        // written by the launch before step 0 (so from step 1 on, they are launches upstream).
+        if (e == cudaSuccess) e = forward(s, M, batch, st, &la, true, t > 0);
         if (e == cudaSuccess) e = backward(s, M, batch, st);
         ++s->step;
         aa.lr = static_cast<float>(0.5 * lr0 * (1.0 + std::cos(M_PI * static_cast<double>(t) / steps)));
