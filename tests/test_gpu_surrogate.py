@@ -164,6 +164,31 @@ def test_training_on_traced_rays_reduces_loss(cuda, ctx):
         assert acc > prior + 0.2, (acc, prior)
 
 
+@pytest.mark.parametrize("width", [256, 64])
+def test_every_training_step_starts_from_zeroed_gradient_and_loss(cuda, width):
+    """The optimiser step zeroes the gradient and the loss terms it has used, so that the next step
+    accumulates from zero. Two steps on the same batch at a learning rate too small to move the BF16
+    weights see the same gradient: the second step's loss terms equal the first's (not twice them), and
+    Adam's first moment after them is (0.9 * 0.1 + 0.1) g = 1.9 times the one-step moment 0.1 g (2.9
+    times, were the second gradient added to the first)."""
+    from black_simulation_gb300.surrogate import Surrogate
+    x, cls, tgt, xd, cd, td = _batch(1024, 31)
+    with Surrogate(0, seed=5, max_batch=1024, width=width) as s:
+        p0 = s.params()
+        m0, v0, st0 = s.adam_state()
+        h1 = s.train(xd, cd, td, batch=1024, steps=1, lr=1e-20)
+        m1, _, _ = s.adam_state()
+        s.set_params(p0)
+        s.set_adam_state(m0, v0, st0)
+        h2 = s.train(xd, cd, td, batch=1024, steps=2, lr=1e-20)
+        m2, _, _ = s.adam_state()
+    assert np.allclose(h2[1], h2[0], rtol=1e-4, atol=1e-7), h2
+    assert np.allclose(h2[0], h1[0], rtol=1e-4, atol=1e-7), (h1, h2)
+    big = np.abs(m1) > 1e-3 * np.abs(m1).max()
+    assert big.sum() > 1000
+    assert np.allclose(m2[big], 1.9 * m1[big], rtol=2e-3), np.abs(m2[big] / m1[big] - 1.9).max()
+
+
 def test_checkpoint_round_trip(cuda, tmp_path):
     """Parameters, Fourier matrix and Adam state survive save/load; training resumes as before."""
     from black_simulation_gb300.surrogate import Surrogate
