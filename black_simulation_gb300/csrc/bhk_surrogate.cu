@@ -1022,13 +1022,14 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
 // accumulated in TMEM columns 32-63 over the CTA's tiles and added into the FP32 gradient with TMA
 // reductions at the end. The MMA thread runs Y(t) before the weight gradient of tile t - 1, so that tile
 // t's epilogue overlaps it. Persistent: CTA c takes tiles c, c + grid, ..., three A3 tiles in flight;
-// warp 0 loads, warp 1 issues, warps 2-5 (one per TMEM lane quadrant) are the epilogue.
-constexpr int kHeadThreads = 32 * 6;
+// warp 0 loads, warp 1 issues, warps 2-9 are the epilogue in two groups of four (one warp per TMEM lane
+// quadrant) that take the even and the odd tiles, so that two tiles' epilogues overlap.
+constexpr int kHeadThreads = 32 * 10;
 constexpr int kHeadTileBytes = 4 * kABytes;  // 128 rows x 256 BF16, four [128 x 64] chunks
 constexpr int kHeadBufs = 3;                 // A3 tiles in flight per CTA
 constexpr int kHeadW5Bytes = 16 * 64 * 2;    // one [16 x 64] chunk of W5 (or of dY^T)
 constexpr int kHeadSmem = kHeadBufs * kHeadTileBytes + 4 * kHeadW5Bytes + 2 * 2 * kHeadW5Bytes + 1024 /* alignment */ + 256 +
-                          4 * 20 * 4 + 256;
+                          8 * 20 * 4 + 256;
 
 __global__ void __launch_bounds__(kHeadThreads, 1)
 head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW,
@@ -1146,8 +1147,9 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             tc::mma_commit(wdone);  // every MMA issued has completed when this arrives
         }
     } else {
-        // ---- epilogue: lane = row of the tile (warp w reads TMEM lanes 32 (w % 4) ..)
-        const int quad = warp & 3;
+        // ---- epilogue: lane = row of the tile (warp w reads TMEM lanes 32 (w % 4) ..); group grp takes
+        // the tiles t with t & 1 == grp, whose accumulator and dY^T buffers are its own
+        const int quad = warp & 3, grp = (warp - 2) >> 2;
         const int row = 32 * quad + lane;
         float csum[kOutPad], tsum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -1156,7 +1158,7 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         float bias[kOutPad];  // the head's bias, once
 #pragma unroll
         for (int i = 0; i < kOutPad; ++i) bias[i] = ea.bias[i];
-        for (int t = 0; t < my && ok; ++t) {
+        for (int t = grp; t < my && ok; t += 2) {
             const int b = t & 1;
             const int m = (blockIdx.x + t * gridDim.x) * kTileM + row;
             // The row's class and targets, loaded while the tile's MMAs run.
@@ -1220,17 +1222,17 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             if (lane == 0) tc::mbar_arrive(&dyready[b]);
         }
         if (!ok && lane == 0) *fail = 1;
-        // The bias gradient and the loss terms of the CTA's rows: warp sums, then the four warps.
+        // The bias gradient and the loss terms of the CTA's rows: warp sums, then the eight warps.
 #pragma unroll
         for (int i = 0; i < kOutPad + 4; ++i) {
             float v = i < kOutPad ? csum[i] : tsum[i - kOutPad] * ea.inv_n;
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) red[quad * (kOutPad + 4) + i] = v;
+            if (lane == 0) red[(warp - 2) * (kOutPad + 4) + i] = v;
         }
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (warp == 2 && lane < kOutPad + 4 && ok && my > 0) {
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        if (warp == 2 && lane < kOutPad + 4 && !*fail && my > 0) {
             float v = 0.0f;
-            for (int q = 0; q < 4; ++q) v += red[q * (kOutPad + 4) + lane];
+            for (int q = 0; q < 8; ++q) v += red[q * (kOutPad + 4) + lane];
             if (lane < kOutPad) {
                 if (v != 0.0f) atomicAdd(&ea.colsum[lane], v);
             } else {
@@ -1238,14 +1240,14 @@ head_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             }
         }
         // dW5 += the CTA's partial: TMEM lane c of columns 32 + 16 p holds dW5[.][128 p + c] (c = 32 quad +
-        // lane); each warp stages its [16 x 32] block per p as a [32 x 32] FP32 box (rows 16-31 lie past
-        // the 16 rows of W5 and are not written) in the idle A3 buffers and adds it with a TMA reduction.
+        // lane); group p's warps stage their [16 x 32] blocks as [32 x 32] FP32 boxes (rows 16-31 lie past
+        // the 16 rows of W5 and are not written) in the idle A3 buffers and add them with TMA reductions.
         if (my > 0) {
             ok = __all_sync(0xffffffffu, tc::mbar_wait(wdone, 0) ? 1 : 0) != 0 && !*fail;
             if (ok) {
                 tc::fence_after_sync();
-#pragma unroll
-                for (int p = 0; p < 2; ++p) {
+                {
+                    const int p = grp;
                     uint32_t v[16];
                     tc::tmem_ld16_issue(tmem + (static_cast<uint32_t>(32 * quad) << 16) + 32 + 16 * p, v);
                     tc::tmem_wait16(v);
