@@ -2190,9 +2190,10 @@ bhk_status bhk_surrogate_train(bhk_surrogate* s, const float* x, const uint8_t* 
         return BHK_ECUDA;
     }
     const int64_t nb = n / batch;
-    // The features of all the batches' rows, once per call (the Fourier matrix does not change during
-    // training); each step reads its batch's rows at their offset.
-    const int64_t rows = nb * batch;
+    // The features of the rows of every batch the call visits (steps cycle through the nb batches), once
+    // per call: the Fourier matrix does not change during training; each step reads its batch's rows at
+    // their offset.
+    const int64_t rows = std::min<int64_t>(nb, steps) * batch;
     if (rows > INT32_MAX) {
         set_last_error("bhk_surrogate_train: at most 2^31 - 1 training rows per call");
         return BHK_EINVAL;
