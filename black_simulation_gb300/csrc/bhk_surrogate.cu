@@ -52,6 +52,7 @@ struct EpiArgs {
     int ld_f32;
     float* colsum;         // kDsilu: column sums of the output (bias gradient), atomically
     int no_store;          // kDsilu in layer_kernel: dZ is not written (only the fused gradients are used)
+    int wg;                // layer_kernel<kDsilu, 256>: the fused weight gradient's width, 64 or 256 (0: 256)
     int late_weights;      // layer_kernel: the weights and biases were written by the kernel launched just
                            // before (the optimiser step): load them after the programmatic-launch wait
     int early_a;           // layer_kernel (forward): A was written at least two launches upstream, so the
@@ -577,7 +578,7 @@ __host__ __device__ constexpr int layer_smem_bytes(int epi) {
 // activations, row-major [rows x WG], map tmB2 in [32 rows x 64] boxes): per tile one more set of MMAs
 // (M = 128 dZ columns, N = WG, K = the tile's 128 rows), both operands MN-major -- dZ straight from the
 // epilogue's staging boxes, which are laid out as the 128-byte-swizzled MN-major operand, Ain through
-// the ring (as many 32-row chunks per stage as fit: one for WG 256, four for WG 64) -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
+// the ring (as many 32-row chunks per stage as fit: one at width 256, four at width 64) -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
 // FP32 gradient (map tmG) with TMA reductions at the end. The ring carries the tiles' chunks in the
 // order D(0), D(1), G(0), D(2), G(1), ... (D = the layer GEMM's A, G = Ain), so that the weight
 // gradient of tile t, which waits for tile t's epilogue, never holds up the MMAs of tile t + 1.
@@ -593,10 +594,14 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     constexpr int kLayerRing = layer_ring(EPI);
     constexpr int kLayerStage = layer_stage(EPI);
     constexpr uint32_t kIdesc = tc::idesc_bf16(kTileM, kLayerN);
-    constexpr uint32_t kIdescG = tc::idesc_bf16(kTileM, WG ? WG : 64, true, true);
     constexpr uint32_t kTmemCols = WG ? 512 : 2 * kLayerN;
-    constexpr int kGBytes = WG * 32 * 2;  // one 32-row chunk of Ain
-    constexpr int kGRows = WG ? 32 * (kABytes / kGBytes) : 32;  // Ain rows per ring stage (128 for WG 64)
+    // The fused weight gradient's width: WG, or (WG = 256) the launch's 64 -- the first layer's, against the
+    // 64 features -- so that every backward layer runs the same code, which the previous launch has
+    // brought into the SM's caches.
+    const int wg = WG == 256 && ea.wg == 64 ? 64 : WG;
+    const uint32_t idescG = tc::idesc_bf16(kTileM, wg ? wg : 64, true, true);
+    const int gbytes = wg * 32 * 2;                            // one 32-row chunk of Ain
+    const int grows = wg ? 32 * (kABytes / gbytes) : 32;       // Ain rows per ring stage (128 at width 64)
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* sW = smem;
@@ -716,16 +721,16 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
                 }
                 if constexpr (WG > 0) {
-                    if (t >= 1 && ok) {  // G(t - 1): the weight gradient's Ain rows, kGRows per stage
+                    if (t >= 1 && ok) {  // G(t - 1): the weight gradient's Ain rows, grows per stage
                         const int m0 = (pair + (t - 1) * pairs) * kTileM;
-                        for (int c = 0; c < kTileM / kGRows && ok; ++c) {
+                        for (int c = 0; c < kTileM / grows && ok; ++c) {
                             int s;
                             if (!(ok = next_stage(s))) break;
-                            tc::mbar_expect_tx(&full[s], (kGRows / 32) * kGBytes);
-                            for (int q = 0; q < kGRows / 32; ++q)
-                                for (int j = 0; j < WG / 64; ++j)
-                                    tc::tma_load_2d(sRing + s * kABytes + q * kGBytes + j * 4096, &tmB2, 64 * j,
-                                                    m0 + kGRows * c + 32 * q, &full[s]);
+                            tc::mbar_expect_tx(&full[s], (grows / 32) * gbytes);
+                            for (int q = 0; q < grows / 32; ++q)
+                                for (int j = 0; j < wg / 64; ++j)
+                                    tc::tma_load_2d(sRing + s * kABytes + q * gbytes + j * 4096, &tmB2, 64 * j,
+                                                    m0 + grows * c + 32 * q, &full[s]);
                             ++issued;
                         }
                     }
@@ -774,20 +779,19 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         const int tg = t - 1, b = tg & 1;
                         ok = tc::mbar_wait(&dzready[b], (tg >> 1) & 1) && !*fail;
                         tc::fence_after_sync();
-                        for (int c = 0; c < kTileM / kGRows && ok; ++c) {
+                        for (int c = 0; c < kTileM / grows && ok; ++c) {
                             int s;
                             if (!(ok = take(s))) break;
-#pragma unroll
-                            for (int q = 0; q < kGRows / 32; ++q) {
-                                const int r32 = c * (kGRows / 32) + q;  // rows 32 r32 .. + 31: quad r32's boxes
+                            for (int q = 0; q < grows / 32; ++q) {
+                                const int r32 = c * (grows / 32) + q;  // rows 32 r32 .. + 31: quad r32's boxes
 #pragma unroll
                                 for (int h = 0; h < 2; ++h) {
                                     // dZ: M = the CTA's 128 columns (part 0 and part 1 boxes, 4 warps apart)
                                     const uint64_t ad = tc::smem_desc_sw128_mn(
                                         sStage + r32 * kLayerStage + b * 4096 + h * 2048, 4 * kLayerStage);
                                     const uint64_t bd =
-                                        tc::smem_desc_sw128_mn(sRing + s * kABytes + q * kGBytes + h * 2048, 4096);
-                                    tc::mma_bf16(tmem + 2 * kLayerN, ad, bd, kIdescG,
+                                        tc::smem_desc_sw128_mn(sRing + s * kABytes + q * gbytes + h * 2048, 4096);
+                                    tc::mma_bf16(tmem + 2 * kLayerN, ad, bd, idescG,
                                                  (tg > 0 || r32 > 0 || h > 0) ? 1u : 0u);
                                 }
                             }
@@ -969,10 +973,10 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             }
             if (ok) {
                 tc::fence_after_sync();
-                constexpr int kColsW = WG / 2;
-                const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16) + 2 * kLayerN + part * kColsW;
+                const int colsw = wg / 2;
+                const uint32_t trow = tmem + (static_cast<uint32_t>(32 * quad) << 16) + 2 * kLayerN + part * colsw;
 #pragma unroll 1
-                for (int j = 0; j < kColsW / 32; ++j) {
+                for (int j = 0; j < colsw / 32; ++j) {
                     uint32_t r[32];
                     tc::tmem_ld32_issue(trow + 32 * j, r);
                     tc::tmem_wait32(r);
@@ -987,7 +991,7 @@ layer_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     tc::fence_proxy_async();
                     __syncwarp();
                     if (lane == 0) {
-                        tc::tma_reduce_add_2d(&tmG, box, part * kColsW + 32 * j, n0 + 32 * quad);
+                        tc::tma_reduce_add_2d(&tmG, box, part * colsw + 32 * j, n0 + 32 * quad);
                         tc::bulk_commit();
                     }
                 }
@@ -1900,8 +1904,9 @@ cudaError_t backward(bhk_surrogate* s, const Maps& M, int n, cudaStream_t st) {
             const CUtensorMap& A = l == 3 ? M.dy_rm : M.dz_rm[(2 - l) & 1];
             const CUtensorMap& W = M.Wtl[l + 1];
             const int K = l == 3 ? kOutPad : H;
-            e = l == 0 ? launch_layer<kDsilu, kFeat>(A, W, om, ex, K, s->sms, s->err, st, &M.Fs, &M.gm[0])
-                       : launch_layer<kDsilu, kLayerN * 2>(A, W, om, ex, K, s->sms, s->err, st, &M.as[l - 1], &M.gm[l]);
+            ex.wg = l == 0 ? kFeat : kLayerN * 2;
+            e = launch_layer<kDsilu, kLayerN * 2>(A, W, om, ex, K, s->sms, s->err, st, l == 0 ? &M.Fs : &M.as[l - 1],
+                                                  &M.gm[l]);
         }
         return e;
     }
