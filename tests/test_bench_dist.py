@@ -61,3 +61,21 @@ def test_reference_arm_under_torchrun_prints_one_line():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_training_hbm_accounting_counts_each_tensor_once():
+    """The training line's HBM roofline rests on bench.train_bytes_per_row: per row of the width-256
+    step, the features written once and read by the first layer's forward and backward (128 B each),
+    four hidden layers each reading its input and writing Z and A (3 x 512 B, the first reading the
+    features instead), the head reading A3 and the targets (8 floats and a class byte) and writing dY
+    (32 B), and the backward reading dY / dZ, Z and the layer input and writing dZ (not dZ0)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    a, f, o = 512, 128, 32
+    forward = (f + 2 * a) + 3 * (3 * a) + (a + 33 + o)
+    backward = (o + 3 * a) + 2 * (4 * a) + (2 * a + f)
+    assert bench.train_bytes_per_row(256) == f + forward + backward == 13281
+    # width 64 keeps a separate head weight gradient (dY^T and A3 read again, dY written twice)
+    a = 128
+    assert bench.train_bytes_per_row(64) == f + ((f + 2 * a) + 3 * (3 * a) + (a + 33 + 2 * o)) + \
+        ((o + a) + (o + 3 * a) + 2 * (4 * a) + (2 * a + f))
