@@ -2317,17 +2317,30 @@ struct SurFrame {
     float snap;              // |alpha| below this: the axis-snap strip of kerr.h's kAxisSnap
     int curve_ok;
     float pad[2];
+    // Fourier projections p_j = sum_i B_ji u_i of the frame's rays: (c_j, B_j3, B_j4) with c_j the
+    // frame-constant part over u_0..u_2 (spin, inclination, log r), so that a ray's p_j is
+    // fma(B_j4, u_4, fma(B_j3, u_3, c_j)) -- the same operations, in the same order, as the full sum.
+    float4 proj[kFreq];
     float rho[kCurveBins];   // curve radius at psi_j = pi (j + 0.5) / kCurveBins, psi = atan2(|beta|, alpha - alpha_c)
     float kn[kCurveBins];    // rho / sqrt(rho^2 + (d rho / d psi)^2): radial offset -> normal distance
 };
 
 // Polar table of each frame's critical curve (one block per frame).
-__global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc) {
+__global__ void curve_table_kernel(SurFrame* frames, const bhk_frame_desc* desc, const float* __restrict__ Bm) {
     __shared__ float sa[kCurveSamples], sbt[kCurveSamples];
     __shared__ float s_min, s_max;
     __shared__ int s_any;
     SurFrame& f = frames[blockIdx.x];
     const bhk_frame_desc d = desc[blockIdx.x];
+    if (threadIdx.x < kFreq) {  // the frame's part of the Fourier projections
+        const int j = threadIdx.x;
+        const float x[kIn] = {f.a, f.th, f.log_r, 0.0f, 0.0f};
+        float u[kIn];
+        normalise(x, u);
+        const float* b = Bm + j * kIn;
+        const float c = fmaf(b[2], u[2], fmaf(b[1], u[1], b[0] * u[0]));
+        f.proj[j] = make_float4(c, b[3], b[4], 0.0f);
+    }
     for (int k = threadIdx.x; k < kCurveSamples; k += blockDim.x) {
         double al, be;
         const bool ok = critical_point(d.a, d.r_obs, d.theta_obs, static_cast<double>(k) / (kCurveSamples - 1), &al, &be);
@@ -2401,7 +2414,7 @@ __host__ __device__ constexpr int inf_epi_warps() { return HID == 64 ? 28 : 16; 
 template <int HID>
 __host__ __device__ constexpr int inf_threads() { return 64 + 32 * inf_epi_warps<HID>(); }
 constexpr int kInfBars = 32;  // 64-bit mbarrier words reserved in shared memory
-constexpr int kInfMisc = 8 * kInfBars + 16 + kFreq * kIn * 4;  // barriers, TMEM slot/flag, Fourier matrix
+constexpr int kInfMisc = 8 * kInfBars + 16;  // barriers, TMEM slot and abort flag
 // Per hidden width HID: one tile's activations (HID / 64 chunks of 64 columns), one weight chunk (all
 // HID output rows x 64 K of a hidden layer), the shared memory of the kernel.
 template <int HID>
@@ -2523,14 +2536,12 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
     uint64_t* drain = acc_full + NS;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(full + kInfBars);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    float* sB = reinterpret_cast<float*>(tmem_slot + 4);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long ntiles = (ia.n + kTileRays - 1) / kTileRays;
     const long long cid = blockIdx.x, ncl = gridDim.x;
     const long long n_my = cid < ntiles ? (ntiles - cid + ncl - 1) / ncl : 0;
     const long long groups = (n_my + NS - 1) / NS;
-    for (int i = threadIdx.x; i < kFreq * kIn; i += blockDim.x) sB[i] = ia.Bm[i];
     if (threadIdx.x == 0) {
         for (int st = 0; st < kInfStages; ++st) {
             tc::mbar_init(&full[st], 1);
@@ -2782,10 +2793,8 @@ infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CU
                             float sv[2], cv[2];
 #pragma unroll
                             for (int e = 0; e < 2; ++e) {
-                                const int jj = j0 + j + e;
-                                float pp = 0.0f;
-#pragma unroll
-                                for (int i = 0; i < kIn; ++i) pp += sB[jj * kIn + i] * u[i];
+                                const float4 pj = ia.frames[fi[v]].proj[j0 + j + e];
+                                const float pp = fmaf(pj.z, u[4], fmaf(pj.y, u[3], pj.x));
                                 __sincosf(6.28318530717958648f * (pp - rintf(pp)), &sv[e], &cv[e]);
                             }
                             fs[j >> 1] = pack_bf16(sv[0], sv[1]);
@@ -3050,7 +3059,7 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ddesc, frames, sizeof(bhk_frame_desc) * nframes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail_cuda(e, "frame upload");
-    curve_table_kernel<<<nframes, 256, 0, st>>>(dframes, ddesc);
+    curve_table_kernel<<<nframes, 256, 0, st>>>(dframes, ddesc, s->Bm);
     const int H = s->hid;
     auto* kern = H == 64 ? &infer_kernel<64> : &infer_kernel<256>;
     const int smem = H == 64 ? inf_smem<64>() : inf_smem<256>();
