@@ -574,12 +574,14 @@ __host__ __device__ constexpr int layer_smem_bytes(int epi) {
 }
 
 // WG > 0 (kDsilu only): the kernel also computes the weight gradient of the layer whose dZ it produces,
-// dW[n0 + i][j] += sum over the tile's rows r of dZ[r][n0 + i] Ain[r][j] (j < WG, Ain = the layer's input
-// activations, row-major [rows x WG], map tmB2 in [32 rows x 64] boxes): per tile one more set of MMAs
-// (M = 128 dZ columns, N = WG, K = the tile's 128 rows), both operands MN-major -- dZ straight from the
+// dW[n0 + i][j] += sum over the tile's rows r of dZ[r][n0 + i] Ain[r][j] (j < wg, Ain = the layer's input
+// activations, row-major [rows x wg], map tmB2 in [32 rows x 64] boxes; wg = WG, or 64 when WG = 256 and
+// ea.wg = 64 -- the first layer, whose input is the 64 features): per tile one more set of MMAs
+// (M = 128 dZ columns, N = wg, K = the tile's 128 rows), both operands MN-major -- dZ straight from the
 // epilogue's staging boxes, which are laid out as the 128-byte-swizzled MN-major operand, Ain through
-// the ring (as many 32-row chunks per stage as fit: one at width 256, four at width 64) -- accumulated in TMEM columns 256 .. 256 + WG over all of the CTA's tiles and added into the
-// FP32 gradient (map tmG) with TMA reductions at the end. The ring carries the tiles' chunks in the
+// the ring (as many 32-row chunks per stage as fit: one at width 256, four at width 64) -- accumulated
+// in TMEM columns 256 .. 256 + wg over all of the CTA's tiles and added into the FP32 gradient (map
+// tmG) with TMA reductions at the end. The ring carries the tiles' chunks in the
 // order D(0), D(1), G(0), D(2), G(1), ... (D = the layer GEMM's A, G = Ain), so that the weight
 // gradient of tile t, which waits for tile t's epilogue, never holds up the MMAs of tile t + 1.
 template <int EPI, int WG = 0>
@@ -1401,8 +1403,8 @@ int box_rows_for(int N) { return N <= 16 ? 16 : (N <= 64 ? 64 : 256); }
 // The persistent hidden-layer GEMM of a width-256 network: A (rows x K, K <= 256) row-major with a
 // [128 rows x 64] box map, W [256 x K] with a [128 x 64] box map, the staged epilogue's maps; one CTA per
 // SM (CTA pairs over the two column halves) or fewer for small batches. WG > 0 (kDsilu): with the fused
-// weight gradient of width WG, from the input activations' [32 x 64]-box map `ain` into the FP32
-// gradient's [32 x 32]-box map `grad`.
+// weight gradient of width WG (or ea.wg, 64, at WG = 256), from the input activations' [32 x 64]-box map
+// `ain` into the FP32 gradient's [32 x 32]-box map `grad`.
 template <int EPI, int WG = 0>
 cudaError_t launch_layer(const CUtensorMap& a, const CUtensorMap& w, const OutMaps& om, const EpiArgs& ea, int K,
                          int sms, int* err, cudaStream_t s, const CUtensorMap* ain = nullptr,
