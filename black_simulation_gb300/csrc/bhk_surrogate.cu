@@ -2458,7 +2458,6 @@ struct InferArgs {
     const SurFrame* frames;
     int nframes;
     long long n;
-    const float* Bm;
     const float* bias[kLayers];
     const float* half_bias;  // [4][HID]: the hidden layers' biases halved
     uint8_t* outcome;
@@ -3100,7 +3099,6 @@ extern "C" bhk_status bhk_surrogate_render(bhk_surrogate* s, bhk_context* ctx, c
     ia.frames = dframes;
     ia.nframes = nframes;
     ia.n = total;
-    ia.Bm = s->Bm;
     for (int l = 0; l < kLayers; ++l) ia.bias[l] = s->p + s->L.b[l];
     ia.outcome = out->outcome;
     ia.r_disk = out->r_disk;
